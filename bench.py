@@ -1,0 +1,344 @@
+"""Benchmark of the GB300 RNS-BFV hot path.
+
+Workload (one step): `Multiplicator::multiply` with relinearization on a batch
+of 64 ciphertext pairs at N = 2^14 with six 62-bit moduli, the default
+extension basis of seven 62-bit primes, t = 65537, relinearization key
+resident on the device. Ciphertexts are synthetic: real encryptions made by
+the CPU oracle from a seeded RNG. The metric is ciphertext products per second
+(whole job). Besides the device-resident number the line carries:
+  e2e           the same metric through the host entry point (pinned host
+                buffers, H2D + compute + D2H inside the timed region);
+  single        64 one-ciphertext launches (the unbatched GPU path);
+  roofline      the batched NTT kernels against the measured HBM bandwidth;
+  cpu_baseline  the oracle (C++/Python restatement of fhe.rs) on host cores.
+`--impl reference` times the CPU restatement alone on all host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, L, T = 1 << 14, 6, 65537
+METRIC = "BFV mul+relin ct/s N=2^14 L=6, batched vs single, bit-exact; NTT % HBM peak"
+UNIT = "ct/s"
+# DRAM bytes per launch of the forward NTT kernel (k_ntt_fwd<14>) on the
+# bench's 1536-limb batch, from an ncu capture (profiles/ntt_fwd_n16384.md);
+# None until a capture exists.
+NTT_FWD_TRAFFIC_BYTES = None
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(ora, batch: int, seed: int = 2026, distinct: int = 16):
+    """Keys and `batch` ciphertext pairs (cycled from `distinct` encryptions)."""
+    rng = np.random.default_rng(seed)
+    par = ora.BfvParameters(N, T, moduli_sizes=[62] * L)
+    sk = ora.SecretKey.random(par, rng)
+    rk = ora.RelinearizationKey(sk, rng)
+    cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, N, dtype=np.uint64), "simd", par), rng)
+           for _ in range(distinct)]
+    arrs = [c.to_array() for c in cts]
+    lhs = np.stack([arrs[i % distinct] for i in range(batch)])
+    rhs = np.stack([arrs[(7 * i + 3) % distinct] for i in range(batch)])
+    return par, sk, rk, cts, lhs, rhs
+
+
+def cpu_multiply_rate(ora, rk, cts, threads: int, per_thread: int):
+    """Oracle products per second with `threads` host threads (independent
+    ciphertexts, the reference has no internal parallelism)."""
+    mult = ora.Multiplicator.default(rk)
+
+    def work(tid):
+        for k in range(per_thread):
+            mult.multiply(cts[(tid + k) % len(cts)], cts[(tid * 3 + k + 1) % len(cts)])
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    dt = time.perf_counter() - t0
+    return threads * per_thread / dt, dt
+
+
+def run_reference(args, rank: int):
+    from oracle import build as oracle_build
+    from oracle import ora
+
+    if rank != 0:
+        return
+    oracle_build.build()
+    par, sk, rk, cts, _, _ = make_inputs(ora, 8, distinct=8)
+    cores = os.cpu_count() or 1
+    cpu_multiply_rate(ora, rk, cts, 1, 1)  # warm the caches of the oracle
+    rates = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_multiply_rate(ora, rk, cts, cores, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, _ = cpu_multiply_rate(ora, rk, cts, cores, 1)
+        rates.append(r)
+    total = time.perf_counter() - t0
+    value = args.steps * cores / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "bfv_mul_relin", "degree": N, "moduli": L, "moduli_bits": 62, "plaintext": T,
+                   "batch_pairs_per_step": cores, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} products per step (one per host thread) of the CPU restatement of "
+                                   "fhe.rs Multiplicator::default().multiply; the Rust reference cannot be built "
+                                   "(no Rust toolchain)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int):
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    B = args.batch
+    par_o, sk, rk_o, cts, lhs, rhs = make_inputs(ora, B)
+    par = fg.BfvParameters(N, par_o.moduli, T)
+    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
+    mult = fg.Multiplicator.default(rk)
+    lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
+    out_d = fg.empty((B, 2, L, N))
+    stream = torch.cuda.current_stream()
+
+    # Parity gate: two products of the batch against the oracle.
+    mult.multiply(lhs_d, rhs_d, out_d)
+    torch.cuda.synchronize()
+    got = fg.to_host(out_d)
+    mult_o = ora.Multiplicator.default(rk_o)
+    for b in (0, B - 1):
+        lo = ora.Ciphertext.from_array(par_o, lhs[b], 0)
+        ro = ora.Ciphertext.from_array(par_o, rhs[b], 0)
+        if not np.array_equal(got[b], mult_o.multiply(lo, ro).to_array()):
+            raise SystemExit(f"bench: GPU product {b} is not bit-exact with the oracle")
+
+    for _ in range(args.warmup):
+        mult.multiply(lhs_d, rhs_d, out_d)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(dev) as clocks:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            mult.multiply(lhs_d, rhs_d, out_d)
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = fg.kernel_launch_count() - launches0
+    ms = start.elapsed_time(end) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * B / (ms / 1000.0)
+
+    # The unbatched path: 64 one-ciphertext launches.
+    one_l, one_r, one_o = lhs_d[:1], rhs_d[:1], out_d[:1]
+    for _ in range(3):
+        mult.multiply(one_l, one_r, one_o)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for b in range(B):
+        mult.multiply(lhs_d[b:b + 1], rhs_d[b:b + 1], out_d[b:b + 1])
+    end.record(stream)
+    torch.cuda.synchronize()
+    single_ms = start.elapsed_time(end)
+    single_rate = B / (single_ms / 1000.0)
+
+    # End to end through the host entry point (pinned buffers).
+    h_l = torch.from_numpy(lhs.view(np.int64)).pin_memory().numpy().view(np.uint64)
+    h_r = torch.from_numpy(rhs.view(np.int64)).pin_memory().numpy().view(np.uint64)
+    h_o = torch.empty((B, 2, L, N), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    for _ in range(2):
+        mult.multiply_host(h_l, h_r, h_o)
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        mult.multiply_host(h_l, h_r, h_o)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if not np.array_equal(h_o, got):
+        raise SystemExit("bench: host entry point result differs from the device result")
+
+    # Roofline of the batched NTT kernels: 256 polynomials x 6 limbs (201 MB,
+    # larger than L2), forward and inverse timed separately.
+    ctx = par.context_at_level(0)
+    polys = 256
+    buf = fg.to_device(np.tile(lhs[:1, 0], (polys, 1, 1)))
+    fg.ntt_forward(ctx, buf)
+    fg.ntt_backward(ctx, buf)
+    torch.cuda.synchronize()
+    reps = 10
+    start.record(stream)
+    for _ in range(reps):
+        fg.ntt_forward(ctx, buf)
+    end.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = start.elapsed_time(end) / reps
+    start.record(stream)
+    for _ in range(reps):
+        fg.ntt_backward(ctx, buf)
+    end.record(stream)
+    torch.cuda.synchronize()
+    inv_ms = start.elapsed_time(end) / reps
+    data_bytes = 2 * 8 * polys * L * N  # read + write of every residue
+    tw_bytes = 2 * 8 * L * N  # twiddles and their Shoup companions, one direction
+    fwd_gbs = (data_bytes + tw_bytes) / (fwd_ms / 1000.0) / 1e9
+    inv_gbs = (data_bytes + tw_bytes) / (inv_ms / 1000.0) / 1e9
+    peak, peak_kind = _peaks()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        cpu_multiply_rate(ora, rk_o, cts, 1, 1)
+        single_thread, st_s = cpu_multiply_rate(ora, rk_o, cts, 1, 2)
+        per_thread = max(1, min(4, int(args.cpu_seconds / max(st_s / 2, 1e-3) / 1)))
+        rate, dt = cpu_multiply_rate(ora, rk_o, cts, cores, per_thread)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cores * per_thread} products on {cores} host threads ({dt:.1f} s); single-thread "
+                         f"{single_thread:.2f} ct/s; CPU restatement of fhe.rs Multiplicator::multiply "
+                         "(the Rust reference cannot be built here)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions by the CPU oracle)",
+            "config": {"workload": "bfv_mul_relin_batched", "degree": N, "moduli": L, "moduli_bits": 62,
+                       "extension_moduli": 7, "plaintext": T, "batch_pairs": B, "keys": "device resident",
+                       "l2": "no flush: each step streams > 1 GB (inputs 201 MB, outputs 100 MB, scratch) through "
+                             "the 126 MB L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "single": {"value": single_rate, "unit": UNIT, "note": f"{B} one-ciphertext launches"},
+            "batch_vs_single": value / world / single_rate,
+            "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
+                    "d2h_bytes_per_step": int(h_o.nbytes)},
+            "roofline": {"bound": "hbm", "achieved": fwd_gbs, "peak": peak, "unit": "GB/s", "frac": fwd_gbs / peak,
+                         "traffic": NTT_FWD_TRAFFIC_BYTES, "kernel": "k_ntt_fwd<14> (forward NTT, 1536 limbs)",
+                         "peak_kind": peak_kind, "inverse_achieved": inv_gbs, "inverse_frac": inv_gbs / peak,
+                         "fwd_ms": fwd_ms, "inv_ms": inv_ms},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,551 @@
+"""GB300 RNS-BFV hot path: a Python mirror of the fhe.rs API over libfheg.
+
+The classes keep the names and argument meaning of the reference types
+(fhe-math `rq::Context`, `rq::Poly`, `ntt::NttOperator`, `rq::Scaler`,
+`rns::ScalingFactor`; fhe `bfv::BfvParameters`, `Ciphertext`,
+`RelinearizationKey`, `EvaluationKey`/`GaloisKey`, `Multiplicator`) and call
+the C ABI declared in include/fheg.h through ctypes. Device buffers are torch
+tensors (int64 storage holding u64 residues bit for bit); torch is only used
+for device memory and streams. Every compute call runs a CUDA kernel of
+libfheg.so: there is no CPU fallback, and a missing library raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfheg.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "fheg.h")
+
+_lib = None
+
+POWER_BASIS, NTT = 0, 1
+
+c_u64 = ctypes.c_uint64
+c_size = ctypes.c_size_t
+P_u64 = ctypes.POINTER(ctypes.c_uint64)
+c_vp = ctypes.c_void_p
+
+
+class FhegError(RuntimeError):
+    """A non-zero status returned by libfheg (see `fheg_status` in fheg.h)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+# Status codes (include/fheg.h `fheg_status`).
+OK, ERR_INVALID_ARGUMENT, ERR_INVALID_MODULUS, ERR_NTT_UNSUPPORTED, ERR_INVALID_CONTEXT, ERR_INVALID_LEVEL, \
+    ERR_KEY_MISMATCH, ERR_WRONG_PARTS, ERR_NO_MORE_CONTEXT, ERR_BUDGET, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED, \
+    ERR_INTERNAL = range(14)
+
+
+def build(force: bool = False) -> str:
+    from importlib import util
+
+    spec = util.spec_from_file_location("_fheg_build", os.path.join(_HERE, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libfheg.so. Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with build() first (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L):
+    i = ctypes.c_int
+    sig = {
+        "fheg_version": (ctypes.c_char_p, []),
+        "fheg_status_string": (ctypes.c_char_p, [i]),
+        "fheg_last_error": (ctypes.c_char_p, []),
+        "fheg_kernel_launch_count": (c_u64, []),
+        "fheg_generate_prime": (i, [ctypes.c_uint32, c_u64, c_u64, P_u64]),
+        "fheg_supports_ntt": (i, [c_u64, c_size]),
+        "fheg_ntt_default_root": (i, [c_u64, c_size, P_u64]),
+        "fheg_ntt_tables_host": (i, [c_u64, c_size, c_u64, P_u64, P_u64, P_u64, P_u64, P_u64]),
+        "fheg_rns_scaler_constants_host": (i, [P_u64, c_size, P_u64, c_size, P_u64, c_size, P_u64, c_size, P_u64,
+                                               c_size]),
+        "fheg_context_create": (i, [P_u64, c_size, c_size, P_u64, ctypes.POINTER(c_vp)]),
+        "fheg_context_destroy": (None, [c_vp]),
+        "fheg_context_num_moduli": (c_size, [c_vp]),
+        "fheg_context_degree": (c_size, [c_vp]),
+        "fheg_ntt_forward": (i, [c_vp, c_vp, c_size, i, c_vp]),
+        "fheg_ntt_backward": (i, [c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_op": (i, [c_vp, i, c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_substitute": (i, [c_vp, c_size, i, c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_switch_down": (i, [c_vp, i, c_vp, c_vp, c_size, c_vp]),
+        "fheg_scaler_create": (i, [c_vp, c_vp, P_u64, c_size, P_u64, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_scaler_destroy": (None, [c_vp]),
+        "fheg_scaler_scale": (i, [c_vp, i, c_vp, c_vp, c_size, c_vp]),
+        "fheg_params_create": (i, [c_size, P_u64, c_size, c_u64, ctypes.POINTER(c_vp)]),
+        "fheg_params_destroy": (None, [c_vp]),
+        "fheg_params_context_at_level": (i, [c_vp, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_params_max_level": (c_size, [c_vp]),
+        "fheg_ksk_create": (i, [c_vp, c_size, c_size, P_u64, P_u64, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_ksk_destroy": (None, [c_vp]),
+        "fheg_relinearize": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_galois_relinearize": (i, [c_vp, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_ciphertext_switch_down": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_ciphertext_add": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_multiplicator_create_default": (i, [c_vp, ctypes.POINTER(c_vp)]),
+        "fheg_multiplicator_create": (i, [c_vp, c_size, P_u64, c_size, P_u64, c_size, P_u64, c_size, P_u64, c_size,
+                                          P_u64, c_size, P_u64, c_size, P_u64, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_multiplicator_destroy": (None, [c_vp]),
+        "fheg_multiplicator_enable_relinearization": (i, [c_vp, c_vp]),
+        "fheg_multiplicator_enable_mod_switching": (i, [c_vp]),
+        "fheg_multiplicator_output_shape": (i, [c_vp, ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
+        "fheg_multiplicator_multiply": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_multiplicator_multiply_host": (i, [c_vp, P_u64, P_u64, P_u64, c_size]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def check(status: int):
+    if status != OK:
+        raise FhegError(status, lib().fheg_last_error().decode())
+
+
+def _u64(values) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(values, dtype=np.uint64))
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.uint64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(P_u64)
+
+
+def _words(x: int) -> np.ndarray:
+    """Little-endian u64 words of a non-negative integer."""
+    x = int(x)
+    out = []
+    while True:
+        out.append(x & ((1 << 64) - 1))
+        x >>= 64
+        if x == 0:
+            break
+    return _u64(out)
+
+
+def kernel_launch_count() -> int:
+    return int(lib().fheg_kernel_launch_count())
+
+
+# ---------------------------------------------------------------------------
+# Device buffers (torch is plumbing only).
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def to_device(arr: np.ndarray, device="cuda"):
+    """Uploads a u64 numpy array to a device tensor (int64 storage)."""
+    torch = _torch()
+    a = np.ascontiguousarray(arr, dtype=np.uint64).view(np.int64)
+    return torch.from_numpy(a.copy()).to(device)
+
+
+def to_host(t) -> np.ndarray:
+    return t.detach().cpu().numpy().view(np.uint64)
+
+
+def _dp(t) -> int:
+    torch = _torch()
+    assert t.is_cuda and t.dtype == torch.int64 and t.is_contiguous()
+    return t.data_ptr()
+
+
+def _stream() -> int:
+    torch = _torch()
+    return torch.cuda.current_stream().cuda_stream
+
+
+def empty(shape, device="cuda"):
+    torch = _torch()
+    return torch.empty(tuple(shape), dtype=torch.int64, device=device)
+
+
+# ---------------------------------------------------------------------------
+# Host-only number theory (fhe-math zq / ntt).
+
+
+def generate_prime(num_bits: int, modulo: int, upper_bound: int) -> Optional[int]:
+    """fhe-math/src/zq/primes.rs:30-59 `generate_prime`."""
+    out = c_u64(0)
+    check(lib().fheg_generate_prime(num_bits, modulo, upper_bound, ctypes.byref(out)))
+    return out.value or None
+
+
+def supports_ntt(p: int, n: int) -> bool:
+    return bool(lib().fheg_supports_ntt(p, n))
+
+
+def ntt_default_root(p: int, n: int) -> int:
+    out = c_u64(0)
+    check(lib().fheg_ntt_default_root(p, n, ctypes.byref(out)))
+    return out.value
+
+
+def ntt_tables_host(p: int, n: int, root: int = 0):
+    """The four twiddle tables and (size_inv, size_inv_shoup) of NttOperator::new."""
+    t = [np.zeros(n, dtype=np.uint64) for _ in range(4)]
+    inv = np.zeros(2, dtype=np.uint64)
+    check(lib().fheg_ntt_tables_host(p, n, root, *[_ptr(x) for x in t], _ptr(inv)))
+    return t, (int(inv[0]), int(inv[1]))
+
+
+def rns_scaler_constants_host(from_moduli: Sequence[int], to_moduli: Sequence[int], num: int, den: int) -> dict:
+    F, T = len(from_moduli), len(to_moduli)
+    words = 5 + 2 * T + 2 * T * F + 5 * F
+    out = np.zeros(words, dtype=np.uint64)
+    fm, tm, nw, dw = _u64(from_moduli), _u64(to_moduli), _words(num), _words(den)
+    check(lib().fheg_rns_scaler_constants_host(_ptr(fm), F, _ptr(tm), T, _ptr(nw), len(nw), _ptr(dw), len(dw),
+                                               _ptr(out), words))
+    o = 5
+    r = {"theta_garner_shift": int(out[0]), "is_one": bool(out[1]),
+         "theta_gamma": (int(out[2]), int(out[3]), bool(out[4]))}
+    r["gamma"] = out[o:o + T]; o += T
+    r["gamma_shoup"] = out[o:o + T]; o += T
+    r["omega"] = out[o:o + T * F].reshape(T, F); o += T * F
+    r["omega_shoup"] = out[o:o + T * F].reshape(T, F); o += T * F
+    r["theta_omega_lo"] = out[o:o + F]; o += F
+    r["theta_omega_hi"] = out[o:o + F]; o += F
+    r["theta_omega_sign"] = out[o:o + F]; o += F
+    r["theta_garner_lo"] = out[o:o + F]; o += F
+    r["theta_garner_hi"] = out[o:o + F]; o += F
+    return r
+
+
+# ---------------------------------------------------------------------------
+# fhe-math rq
+
+
+class Context:
+    """rq::Context (fhe-math/src/rq/context.rs:9-93), resident on the device."""
+
+    def __init__(self, moduli: Sequence[int], degree: int, roots: Optional[Sequence[int]] = None, _handle=None,
+                 _owner=None):
+        self.moduli = [int(m) for m in moduli]
+        self.degree = degree
+        self._owner = _owner
+        if _handle is not None:
+            self._h = _handle
+            self._owned = False
+            return
+        h = c_vp()
+        m = _u64(self.moduli)
+        r = _u64(roots) if roots is not None else None
+        check(lib().fheg_context_create(_ptr(m), len(m), degree, _ptr(r) if r is not None else None,
+                                        ctypes.byref(h)))
+        self._h = h
+        self._owned = True
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and _lib is not None:
+            _lib.fheg_context_destroy(self._h)
+            self._owned = False
+
+    @property
+    def L(self) -> int:
+        return len(self.moduli)
+
+    def shape(self, count: int = 1):
+        return (count, self.L, self.degree)
+
+
+class NttOperator:
+    """ntt::NttOperator (fhe-math/src/ntt/native.rs) for one modulus, applied
+    to device buffers of shape [..., size]."""
+
+    def __init__(self, p: int, size: int, root: Optional[int] = None):
+        self.ctx = Context([p], size, [root] if root else None)
+        self.size = size
+
+    def forward(self, t, lazy: bool = False):
+        """In place; `forward` (lazy=False) or `forward_vt_lazy` (lazy=True)."""
+        check(lib().fheg_ntt_forward(self.ctx._h, _dp(t), t.numel() // self.size, int(lazy), _stream()))
+
+    def backward(self, t):
+        check(lib().fheg_ntt_backward(self.ctx._h, _dp(t), t.numel() // self.size, _stream()))
+
+
+def ntt_forward(ctx: Context, t, lazy: bool = False):
+    """Poly::into_ntt on a batch [count][L][N] (in place)."""
+    count = t.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_ntt_forward(ctx._h, _dp(t), count, int(lazy), _stream()))
+
+
+def ntt_backward(ctx: Context, t):
+    """Poly::into_power_basis on a batch [count][L][N] (in place)."""
+    count = t.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_ntt_backward(ctx._h, _dp(t), count, _stream()))
+
+
+def poly_op(ctx: Context, op: str, a, b=None):
+    """Coefficient-wise `+`, `-`, `*` (Ntt x Ntt) or negation of batches."""
+    code = {"add": 0, "sub": 1, "mul": 2, "neg": 3}[op]
+    out = empty(a.shape, a.device)
+    count = a.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_poly_op(ctx._h, code, _dp(a), _dp(b) if b is not None else None, _dp(out), count, _stream()))
+    return out
+
+
+def substitute(ctx: Context, t, exponent: int, representation: int):
+    """Poly::substitute (rq/mod.rs:319-369) on a batch."""
+    out = empty(t.shape, t.device)
+    count = t.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_poly_substitute(ctx._h, exponent, representation, _dp(t), _dp(out), count, _stream()))
+    return out
+
+
+def switch_down(ctx: Context, t, representation: int):
+    """Poly::switch_down (rq/mod.rs:390-448); returns [count][L-1][N]. `t` is
+    consumed as scratch in Ntt representation."""
+    count = t.numel() // (ctx.L * ctx.degree)
+    out = empty((count, ctx.L - 1, ctx.degree), t.device)
+    check(lib().fheg_poly_switch_down(ctx._h, representation, _dp(t), _dp(out), count, _stream()))
+    return out
+
+
+class ScalingFactor:
+    """rns::ScalingFactor (fhe-math/src/rns/scaler.rs:19-47)."""
+
+    def __init__(self, numerator: int, denominator: int):
+        if denominator == 0:
+            raise ValueError("denominator is zero")
+        self.numerator, self.denominator = int(numerator), int(denominator)
+
+    @staticmethod
+    def one() -> "ScalingFactor":
+        return ScalingFactor(1, 1)
+
+    @property
+    def is_one(self):
+        return self.numerator == self.denominator
+
+
+class Scaler:
+    """rq::Scaler (fhe-math/src/rq/scaler.rs:17-126)."""
+
+    def __init__(self, frm: Context, to: Context, factor: ScalingFactor):
+        self.frm, self.to = frm, to
+        n, d = _words(factor.numerator), _words(factor.denominator)
+        h = c_vp()
+        check(lib().fheg_scaler_create(frm._h, to._h, _ptr(n), len(n), _ptr(d), len(d), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_scaler_destroy(self._h)
+            self._h = None
+
+    def scale(self, t, representation: int):
+        """Poly::scale on a batch [count][L_from][N] -> [count][L_to][N]."""
+        count = t.numel() // (self.frm.L * self.frm.degree)
+        out = empty((count, self.to.L, self.to.degree), t.device)
+        check(lib().fheg_scaler_scale(self._h, representation, _dp(t), _dp(out), count, _stream()))
+        return out
+
+
+# ---------------------------------------------------------------------------
+# fhe bfv
+
+
+class BfvParameters:
+    """bfv::BfvParameters (fhe/src/bfv/parameters.rs): the level chain."""
+
+    def __init__(self, degree: int, moduli: Sequence[int], plaintext: int):
+        self.degree, self.moduli, self.plaintext = degree, [int(m) for m in moduli], plaintext
+        m = _u64(self.moduli)
+        h = c_vp()
+        check(lib().fheg_params_create(degree, _ptr(m), len(m), plaintext, ctypes.byref(h)))
+        self._h = h
+        self._ctx = {}
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_params_destroy(self._h)
+            self._h = None
+
+    def max_level(self) -> int:
+        return len(self.moduli) - 1
+
+    def context_at_level(self, level: int) -> Context:
+        if level not in self._ctx:
+            h = c_vp()
+            check(lib().fheg_params_context_at_level(self._h, level, ctypes.byref(h)))
+            self._ctx[level] = Context(self.moduli[:len(self.moduli) - level], self.degree, _handle=h, _owner=self)
+        return self._ctx[level]
+
+
+class KeySwitchingKey:
+    """bfv KeySwitchingKey (fhe/src/bfv/keys/key_switching_key.rs:21-45),
+    uploaded from its c0 / c1 polynomials ([count][L_ksk][N], Ntt values)."""
+
+    def __init__(self, par: BfvParameters, c0: np.ndarray, c1: np.ndarray, ciphertext_level: int = 0,
+                 ksk_level: int = 0):
+        self.par = par
+        self.ciphertext_level, self.ksk_level = ciphertext_level, ksk_level
+        c0, c1 = _u64(c0), _u64(c1)
+        h = c_vp()
+        check(lib().fheg_ksk_create(par._h, ciphertext_level, ksk_level, _ptr(c0), _ptr(c1), c0.shape[0],
+                                    ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_ksk_destroy(self._h)
+            self._h = None
+
+
+class RelinearizationKey(KeySwitchingKey):
+    """bfv::RelinearizationKey (fhe/src/bfv/keys/relinearization_key.rs)."""
+
+    def relinearizes(self, ct3):
+        """relinearization_key.rs:71-98 on a batch [count][3][L][N]."""
+        ctx = self.par.context_at_level(self.ciphertext_level)
+        if ct3.dim() != 4 or ct3.shape[1] != 3:
+            raise FhegError(ERR_WRONG_PARTS, "Only supports relinearization of ciphertext with 3 parts")
+        count = ct3.shape[0]
+        out = empty((count, 2, ctx.L, ctx.degree), ct3.device)
+        check(lib().fheg_relinearize(self._h, _dp(ct3), _dp(out), count, _stream()))
+        return out
+
+
+class GaloisKey(KeySwitchingKey):
+    """GaloisKey (fhe/src/bfv/keys/galois_key.rs) for one exponent."""
+
+    def __init__(self, par, exponent: int, c0, c1, ciphertext_level: int = 0, ksk_level: int = 0):
+        super().__init__(par, c0, c1, ciphertext_level, ksk_level)
+        self.exponent = exponent % (2 * par.degree)
+
+    def relinearize(self, ct):
+        """galois_key.rs:63-124 on a batch [count][2][L][N]."""
+        ctx = self.par.context_at_level(self.ciphertext_level)
+        count = ct.shape[0]
+        out = empty((count, 2, ctx.L, ctx.degree), ct.device)
+        check(lib().fheg_galois_relinearize(self._h, self.exponent, _dp(ct), _dp(out), count, _stream()))
+        return out
+
+
+class EvaluationKey:
+    """EvaluationKey (fhe/src/bfv/keys/evaluation_key.rs:23-131): rotations."""
+
+    def __init__(self, par: BfvParameters, galois_keys: Sequence[GaloisKey]):
+        self.par = par
+        self.gk = {g.exponent: g for g in galois_keys}
+
+    def rotates_rows(self, ct):
+        return self.gk[2 * self.par.degree - 1].relinearize(ct)
+
+    def rotates_columns_by(self, ct, i: int):
+        return self.gk[pow(3, i, 2 * self.par.degree)].relinearize(ct)
+
+
+def ciphertext_switch_down(par: BfvParameters, level: int, ct):
+    """Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) on a batch
+    [count][parts][L][N]; `ct` is consumed as scratch."""
+    count, parts = ct.shape[0], ct.shape[1]
+    ctx = par.context_at_level(level)
+    out = empty((count, parts, ctx.L - 1, ctx.degree), ct.device)
+    check(lib().fheg_ciphertext_switch_down(par._h, level, parts, _dp(ct), _dp(out), count, _stream()))
+    return out
+
+
+def ciphertext_add(par: BfvParameters, level: int, a, b):
+    """Add<&Ciphertext> (fhe/src/bfv/ops/mod.rs:15-43) on batches."""
+    out = empty(a.shape, a.device)
+    check(lib().fheg_ciphertext_add(par._h, level, a.shape[1], _dp(a), _dp(b), _dp(out), a.shape[0], _stream()))
+    return out
+
+
+class Multiplicator:
+    """bfv::Multiplicator (fhe/src/bfv/ops/mul.rs:21-227)."""
+
+    def __init__(self, handle, par: BfvParameters, keep=()):
+        self._h = handle
+        self.par = par
+        self._keep = list(keep)
+
+    @staticmethod
+    def default(rk: RelinearizationKey) -> "Multiplicator":
+        """mul.rs:101-130."""
+        h = c_vp()
+        check(lib().fheg_multiplicator_create_default(rk._h, ctypes.byref(h)))
+        return Multiplicator(h, rk.par, [rk])
+
+    @staticmethod
+    def new_leveled(lhs: ScalingFactor, rhs: ScalingFactor, extended_basis: Sequence[int], post: ScalingFactor,
+                    level: int, par: BfvParameters) -> "Multiplicator":
+        """mul.rs:56-98."""
+        ws = [_words(x) for x in (lhs.numerator, lhs.denominator, rhs.numerator, rhs.denominator)]
+        pn, pd = _words(post.numerator), _words(post.denominator)
+        eb = _u64(extended_basis)
+        h = c_vp()
+        args = []
+        for w in ws:
+            args += [_ptr(w), len(w)]
+        check(lib().fheg_multiplicator_create(par._h, level, *args, _ptr(eb), len(eb), _ptr(pn), len(pn), _ptr(pd),
+                                              len(pd), ctypes.byref(h)))
+        return Multiplicator(h, par)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_multiplicator_destroy(self._h)
+            self._h = None
+
+    def enable_relinearization(self, rk: RelinearizationKey):
+        check(lib().fheg_multiplicator_enable_relinearization(self._h, rk._h))
+        self._keep.append(rk)
+
+    def enable_mod_switching(self):
+        check(lib().fheg_multiplicator_enable_mod_switching(self._h))
+
+    def output_shape(self):
+        parts, level = c_size(0), c_size(0)
+        check(lib().fheg_multiplicator_output_shape(self._h, ctypes.byref(parts), ctypes.byref(level)))
+        return parts.value, level.value
+
+    def multiply(self, lhs, rhs, out=None, stream: Optional[int] = None):
+        """mul.rs:158-227 on batches [count][2][L][N] (device tensors)."""
+        if lhs.shape != rhs.shape or lhs.dim() != 4 or lhs.shape[1] != 2:
+            raise FhegError(ERR_WRONG_PARTS, "Multiplication can only be performed on ciphertexts of size 2")
+        parts, level = self.output_shape()
+        count = lhs.shape[0]
+        ctx = self.par.context_at_level(level)
+        if out is None:
+            out = empty((count, parts, ctx.L, ctx.degree), lhs.device)
+        check(lib().fheg_multiplicator_multiply(self._h, _dp(lhs), _dp(rhs), _dp(out), count,
+                                                _stream() if stream is None else stream))
+        return out
+
+    def multiply_host(self, lhs: np.ndarray, rhs: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """End to end from host arrays [count][2][L][N] (u64)."""
+        parts, level = self.output_shape()
+        count = lhs.shape[0]
+        ctx_l = len(self.par.moduli) - level
+        if out is None:
+            out = np.empty((count, parts, ctx_l, self.par.degree), dtype=np.uint64)
+        lhs, rhs = np.ascontiguousarray(lhs, dtype=np.uint64), np.ascontiguousarray(rhs, dtype=np.uint64)
+        check(lib().fheg_multiplicator_multiply_host(self._h, _ptr(lhs), _ptr(rhs), _ptr(out), count))
+        return out

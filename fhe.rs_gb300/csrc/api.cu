@@ -1,0 +1,464 @@
+// C ABI of libfheg (declarations and reference mapping in include/fheg.h).
+
+#include <cstring>
+#include <string>
+
+#include "fheg.h"
+#include "lib.hpp"
+
+using namespace fheg;
+
+struct fheg_context {
+  std::shared_ptr<Context> c;
+};
+struct fheg_scaler {
+  std::unique_ptr<Scaler> s;
+  DevBuf scratch;
+};
+struct fheg_params {
+  std::unique_ptr<Params> p;
+  std::vector<fheg_context> level_handles;
+};
+struct fheg_ksk {
+  Ksk k;
+};
+struct fheg_multiplicator {
+  std::unique_ptr<Multiplicator> m;
+  cudaStream_t copy_stream = nullptr;
+  ~fheg_multiplicator() {
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+  }
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guard(F&& f) {
+  try {
+    g_last_error.clear();
+    f();
+    return FHEG_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return FHEG_ERR_BUDGET;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return FHEG_ERR_INTERNAL;
+  }
+}
+
+void need(bool cond, const char* what) {
+  if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
+}
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+BigUint big(const uint64_t* w, size_t n) { return w && n ? BigUint::from_words(w, n) : BigUint(); }
+
+}  // namespace
+
+FHEG_API const char* fheg_version(void) { return "fheg 0.1.0 (sm_103a)"; }
+
+FHEG_API const char* fheg_status_string(int s) {
+  switch (s) {
+    case FHEG_OK: return "ok";
+    case FHEG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FHEG_ERR_INVALID_MODULUS: return "invalid modulus";
+    case FHEG_ERR_NTT_UNSUPPORTED: return "NTT not supported for this modulus and degree";
+    case FHEG_ERR_INVALID_CONTEXT: return "invalid context";
+    case FHEG_ERR_INVALID_LEVEL: return "invalid level";
+    case FHEG_ERR_KEY_MISMATCH: return "key does not match the ciphertext";
+    case FHEG_ERR_WRONG_PARTS: return "wrong number of ciphertext parts";
+    case FHEG_ERR_NO_MORE_CONTEXT: return "no more context";
+    case FHEG_ERR_BUDGET: return "memory budget exhausted";
+    case FHEG_ERR_CUDA: return "CUDA error";
+    case FHEG_ERR_TIMEOUT: return "timeout";
+    case FHEG_ERR_UNSUPPORTED: return "unsupported";
+    default: return "internal error";
+  }
+}
+
+FHEG_API const char* fheg_last_error(void) { return g_last_error.c_str(); }
+
+FHEG_API uint64_t fheg_kernel_launch_count(void) { return g_launches.load(); }
+
+// ---------------------------------------------------------------------------
+// Host-only number theory.
+
+FHEG_API int fheg_generate_prime(uint32_t num_bits, uint64_t modulo, uint64_t upper_bound, uint64_t* out) {
+  return guard([&] {
+    need(out != nullptr && modulo != 0, "null output or zero modulo");
+    *out = generate_prime(num_bits, modulo, upper_bound);
+  });
+}
+
+FHEG_API int fheg_supports_ntt(uint64_t p, size_t n) {
+  if (n < 8 || (n & (n - 1))) return 0;
+  return supports_ntt(p, n) ? 1 : 0;
+}
+
+FHEG_API int fheg_ntt_default_root(uint64_t p, size_t n, uint64_t* out_root) {
+  return guard([&] {
+    need(out_root != nullptr, "null output");
+    *out_root = default_ntt_root(p, n);
+  });
+}
+
+FHEG_API int fheg_ntt_tables_host(uint64_t p, size_t n, uint64_t root, uint64_t* omegas, uint64_t* omegas_shoup,
+                                  uint64_t* zetas_inv, uint64_t* zetas_inv_shoup, uint64_t* out_size_inv) {
+  return guard([&] {
+    need(omegas && omegas_shoup && zetas_inv && zetas_inv_shoup && out_size_inv, "null output");
+    NttTablesHost t = make_ntt_tables(p, n, root);
+    std::memcpy(omegas, t.omegas.data(), n * 8);
+    std::memcpy(omegas_shoup, t.omegas_shoup.data(), n * 8);
+    std::memcpy(zetas_inv, t.zetas_inv.data(), n * 8);
+    std::memcpy(zetas_inv_shoup, t.zetas_inv_shoup.data(), n * 8);
+    out_size_inv[0] = t.size_inv;
+    out_size_inv[1] = t.size_inv_shoup;
+  });
+}
+
+FHEG_API int fheg_rns_scaler_constants_host(const uint64_t* from_moduli, size_t from_len, const uint64_t* to_moduli,
+                                            size_t to_len, const uint64_t* num, size_t num_words,
+                                            const uint64_t* den, size_t den_words, uint64_t* out,
+                                            size_t out_words) {
+  return guard([&] {
+    need(from_moduli && to_moduli && out && from_len && to_len, "null or empty input");
+    const size_t F = from_len, T = to_len;
+    need(out_words >= 5 + 2 * T + 2 * T * F + 5 * F, "output too small");
+    RnsContextHost from(std::vector<uint64_t>(from_moduli, from_moduli + F));
+    RnsContextHost to(std::vector<uint64_t>(to_moduli, to_moduli + T));
+    RnsScalerHost s = make_rns_scaler(from, to, big(num, num_words), big(den, den_words));
+    size_t o = 0;
+    out[o++] = s.theta_garner_shift;
+    out[o++] = s.is_one ? 1 : 0;
+    out[o++] = s.theta_gamma_lo;
+    out[o++] = s.theta_gamma_hi;
+    out[o++] = s.theta_gamma_sign ? 1 : 0;
+    for (auto v : s.gamma) out[o++] = v;
+    for (auto v : s.gamma_shoup) out[o++] = v;
+    for (auto v : s.omega) out[o++] = v;
+    for (auto v : s.omega_shoup) out[o++] = v;
+    for (auto v : s.theta_omega_lo) out[o++] = v;
+    for (auto v : s.theta_omega_hi) out[o++] = v;
+    for (auto v : s.theta_omega_sign) out[o++] = v;
+    for (auto v : s.theta_garner_lo) out[o++] = v;
+    for (auto v : s.theta_garner_hi) out[o++] = v;
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Contexts and polynomial operations.
+
+FHEG_API int fheg_context_create(const uint64_t* moduli, size_t num_moduli, size_t degree, const uint64_t* roots,
+                                 fheg_context** out) {
+  return guard([&] {
+    need(moduli && num_moduli && out, "null or empty input");
+    auto h = new fheg_context();
+    try {
+      h->c = std::make_shared<Context>(std::vector<uint64_t>(moduli, moduli + num_moduli), degree, roots);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_context_destroy(fheg_context* ctx) { delete ctx; }
+FHEG_API size_t fheg_context_num_moduli(const fheg_context* ctx) { return ctx ? ctx->c->L() : 0; }
+FHEG_API size_t fheg_context_degree(const fheg_context* ctx) { return ctx ? ctx->c->N() : 0; }
+
+FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t count, int lazy, void* stream) {
+  return guard([&] {
+    need(ctx && (d_polys || !count), "null input");
+    PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
+    ntt_forward(*ctx->c, r, r, count, lazy != 0, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_t count, void* stream) {
+  return guard([&] {
+    need(ctx && (d_polys || !count), "null input");
+    PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
+    ntt_backward(*ctx->c, r, r, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out,
+                          size_t count, void* stream) {
+  return guard([&] {
+    need(ctx && op >= 0 && op <= 3, "bad context or op");
+    need((d_a && d_out && (op == 3 || d_b)) || !count, "null input");
+    const Context& c = *ctx->c;
+    PolyRef a = plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn);
+    PolyRef b = plain_ref(const_cast<uint64_t*>(d_b ? d_b : d_a), c.L(), c.logn);
+    PolyRef o = plain_ref(d_out, c.L(), c.logn);
+    poly_op(c, op, a, b, o, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation, const uint64_t* d_in,
+                                  uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(ctx && ((d_in && d_out) || !count), "null input");
+    need(d_in != d_out || !count, "d_out must not alias d_in");
+    const Context& c = *ctx->c;
+    PolyRef i = plain_ref(const_cast<uint64_t*>(d_in), c.L(), c.logn);
+    PolyRef o = plain_ref(d_out, c.L(), c.logn);
+    poly_substitute(c, exponent, representation != 0, i, o, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_poly_switch_down(const fheg_context* ctx, int representation, uint64_t* d_in, uint64_t* d_out,
+                                   size_t count, void* stream) {
+  return guard([&] {
+    need(ctx && ((d_in && d_out) || !count), "null input");
+    const Context& c = *ctx->c;
+    PolyRef i = plain_ref(d_in, c.L(), c.logn);
+    PolyRef o = plain_ref(d_out, c.L() - 1, c.logn);
+    if (representation) poly_switch_down_ntt(c, i, o, count, as_stream(stream));
+    else poly_switch_down_pb(c, i, o, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_scaler_create(const fheg_context* from, const fheg_context* to, const uint64_t* num,
+                                size_t num_words, const uint64_t* den, size_t den_words, fheg_scaler** out) {
+  return guard([&] {
+    need(from && to && out, "null input");
+    BigUint d = big(den, den_words);
+    need(!d.is_zero(), "ScalingFactor denominator is zero");
+    auto h = new fheg_scaler();
+    try {
+      h->s.reset(new Scaler(from->c, to->c, big(num, num_words), d));
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_scaler_destroy(fheg_scaler* s) { delete s; }
+
+FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const uint64_t* d_in, uint64_t* d_out,
+                               size_t count, void* stream) {
+  return guard([&] {
+    need(s && ((d_in && d_out) || !count), "null input");
+    need(d_in != d_out || !count, "d_out must not alias d_in");
+    const Scaler& sc = *s->s;
+    PolyRef i = plain_ref(const_cast<uint64_t*>(d_in), sc.from->L(), sc.from->logn);
+    PolyRef o = plain_ref(d_out, sc.to->L(), sc.to->logn);
+    fheg_scaler* ms = const_cast<fheg_scaler*>(s);
+    if (representation) ms->scratch.reserve(count * sc.from->L() * sc.from->N() * 8);
+    scaler_scale(sc, representation != 0, i, o, count, ms->scratch.u64(), as_stream(stream));
+  });
+}
+
+// ---------------------------------------------------------------------------
+// BFV
+
+FHEG_API int fheg_params_create(size_t degree, const uint64_t* moduli, size_t num_moduli, uint64_t plaintext,
+                                fheg_params** out) {
+  return guard([&] {
+    need(moduli && num_moduli && out, "null or empty input");
+    auto h = new fheg_params();
+    try {
+      h->p.reset(new Params(degree, std::vector<uint64_t>(moduli, moduli + num_moduli), plaintext));
+      for (auto& c : h->p->levels) h->level_handles.push_back(fheg_context{c});
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_params_destroy(fheg_params* par) { delete par; }
+
+FHEG_API int fheg_params_context_at_level(const fheg_params* par, size_t level, const fheg_context** out) {
+  return guard([&] {
+    need(par && out, "null input");
+    if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    *out = &par->level_handles[level];
+  });
+}
+
+FHEG_API size_t fheg_params_max_level(const fheg_params* par) { return par ? par->p->max_level() : 0; }
+
+FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
+                             const uint64_t* h_c1, size_t count, fheg_ksk** out) {
+  return guard([&] {
+    need(par && h_c0 && h_c1 && out, "null input");
+    const Params& p = *par->p;
+    if (ciphertext_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    if (ksk_level > ciphertext_level) throw Error(FHEG_ERR_INVALID_LEVEL, "Unexpected levels");
+    auto h = new fheg_ksk();
+    try {
+      Ksk& k = h->k;
+      k.par = &p;
+      k.ciphertext_level = ciphertext_level;
+      k.ksk_level = ksk_level;
+      k.ctx_ct = p.ctx(ciphertext_level);
+      k.ctx_ksk = p.ctx(ksk_level);
+      if (k.ctx_ksk->L() < 2) throw Error(FHEG_ERR_UNSUPPORTED, "These parameters do not support key switching");
+      if (count != k.ctx_ct->L()) throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
+      k.count = count;
+      const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
+      k.keys.alloc(4 * words * 8);
+      upload(k.values(0), h_c0, words * 8);
+      upload(k.values(1), h_c1, words * 8);
+      compute_shoup(*k.ctx_ksk, k.values(0), k.shoup(0), count, nullptr);
+      compute_shoup(*k.ctx_ksk, k.values(1), k.shoup(1), count, nullptr);
+      check_cuda(cudaDeviceSynchronize(), "ksk upload");
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_ksk_destroy(fheg_ksk* k) { delete k; }
+
+FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(rk && ((d_ct3 && d_out) || !count), "null input");
+    relinearize(rk->k, d_ct3, d_out, count, rk->k.ws, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const uint64_t* d_ct, uint64_t* d_out,
+                                     size_t count, void* stream) {
+  return guard([&] {
+    need(gk && ((d_ct && d_out) || !count), "null input");
+    need(d_ct != d_out || !count, "d_out must not alias d_ct");
+    galois_relinearize(gk->k, exponent, d_ct, d_out, count, gk->k.ws, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts, uint64_t* d_ct,
+                                         uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(par && parts >= 1 && ((d_ct && d_out) || !count), "null input");
+    ciphertext_switch_down(*par->p, level, parts, d_ct, d_out, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_a,
+                                 const uint64_t* d_b, uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(par && ((d_a && d_b && d_out) || !count), "null input");
+    const Context& c = *par->p->ctx(level);
+    PolyRef a = plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn);
+    PolyRef b = plain_ref(const_cast<uint64_t*>(d_b), c.L(), c.logn);
+    PolyRef o = plain_ref(d_out, c.L(), c.logn);
+    poly_op(c, 0, a, b, o, count * parts, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_multiplicator_create_default(const fheg_ksk* rk, fheg_multiplicator** out) {
+  return guard([&] {
+    need(rk && out, "null input");
+    auto h = new fheg_multiplicator();
+    try {
+      h->m = make_default_multiplicator(rk->k);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API int fheg_multiplicator_create(const fheg_params* par, size_t level, const uint64_t* lhs_num,
+                                       size_t lhs_num_words, const uint64_t* lhs_den, size_t lhs_den_words,
+                                       const uint64_t* rhs_num, size_t rhs_num_words, const uint64_t* rhs_den,
+                                       size_t rhs_den_words, const uint64_t* extended_basis, size_t extended_len,
+                                       const uint64_t* post_num, size_t post_num_words, const uint64_t* post_den,
+                                       size_t post_den_words, fheg_multiplicator** out) {
+  return guard([&] {
+    need(par && extended_basis && extended_len && out, "null input");
+    BigUint ld = big(lhs_den, lhs_den_words), rd = big(rhs_den, rhs_den_words), pd = big(post_den, post_den_words);
+    need(!ld.is_zero() && !rd.is_zero() && !pd.is_zero(), "ScalingFactor denominator is zero");
+    auto h = new fheg_multiplicator();
+    try {
+      h->m = make_multiplicator(*par->p, level, big(lhs_num, lhs_num_words), ld, big(rhs_num, rhs_num_words), rd,
+                                std::vector<uint64_t>(extended_basis, extended_basis + extended_len),
+                                big(post_num, post_num_words), pd);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_multiplicator_destroy(fheg_multiplicator* m) { delete m; }
+
+FHEG_API int fheg_multiplicator_enable_relinearization(fheg_multiplicator* m, const fheg_ksk* rk) {
+  return guard([&] {
+    need(m && rk, "null input");
+    // mul.rs:133-142
+    if (!rk->k.ctx_ct->same_as(*m->m->base) || rk->k.par != m->m->par)
+      throw Error(FHEG_ERR_KEY_MISMATCH, "Invalid relinearization key context");
+    if (rk->k.ctx_ksk->L() != rk->k.ctx_ct->L())
+      throw Error(FHEG_ERR_UNSUPPORTED, "key switching keys at a lower level than the ciphertext are not supported");
+    m->m->rk = &rk->k;
+  });
+}
+
+FHEG_API int fheg_multiplicator_enable_mod_switching(fheg_multiplicator* m) {
+  return guard([&] {
+    need(m != nullptr, "null input");
+    // mul.rs:146-155
+    if (m->m->level >= m->m->par->max_level())
+      throw Error(FHEG_ERR_NO_MORE_CONTEXT, "Cannot modulo switch as this is already the last level");
+    m->m->mod_switch = true;
+  });
+}
+
+FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t* parts, size_t* level) {
+  return guard([&] {
+    need(m && parts && level, "null input");
+    *parts = m->m->out_parts();
+    *level = m->m->out_level();
+  });
+}
+
+FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
+                                         uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(m && ((d_lhs && d_rhs && d_out) || !count), "null input");
+    m->m->multiply(d_lhs, d_rhs, d_out, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs, const uint64_t* h_rhs,
+                                              uint64_t* h_out, size_t count) {
+  return guard([&] {
+    need(m && ((h_lhs && h_rhs && h_out) || !count), "null input");
+    if (!count) return;
+    Multiplicator& mm = *m->m;
+    const size_t N = mm.base->N(), L = mm.base->L();
+    const size_t in_words = count * 2 * L * N;
+    const size_t out_L = mm.mod_switch ? L - 1 : L;
+    const size_t out_words = count * mm.out_parts() * out_L * N;
+    mm.staging.reserve((2 * in_words + out_words) * 8);
+    uint64_t* d_lhs = mm.staging.u64();
+    uint64_t* d_rhs = d_lhs + in_words;
+    uint64_t* d_out = d_rhs + in_words;
+    if (!m->copy_stream) check_cuda(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking), "stream");
+    cudaStream_t st = m->copy_stream;
+    check_cuda(cudaMemcpyAsync(d_lhs, h_lhs, in_words * 8, cudaMemcpyHostToDevice, st), "H2D");
+    check_cuda(cudaMemcpyAsync(d_rhs, h_rhs, in_words * 8, cudaMemcpyHostToDevice, st), "H2D");
+    mm.multiply(d_lhs, d_rhs, d_out, count, st);
+    check_cuda(cudaMemcpyAsync(h_out, d_out, out_words * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
+}

@@ -1,0 +1,159 @@
+// Device-side modular arithmetic and shared structures for the GB300
+// RNS-BFV kernels. All arithmetic is exact u64 residue arithmetic for primes
+// below 2^62, as in fhe-math/src/zq/mod.rs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+#include "host_math.hpp"
+#include "fheg.h"
+
+namespace fheg {
+
+// Per-prime constants and twiddle tables resident on the device. One entry
+// per modulus of a context; kernels index it by limb.
+struct DevPrime {
+  uint64_t p;           // modulus, < 2^62
+  uint64_t p2;          // 2p
+  uint64_t bhi, blo;    // floor(2^128 / p), the Barrett constant of zq/mod.rs:83-98
+  uint64_t ninv;        // N^-1 mod p
+  uint64_t ninv_shoup;  // Shoup companion of ninv
+  const uint64_t* w;    // omegas (bit-reversed powers of the 2N-th root), native.rs:51-56
+  const uint64_t* ws;   // Shoup companions of w
+  const uint64_t* zi;   // zetas_inv
+  const uint64_t* zis;  // Shoup companions of zi
+};
+
+// Counts every kernel launch issued by the library (reported by benchmarks).
+extern std::atomic<uint64_t> g_launches;
+
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(10 /*FHEG_ERR_CUDA*/, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Checks the launch that was just issued and counts it.
+inline void after_launch(const char* what) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  check_cuda(cudaGetLastError(), what);
+}
+
+// Generalised polynomial batch addressing used by the kernels: polynomial
+// `poly` lives at base + (poly / grp) * grp_stride + (poly % grp) * poly_stride,
+// limb l at + (l << logn).
+struct PolyRef {
+  uint64_t* base;
+  uint64_t grp_stride;
+  uint64_t poly_stride;
+  uint32_t grp;
+  uint32_t logn;
+  __host__ __device__ __forceinline__ uint64_t* at(uint32_t poly, uint32_t limb) const {
+    return base + (uint64_t)(poly / grp) * grp_stride + (uint64_t)(poly % grp) * poly_stride +
+           ((uint64_t)limb << logn);
+  }
+};
+
+inline PolyRef plain_ref(uint64_t* base, size_t limbs, uint32_t logn) {
+  PolyRef r;
+  r.base = base;
+  r.grp = 1;
+  r.poly_stride = (uint64_t)limbs << logn;
+  r.grp_stride = r.poly_stride;
+  r.logn = logn;
+  return r;
+}
+
+// Polynomials `first .. first+take-1` of every group of `grp` polynomials
+// with `limbs` limbs each.
+inline PolyRef sub_ref(uint64_t* base, size_t limbs, uint32_t logn, uint32_t grp, uint32_t first,
+                       uint32_t take) {
+  PolyRef r;
+  r.poly_stride = (uint64_t)limbs << logn;
+  r.grp_stride = r.poly_stride * grp;
+  r.base = base + r.poly_stride * first;
+  r.grp = take;
+  r.logn = logn;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Device arithmetic
+
+// zq/mod.rs:224-234 `lazy_mul_shoup`: a * b mod p in [0, 2p) for any a < 2^64.
+__device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t a, uint64_t b, uint64_t b_shoup, uint64_t p) {
+  uint64_t q = __umul64hi(a, b_shoup);
+  return a * b - q * p;
+}
+
+__device__ __forceinline__ uint64_t reduce_once(uint64_t x, uint64_t p) { return x >= p ? x - p : x; }
+
+__device__ __forceinline__ uint64_t mul_shoup(uint64_t a, uint64_t b, uint64_t b_shoup, uint64_t p) {
+  return reduce_once(mul_shoup_lazy(a, b, b_shoup, p), p);
+}
+
+// Barrett reduction of the 128-bit value hi:lo into [0, 2p) for hi < 2^63
+// (zq/mod.rs:693-707 `lazy_reduce_u128`).
+__device__ __forceinline__ uint64_t reduce128_lazy(uint64_t hi, uint64_t lo, const DevPrime& pr) {
+  uint64_t t0 = __umul64hi(lo, pr.blo);
+  // mid = lo * bhi + hi * blo + t0 (a 129-bit sum kept as hi word + carry)
+  uint64_t m1_lo = lo * pr.bhi, m1_hi = __umul64hi(lo, pr.bhi);
+  uint64_t m2_lo = hi * pr.blo, m2_hi = __umul64hi(hi, pr.blo);
+  uint64_t s = m1_lo + m2_lo;
+  uint64_t c = s < m1_lo;
+  uint64_t s2 = s + t0;
+  c += s2 < s;
+  uint64_t q = m1_hi + m2_hi + c + hi * pr.bhi;
+  return lo - q * pr.p;
+}
+
+__device__ __forceinline__ uint64_t reduce128(uint64_t hi, uint64_t lo, const DevPrime& pr) {
+  return reduce_once(reduce128_lazy(hi, lo, pr), pr.p);
+}
+
+// a * b mod p for a, b < 2^64 with a * b < 2^126 (Barrett).
+__device__ __forceinline__ uint64_t mul_mod(uint64_t a, uint64_t b, const DevPrime& pr) {
+  return reduce128(__umul64hi(a, b), a * b, pr);
+}
+
+// Lazy reduction of a single word into [0, 2p) (zq/mod.rs:712-723 `lazy_reduce`).
+__device__ __forceinline__ uint64_t reduce64_lazy(uint64_t a, const DevPrime& pr) {
+  // q = floor((a * bhi + floor(a * blo / 2^64)) / 2^64)
+  uint64_t t = __umul64hi(a, pr.blo);
+  uint64_t lo = a * pr.bhi;
+  uint64_t hi = __umul64hi(a, pr.bhi);
+  uint64_t s = lo + t;
+  hi += s < lo;
+  return a - hi * pr.p;
+}
+
+__device__ __forceinline__ uint64_t add_mod(uint64_t a, uint64_t b, uint64_t p) { return reduce_once(a + b, p); }
+__device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uint64_t p) { return reduce_once(a + p - b, p); }
+
+// Harvey forward butterfly (native.rs:256-269): x, y in [0, 4p) -> [0, 4p).
+__device__ __forceinline__ void fwd_bfly(uint64_t& x, uint64_t& y, uint64_t w, uint64_t ws, uint64_t p,
+                                         uint64_t p2) {
+  uint64_t a = x >= p2 ? x - p2 : x;
+  uint64_t t = mul_shoup_lazy(y, w, ws, p);
+  x = a + t;
+  y = a + p2 - t;
+}
+
+// Gentleman-Sande inverse butterfly (native.rs:288-300): x, y in [0, 2p).
+__device__ __forceinline__ void inv_bfly(uint64_t& x, uint64_t& y, uint64_t z, uint64_t zs, uint64_t p,
+                                         uint64_t p2) {
+  uint64_t t = x;
+  uint64_t s = x + y;
+  x = s >= p2 ? s - p2 : s;
+  y = mul_shoup_lazy(t + p2 - y, z, zs, p);
+}
+
+// native.rs:238-243 `reduce3`: [0, 4p) -> [0, p).
+__device__ __forceinline__ uint64_t reduce4(uint64_t x, uint64_t p, uint64_t p2) {
+  x = x >= p2 ? x - p2 : x;
+  return x >= p ? x - p : x;
+}
+
+}  // namespace fheg

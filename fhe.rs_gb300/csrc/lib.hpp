@@ -1,0 +1,198 @@
+// Internal object model of libfheg (the C ABI in include/fheg.h wraps these).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "host_math.hpp"
+
+namespace fheg {
+
+// Owning device buffer.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() {}
+  explicit DevBuf(size_t b) { alloc(b); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void alloc(size_t b) {
+    release();
+    if (b) check_cuda(cudaMalloc(&ptr, b), "cudaMalloc");
+    bytes = b;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  // Grows (never shrinks) to at least b bytes; contents are not preserved.
+  void reserve(size_t b) {
+    if (b > bytes) alloc(b);
+  }
+  uint64_t* u64() const { return static_cast<uint64_t*>(ptr); }
+};
+
+void upload(void* dst, const void* src, size_t bytes);
+
+// NTT tables of one prime for one degree, resident on one device. Shared by
+// every context that uses the prime (registry keyed by device, p, n, root).
+struct PrimeTables {
+  NttTablesHost host;
+  DevBuf tables;  // 4 * n words: omegas, omegas_shoup, zetas_inv, zetas_inv_shoup
+  DevPrime dev;
+};
+std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t root);
+
+// rq::Context (fhe-math/src/rq/context.rs:9-19) on the device.
+struct Context {
+  size_t degree = 0;
+  uint32_t logn = 0;
+  std::vector<uint64_t> moduli;
+  std::vector<std::shared_ptr<PrimeTables>> primes;
+  DevBuf d_primes;  // DevPrime[L]
+  // rq/context.rs:66-73: inv_last_qi_mod_qj and Shoup values for i < L-1,
+  // followed by (q_i - (floor(q_last/2) mod q_i)) for i < L-1.
+  DevBuf d_switch;
+  std::unique_ptr<RnsContextHost> rns;
+  int device = 0;
+
+  Context(const std::vector<uint64_t>& moduli, size_t degree, const uint64_t* roots);
+  size_t L() const { return moduli.size(); }
+  size_t N() const { return degree; }
+  const DevPrime* primes_dev() const { return static_cast<const DevPrime*>(d_primes.ptr); }
+  std::vector<uint64_t> roots() const;
+  bool same_as(const Context& o) const { return degree == o.degree && moduli == o.moduli; }
+  // Context with the first `count` moduli (the same roots).
+  std::shared_ptr<Context> prefix(size_t count) const;
+};
+
+// rns::RnsScaler (fhe-math/src/rns/scaler.rs:51-72) on the device.
+struct ScalerDev {
+  uint32_t from_len, to_len, is_one, shift;
+  uint64_t tg_lo, tg_hi;
+  uint32_t tg_sign, pad;
+  const uint64_t* gamma;        // [to]
+  const uint64_t* gamma_shoup;  // [to]
+  const uint64_t* omega;        // [to][from]
+  const uint64_t* omega_shoup;  // [to][from]
+  const uint64_t* to_lo;        // theta_omega lo [from]
+  const uint64_t* to_hi;        // theta_omega hi [from]
+  const uint64_t* to_sign;      // theta_omega sign [from]
+  const uint64_t* tgar_lo;      // theta_garner lo [from]
+  const uint64_t* tgar_hi;      // theta_garner hi [from]
+  const DevPrime* to_primes;    // [to]
+};
+
+struct RnsScalerD {
+  RnsScalerHost host;
+  DevBuf buf;
+  ScalerDev dev;
+  RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den);
+};
+
+// rq::Scaler (fhe-math/src/rq/scaler.rs:17-23).
+struct Scaler {
+  std::shared_ptr<Context> from, to;
+  size_t number_common_moduli = 0;
+  BigUint num, den;
+  std::unique_ptr<RnsScalerD> rns;
+  Scaler(std::shared_ptr<Context> from, std::shared_ptr<Context> to, const BigUint& num, const BigUint& den);
+  bool is_one() const { return rns->host.is_one; }
+};
+
+// ---- operations on contexts (ops.cu) ----
+void ntt_forward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, bool lazy, cudaStream_t st);
+void ntt_backward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, cudaStream_t st);
+void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint64_t polys, cudaStream_t st);
+void poly_substitute(const Context& ctx, uint64_t exponent, bool ntt, PolyRef in, PolyRef out, uint64_t polys,
+                     cudaStream_t st);
+// Power-basis switch-down: in [L] limbs -> out [L-1] limbs.
+void poly_switch_down_pb(const Context& ctx, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st);
+// NTT switch-down: `in` is overwritten (it holds the power basis afterwards).
+void poly_switch_down_ntt(const Context& ctx, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st);
+// RnsScaler::scale over all coefficients: `in` power basis [from_len] limbs,
+// `out` limbs k = 0..out_len-1 receive target modulus start + k.
+void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
+               uint64_t polys, cudaStream_t st);
+// Scaler::scale. `scratch` must hold polys * max(L_from, L_to) * N words.
+void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t polys, uint64_t* scratch,
+                  cudaStream_t st);
+
+// ---- BFV (bfv.cu) ----
+struct Params {
+  size_t degree = 0;
+  std::vector<uint64_t> moduli;
+  uint64_t plaintext = 0;
+  std::vector<std::shared_ptr<Context>> levels;  // level l: first L-l moduli
+  Params(size_t degree, const std::vector<uint64_t>& moduli, uint64_t plaintext);
+  size_t max_level() const { return moduli.size() - 1; }
+  const std::shared_ptr<Context>& ctx(size_t level) const;
+};
+
+struct Workspace {
+  DevBuf buf;
+  uint64_t* take(size_t words, size_t* offset) {
+    uint64_t* p = buf.u64() + *offset;
+    *offset += (words + 31) & ~(size_t)31;
+    return p;
+  }
+};
+
+struct Ksk {
+  const Params* par = nullptr;
+  size_t ciphertext_level = 0, ksk_level = 0;
+  std::shared_ptr<Context> ctx_ct, ctx_ksk;
+  size_t count = 0;  // digits = moduli of the ciphertext context
+  // [2 parts][count][Lk][N] values, then the same layout of Shoup companions.
+  DevBuf keys;
+  mutable Workspace ws;  // scratch of relinearize / galois_relinearize
+  uint64_t* values(int part) const { return keys.u64() + (size_t)part * count * ctx_ksk->L() * ctx_ksk->N(); }
+  uint64_t* shoup(int part) const {
+    return keys.u64() + (size_t)(2 + part) * count * ctx_ksk->L() * ctx_ksk->N();
+  }
+};
+
+
+// Key switch of digits already in the power basis: (out0, out1) =
+// (add0 + sum_i NTT(d_i) * k0_i, add1 + sum_i NTT(d_i) * k1_i) where add0/add1
+// are optional Ntt polynomials (with an optional substitution gather on add0).
+void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* add0, uint64_t add0_poly_stride,
+                uint64_t add0_exponent, const uint64_t* add1, uint64_t add1_poly_stride, uint64_t* out,
+                uint64_t out_poly_stride, uint64_t* D, cudaStream_t st);
+// Shoup companions of the Ntt values of `polys` polynomials over context c.
+void compute_shoup(const Context& c, const uint64_t* vals, uint64_t* out, uint64_t polys, cudaStream_t st);
+
+struct Multiplicator {
+  const Params* par = nullptr;
+  size_t level = 0;
+  std::shared_ptr<Context> base, mul;
+  std::unique_ptr<Scaler> ext_lhs, ext_rhs, down;
+  const Ksk* rk = nullptr;
+  bool mod_switch = false;
+  Workspace ws;
+  DevBuf staging;  // device copies for the host entry point
+  void multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count, cudaStream_t st);
+  size_t out_parts() const { return rk ? 2 : 3; }
+  size_t out_level() const { return mod_switch ? level + 1 : level; }
+};
+
+std::unique_ptr<Multiplicator> make_multiplicator(const Params& par, size_t level, const BigUint& lhs_n,
+                                                  const BigUint& lhs_d, const BigUint& rhs_n, const BigUint& rhs_d,
+                                                  const std::vector<uint64_t>& ext, const BigUint& post_n,
+                                                  const BigUint& post_d);
+std::unique_ptr<Multiplicator> make_default_multiplicator(const Ksk& rk);
+
+void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st);
+void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
+                        Workspace& ws, cudaStream_t st);
+void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
+                            uint64_t count, cudaStream_t st);
+
+}  // namespace fheg

@@ -1,0 +1,508 @@
+// Batched negacyclic NTT kernels for sm_103a.
+//
+// The transforms compute exactly what fhe-math/src/ntt/native.rs computes:
+//   forward  (77-102):  Cooley-Tukey, bit-reversed output, Shoup twiddles
+//                       omegas[m + chunk] at the stage with m chunks;
+//   backward (106-132): Gentleman-Sande with zetas_inv[N - 2m + chunk],
+//                       then multiplication by N^-1.
+// Residues stay in Harvey's lazy ranges ([0, 4p) forward, [0, 2p) inverse)
+// and are reduced at the end, so outputs are bit-identical to the reference.
+//
+// Layout: one CTA transforms one limb of one polynomial (N <= 2^14 words,
+// resident in shared memory). Each thread keeps 16 residues in registers and
+// runs up to four butterfly stages on them (a radix-16 round); rounds
+// exchange data through shared memory with an XOR swizzle that keeps 64-bit
+// accesses free of bank conflicts. For N = 2^15 and 2^16 the first (forward)
+// or last (inverse) one or two stages run in a separate pass over strided
+// groups, and the remaining stages run in this kernel over blocks of 2^14.
+//
+// The kernels are templates over a source functor (produces the input
+// residue of element i; fuses element-wise prologues such as the BFV tensor
+// product) and a destination functor (consumes the output; fuses epilogues
+// such as the key-switching inner product).
+#pragma once
+
+#include "common.cuh"
+
+namespace fheg {
+
+// Job decoding shared by all NTT kernels: blockIdx.x enumerates
+// (poly, limb, block) with block fastest.
+struct NttGeom {
+  const DevPrime* primes;  // one entry per limb
+  uint32_t limbs;          // limbs per polynomial
+  uint32_t s1;             // stages handled by the strided pass (0, 1 or 2)
+};
+
+struct NttJob {
+  uint32_t poly, limb, beta;
+};
+
+__device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
+  uint32_t job = blockIdx.x;
+  NttJob j;
+  j.beta = job & ((1u << g.s1) - 1);
+  job >>= g.s1;
+  j.limb = job % g.limbs;
+  j.poly = job / g.limbs;
+  return j;
+}
+
+// Shared-memory swizzle: XOR bits 4-5 into bits 0-1 and bits 6-7 into bits
+// 2-3 of the word index. Every access pattern of the rounds below then maps
+// the 16 threads of a half warp to 16 distinct 8-byte bank pairs.
+__device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 3) ^ (((i >> 6) & 3) << 2); }
+
+template <int LOGN>
+struct NttShape {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int E = N < 16 ? N : 16;  // residues per thread
+  static constexpr int T = N / E;            // threads per CTA
+};
+
+// One forward round: global stages S0 .. S0+K-1 of a transform of size 2^LOGN
+// held as E residues per thread (E / 2^K groups of 2^K). Group g holds
+// elements c * 2^(LOGN-S0) + b + t * 2^(LOGN-S0-K) for t < 2^K.
+template <int LOGN, int S0, int K>
+__device__ __forceinline__ void fwd_round(uint64_t* x, uint32_t tid, const DevPrime& pr, uint32_t tw_mult) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int G = E >> K;
+  constexpr int LMIN_LOG = LOGN - S0 - K;
+#pragma unroll
+  for (int q = 0; q < G; q++) {
+    const uint32_t g = tid + q * T;
+    const uint32_t c = g >> LMIN_LOG;
+    uint64_t* xx = x + q * (1 << K);
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+      const int half = 1 << (K - 1 - r);
+#pragma unroll
+      for (int k = 0; k < (1 << r); k++) {
+        const uint32_t idx = (1u << (S0 + r)) * tw_mult + (c << r) + k;
+        const uint64_t w = __ldg(pr.w + idx);
+        const uint64_t ws = __ldg(pr.ws + idx);
+#pragma unroll
+        for (int u = 0; u < half; u++) {
+          const int t = (k << (K - r)) + u;
+          fwd_bfly(xx[t], xx[t + half], w, ws, pr.p, pr.p2);
+        }
+      }
+    }
+  }
+}
+
+// Index of element (q, t) of a forward round.
+template <int LOGN, int S0, int K>
+__device__ __forceinline__ uint32_t fwd_index(uint32_t tid, int q, int t) {
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int LMIN_LOG = LOGN - S0 - K;
+  const uint32_t g = tid + q * T;
+  const uint32_t c = g >> LMIN_LOG;
+  const uint32_t b = g & ((1u << LMIN_LOG) - 1);
+  return (c << (LOGN - S0)) + b + ((uint32_t)t << LMIN_LOG);
+}
+
+template <int LOGN, int S0, int K>
+__device__ __forceinline__ void fwd_to_smem(const uint64_t* x, uint64_t* sm, uint32_t tid) {
+  constexpr int E = NttShape<LOGN>::E;
+#pragma unroll
+  for (int e = 0; e < E; e++) sm[swz(fwd_index<LOGN, S0, K>(tid, e >> K, e & ((1 << K) - 1)))] = x[e];
+}
+
+template <int LOGN, int S0, int K>
+__device__ __forceinline__ void fwd_from_smem(uint64_t* x, const uint64_t* sm, uint32_t tid) {
+  constexpr int E = NttShape<LOGN>::E;
+#pragma unroll
+  for (int e = 0; e < E; e++) x[e] = sm[swz(fwd_index<LOGN, S0, K>(tid, e >> K, e & ((1 << K) - 1)))];
+}
+
+// Applies forward rounds S0, S0+4, ... up to LOGN, exchanging through smem.
+template <int LOGN, int S0>
+__device__ __forceinline__ void fwd_rounds(uint64_t* x, uint64_t* sm, uint32_t tid, const DevPrime& pr,
+                                           uint32_t tw_mult) {
+  constexpr int K = (LOGN - S0) < 4 ? (LOGN - S0) : 4;
+  fwd_round<LOGN, S0, K>(x, tid, pr, tw_mult);
+  if constexpr (S0 + K < LOGN) {
+    constexpr int K2 = (LOGN - S0 - K) < 4 ? (LOGN - S0 - K) : 4;
+    __syncthreads();
+    fwd_to_smem<LOGN, S0, K>(x, sm, tid);
+    __syncthreads();
+    fwd_from_smem<LOGN, S0 + K, K2>(x, sm, tid);
+    fwd_rounds<LOGN, S0 + K>(x, sm, tid, pr, tw_mult);
+  } else {
+    // Leave the output in shared memory for a coalesced store.
+    __syncthreads();
+    fwd_to_smem<LOGN, S0, K>(x, sm, tid);
+    __syncthreads();
+  }
+}
+
+// Forward NTT of blocks of 2^LOGN elements. With g.s1 > 0 the block is block
+// `beta` of a transform of size 2^(LOGN + s1) whose first s1 stages already
+// ran (ntt_fwd_top). REDUCE selects reduced ([0, p)) or lazy ([0, 4p)) output.
+template <int LOGN, bool REDUCE, class Src, class Dst>
+__global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_fwd(NttGeom g, Src src, Dst dst) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int N = 1 << LOGN;
+  extern __shared__ uint64_t sm[];
+  const uint32_t tid = threadIdx.x;
+  const NttJob jb = decode_job(g);
+  const DevPrime pr = g.primes[jb.limb];
+  const uint32_t base = jb.beta << LOGN;
+  uint64_t x[E];
+  // Round 0 holds elements tid + e*T: coalesced loads.
+#pragma unroll
+  for (int e = 0; e < E; e++) x[e] = src(jb, pr, base + tid + e * T);
+  fwd_rounds<LOGN, 0>(x, sm, tid, pr, (1u << g.s1) + jb.beta);
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const uint32_t i = tid + e * T;
+    uint64_t v = sm[swz(i)];
+    if (REDUCE) v = reduce4(v, pr.p, pr.p2);
+    dst(jb, pr, base + i, v);
+  }
+  (void)N;
+}
+
+// ---------------------------------------------------------------------------
+// Inverse rounds: global GS stages with half-size l = 2^(U0+r), r < K.
+// Group g = c * 2^U0 + b holds elements c * 2^(U0+K) + b + t * 2^U0.
+template <int LOGN, int U0, int K>
+__device__ __forceinline__ uint32_t inv_index(uint32_t tid, int q, int t) {
+  constexpr int T = NttShape<LOGN>::T;
+  const uint32_t g = tid + q * T;
+  const uint32_t c = g >> U0;
+  const uint32_t b = g & ((1u << U0) - 1);
+  return (c << (U0 + K)) + b + ((uint32_t)t << U0);
+}
+
+template <int LOGN, int U0, int K>
+__device__ __forceinline__ void inv_round(uint64_t* x, uint32_t tid, const DevPrime& pr, uint32_t n_total,
+                                          uint32_t s1, uint32_t beta) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int G = E >> K;
+#pragma unroll
+  for (int q = 0; q < G; q++) {
+    const uint32_t g = tid + q * T;
+    const uint32_t c = g >> U0;
+    uint64_t* xx = x + q * (1 << K);
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+      // m_local = N_local / (2l) chunks of this block at this stage.
+      const uint32_t m_local = 1u << (LOGN - 1 - U0 - r);
+      const uint32_t idx0 = n_total - (m_local << (s1 + 1)) + beta * m_local + (c << (K - 1 - r));
+      const int span = 1 << r;
+#pragma unroll
+      for (int k = 0; k < (1 << (K - 1 - r)); k++) {
+        const uint64_t z = __ldg(pr.zi + idx0 + k);
+        const uint64_t zs = __ldg(pr.zis + idx0 + k);
+#pragma unroll
+        for (int u = 0; u < span; u++) {
+          const int t = (k << (r + 1)) + u;
+          inv_bfly(xx[t], xx[t + span], z, zs, pr.p, pr.p2);
+        }
+      }
+    }
+  }
+}
+
+template <int LOGN, int U0, int K>
+__device__ __forceinline__ void inv_to_smem(const uint64_t* x, uint64_t* sm, uint32_t tid) {
+  constexpr int E = NttShape<LOGN>::E;
+#pragma unroll
+  for (int e = 0; e < E; e++) sm[swz(inv_index<LOGN, U0, K>(tid, e >> K, e & ((1 << K) - 1)))] = x[e];
+}
+
+template <int LOGN, int U0, int K>
+__device__ __forceinline__ void inv_from_smem(uint64_t* x, const uint64_t* sm, uint32_t tid) {
+  constexpr int E = NttShape<LOGN>::E;
+#pragma unroll
+  for (int e = 0; e < E; e++) x[e] = sm[swz(inv_index<LOGN, U0, K>(tid, e >> K, e & ((1 << K) - 1)))];
+}
+
+// Size of the first inverse round: the remainder, so that later rounds are
+// radix-16 and the last round stores coalesced.
+template <int LOGN>
+struct InvFirst {
+  static constexpr int K = (LOGN % 4) ? (LOGN % 4) : (LOGN < 4 ? LOGN : 4);
+};
+
+template <int LOGN, int U0, int K>
+__device__ __forceinline__ void inv_rounds(uint64_t* x, uint64_t* sm, uint32_t tid, const DevPrime& pr,
+                                           uint32_t n_total, uint32_t s1, uint32_t beta) {
+  inv_round<LOGN, U0, K>(x, tid, pr, n_total, s1, beta);
+  if constexpr (U0 + K < LOGN) {
+    constexpr int K2 = (LOGN - U0 - K) < 4 ? (LOGN - U0 - K) : 4;
+    __syncthreads();
+    inv_to_smem<LOGN, U0, K>(x, sm, tid);
+    __syncthreads();
+    inv_from_smem<LOGN, U0 + K, K2>(x, sm, tid);
+    inv_rounds<LOGN, U0 + K, K2>(x, sm, tid, pr, n_total, s1, beta);
+  }
+}
+
+// Inverse NTT of blocks of 2^LOGN elements (all GS stages with l < 2^LOGN).
+// With g.s1 = 0 this is the whole `backward`, including the N^-1 scaling
+// (FINAL). With g.s1 > 0 the remaining stages run in ntt_inv_top.
+template <int LOGN, bool FINAL, class Src, class Dst>
+__global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_inv(NttGeom g, Src src, Dst dst) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int K0 = InvFirst<LOGN>::K;
+  extern __shared__ uint64_t sm[];
+  const uint32_t tid = threadIdx.x;
+  const NttJob jb = decode_job(g);
+  const DevPrime pr = g.primes[jb.limb];
+  const uint32_t base = jb.beta << LOGN;
+  uint64_t x[E];
+  // Coalesced loads, then regroup through shared memory for the first round.
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const uint32_t i = tid + e * T;
+    sm[swz(i)] = src(jb, pr, base + i);
+  }
+  __syncthreads();
+  inv_from_smem<LOGN, 0, K0>(x, sm, tid);
+  inv_rounds<LOGN, 0, K0>(x, sm, tid, pr, 1u << (LOGN + g.s1), g.s1, jb.beta);
+  // The last round holds elements tid + e*T (b = tid, c = 0): coalesced stores.
+  constexpr int KL = LOGN < 4 ? LOGN : 4;
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    uint64_t v = x[e];
+    if (FINAL) v = mul_shoup(v, pr.ninv, pr.ninv_shoup, pr.p);
+    const uint32_t i = (LOGN >= 4) ? (tid + e * T) : inv_index<LOGN, 0, KL>(tid, 0, e);
+    dst(jb, pr, base + i, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Strided passes for N = 2^(LOGB + S1) with S1 in {1, 2}: the first S1
+// forward stages / the last S1 inverse stages, on groups of 2^S1 elements
+// b + t * 2^LOGB. One thread per group.
+
+template <int S1, class Src, class Dst>
+__global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
+                                                     uint64_t total, Src src, Dst dst) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t b = gid % groups_per_limb;
+  const uint64_t job = gid / groups_per_limb;
+  NttJob jb;
+  jb.limb = job % g.limbs;
+  jb.poly = job / g.limbs;
+  jb.beta = 0;
+  const DevPrime pr = g.primes[jb.limb];
+  uint64_t x[1 << S1];
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+#pragma unroll
+  for (int s = 0; s < S1; s++) {
+    const int half = 1 << (S1 - 1 - s);
+#pragma unroll
+    for (int k = 0; k < (1 << s); k++) {
+      const uint32_t idx = (1u << s) + k;
+      const uint64_t w = __ldg(pr.w + idx), ws = __ldg(pr.ws + idx);
+#pragma unroll
+      for (int u = 0; u < half; u++) {
+        const int t = (k << (S1 - s)) + u;
+        fwd_bfly(x[t], x[t + half], w, ws, pr.p, pr.p2);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) dst(jb, pr, b + ((uint32_t)t << logb), x[t]);
+}
+
+template <int S1, class Src, class Dst>
+__global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
+                                                     uint64_t total, Src src, Dst dst) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t b = gid % groups_per_limb;
+  const uint64_t job = gid / groups_per_limb;
+  NttJob jb;
+  jb.limb = job % g.limbs;
+  jb.poly = job / g.limbs;
+  jb.beta = 0;
+  const DevPrime pr = g.primes[jb.limb];
+  const uint32_t n_total = 1u << (logb + S1);
+  uint64_t x[1 << S1];
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+#pragma unroll
+  for (int r = 0; r < S1; r++) {
+    const int span = 1 << r;
+    const uint32_t m = 1u << (S1 - 1 - r);  // chunks at this stage
+#pragma unroll
+    for (int k = 0; k < (1 << (S1 - 1 - r)); k++) {
+      const uint32_t idx = n_total - 2 * m + k;
+      const uint64_t z = __ldg(pr.zi + idx), zs = __ldg(pr.zis + idx);
+#pragma unroll
+      for (int u = 0; u < span; u++) {
+        const int t = (k << (r + 1)) + u;
+        inv_bfly(x[t], x[t + span], z, zs, pr.p, pr.p2);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++)
+    dst(jb, pr, b + ((uint32_t)t << logb), mul_shoup(x[t], pr.ninv, pr.ninv_shoup, pr.p));
+}
+
+// ---------------------------------------------------------------------------
+// Basic source / destination functors.
+
+struct SrcPoly {
+  PolyRef r;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    return r.at(j.poly, j.limb)[i];
+  }
+};
+
+struct DstPoly {
+  PolyRef r;
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    r.at(j.poly, j.limb)[i] = v;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Launch helpers.
+
+template <int LOGN>
+inline size_t ntt_smem_bytes() {
+  return sizeof(uint64_t) << LOGN;
+}
+
+// Opts a kernel into more than 48 KB of dynamic shared memory (once per
+// kernel; `done` is a per-instantiation flag).
+template <class K>
+inline void set_smem(K kernel, size_t bytes, bool* done) {
+  if (bytes > 48 * 1024 && !*done) {
+    check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+               "cudaFuncSetAttribute");
+    *done = true;
+  }
+}
+
+template <int LOGN, bool REDUCE, class Src, class Dst>
+void launch_fwd_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  auto kern = k_ntt_fwd<LOGN, REDUCE, Src, Dst>;
+  const size_t smem = ntt_smem_bytes<LOGN>();
+  static bool done = false;
+  set_smem(kern, smem, &done);
+  const uint64_t blocks = polys * g.limbs << g.s1;
+  kern<<<(unsigned)blocks, NttShape<LOGN>::T, smem, st>>>(g, src, dst);
+  after_launch("k_ntt_fwd");
+}
+
+template <int LOGN, bool FINAL, class Src, class Dst>
+void launch_inv_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  auto kern = k_ntt_inv<LOGN, FINAL, Src, Dst>;
+  const size_t smem = ntt_smem_bytes<LOGN>();
+  static bool done = false;
+  set_smem(kern, smem, &done);
+  const uint64_t blocks = polys * g.limbs << g.s1;
+  kern<<<(unsigned)blocks, NttShape<LOGN>::T, smem, st>>>(g, src, dst);
+  after_launch("k_ntt_inv");
+}
+
+// Dispatch over log2(N) for a single-pass transform (3 <= logn <= 14).
+template <bool REDUCE, class Src, class Dst>
+void ntt_fwd_single(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  switch (logn) {
+    case 3: launch_fwd_block<3, REDUCE>(g, polys, src, dst, st); break;
+    case 4: launch_fwd_block<4, REDUCE>(g, polys, src, dst, st); break;
+    case 5: launch_fwd_block<5, REDUCE>(g, polys, src, dst, st); break;
+    case 6: launch_fwd_block<6, REDUCE>(g, polys, src, dst, st); break;
+    case 7: launch_fwd_block<7, REDUCE>(g, polys, src, dst, st); break;
+    case 8: launch_fwd_block<8, REDUCE>(g, polys, src, dst, st); break;
+    case 9: launch_fwd_block<9, REDUCE>(g, polys, src, dst, st); break;
+    case 10: launch_fwd_block<10, REDUCE>(g, polys, src, dst, st); break;
+    case 11: launch_fwd_block<11, REDUCE>(g, polys, src, dst, st); break;
+    case 12: launch_fwd_block<12, REDUCE>(g, polys, src, dst, st); break;
+    case 13: launch_fwd_block<13, REDUCE>(g, polys, src, dst, st); break;
+    case 14: launch_fwd_block<14, REDUCE>(g, polys, src, dst, st); break;
+    default: throw Error(12, "unsupported NTT size");
+  }
+}
+
+template <bool FINAL, class Src, class Dst>
+void ntt_inv_single(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  switch (logn) {
+    case 3: launch_inv_block<3, FINAL>(g, polys, src, dst, st); break;
+    case 4: launch_inv_block<4, FINAL>(g, polys, src, dst, st); break;
+    case 5: launch_inv_block<5, FINAL>(g, polys, src, dst, st); break;
+    case 6: launch_inv_block<6, FINAL>(g, polys, src, dst, st); break;
+    case 7: launch_inv_block<7, FINAL>(g, polys, src, dst, st); break;
+    case 8: launch_inv_block<8, FINAL>(g, polys, src, dst, st); break;
+    case 9: launch_inv_block<9, FINAL>(g, polys, src, dst, st); break;
+    case 10: launch_inv_block<10, FINAL>(g, polys, src, dst, st); break;
+    case 11: launch_inv_block<11, FINAL>(g, polys, src, dst, st); break;
+    case 12: launch_inv_block<12, FINAL>(g, polys, src, dst, st); break;
+    case 13: launch_inv_block<13, FINAL>(g, polys, src, dst, st); break;
+    case 14: launch_inv_block<14, FINAL>(g, polys, src, dst, st); break;
+    default: throw Error(12, "unsupported NTT size");
+  }
+}
+
+constexpr uint32_t kMaxSmemLogN = 14;
+
+// Full forward NTT, any 3 <= logn <= 16. For logn > 14 the source is read by
+// the strided pass and the result goes through `dst` twice: the strided pass
+// writes its lazy output to dst, and the block pass reads it back from dst
+// (so dst must be a plain polynomial batch: a DstPoly).
+template <bool REDUCE, class Src>
+void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly dst, cudaStream_t st) {
+  if (logn <= kMaxSmemLogN) {
+    g.s1 = 0;
+    ntt_fwd_single<REDUCE>(logn, g, polys, src, dst, st);
+    return;
+  }
+  const uint32_t s1 = logn - kMaxSmemLogN;
+  const uint32_t groups = 1u << kMaxSmemLogN;
+  const uint64_t threads = polys * g.limbs * groups;
+  g.s1 = 0;
+  if (s1 == 1) {
+    k_ntt_fwd_top<1><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, src, dst);
+  } else if (s1 == 2) {
+    k_ntt_fwd_top<2><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, src, dst);
+  } else {
+    throw Error(12, "unsupported NTT size");
+  }
+  after_launch("k_ntt_fwd_top");
+  g.s1 = s1;
+  SrcPoly mid{dst.r};
+  launch_fwd_block<kMaxSmemLogN, REDUCE>(g, polys, mid, dst, st);
+}
+
+// Full inverse NTT, any 3 <= logn <= 16. For logn > 14 the block pass writes
+// to `dst` and the strided pass finishes in place (dst must be a DstPoly).
+template <class Src>
+void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly dst, cudaStream_t st) {
+  if (logn <= kMaxSmemLogN) {
+    g.s1 = 0;
+    ntt_inv_single<true>(logn, g, polys, src, dst, st);
+    return;
+  }
+  const uint32_t s1 = logn - kMaxSmemLogN;
+  g.s1 = s1;
+  launch_inv_block<kMaxSmemLogN, false>(g, polys, src, dst, st);
+  const uint32_t groups = 1u << kMaxSmemLogN;
+  const uint64_t threads = polys * g.limbs * groups;
+  g.s1 = 0;
+  SrcPoly mid{dst.r};
+  if (s1 == 1) {
+    k_ntt_inv_top<1><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, mid, dst);
+  } else if (s1 == 2) {
+    k_ntt_inv_top<2><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, mid, dst);
+  } else {
+    throw Error(12, "unsupported NTT size");
+  }
+  after_launch("k_ntt_inv_top");
+}
+
+}  // namespace fheg

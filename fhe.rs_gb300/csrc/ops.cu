@@ -1,0 +1,521 @@
+// Ring-level operations: contexts, NTTs, element-wise ops, substitution,
+// modulus switch-down and RNS scaling (fhe-math `rq`, `ntt`, `rns`).
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "lib.hpp"
+#include "ntt.cuh"
+
+namespace fheg {
+
+std::atomic<uint64_t> g_launches{0};
+
+void upload(void* dst, const void* src, size_t bytes) {
+  check_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+}
+
+// ---------------------------------------------------------------------------
+// Prime table registry.
+
+std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t root) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint64_t, size_t, uint64_t>, std::weak_ptr<PrimeTables>> registry;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (root == 0) root = default_ntt_root(p, n);
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_tuple(dev, p, n, root);
+  auto it = registry.find(key);
+  if (it != registry.end()) {
+    if (auto sp = it->second.lock()) return sp;
+  }
+  auto t = std::make_shared<PrimeTables>();
+  t->host = make_ntt_tables(p, n, root);
+  t->tables.alloc(4 * n * sizeof(uint64_t));
+  uint64_t* d = t->tables.u64();
+  upload(d, t->host.omegas.data(), n * 8);
+  upload(d + n, t->host.omegas_shoup.data(), n * 8);
+  upload(d + 2 * n, t->host.zetas_inv.data(), n * 8);
+  upload(d + 3 * n, t->host.zetas_inv_shoup.data(), n * 8);
+  DevPrime& dp = t->dev;
+  dp.p = p;
+  dp.p2 = 2 * p;
+  barrett128(p, &dp.bhi, &dp.blo);
+  dp.ninv = t->host.size_inv;
+  dp.ninv_shoup = t->host.size_inv_shoup;
+  dp.w = d;
+  dp.ws = d + n;
+  dp.zi = d + 2 * n;
+  dp.zis = d + 3 * n;
+  registry[key] = t;
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Context
+
+Context::Context(const std::vector<uint64_t>& m, size_t n, const uint64_t* roots) : degree(n), moduli(m) {
+  if (n < 8 || (n & (n - 1))) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The degree is not a power of two larger or equal to 8");
+  if (n > (1u << 16)) throw Error(FHEG_ERR_UNSUPPORTED, "degrees above 2^16 are not supported");
+  if (m.empty()) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The list of moduli is empty");
+  logn = 0;
+  while (((size_t)1 << logn) < n) logn++;
+  check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+  rns.reset(new RnsContextHost(m));
+  std::vector<DevPrime> host(m.size());
+  for (size_t i = 0; i < m.size(); i++) {
+    if (m[i] < 2 || (m[i] >> 62) != 0) throw Error(FHEG_ERR_INVALID_MODULUS, "InvalidModulus");
+    primes.push_back(get_prime_tables(m[i], n, roots ? roots[i] : 0));
+    host[i] = primes.back()->dev;
+  }
+  d_primes.alloc(sizeof(DevPrime) * m.size());
+  upload(d_primes.ptr, host.data(), sizeof(DevPrime) * m.size());
+  // rq/context.rs:66-73 plus the constant of rq/mod.rs:427.
+  size_t L = m.size();
+  std::vector<uint64_t> sw(3 * (L > 1 ? L - 1 : 1), 0);
+  if (L > 1) {
+    uint64_t q_last = m[L - 1];
+    for (size_t i = 0; i + 1 < L; i++) {
+      uint64_t inv = invmod(q_last % m[i], m[i]);
+      sw[i] = inv;
+      sw[(L - 1) + i] = shoup(inv, m[i]);
+      sw[2 * (L - 1) + i] = m[i] - (q_last / 2) % m[i];
+    }
+  }
+  d_switch.alloc(sw.size() * 8);
+  upload(d_switch.ptr, sw.data(), sw.size() * 8);
+}
+
+std::vector<uint64_t> Context::roots() const {
+  std::vector<uint64_t> r;
+  for (auto& p : primes) r.push_back(p->host.root);
+  return r;
+}
+
+std::shared_ptr<Context> Context::prefix(size_t count) const {
+  std::vector<uint64_t> m(moduli.begin(), moduli.begin() + count);
+  std::vector<uint64_t> r = roots();
+  return std::make_shared<Context>(m, degree, r.data());
+}
+
+// ---------------------------------------------------------------------------
+// NTT on whole contexts.
+
+void ntt_forward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, bool lazy, cudaStream_t st) {
+  if (polys == 0) return;
+  NttGeom g{ctx.primes_dev(), (uint32_t)ctx.L(), 0};
+  if (lazy) ntt_forward_any<false>(ctx.logn, g, polys, SrcPoly{src}, DstPoly{dst}, st);
+  else ntt_forward_any<true>(ctx.logn, g, polys, SrcPoly{src}, DstPoly{dst}, st);
+}
+
+void ntt_backward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, cudaStream_t st) {
+  if (polys == 0) return;
+  NttGeom g{ctx.primes_dev(), (uint32_t)ctx.L(), 0};
+  ntt_inverse_any(ctx.logn, g, polys, SrcPoly{src}, DstPoly{dst}, st);
+}
+
+// ---------------------------------------------------------------------------
+// Element-wise kernels. One thread per (poly, limb, coefficient).
+
+__global__ void k_poly_op(const DevPrime* primes, uint32_t limbs, uint32_t logn, int op, PolyRef a, PolyRef b,
+                          PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  const uint32_t limb = job % limbs;
+  const uint32_t poly = job / limbs;
+  const DevPrime pr = primes[limb];
+  const uint64_t x = a.at(poly, limb)[i];
+  uint64_t r;
+  if (op == 3) {
+    r = x ? pr.p - x : 0;  // zq/mod.rs:175-178 `neg`
+  } else {
+    const uint64_t y = b.at(poly, limb)[i];
+    if (op == 0) r = add_mod(x, y, pr.p);
+    else if (op == 1) r = sub_mod(x, y, pr.p);
+    else r = mul_mod(x, y, pr);
+  }
+  out.at(poly, limb)[i] = r;
+}
+
+static unsigned blocks_for(uint64_t total, unsigned threads) { return (unsigned)((total + threads - 1) / threads); }
+
+void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint64_t polys, cudaStream_t st) {
+  uint64_t total = polys * ctx.L() << ctx.logn;
+  if (total == 0) return;
+  k_poly_op<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), (uint32_t)ctx.L(), ctx.logn, op, a, b, out,
+                                                    total);
+  after_launch("k_poly_op");
+}
+
+// Poly::substitute (rq/mod.rs:319-369).
+//  Ntt:        q[bitrev[j]] = p[power_bitrev[j]], power_bitrev[j] =
+//              bitrev(((e-1)/2 + j*e) mod N): output i reads input g(i)
+//              with g(i) = bitrev(((e-1)/2 + bitrev(i)*e) mod N).
+//  PowerBasis: coefficient j moves to (j*e) mod N, negated when
+//              (j*e) mod 2N >= N.
+__device__ __forceinline__ uint32_t brev(uint32_t x, uint32_t logn) { return __brev(x) >> (32 - logn); }
+
+__device__ __forceinline__ uint32_t subst_gather(uint32_t i, uint64_t e, uint32_t logn) {
+  const uint64_t mask = (1ull << logn) - 1;
+  const uint64_t power = (((e - 1) >> 1) + (uint64_t)brev(i, logn) * e) & mask;
+  return brev((uint32_t)power, logn);
+}
+
+__global__ void k_substitute(const DevPrime* primes, uint32_t limbs, uint32_t logn, uint64_t e, int ntt, PolyRef in,
+                             PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  const uint32_t limb = job % limbs;
+  const uint32_t poly = job / limbs;
+  if (ntt) {
+    out.at(poly, limb)[i] = in.at(poly, limb)[subst_gather(i, e, logn)];
+  } else {
+    const uint64_t n = 1ull << logn;
+    const uint64_t pw = ((uint64_t)i * e) & (2 * n - 1);
+    const uint64_t v = in.at(poly, limb)[i];
+    const uint64_t p = primes[limb].p;
+    out.at(poly, limb)[pw & (n - 1)] = (pw & n) ? (v ? p - v : 0) : v;
+  }
+}
+
+void poly_substitute(const Context& ctx, uint64_t exponent, bool ntt, PolyRef in, PolyRef out, uint64_t polys,
+                     cudaStream_t st) {
+  uint64_t e = exponent % (2 * ctx.N());
+  if ((e & 1) == 0) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
+  uint64_t total = polys * ctx.L() << ctx.logn;
+  if (total == 0) return;
+  k_substitute<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), (uint32_t)ctx.L(), ctx.logn, e, ntt ? 1 : 0,
+                                                       in, out, total);
+  after_launch("k_substitute");
+}
+
+// ---------------------------------------------------------------------------
+// Modulus switch-down (rq/mod.rs:390-448) of coefficient i of limb `limb`,
+// given the power-basis residues x_i (mod q_i) and x_L (mod q_last).
+struct SwitchConsts {
+  const uint64_t* sw;  // inv[L-1], inv_shoup[L-1], (q_i - (q_last/2 mod q_i))[L-1]
+  uint64_t q_last;
+  uint32_t lm1;  // L - 1
+};
+
+__device__ __forceinline__ uint64_t switch_down_value(const SwitchConsts& c, uint32_t limb, const DevPrime& pr,
+                                                      uint64_t xi, uint64_t xl) {
+  const uint64_t last = reduce_once(xl + (c.q_last >> 1), c.q_last);  // rq/mod.rs:417-419
+  const uint64_t tmp = reduce64_lazy(last, pr) + __ldg(c.sw + 2 * c.lm1 + limb);  // rq/mod.rs:430
+  const uint64_t coeff = xi + 3 * pr.p - tmp;                                     // rq/mod.rs:434
+  return mul_shoup(coeff, __ldg(c.sw + limb), __ldg(c.sw + c.lm1 + limb), pr.p);  // rq/mod.rs:437
+}
+
+__global__ void k_switch_down_pb(const DevPrime* primes, SwitchConsts c, uint32_t logn, PolyRef in, PolyRef out,
+                                 uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  const uint32_t limb = job % c.lm1;
+  const uint32_t poly = job / c.lm1;
+  const DevPrime pr = primes[limb];
+  out.at(poly, limb)[i] = switch_down_value(c, limb, pr, in.at(poly, limb)[i], in.at(poly, c.lm1)[i]);
+}
+
+static SwitchConsts switch_consts(const Context& ctx) {
+  if (ctx.L() < 2) throw Error(FHEG_ERR_NO_MORE_CONTEXT, "NoMoreContext");
+  SwitchConsts c;
+  c.sw = ctx.d_switch.u64();
+  c.q_last = ctx.moduli.back();
+  c.lm1 = (uint32_t)(ctx.L() - 1);
+  return c;
+}
+
+void poly_switch_down_pb(const Context& ctx, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st) {
+  SwitchConsts c = switch_consts(ctx);
+  uint64_t total = polys * c.lm1 << ctx.logn;
+  if (total == 0) return;
+  k_switch_down_pb<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), c, ctx.logn, in, out, total);
+  after_launch("k_switch_down_pb");
+}
+
+// Forward-NTT source that performs the switch-down on the fly from a
+// power-basis batch: fuses rq/mod.rs:390-448 into the next `into_ntt`.
+struct SrcSwitchDown {
+  PolyRef pb;
+  SwitchConsts c;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
+    return switch_down_value(c, j.limb, pr, pb.at(j.poly, j.limb)[i], pb.at(j.poly, c.lm1)[i]);
+  }
+};
+
+void poly_switch_down_ntt(const Context& ctx, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st) {
+  SwitchConsts c = switch_consts(ctx);
+  if (polys == 0) return;
+  ntt_backward(ctx, in, in, polys, st);
+  NttGeom g{ctx.primes_dev(), c.lm1, 0};
+  ntt_forward_any<true>(ctx.logn, g, polys, SrcSwitchDown{in, c}, DstPoly{out}, st);
+}
+
+// ---------------------------------------------------------------------------
+// RNS scaling (rns/scaler.rs:249-352), one thread per coefficient.
+
+struct U192 {
+  uint64_t w0, w1, w2;
+};
+
+__device__ __forceinline__ void mac_192(U192& acc, uint64_t r, uint64_t lo, uint64_t hi) {
+  // acc += r * (hi:lo), r < 2^64, product < 2^192.
+  const uint64_t p0l = r * lo, p0h = __umul64hi(r, lo);
+  const uint64_t p1l = r * hi, p1h = __umul64hi(r, hi);
+  unsigned __int128 s = (unsigned __int128)acc.w0 + p0l;
+  acc.w0 = (uint64_t)s;
+  s = (s >> 64) + acc.w1 + p0h + (unsigned __int128)p1l;
+  acc.w1 = (uint64_t)s;
+  acc.w2 = acc.w2 + p1h + (uint64_t)(s >> 64);
+}
+
+struct U256d {
+  uint64_t w[4];
+};
+
+__device__ __forceinline__ void add256(U256d& a, const U256d& b) {
+  unsigned __int128 c = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    c += (unsigned __int128)a.w[i] + b.w[i];
+    a.w[i] = (uint64_t)c;
+    c >>= 64;
+  }
+}
+
+__device__ __forceinline__ void sub256(U256d& a, const U256d& b) {
+  uint64_t borrow = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint64_t ai = a.w[i], bi = b.w[i];
+    const uint64_t d = ai - bi - borrow;
+    borrow = (ai < bi) || (ai == bi && borrow) ? 1 : 0;
+    a.w[i] = d;
+  }
+}
+
+// r (< 2^128) times (hi:lo) as a full 256-bit product.
+__device__ __forceinline__ U256d mul_128x128(uint64_t a0, uint64_t a1, uint64_t b0, uint64_t b1) {
+  U256d r;
+  unsigned __int128 p00 = (unsigned __int128)a0 * b0, p01 = (unsigned __int128)a0 * b1;
+  unsigned __int128 p10 = (unsigned __int128)a1 * b0, p11 = (unsigned __int128)a1 * b1;
+  r.w[0] = (uint64_t)p00;
+  unsigned __int128 mid = (p00 >> 64) + (uint64_t)p01 + (uint64_t)p10;
+  r.w[1] = (uint64_t)mid;
+  unsigned __int128 hi = (mid >> 64) + (p01 >> 64) + (p10 >> 64) + (uint64_t)p11;
+  r.w[2] = (uint64_t)hi;
+  r.w[3] = (uint64_t)(hi >> 64) + (uint64_t)(p11 >> 64);
+  return r;
+}
+
+// Low 128 bits of (w >> s) for a 4-word value, 0 <= s < 256.
+__device__ __forceinline__ void shr_low128(const uint64_t* w, int nw, uint32_t s, uint64_t* lo, uint64_t* hi) {
+  uint64_t out[2] = {0, 0};
+  const uint32_t ws = s >> 6, bs = s & 63;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const uint32_t idx = ws + k;
+    uint64_t v = idx < (uint32_t)nw ? w[idx] : 0;
+    uint64_t nx = (idx + 1) < (uint32_t)nw ? w[idx + 1] : 0;
+    out[k] = bs ? ((v >> bs) | (nx << (64 - bs))) : v;
+  }
+  *lo = out[0];
+  *hi = out[1];
+}
+
+template <int MAXF>
+__global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, PolyRef in, PolyRef out,
+                                                   uint32_t start, uint32_t out_len, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint32_t poly = (uint32_t)(gid >> logn);
+  const uint32_t F = s.from_len;
+  uint64_t r[MAXF];
+#pragma unroll
+  for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? in.at(poly, k)[i] : 0;
+
+  // scaler.rs:260-272: v = ceil((sum r_k theta_garner_k) >> (shift - 1) / 2).
+  U192 g = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < MAXF; k++)
+    if (k < (int)F) mac_192(g, r[k], __ldg(s.tgar_lo + k), __ldg(s.tgar_hi + k));
+  uint64_t gw[3] = {g.w0, g.w1, g.w2};
+  uint64_t vlo, vhi;
+  shr_low128(gw, 3, s.shift - 1, &vlo, &vhi);
+  {  // div_ceil(2)
+    const uint64_t odd = vlo & 1;
+    vlo = (vlo >> 1) | (vhi << 63);
+    vhi >>= 1;
+    vlo += odd;
+    vhi += (vlo < odd);
+  }
+
+  // scaler.rs:276-314.
+  bool w_sign = false;
+  uint64_t wlo = 0, whi = 0;
+  if (!s.is_one) {
+    U256d acc = {{0, 0, 0, 0}};
+#pragma unroll
+    for (int k = 0; k < MAXF; k++) {
+      if (k < (int)F) {
+        U256d prod = mul_128x128(r[k], 0, __ldg(s.to_lo + k), __ldg(s.to_hi + k));
+        if (__ldg(s.to_sign + k)) sub256(acc, prod);
+        else add256(acc, prod);
+      }
+    }
+    U256d vt = mul_128x128(vlo, vhi, s.tg_lo, s.tg_hi);
+    if (s.tg_sign) add256(acc, vt);
+    else sub256(acc, vt);
+    w_sign = (acc.w[3] >> 63) != 0;
+    if (w_sign) {
+      uint64_t nw[4] = {~acc.w[0], ~acc.w[1], ~acc.w[2], ~acc.w[3]};
+      shr_low128(nw, 4, 126, &wlo, &whi);
+      wlo += 1;
+      whi += (wlo == 0);
+      wlo = (wlo >> 1) | (whi << 63);
+      whi >>= 1;
+    } else {
+      shr_low128(acc.w, 4, 126, &wlo, &whi);
+      const uint64_t odd = wlo & 1;
+      wlo = (wlo >> 1) | (whi << 63);
+      whi >>= 1;
+      wlo += odd;
+      whi += (wlo < odd);
+    }
+  }
+
+  // scaler.rs:316-351.
+  for (uint32_t o = 0; o < out_len; o++) {
+    const uint32_t j = start + o;
+    const DevPrime pr = s.to_primes[j];
+    const uint64_t vj = reduce128(vhi, vlo, pr);
+    unsigned __int128 y =
+        (unsigned __int128)(pr.p2 - mul_shoup_lazy(vj, __ldg(s.gamma + j), __ldg(s.gamma_shoup + j), pr.p));
+    if (!s.is_one) {
+      const uint64_t wj = reduce128_lazy(whi, wlo, pr);
+      y += w_sign ? pr.p2 - wj : wj;
+    }
+    const uint64_t* om = s.omega + (uint64_t)j * F;
+    const uint64_t* oms = s.omega_shoup + (uint64_t)j * F;
+#pragma unroll
+    for (int k = 0; k < MAXF; k++)
+      if (k < (int)F) y += mul_shoup_lazy(r[k], __ldg(om + k), __ldg(oms + k), pr.p);
+    out.at(poly, o)[i] = reduce128((uint64_t)(y >> 64), (uint64_t)y, pr);
+  }
+}
+
+void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
+               uint64_t polys, cudaStream_t st) {
+  const uint64_t total = polys << logn;
+  if (total == 0 || out_len == 0) return;
+  const uint32_t F = s.dev.from_len;
+  const unsigned threads = 128;
+  if (F <= 8) k_rns_scale<8><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
+  else if (F <= 16) k_rns_scale<16><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
+  else if (F <= 32) k_rns_scale<32><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
+  else throw Error(FHEG_ERR_UNSUPPORTED, "RNS scaling from more than 32 moduli is not supported");
+  after_launch("k_rns_scale");
+}
+
+RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den)
+    : host(make_rns_scaler(*from.rns, *to.rns, num, den)) {
+  const size_t F = host.from_len, T = host.to_len;
+  std::vector<uint64_t> flat;
+  auto put = [&](const std::vector<uint64_t>& v) {
+    size_t off = flat.size();
+    flat.insert(flat.end(), v.begin(), v.end());
+    return off;
+  };
+  size_t o_gamma = put(host.gamma), o_gs = put(host.gamma_shoup), o_om = put(host.omega),
+         o_oms = put(host.omega_shoup), o_tol = put(host.theta_omega_lo), o_toh = put(host.theta_omega_hi);
+  std::vector<uint64_t> sign(host.theta_omega_sign.begin(), host.theta_omega_sign.end());
+  size_t o_tos = put(sign), o_tgl = put(host.theta_garner_lo), o_tgh = put(host.theta_garner_hi);
+  buf.alloc(std::max<size_t>(flat.size(), 1) * 8);
+  upload(buf.ptr, flat.data(), flat.size() * 8);
+  uint64_t* b = buf.u64();
+  dev.from_len = (uint32_t)F;
+  dev.to_len = (uint32_t)T;
+  dev.is_one = host.is_one ? 1 : 0;
+  dev.shift = (uint32_t)host.theta_garner_shift;
+  dev.tg_lo = host.theta_gamma_lo;
+  dev.tg_hi = host.theta_gamma_hi;
+  dev.tg_sign = host.theta_gamma_sign ? 1 : 0;
+  dev.pad = 0;
+  dev.gamma = b + o_gamma;
+  dev.gamma_shoup = b + o_gs;
+  dev.omega = b + o_om;
+  dev.omega_shoup = b + o_oms;
+  dev.to_lo = b + o_tol;
+  dev.to_hi = b + o_toh;
+  dev.to_sign = b + o_tos;
+  dev.tgar_lo = b + o_tgl;
+  dev.tgar_hi = b + o_tgh;
+  dev.to_primes = to.primes_dev();
+}
+
+Scaler::Scaler(std::shared_ptr<Context> f, std::shared_ptr<Context> t, const BigUint& n, const BigUint& d)
+    : from(std::move(f)), to(std::move(t)), num(n), den(d) {
+  if (from->degree != to->degree) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incompatible degrees");
+  rns.reset(new RnsScalerD(*from, *to, num, den));
+  number_common_moduli = 0;
+  if (rns->host.is_one) {  // rq/scaler.rs:32-40
+    while (number_common_moduli < from->L() && number_common_moduli < to->L() &&
+           from->moduli[number_common_moduli] == to->moduli[number_common_moduli])
+      number_common_moduli++;
+  }
+}
+
+__global__ void k_copy_limbs(PolyRef in, PolyRef out, uint32_t limbs, uint32_t logn, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  const uint32_t limb = job % limbs;
+  const uint32_t poly = job / limbs;
+  out.at(poly, limb)[i] = in.at(poly, limb)[i];
+}
+
+void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t polys, uint64_t* scratch,
+                  cudaStream_t st) {
+  if (polys == 0) return;
+  const uint32_t logn = s.from->logn;
+  const size_t ncm = s.number_common_moduli;
+  const size_t Lt = s.to->L();
+  if (ncm > 0) {  // rq/scaler.rs:60-64
+    uint64_t total = polys * ncm << logn;
+    k_copy_limbs<<<blocks_for(total, 256), 256, 0, st>>>(in, out, (uint32_t)ncm, logn, total);
+    after_launch("k_copy_limbs");
+  }
+  if (ncm >= Lt) return;
+  PolyRef src = in;
+  if (ntt) {  // rq/scaler.rs:67-81: backward NTT of a copy
+    PolyRef tmp = plain_ref(scratch, s.from->L(), logn);
+    ntt_backward(*s.from, in, tmp, polys, st);
+    src = tmp;
+  }
+  // Output limbs ncm.. of `out`.
+  PolyRef dst = out;
+  dst.base = out.base + ((uint64_t)ncm << logn);
+  rns_scale(*s.rns, logn, src, dst, (uint32_t)ncm, (uint32_t)(Lt - ncm), polys, st);
+  if (ntt) {  // rq/scaler.rs:96-114: forward NTT of the new limbs.
+    // The target context restricted to limbs ncm.. : same tables, offset primes.
+    NttGeom g{s.to->primes_dev() + ncm, (uint32_t)(Lt - ncm), 0};
+    if (s.to->logn <= kMaxSmemLogN) {
+      ntt_fwd_single<true>(logn, g, polys, SrcPoly{dst}, DstPoly{dst}, st);
+    } else {
+      ntt_forward_any<true>(logn, g, polys, SrcPoly{dst}, DstPoly{dst}, st);
+    }
+  }
+}
+
+}  // namespace fheg

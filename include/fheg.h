@@ -1,0 +1,233 @@
+/*
+ * fheg.h — C ABI of the GB300 RNS-BFV hot-path library (libfheg.so).
+ *
+ * This is the drop-in boundary for the ciphertext hot path of fhe.rs
+ * (crates fhe-math and fhe). A Rust `-sys` crate binds these symbols and the
+ * reference types forward to them; every entry point names the reference
+ * interface it replaces (paths relative to the fhe.rs repository root).
+ *
+ * Conventions
+ *  - All functions return an `int` status (FHEG_OK = 0). On failure a
+ *    thread-local message is available from fheg_last_error().
+ *  - Polynomials are limb-major arrays of u64 residues: a polynomial over a
+ *    context with L moduli and degree N is `uint64_t[L][N]`, exactly the
+ *    layout of `Poly::coefficients` (fhe-math/src/rq/mod.rs:124-132). A batch
+ *    of `count` polynomials is `uint64_t[count][L][N]`; a batch of
+ *    ciphertexts with `parts` polynomials each is `uint64_t[count][parts][L][N]`.
+ *  - `d_` pointers are device pointers (any CUDA allocation on the current
+ *    device); `h_` pointers are host pointers. `stream` is a `cudaStream_t`
+ *    (NULL = the legacy default stream).
+ *  - Representations follow `rq::Representation`
+ *    (fhe-math/src/rq/mod.rs:37-47): 0 = PowerBasis, 1 = Ntt.
+ *  - Handles are opaque and thread-compatible: a handle may be used from
+ *    several threads as long as calls on the same multiplicator or server are
+ *    not concurrent.
+ *  - Big integers (scaling factors) are little-endian arrays of u64 words.
+ */
+#ifndef FHEG_H
+#define FHEG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define FHEG_EXTERN extern "C"
+#else
+#define FHEG_EXTERN extern
+#endif
+#define FHEG_API FHEG_EXTERN __attribute__((visibility("default")))
+
+/* Status codes, mirroring the error kinds of fhe_math::Error
+ * (fhe-math/src/errors.rs:9-40) and fhe::Error (fhe/src/errors.rs:15-129). */
+enum fheg_status {
+  FHEG_OK = 0,
+  FHEG_ERR_INVALID_ARGUMENT = 1,   /* malformed sizes, null pointers */
+  FHEG_ERR_INVALID_MODULUS = 2,    /* fhe_math::Error::InvalidModulus */
+  FHEG_ERR_NTT_UNSUPPORTED = 3,    /* "Impossible to construct a Ntt operator" */
+  FHEG_ERR_INVALID_CONTEXT = 4,    /* fhe_math::Error::InvalidContext / wrong poly context */
+  FHEG_ERR_INVALID_LEVEL = 5,      /* fhe::Error::InvalidLevel */
+  FHEG_ERR_KEY_MISMATCH = 6,       /* key / ciphertext level or context mismatch */
+  FHEG_ERR_WRONG_PARTS = 7,        /* ciphertext has the wrong number of parts */
+  FHEG_ERR_NO_MORE_CONTEXT = 8,    /* fhe_math::Error::NoMoreContext */
+  FHEG_ERR_BUDGET = 9,             /* device memory budget exhausted */
+  FHEG_ERR_CUDA = 10,              /* CUDA runtime error */
+  FHEG_ERR_TIMEOUT = 11,           /* bounded wait expired */
+  FHEG_ERR_UNSUPPORTED = 12,       /* valid request outside this library's scope */
+  FHEG_ERR_INTERNAL = 13
+};
+
+typedef struct fheg_context fheg_context;
+typedef struct fheg_scaler fheg_scaler;
+typedef struct fheg_params fheg_params;
+typedef struct fheg_ksk fheg_ksk;
+typedef struct fheg_multiplicator fheg_multiplicator;
+
+/* ------------------------------------------------------------------------ */
+/* Library                                                                    */
+
+FHEG_API const char* fheg_version(void);
+FHEG_API const char* fheg_status_string(int status);
+/* Message of the last failed call on this thread ("" if none). */
+FHEG_API const char* fheg_last_error(void);
+/* Number of kernels this library has launched in this process (all devices).
+ * Used by benchmarks to report how many of the library's kernels ran. */
+FHEG_API uint64_t fheg_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* Host-only number theory (no device work).                                  */
+
+/* fhe-math/src/zq/primes.rs:30-59 `generate_prime`. *out = 0 when none. */
+FHEG_API int fheg_generate_prime(uint32_t num_bits, uint64_t modulo, uint64_t upper_bound, uint64_t* out);
+/* fhe-math/src/ntt/mod.rs:19-23 `supports_ntt`: 1 if p is prime and p = 1 mod 2n. */
+FHEG_API int fheg_supports_ntt(uint64_t p, size_t n);
+/* The default 2n-th root used by `NttOperator::new`
+ * (fhe-math/src/ntt/native.rs:320-336). */
+FHEG_API int fheg_ntt_default_root(uint64_t p, size_t n, uint64_t* out_root);
+/* Host copy of the twiddle tables `NttOperator::new` builds
+ * (fhe-math/src/ntt/native.rs:35-73): four arrays of n words each, and
+ * size_inv / size_inv_shoup in out_size_inv[0..2]. root = 0 selects the
+ * default root. */
+FHEG_API int fheg_ntt_tables_host(uint64_t p, size_t n, uint64_t root, uint64_t* omegas,
+                                  uint64_t* omegas_shoup, uint64_t* zetas_inv,
+                                  uint64_t* zetas_inv_shoup, uint64_t* out_size_inv);
+/* Host copy of the RnsScaler constants (fhe-math/src/rns/scaler.rs:79-175)
+ * for the scaling from `from_moduli` to `to_moduli` by num/den. Output layout:
+ *   out[0] = theta_garner_shift, out[1] = is_one,
+ *   out[2..5] = theta_gamma (lo, hi, sign),
+ *   then to_len gamma, to_len gamma_shoup,
+ *   then to_len*from_len omega, to_len*from_len omega_shoup (row = target modulus),
+ *   then from_len theta_omega_lo, from_len theta_omega_hi, from_len theta_omega_sign,
+ *   then from_len theta_garner_lo, from_len theta_garner_hi.
+ * `out_words` must be at least 5 + 2*to + 2*to*from + 5*from. */
+FHEG_API int fheg_rns_scaler_constants_host(const uint64_t* from_moduli, size_t from_len,
+                                            const uint64_t* to_moduli, size_t to_len,
+                                            const uint64_t* num, size_t num_words,
+                                            const uint64_t* den, size_t den_words,
+                                            uint64_t* out, size_t out_words);
+
+/* ------------------------------------------------------------------------ */
+/* Ring contexts and polynomial operations (fhe-math `rq`, `ntt`, `rns`).     */
+
+/* rq::Context::new (fhe-math/src/rq/context.rs:42-93). Uploads the NTT tables
+ * of every modulus to the current device. `roots` (nullable) injects the 2N-th
+ * root of each modulus, e.g. the root a caller's own `NttOperator` picked. */
+FHEG_API int fheg_context_create(const uint64_t* moduli, size_t num_moduli, size_t degree,
+                                 const uint64_t* roots, fheg_context** out);
+FHEG_API void fheg_context_destroy(fheg_context* ctx);
+FHEG_API size_t fheg_context_num_moduli(const fheg_context* ctx);
+FHEG_API size_t fheg_context_degree(const fheg_context* ctx);
+
+/* NttOperator::forward / forward_vt_lazy / backward
+ * (fhe-math/src/ntt/native.rs:77-233) applied to every limb of `count`
+ * polynomials in place: `Poly::into_ntt` / `into_power_basis`
+ * (fhe-math/src/rq/mod.rs:294-313, 488-579). lazy = 1 leaves forward outputs
+ * in [0, 4p) like `forward_vt_lazy`; otherwise outputs are reduced. */
+FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t count, int lazy,
+                              void* stream);
+FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_t count, void* stream);
+
+/* Coefficient-wise ring operations (fhe-math/src/rq/ops.rs:10-418):
+ * op 0 = add, 1 = sub, 2 = mul (both Ntt, `MulAssign<&Poly<Ntt>>`),
+ * 3 = neg (b ignored). d_out may alias d_a. */
+FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b,
+                          uint64_t* d_out, size_t count, void* stream);
+
+/* Poly::substitute (fhe-math/src/rq/mod.rs:319-369) for an odd exponent,
+ * in Ntt (representation 1) or PowerBasis (0). d_out must not alias d_in. */
+FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation,
+                                  const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream);
+
+/* Poly::switch_down (fhe-math/src/rq/mod.rs:390-448): drops the last modulus
+ * with rounding. d_in is [count][L][N], d_out is [count][L-1][N]. In Ntt
+ * representation the polynomial goes through the power basis like
+ * `Ciphertext::switch_down` (fhe/src/bfv/ciphertext.rs:86-97). d_in is used as
+ * scratch and is overwritten. */
+FHEG_API int fheg_poly_switch_down(const fheg_context* ctx, int representation, uint64_t* d_in,
+                                   uint64_t* d_out, size_t count, void* stream);
+
+/* rq::Scaler::new (fhe-math/src/rq/scaler.rs:27-49) with the scaling factor
+ * num/den (`ScalingFactor::new`, fhe-math/src/rns/scaler.rs:29-36). */
+FHEG_API int fheg_scaler_create(const fheg_context* from, const fheg_context* to, const uint64_t* num,
+                                size_t num_words, const uint64_t* den, size_t den_words,
+                                fheg_scaler** out);
+FHEG_API void fheg_scaler_destroy(fheg_scaler* s);
+/* Poly::scale / Scaler::scale (fhe-math/src/rq/scaler.rs:52-126):
+ * d_in [count][L_from][N] -> d_out [count][L_to][N] in the same
+ * representation. d_in is not modified. */
+FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const uint64_t* d_in,
+                               uint64_t* d_out, size_t count, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* BFV (crate fhe).                                                           */
+
+/* BfvParametersBuilder::build (fhe/src/bfv/parameters.rs:431-641) for the
+ * parts the hot path needs: the context chain, one context per level
+ * (level l keeps the first L-l moduli). */
+FHEG_API int fheg_params_create(size_t degree, const uint64_t* moduli, size_t num_moduli,
+                                uint64_t plaintext, fheg_params** out);
+FHEG_API void fheg_params_destroy(fheg_params* par);
+/* BfvParameters::context_at_level (parameters.rs:155-177). The context is
+ * owned by the parameters. */
+FHEG_API int fheg_params_context_at_level(const fheg_params* par, size_t level, const fheg_context** out);
+FHEG_API size_t fheg_params_max_level(const fheg_params* par);
+
+/* A key-switching key resident on the device: `KeySwitchingKey`
+ * (fhe/src/bfv/keys/key_switching_key.rs:21-45), RNS-digit form. h_c0 and
+ * h_c1 hold the `c0[i]` / `c1[i]` polynomials (Ntt values, canonical) as
+ * [count][L_ksk][N] host arrays with count = number of ciphertext moduli;
+ * the Shoup companions are computed here. */
+FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
+                             const uint64_t* h_c0, const uint64_t* h_c1, size_t count, fheg_ksk** out);
+FHEG_API void fheg_ksk_destroy(fheg_ksk* k);
+
+/* RelinearizationKey::relinearizes (fhe/src/bfv/keys/relinearization_key.rs:71-98):
+ * d_ct3 [count][3][L][N] (Ntt) -> d_out [count][2][L][N] (Ntt). */
+FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
+                              void* stream);
+
+/* GaloisKey::relinearize / relinearize_into (fhe/src/bfv/keys/galois_key.rs:63-124),
+ * reached through EvaluationKey::rotates_columns_by (exponent 3^i mod 2N) and
+ * rotates_rows (exponent 2N-1) (fhe/src/bfv/keys/evaluation_key.rs:92-131).
+ * d_ct [count][2][L][N] (Ntt) -> d_out [count][2][L][N] (Ntt). */
+FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const uint64_t* d_ct,
+                                     uint64_t* d_out, size_t count, void* stream);
+
+/* Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) for ciphertexts
+ * at `level` with `parts` polynomials: d_ct [count][parts][L][N] ->
+ * d_out [count][parts][L-1][N]. d_ct is used as scratch. */
+FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts,
+                                         uint64_t* d_ct, uint64_t* d_out, size_t count, void* stream);
+
+/* Add<&Ciphertext> (fhe/src/bfv/ops/mod.rs:15-43). */
+FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_a,
+                                 const uint64_t* d_b, uint64_t* d_out, size_t count, void* stream);
+
+/* Multiplicator::default(&rk) (fhe/src/bfv/ops/mul.rs:101-130): extension
+ * basis generated as the reference does, relinearization enabled. */
+FHEG_API int fheg_multiplicator_create_default(const fheg_ksk* rk, fheg_multiplicator** out);
+/* Multiplicator::new_leveled (fhe/src/bfv/ops/mul.rs:56-98) with explicit
+ * scaling factors and extended basis (whose first moduli must be the level's
+ * moduli when a factor is one). */
+FHEG_API int fheg_multiplicator_create(const fheg_params* par, size_t level, const uint64_t* lhs_num,
+                                       size_t lhs_num_words, const uint64_t* lhs_den, size_t lhs_den_words,
+                                       const uint64_t* rhs_num, size_t rhs_num_words, const uint64_t* rhs_den,
+                                       size_t rhs_den_words, const uint64_t* extended_basis,
+                                       size_t extended_len, const uint64_t* post_num, size_t post_num_words,
+                                       const uint64_t* post_den, size_t post_den_words,
+                                       fheg_multiplicator** out);
+FHEG_API void fheg_multiplicator_destroy(fheg_multiplicator* m);
+/* Multiplicator::enable_relinearization / enable_mod_switching (mul.rs:133-155). */
+FHEG_API int fheg_multiplicator_enable_relinearization(fheg_multiplicator* m, const fheg_ksk* rk);
+FHEG_API int fheg_multiplicator_enable_mod_switching(fheg_multiplicator* m);
+/* Shape of the product: parts (2 with relinearization, else 3) and level. */
+FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t* parts, size_t* level);
+/* Multiplicator::multiply (fhe/src/bfv/ops/mul.rs:158-227), batched:
+ * d_lhs, d_rhs [count][2][L][N] (Ntt) -> d_out [count][parts][L'][N]. */
+FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
+                                         uint64_t* d_out, size_t count, void* stream);
+/* Same, end to end from host buffers: copies the inputs to the device,
+ * multiplies, and copies the product back before returning. */
+FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs,
+                                              const uint64_t* h_rhs, uint64_t* h_out, size_t count);
+
+#endif /* FHEG_H */

@@ -1,0 +1,208 @@
+"""GPU BFV hot path (crate fhe) bit-exact against the oracle and decrypting
+correctly: Multiplicator (mul+relin, mod switching, no relinearization, custom
+strategy, levels), relinearization, rotations, switch-down and addition."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+class Setup:
+    def __init__(self, fg, ora, n, L, t, seed, level=0):
+        self.rng = np.random.default_rng(seed)
+        self.ora, self.fg, self.n, self.t, self.level = ora, fg, n, t, level
+        self.par_o = ora.BfvParameters(n, t, moduli_sizes=[62] * L)
+        self.sk = ora.SecretKey.random(self.par_o, self.rng)
+        self.par = fg.BfvParameters(n, self.par_o.moduli, t)
+
+    def encrypt(self, count, level=None):
+        level = self.level if level is None else level
+        vals, cts = [], []
+        for _ in range(count):
+            v = self.rng.integers(0, self.t, self.n, dtype=np.uint64)
+            vals.append(v)
+            cts.append(self.sk.encrypt(self.ora.Plaintext.encode(v, "simd", self.par_o, level), self.rng))
+        return vals, cts
+
+    def rk(self, level=None):
+        level = self.level if level is None else level
+        rk_o = self.ora.RelinearizationKey(self.sk, self.rng, level, level)
+        rk = self.fg.RelinearizationKey(self.par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array(), level, level)
+        return rk_o, rk
+
+    def decrypt(self, arr, level):
+        return self.sk.decrypt(self.ora.Ciphertext.from_array(self.par_o, arr, level)).decode("simd")
+
+    def product(self, a, b):
+        return [int(x) * int(y) % self.t for x, y in zip(a, b)]
+
+
+@pytest.mark.parametrize("n,L,t,B", [(16, 3, 1153, 3), (4096, 2, 65537, 2), (16384, 6, 65537, 2),
+                                     (32768, 3, 65537, 1)])
+def test_multiply_default(fg, ora, cuda, n, L, t, B):
+    s = Setup(fg, ora, n, L, t, seed=n + L)
+    rk_o, rk = s.rk()
+    mult_o = ora.Multiplicator.default(rk_o)
+    mult = fg.Multiplicator.default(rk)
+    vals, cts = s.encrypt(2 * B)
+    lhs = np.stack([c.to_array() for c in cts[:B]])
+    rhs = np.stack([c.to_array() for c in cts[B:]])
+    out = fg.to_host(mult.multiply(fg.to_device(lhs), fg.to_device(rhs)))
+    assert out.shape == (B, 2, L, n)
+    for b in range(B):
+        want = mult_o.multiply(cts[b], cts[B + b]).to_array()
+        assert np.array_equal(out[b], want), f"pair {b}"
+        assert list(s.decrypt(out[b], 0)) == s.product(vals[b], vals[B + b])
+
+
+def test_multiply_variants(fg, ora, cuda):
+    """mul.rs:246-339: mod switching and no relinearization."""
+    s = Setup(fg, ora, 4096, 3, 65537, seed=77)
+    rk_o, rk = s.rk()
+    vals, cts = s.encrypt(2)
+    lhs, rhs = (fg.to_device(c.to_array()[None]) for c in cts)
+    want_vals = s.product(vals[0], vals[1])
+    # mod switching
+    mo = ora.Multiplicator.default(rk_o)
+    mo.enable_mod_switching()
+    m = fg.Multiplicator.default(rk)
+    m.enable_mod_switching()
+    assert m.output_shape() == (2, 1)
+    out = fg.to_host(m.multiply(lhs, rhs))[0]
+    want = mo.multiply(cts[0], cts[1])
+    assert want.level == 1 and np.array_equal(out, want.to_array())
+    assert list(s.decrypt(out, 1)) == want_vals
+    # no relinearization (3 parts), via a leveled multiplicator with the default basis
+    ext = ora.Multiplicator.default_extended_basis(s.par_o, 0)
+    q = s.par_o.context_at_level(0).modulus()
+    mo3 = ora.Multiplicator(ora.ScalingFactor.one(), ora.ScalingFactor.one(), ext,
+                            ora.ScalingFactor(65537, q), 0, s.par_o)
+    m3 = fg.Multiplicator.new_leveled(fg.ScalingFactor.one(), fg.ScalingFactor.one(), ext,
+                                      fg.ScalingFactor(65537, q), 0, s.par)
+    assert m3.output_shape() == (3, 0)
+    out3 = fg.to_host(m3.multiply(lhs, rhs))[0]
+    want3 = mo3.multiply(cts[0], cts[1])
+    assert np.array_equal(out3, want3.to_array())
+    assert list(s.decrypt(out3, 0)) == want_vals
+    # relinearize the 3-part product separately (relinearization_key.rs:71-98)
+    out_r = fg.to_host(rk.relinearizes(fg.to_device(out3[None])))[0]
+    assert np.array_equal(out_r, rk_o.relinearizes(want3).to_array())
+    assert list(s.decrypt(out_r, 0)) == want_vals
+
+
+def test_multiply_custom_strategy(fg, ora, cuda):
+    """mul.rs:341-401: the second strategy of eprint 2021/204 (rhs scaled by P/Q)."""
+    s = Setup(fg, ora, 16, 3, 1153, seed=5)
+    ext = list(s.par_o.moduli)
+    for k in range(3):
+        ext.append(ora.generate_prime(62, 2 * 16, ext[2 + k]))
+    rns = ora.RnsContext(ext[3:])
+    q = s.par_o.context_at_level(0).modulus()
+    args_o = (ora.ScalingFactor.one(), ora.ScalingFactor(rns.modulus(), q), ext,
+              ora.ScalingFactor(1153, rns.modulus()), 0, s.par_o)
+    mo = ora.Multiplicator(*args_o)
+    m = fg.Multiplicator.new_leveled(fg.ScalingFactor.one(), fg.ScalingFactor(rns.modulus(), q), ext,
+                                     fg.ScalingFactor(1153, rns.modulus()), 0, s.par)
+    vals, cts = s.encrypt(2)
+    out = fg.to_host(m.multiply(fg.to_device(cts[0].to_array()[None]), fg.to_device(cts[1].to_array()[None])))[0]
+    want = mo.multiply(cts[0], cts[1])
+    assert np.array_equal(out, want.to_array())
+    assert list(s.decrypt(out, 0)) == s.product(vals[0], vals[1])
+
+
+def test_multiply_at_level(fg, ora, cuda):
+    """mul.rs:281-317: keys and ciphertexts at level 1."""
+    s = Setup(fg, ora, 4096, 3, 65537, seed=9, level=1)
+    rk_o, rk = s.rk()
+    vals, cts = s.encrypt(2)
+    assert cts[0].level == 1
+    mo, m = ora.Multiplicator.default(rk_o), fg.Multiplicator.default(rk)
+    out = fg.to_host(m.multiply(fg.to_device(cts[0].to_array()[None]), fg.to_device(cts[1].to_array()[None])))[0]
+    assert np.array_equal(out, mo.multiply(cts[0], cts[1]).to_array())
+    assert list(s.decrypt(out, 1)) == s.product(vals[0], vals[1])
+
+
+def test_batched_equals_single_and_host(fg, ora, cuda):
+    """A batch of 6 equals 6 single launches and the host entry point."""
+    s = Setup(fg, ora, 4096, 2, 65537, seed=21)
+    _, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(12)
+    lhs = np.stack([c.to_array() for c in cts[:6]])
+    rhs = np.stack([c.to_array() for c in cts[6:]])
+    batched = fg.to_host(m.multiply(fg.to_device(lhs), fg.to_device(rhs)))
+    for b in range(6):
+        single = fg.to_host(m.multiply(fg.to_device(lhs[b:b + 1]), fg.to_device(rhs[b:b + 1])))
+        assert np.array_equal(single[0], batched[b])
+    assert np.array_equal(m.multiply_host(lhs, rhs), batched)
+
+
+@pytest.mark.parametrize("n,L", [(16, 3), (4096, 2), (32768, 4)])
+def test_rotations(fg, ora, cuda, n, L):
+    """evaluation_key.rs:92-131 via GaloisKey::relinearize_into."""
+    s = Setup(fg, ora, n, L, 65537 if n > 16 else 1153, seed=n * 3 + L)
+    steps = [1, 5] if n > 16 else [1, 3]
+    ek_o = ora.EvaluationKey(s.sk, s.rng, columns=steps, row_rotation=True)
+    gks = [fg.GaloisKey(s.par, e, g.ksk.c0_array(), g.ksk.c1_array()) for e, g in ek_o.gk.items()]
+    ek = fg.EvaluationKey(s.par, gks)
+    vals, cts = s.encrypt(2)
+    batch = fg.to_device(np.stack([c.to_array() for c in cts]))
+    half = n // 2
+    for i in steps:
+        got = fg.to_host(ek.rotates_columns_by(batch, i))
+        for b in range(2):
+            assert np.array_equal(got[b], ek_o.rotates_columns_by(cts[b], i).to_array())
+            want = np.concatenate([np.roll(vals[b][:half], -i), np.roll(vals[b][half:], -i)])
+            assert np.array_equal(s.decrypt(got[b], 0), want)
+    got = fg.to_host(ek.rotates_rows(batch))
+    for b in range(2):
+        assert np.array_equal(got[b], ek_o.rotates_rows(cts[b]).to_array())
+
+
+def test_ciphertext_switch_down_and_add(fg, ora, cuda):
+    s = Setup(fg, ora, 4096, 3, 65537, seed=31)
+    vals, cts = s.encrypt(2)
+    a = np.stack([c.to_array() for c in cts])
+    got = fg.to_host(fg.ciphertext_switch_down(s.par, 0, fg.to_device(a)))
+    for b in range(2):
+        want = cts[b].copy().switch_down()
+        assert np.array_equal(got[b], want.to_array())
+        assert np.array_equal(s.decrypt(got[b], 1), vals[b])
+    ssum = fg.to_host(fg.ciphertext_add(s.par, 0, fg.to_device(a[:1]), fg.to_device(a[1:])))[0]
+    assert np.array_equal(ssum, (cts[0] + cts[1]).to_array())
+    assert list(s.decrypt(ssum, 0)) == [(int(x) + int(y)) % 65537 for x, y in zip(vals[0], vals[1])]
+
+
+def test_errors(fg, ora, cuda):
+    """Reference error behaviour at the boundary (mul.rs:146-173,
+    key_switching_key.rs:219-223, relinearization_key.rs:52-56,
+    rq/mod.rs:99-105)."""
+    s = Setup(fg, ora, 16, 3, 1153, seed=41)
+    _, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    x2 = fg.to_device(np.zeros((1, 2, 3, 16), dtype=np.uint64))
+    x3 = fg.to_device(np.zeros((1, 3, 3, 16), dtype=np.uint64))
+    with pytest.raises(fg.FhegError):  # wrong number of parts
+        m.multiply(x2, x3)
+    q = s.par_o.context_at_level(2).modulus()
+    ext = ora.Multiplicator.default_extended_basis(s.par_o, 2)
+    last = fg.Multiplicator.new_leveled(fg.ScalingFactor.one(), fg.ScalingFactor.one(), ext,
+                                        fg.ScalingFactor(1153, q), 2, s.par)
+    with pytest.raises(fg.FhegError) as e:  # already the last level
+        last.enable_mod_switching()
+    assert e.value.code == fg.ERR_NO_MORE_CONTEXT
+    with pytest.raises(fg.FhegError) as e:  # even exponent
+        fg.substitute(s.par.context_at_level(0), x2[0], 2, 1)
+    assert e.value.code == fg.ERR_INVALID_ARGUMENT
+    c = np.zeros((2, 3, 16), dtype=np.uint64)
+    with pytest.raises(fg.FhegError) as e:  # digit count != ciphertext moduli
+        fg.RelinearizationKey(s.par, c, c)
+    assert e.value.code == fg.ERR_KEY_MISMATCH
+    one = np.zeros((1, 1, 16), dtype=np.uint64)
+    with pytest.raises(fg.FhegError) as e:  # single-modulus key context
+        fg.RelinearizationKey(s.par, one, one, 2, 2)
+    assert e.value.code == fg.ERR_UNSUPPORTED
+    with pytest.raises(fg.FhegError) as e:
+        s.par.context_at_level(3)
+    assert e.value.code == fg.ERR_INVALID_LEVEL

@@ -1,0 +1,109 @@
+"""GPU ring operations (fhe-math rq) bit-exact against the oracle: element-wise
+ops, substitution, switch-down and the RNS scaler (rq::Scaler)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+Q = [4611686018282684417, 4611686018326724609, 4611686018309947393]
+P = [4611686018282684417, 4611686018309947393, 4611686018257518593]
+MODULI = [1153, 4611686018326724609, 4611686018309947393, 4611686018232352769, 4611686018171535361]
+
+
+def _rand(rng, moduli, n, B):
+    return np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli]) for _ in range(B)])
+
+
+def test_poly_ops(fg, ora, cuda):
+    rng = np.random.default_rng(1)
+    n, B = 1 << 12, 3
+    ctx_o = ora.Context(Q, n)
+    ctx = fg.Context(Q, n)
+    a, b = _rand(rng, Q, n, B), _rand(rng, Q, n, B)
+    ta, tb = fg.to_device(a), fg.to_device(b)
+    for op in ("add", "sub", "mul", "neg"):
+        got = fg.to_host(fg.poly_op(ctx, op, ta, tb))
+        for k in range(B):
+            pa = ora.Poly(ctx_o, a[k], ora.NTT)
+            pb = ora.Poly(ctx_o, b[k], ora.NTT)
+            want = {"add": lambda: pa + pb, "sub": lambda: pa - pb, "mul": lambda: pa * pb, "neg": lambda: -pa}[op]()
+            assert np.array_equal(got[k], want.coefficients), op
+
+
+@pytest.mark.parametrize("n", [16, 1 << 13, 1 << 15])
+def test_substitute(fg, ora, cuda, n):
+    rng = np.random.default_rng(2)
+    moduli = [m for m in MODULI if ora.supports_ntt(m, n)] or [ora.generate_prime(62, 2 * n, 1 << 62)]
+    ctx_o = ora.Context(moduli, n)
+    ctx = fg.Context(moduli, n)
+    a = _rand(rng, moduli, n, 2)
+    for e in (3, 11, 2 * n - 1, pow(3, 7, 2 * n)):
+        ex = ora.SubstitutionExponent(ctx_o, e)
+        for rep in (ora.POWER_BASIS, ora.NTT):
+            got = fg.to_host(fg.substitute(ctx, fg.to_device(a), e, 0 if rep == ora.POWER_BASIS else 1))
+            for k in range(2):
+                want = ora.Poly(ctx_o, a[k], rep).substitute(ex)
+                assert np.array_equal(got[k], want.coefficients), (e, rep)
+
+
+@pytest.mark.parametrize("n", [16, 1 << 14])
+def test_switch_down(fg, ora, cuda, n):
+    """rq/mod.rs:390-448 in power basis, and in Ntt through the power basis."""
+    rng = np.random.default_rng(3)
+    moduli = [m for m in MODULI if ora.supports_ntt(m, n)]
+    if len(moduli) < 3:
+        moduli, ub = [], 1 << 62
+        while len(moduli) < 4:
+            ub = ora.generate_prime(62, 2 * n, ub)
+            moduli.append(ub)
+    ctx_o = ora.Context(moduli, n)
+    ctx = fg.Context(moduli, n)
+    a = _rand(rng, moduli, n, 3)
+    got = fg.to_host(fg.switch_down(ctx, fg.to_device(a), 0))
+    for k in range(3):
+        want = ora.Poly(ctx_o, a[k], ora.POWER_BASIS).switch_down()
+        assert np.array_equal(got[k], want.coefficients)
+    got = fg.to_host(fg.switch_down(ctx, fg.to_device(a), 1))
+    for k in range(3):
+        want = ora.Poly(ctx_o, a[k], ora.NTT).into_power_basis().switch_down().into_ntt()
+        assert np.array_equal(got[k], want.coefficients)
+
+
+@pytest.mark.parametrize("num,den", [(1, 1), (3, 1001), (4611686018326724610, 4), (1000, 101), (100, 2)])
+def test_scaler(fg, ora, cuda, num, den):
+    """rq/scaler.rs:52-126 in both representations, different contexts."""
+    rng = np.random.default_rng(4)
+    n = 1 << 12
+    frm_o, to_o = ora.Context(Q, n), ora.Context(P, n)
+    sc_o = ora.Scaler(frm_o, to_o, ora.ScalingFactor(num, den))
+    sc = fg.Scaler(fg.Context(Q, n), fg.Context(P, n), fg.ScalingFactor(num, den))
+    a = _rand(rng, Q, n, 2)
+    for rep in (ora.POWER_BASIS, ora.NTT):
+        got = fg.to_host(sc.scale(fg.to_device(a), 0 if rep == ora.POWER_BASIS else 1))
+        for k in range(2):
+            want = sc_o.scale(ora.Poly(frm_o, a[k], rep))
+            assert np.array_equal(got[k], want.coefficients), rep
+
+
+@pytest.mark.parametrize("n,L", [(4096, 2), (16384, 6)])
+def test_mul_scalers(fg, ora, cuda, n, L):
+    """The Multiplicator's scalers: extension Q -> Q u P (factor one, common
+    prefix) and t/Q scale-down Q u P -> Q, in Ntt representation."""
+    rng = np.random.default_rng(5)
+    par = ora.BfvParameters(n, 65537, moduli_sizes=[62] * L)
+    ext = ora.Multiplicator.default_extended_basis(par, 0)
+    base_o, mul_o = par.context_at_level(0), ora.Context(ext, n)
+    base, mul = fg.Context(par.moduli, n), fg.Context(ext, n)
+    up_o = ora.Scaler(base_o, mul_o, ora.ScalingFactor.one())
+    down_o = ora.Scaler(mul_o, base_o, ora.ScalingFactor(65537, base_o.modulus()))
+    up = fg.Scaler(base, mul, fg.ScalingFactor.one())
+    down = fg.Scaler(mul, base, fg.ScalingFactor(65537, base_o.modulus()))
+    a = _rand(rng, par.moduli, n, 2)
+    got = fg.to_host(up.scale(fg.to_device(a), 1))
+    for k in range(2):
+        assert np.array_equal(got[k], up_o.scale(ora.Poly(base_o, a[k], ora.NTT)).coefficients)
+    b = _rand(rng, ext, n, 2)
+    got = fg.to_host(down.scale(fg.to_device(b), 1))
+    for k in range(2):
+        assert np.array_equal(got[k], down_o.scale(ora.Poly(mul_o, b[k], ora.NTT)).coefficients)

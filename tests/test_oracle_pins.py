@@ -1,0 +1,246 @@
+"""Pins the CPU oracle to the reference's own known answers and exact-formula
+tests (fhe-math), restated here. No GPU involved."""
+
+import numpy as np
+import pytest
+
+
+def test_nfl_62bit_primes(ora):
+    """fhe-math/src/zq/primes.rs:67-102: the only literal golden vector."""
+    expected = [
+        4611686018326724609, 4611686018309947393, 4611686018282684417, 4611686018257518593,
+        4611686018232352769, 4611686018171535361, 4611686018106523649, 4611686018058289153,
+        4611686018051997697, 4611686017974403073, 4611686017812922369, 4611686017781465089,
+        4611686017773076481, 4611686017678704641, 4611686017666121729, 4611686017647247361,
+        4611686017590624257, 4611686017554972673, 4611686017529806849, 4611686017517223937,
+    ]
+    generated, ub = [], ((1 << 64) - 1) >> 2
+    while len(generated) != 20:
+        p = ora.generate_prime(62, 2 * 1048576, ub)
+        assert p is not None
+        ub = p
+        generated.append(p)
+    assert generated == expected
+
+
+def test_generate_prime_edges(ora):
+    """primes.rs:104-122."""
+    assert ora.generate_prime(10, 2048, 1 << 10) is None
+    assert ora.generate_prime(11, 16, 1033) is None
+
+
+def test_ntt_constructor(ora):
+    """ntt/mod.rs:30-49."""
+    for size in (32, 1024):
+        for p in (1153, 4611686018326724609):
+            ok = ora.supports_ntt(p, size)
+            if ok:
+                ora.NttOperator(ora.Modulus(p), size)
+            else:
+                with pytest.raises(ValueError):
+                    ora.NttOperator(ora.Modulus(p), size)
+    assert ora.supports_ntt(1153, 32) and not ora.supports_ntt(1153, 1024)
+
+
+@pytest.mark.parametrize("size,p", [(32, 1153), (32, 4611686018326724609), (1024, 4611686018326724609)])
+def test_ntt_bijection_and_lazy(ora, size, p):
+    """ntt/mod.rs:51-112: forward/backward bijection, lazy == reduced."""
+    rng = np.random.default_rng(size + p % 1000)
+    op = ora.NttOperator(ora.Modulus(p), size)
+    for _ in range(20):
+        a = rng.integers(0, p, size, dtype=np.uint64)
+        b = a.copy()
+        op.forward(b)
+        assert not np.array_equal(a, b)
+        lazy = a.copy()
+        op.forward_vt_lazy(lazy)
+        assert (lazy < np.uint64(4 * p)).all()
+        op.p.reduce_vec(lazy)
+        assert np.array_equal(lazy, b)
+        op.backward(b)
+        assert np.array_equal(a, b)
+
+
+def test_ntt_is_evaluation_at_odd_powers(ora):
+    """The forward NTT evaluates the polynomial at psi^(2*bitrev(i)+1)."""
+    p, n = 4611686018326724609, 64
+    op = ora.NttOperator(ora.Modulus(p), n)
+    rng = np.random.default_rng(3)
+    a = rng.integers(0, p, n, dtype=np.uint64)
+    b = a.copy()
+    op.forward(b)
+    for i in range(n):
+        e = 2 * ora.bitrev(i, 6) + 1
+        want = sum(int(a[j]) * pow(op.omega, e * j, p) for j in range(n)) % p
+        assert int(b[i]) == want
+
+
+def _expected_scaled(x, q_mod, t_mod, n, d):
+    """rns/scaler.rs:397-414: centered rounding of x * n / d."""
+    sign = x >= (q_mod >> 1)
+    if sign:
+        x = q_mod - x
+        if d % 2 == 0:
+            return t_mod - ((x * n + ((d >> 1) - 1)) // d) % t_mod
+        return t_mod - ((x * n + (d >> 1)) // d) % t_mod
+    return (x * n + (d >> 1)) // d
+
+
+NUMS = [1, 2, 3, 100, 1000, 4611686018326724610]
+DENS = [1, 2, 3, 4, 100, 101, 1000, 1001, 4611686018326724610]
+
+
+def test_rns_scaler_same_context(ora):
+    """rns/scaler.rs:379-419."""
+    rng = np.random.default_rng(11)
+    q = ora.RnsContext([4, 4611686018326724609, 1153])
+    for n in NUMS:
+        for d in DENS:
+            s = ora.RnsScaler(q, q, ora.ScalingFactor(n, d))
+            for _ in range(40):
+                x = [int(rng.integers(0, m)) for m in q.moduli_u64]
+                lift = q.lift(x)
+                z = s.scale_new(x, len(x))
+                assert z == q.project(_expected_scaled(lift, q.modulus(), q.modulus(), n, d))
+
+
+def test_rns_scaler_different_contexts(ora):
+    """rns/scaler.rs:421-473."""
+    rng = np.random.default_rng(12)
+    q = ora.RnsContext([4, 4611686018326724609, 1153])
+    r = ora.RnsContext([4, 4611686018326724609, 1153, 4611686018309947393, 4611686018282684417,
+                        4611686018257518593, 4611686018232352769, 4611686018171535361, 4611686018106523649,
+                        4611686018058289153])
+    for n in NUMS:
+        for d in DENS:
+            s = ora.RnsScaler(q, r, ora.ScalingFactor(n, d))
+            for _ in range(20):
+                x = [int(rng.integers(0, m)) for m in q.moduli_u64]
+                lift = q.lift(x)
+                y = s.scale_new(x, len(r.moduli))
+                assert y == r.project(_expected_scaled(lift, q.modulus(), r.modulus(), n, d))
+
+
+RQ_Q = [4611686018282684417, 4611686018326724609, 4611686018309947393]
+RQ_P = [4611686018282684417, 4611686018309947393, 4611686018257518593]
+
+
+def test_rq_scaler(ora):
+    """rq/scaler.rs:152-203 (power basis and Ntt give the same result)."""
+    rng = np.random.default_rng(13)
+    frm, to = ora.Context(RQ_Q, 16), ora.Context(RQ_P, 16)
+    for n in NUMS:
+        for d in DENS:
+            sc = ora.Scaler(frm, to, ora.ScalingFactor(n, d))
+            for _ in range(3):
+                p = ora.Poly.random(frm, ora.POWER_BASIS, rng)
+                expected = [_expected_scaled(x, frm.modulus(), to.modulus(), n, d) % to.modulus()
+                            for x in p.to_biguints()]
+                assert sc.scale(p).to_biguints() == expected
+                pn = p.copy().into_ntt()
+                assert sc.scale(pn).into_power_basis().to_biguints() == expected
+
+
+MODULI = [1153, 4611686018326724609, 4611686018309947393, 4611686018232352769, 4611686018171535361]
+
+
+def test_switch_down_formula(ora):
+    """rq/mod.rs:984-1017: switch_down = round(x * Q' / Q)."""
+    rng = np.random.default_rng(14)
+    ctx = ora.Context(MODULI, 16)
+    for _ in range(10):
+        p = ora.Poly.random(ctx, ora.POWER_BASIS, rng)
+        reference = p.to_biguints()
+        cur = ctx
+        while cur.next_context is not None:
+            den = cur.modulus()
+            cur = cur.next_context
+            num = cur.modulus()
+            p.switch_down()
+            got = p.to_biguints()
+            assert got == [((b * num) + (den >> 1)) // den % cur.modulus() for b in reference]
+            reference = got
+
+
+def test_substitute_identities(ora):
+    """rq/mod.rs:892-982."""
+    rng = np.random.default_rng(15)
+    for m in MODULI:
+        ctx = ora.Context([m], 16)
+        p = ora.Poly.random(ctx, ora.POWER_BASIS, rng)
+        p_ntt = p.copy().into_ntt()
+        for e in (0, 2, 16):
+            with pytest.raises(ValueError):
+                ora.SubstitutionExponent(ctx, e)
+        e1, e3, e11 = (ora.SubstitutionExponent(ctx, k) for k in (1, 3, 11))
+        assert np.array_equal(p.substitute(e1).coefficients, p.coefficients)
+        assert np.array_equal(p_ntt.substitute(e1).coefficients, p_ntt.coefficients)
+        q = p.substitute(e3)
+        v = np.zeros(16, dtype=np.uint64)
+        pc = p.coefficients[0]
+        for i in range(16):
+            v[(3 * i) % 16] = m - pc[i] if ((3 * i) // 16) & 1 == 1 and pc[i] > 0 else pc[i]
+        assert np.array_equal(q.coefficients[0], v)
+        assert np.array_equal(p_ntt.substitute(e3).coefficients, q.copy().into_ntt().coefficients)
+        assert np.array_equal(p.substitute(e3).substitute(e11).coefficients, p.coefficients)
+        assert np.array_equal(p_ntt.substitute(e3).substitute(e11).coefficients, p_ntt.coefficients)
+
+
+def test_lazy_constant_ntt(ora):
+    """rq/mod.rs:823-848: lazy reduction then `forward_vt_lazy` of a row."""
+    m = MODULI[0]
+    ctx = ora.Context([m], 16)
+    coeffs = np.array([(i * m + i) % (1 << 64) for i in range(16)], dtype=np.uint64)
+    digits = np.ascontiguousarray(coeffs[None, :])
+    expected = coeffs.copy()
+    ctx.q[0].lazy_reduce_vec(expected)
+    ctx.ops[0].forward_vt_lazy(expected)
+    got = digits.copy()
+    ctx.q[0].lazy_reduce_vec(got[0])
+    ctx.ops[0].forward_vt_lazy(got[0])
+    assert np.array_equal(got[0], expected)
+
+
+@pytest.mark.parametrize("L", [3, 6])
+def test_multiplicator_decrypts(ora, L):
+    """ops/mul.rs:246-339 (N=16, t=1153): product decrypts to the slotwise
+    product, with and without relinearization and mod switching."""
+    rng = np.random.default_rng(100 + L)
+    par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * L)
+    for _ in range(3):
+        values = rng.integers(0, 1153, 16, dtype=np.uint64)
+        expected = (values.astype(object) * values.astype(object)) % 1153
+        sk = ora.SecretKey.random(par, rng)
+        rk = ora.RelinearizationKey(sk, rng)
+        pt = ora.Plaintext.encode(values, "simd", par)
+        ct1, ct2 = sk.encrypt(pt, rng), sk.encrypt(pt, rng)
+        m = ora.Multiplicator.default(rk)
+        ct3 = m.multiply(ct1, ct2)
+        assert list(sk.decrypt(ct3).decode("simd")) == list(expected)
+        m.rk = None
+        ct3 = m.multiply(ct1, ct2)
+        assert len(ct3) == 3
+        assert list(sk.decrypt(ct3).decode("simd")) == list(expected)
+        m.enable_relinearization(rk)
+        m.enable_mod_switching()
+        ct3 = m.multiply(ct1, ct2)
+        assert ct3.level == 1
+        assert list(sk.decrypt(ct3).decode("simd")) == list(expected)
+
+
+def test_rotations_decrypt(ora):
+    """evaluation_key.rs:572-675: row and column rotations."""
+    rng = np.random.default_rng(7)
+    n = 16
+    par = ora.BfvParameters(n, 1153, moduli_sizes=[62] * 3)
+    sk = ora.SecretKey.random(par, rng)
+    ek = ora.EvaluationKey(sk, rng, columns=range(1, n // 2), row_rotation=True)
+    values = rng.integers(0, 1153, n, dtype=np.uint64)
+    ct = sk.encrypt(ora.Plaintext.encode(values, "simd", par), rng)
+    half = n // 2
+    for i in range(1, half):
+        got = sk.decrypt(ek.rotates_columns_by(ct, i)).decode("simd")
+        want = np.concatenate([np.roll(values[:half], -i), np.roll(values[half:], -i)])
+        assert np.array_equal(got, want)
+    got = sk.decrypt(ek.rotates_rows(ct)).decode("simd")
+    assert np.array_equal(got, np.concatenate([values[half:], values[:half]]))
