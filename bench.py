@@ -322,6 +322,71 @@ def run_ours(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+def run_ntt(args):
+    """The batched NTT configuration: forward + inverse over `--polys`
+    polynomials of six 62-bit moduli at N = 2^14 (device resident), GB/s of
+    algorithmic traffic against the measured HBM bandwidth."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    moduli, ub = [], 1 << 62
+    while len(moduli) < L:
+        ub = ora.generate_prime(62, 2 * N, ub)
+        moduli.append(ub)
+    rng = np.random.default_rng(1)
+    polys = args.polys
+    one = np.stack([rng.integers(0, m, N, dtype=np.uint64) for m in moduli])
+    ctx = fg.Context(moduli, N)
+    buf = fg.to_device(np.tile(one[None], (polys, 1, 1)))
+    expect = one.copy()
+    for i, m in enumerate(moduli):
+        ora.ntt_operator(m, N).forward(expect[i])
+    fg.ntt_forward(ctx, buf)
+    torch.cuda.synchronize()
+    got = fg.to_host(buf[:1])[0]
+    if not np.array_equal(got, expect):
+        raise SystemExit("bench: NTT is not bit-exact with the oracle")
+    fg.ntt_backward(ctx, buf)
+    for _ in range(args.warmup):
+        fg.ntt_forward(ctx, buf)
+        fg.ntt_backward(ctx, buf)
+    stream = torch.cuda.current_stream()
+    start, mid, end = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    fwd = inv = 0.0
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            start.record(stream)
+            fg.ntt_forward(ctx, buf)
+            mid.record(stream)
+            fg.ntt_backward(ctx, buf)
+            end.record(stream)
+            torch.cuda.synchronize()
+            fwd += start.elapsed_time(mid)
+            inv += mid.elapsed_time(end)
+    launches = fg.kernel_launch_count() - launches0
+    fwd /= args.steps
+    inv /= args.steps
+    nbytes = 2 * 8 * polys * L * N + 2 * 8 * L * N
+    peak, kind = _peaks()
+    gbs = 2 * nbytes / ((fwd + inv) / 1000.0) / 1e9
+    line = {"metric": "NTT fwd+inv GB/s N=2^14 L=6", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fwd + inv, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "ntt_batched", "degree": N, "moduli": L, "polys": polys,
+                       "l2": f"buffer {polys * L * N * 8 / 1e6:.0f} MB > L2"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "peak_kind": kind, "fwd_ms": fwd, "inv_ms": inv,
+                         "fwd_gbs": nbytes / (fwd / 1000) / 1e9, "inv_gbs": nbytes / (inv / 1000) / 1e9},
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -331,10 +396,14 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt"])
+    ap.add_argument("--polys", type=int, default=256)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
-    if args.impl == "reference":
+    if args.workload == "ntt":
+        run_ntt(args)
+    elif args.impl == "reference":
         run_reference(args, rank)
     else:
         run_ours(args, rank, world)

@@ -25,6 +25,10 @@
 #include "common.cuh"
 
 namespace fheg {
+// Internal linkage: every translation unit that includes this header gets its
+// own kernels and launch helpers (a template kernel instantiated in two units
+// must not share one host-side registration or attribute flag).
+namespace {
 
 // Job decoding shared by all NTT kernels: blockIdx.x enumerates
 // (poly, limb, block) with block fastest.
@@ -505,4 +509,5 @@ void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly 
   after_launch("k_ntt_inv_top");
 }
 
+}  // namespace
 }  // namespace fheg
