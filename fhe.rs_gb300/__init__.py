@@ -111,6 +111,7 @@ def _declare(L):
         "fheg_multiplicator_output_shape": (i, [c_vp, ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
         "fheg_multiplicator_multiply": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_multiplicator_multiply_host": (i, [c_vp, P_u64, P_u64, P_u64, c_size]),
+        "fheg_relinearize_noalloc": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -4,31 +4,10 @@
 #include <string>
 
 #include "fheg.h"
+#include "handles.hpp"
 #include "lib.hpp"
 
 using namespace fheg;
-
-struct fheg_context {
-  std::shared_ptr<Context> c;
-};
-struct fheg_scaler {
-  std::unique_ptr<Scaler> s;
-  DevBuf scratch;
-};
-struct fheg_params {
-  std::unique_ptr<Params> p;
-  std::vector<fheg_context> level_handles;
-};
-struct fheg_ksk {
-  Ksk k;
-};
-struct fheg_multiplicator {
-  std::unique_ptr<Multiplicator> m;
-  cudaStream_t copy_stream = nullptr;
-  ~fheg_multiplicator() {
-    if (copy_stream) cudaStreamDestroy(copy_stream);
-  }
-};
 
 namespace {
 
@@ -61,6 +40,10 @@ cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 BigUint big(const uint64_t* w, size_t n) { return w && n ? BigUint::from_words(w, n) : BigUint(); }
 
 }  // namespace
+
+namespace fheg {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace fheg
 
 FHEG_API const char* fheg_version(void) { return "fheg 0.1.0 (sm_103a)"; }
 

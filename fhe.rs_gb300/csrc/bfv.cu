@@ -227,6 +227,20 @@ void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t cou
   key_switch(rk, dst, count, ct3, 3 * L * N, 0, ct3 + L * N, 3 * L * N, out, 2 * L * N, D, st);
 }
 
+// Relinearization with caller-provided scratch: `digits` holds count*L*N
+// words and `D` count*L*Lk*N words. Same computation as relinearize().
+void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, uint64_t* digits,
+                         uint64_t* D, cudaStream_t st) {
+  require_same_level_key(rk);
+  const Context& c = *rk.ctx_ct;
+  const size_t L = c.L(), N = c.N();
+  if (count == 0) return;
+  PolyRef src = sub_ref(const_cast<uint64_t*>(ct3), L, c.logn, 3, 2, 1);
+  PolyRef dst = plain_ref(digits, L, c.logn);
+  ntt_backward(c, src, dst, count, st);
+  key_switch(rk, dst, count, ct3, 3 * L * N, 0, ct3 + L * N, 3 * L * N, out, 2 * L * N, D, st);
+}
+
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st) {
   require_same_level_key(gk);

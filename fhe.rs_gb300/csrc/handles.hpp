@@ -1,0 +1,31 @@
+// Definitions of the opaque handle types of include/fheg.h.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "fheg.h"
+#include "lib.hpp"
+
+struct fheg_context {
+  std::shared_ptr<fheg::Context> c;
+};
+struct fheg_scaler {
+  std::unique_ptr<fheg::Scaler> s;
+  fheg::DevBuf scratch;
+};
+struct fheg_params {
+  std::unique_ptr<fheg::Params> p;
+  std::vector<fheg_context> level_handles;
+};
+struct fheg_ksk {
+  fheg::Ksk k;
+};
+struct fheg_multiplicator {
+  std::unique_ptr<fheg::Multiplicator> m;
+  cudaStream_t copy_stream = nullptr;
+  ~fheg_multiplicator() {
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+  }
+};
+

@@ -6,6 +6,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -40,6 +41,8 @@ struct DevBuf {
 };
 
 void upload(void* dst, const void* src, size_t bytes);
+// Sets the message returned by fheg_last_error() on this thread.
+void set_last_error(const std::string& msg);
 
 // NTT tables of one prime for one degree, resident on one device. Shared by
 // every context that uses the prime (registry keyed by device, p, n, root).
@@ -190,6 +193,8 @@ std::unique_ptr<Multiplicator> make_multiplicator(const Params& par, size_t leve
 std::unique_ptr<Multiplicator> make_default_multiplicator(const Ksk& rk);
 
 void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st);
+void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, uint64_t* digits,
+                         uint64_t* D, cudaStream_t st);
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,

@@ -230,4 +230,25 @@ FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* 
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs,
                                               const uint64_t* h_rhs, uint64_t* h_out, size_t count);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free relinearization.                                           */
+
+/* No counterpart in the reference: this entry point exists for callers of
+ * this library that cannot let it allocate device memory, such as code
+ * recording into a CUDA stream capture (cudaMalloc cannot be captured),
+ * serving loops that must not stall on an allocation, and applications that
+ * give all device memory to their own pool. It computes what
+ * fheg_relinearize computes (d_ct3 [count][3][L][N] Ntt -> d_out
+ * [count][2][L][N] Ntt) and calls no cudaMalloc / cudaFree: its scratch is a
+ * fixed 16 MiB device array inside the library, which every GPU that loads the
+ * library holds until the process exits. A call needs
+ * 8 * count * L * N * (1 + L_ksk) bytes (each of its two regions rounded up to
+ * 256 bytes); larger batches are rejected with FHEG_ERR_INVALID_ARGUMENT
+ * (split them). The first call on a device looks the array's address up, so
+ * make it before any stream capture. All calls share the array and it keeps
+ * the last call's contents: calls whose work overlaps on the GPU (different
+ * streams, or different threads without ordering) race on it. */
+FHEG_API int fheg_relinearize_noalloc(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
+                                      void* stream);
+
 #endif /* FHEG_H */
