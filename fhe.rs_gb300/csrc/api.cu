@@ -293,12 +293,9 @@ FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, si
       if (count != k.ctx_ct->L()) throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
       k.count = count;
       const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
-      k.keys.alloc(4 * words * 8);
+      k.keys.alloc(2 * words * 8);
       upload(k.values(0), h_c0, words * 8);
       upload(k.values(1), h_c1, words * 8);
-      compute_shoup(*k.ctx_ksk, k.values(0), k.shoup(0), count, nullptr);
-      compute_shoup(*k.ctx_ksk, k.values(1), k.shoup(1), count, nullptr);
-      check_cuda(cudaDeviceSynchronize(), "ksk upload");
     } catch (...) {
       delete h;
       throw;

@@ -9,10 +9,10 @@
 //   C  forward NTT of the new limbs                            (M - L limbs)
 //   D  tensor product fused into the inverse NTT               (3B x M limbs)
 //   E  t/Q scale-and-round per coefficient                     (rns_scale)
-//   F1 digit expansion: lazy forward NTT of every digit of c2 in every key
-//      modulus (key_switching_key.rs:227-235, rq/mod.rs:518-540)
-//   F2 forward NTT of c0, c1 fused with the key inner product and the final
-//      additions (key_switching_key.rs:236-238, mul.rs:208-210)
+//   F  one launch of forward NTTs: every digit of c2 in every key modulus
+//      (key_switching_key.rs:227-235, rq/mod.rs:518-540) and c0, c1
+//   G  key inner product and the final additions, exact 128-bit sums
+//      reduced once (key_switching_key.rs:236-238, mul.rs:208-210)
 // c2 is consumed in the power basis straight out of E: the reference's
 // forward NTT of c2 followed by `into_power_basis` is the identity.
 
@@ -101,34 +101,37 @@ struct SrcSubst {
   }
 };
 
-// Epilogue of F2: out = v + sum_d NTT(digit_d) * key_part[d] (mod q_j).
-struct DstMac {
-  PolyRef D;  // poly b * ndig + d, limb j (lazy NTT values)
-  const uint64_t* k[2];
-  const uint64_t* ks[2];
-  PolyRef out;  // poly b * 2 + part
-  uint32_t ndig, lk, logn;
-  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime& pr, uint32_t i, uint64_t v) const {
-    const uint32_t b = j.poly >> 1, part = j.poly & 1;
-    uint64_t lo = v, hi = 0;
-    const uint64_t* kp = k[part];
-    const uint64_t* ksp = ks[part];
-    for (uint32_t d = 0; d < ndig; d++) {
-      const uint64_t off = (((uint64_t)d * lk + j.limb) << logn) + i;
-      const uint64_t t = mul_shoup_lazy(D.at(b * ndig + d, j.limb)[i], __ldg(kp + off), __ldg(ksp + off), pr.p);
-      lo += t;
-      hi += lo < t;
-    }
-    out.at(j.poly, j.limb)[i] = reduce128(hi, lo, pr);
+// F stage of the multiplication: polynomials [0, B*L) are the digits of c2
+// (digit d of ciphertext b is polynomial b*L + d, lazily reduced into key
+// limb j), polynomials [B*L, B*L + 2B) are c0 and c1 of each product.
+struct SrcKsF {
+  PolyRef digits;  // c2 rows: poly b, limb d
+  PolyRef c01;     // c0 / c1: poly 2b + part
+  uint32_t ndig, ndig_polys;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
+    if (j.poly < ndig_polys) return reduce64_lazy(digits.at(j.poly / ndig, j.poly % ndig)[i], pr);
+    return c01.at(j.poly - ndig_polys, j.limb)[i];
   }
 };
 
-// Element-wise inner product for relinearization / rotations:
-// out_part[j] = add_part[j] + sum_d D[d][j] * key_part[d][j].
-__global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const uint64_t* k0s,
-                          const uint64_t* k1, const uint64_t* k1s, const uint64_t* add0, uint64_t add0_stride,
-                          uint64_t add0_e, const uint64_t* add1, uint64_t add1_stride, uint64_t* out,
-                          uint64_t out_stride, uint32_t ndig, uint32_t lk, uint32_t logn, uint64_t total) {
+struct DstKsF {
+  PolyRef D;    // poly b*L + d
+  PolyRef out;  // poly 2b + part
+  uint32_t ndig_polys;
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    if (j.poly < ndig_polys) D.at(j.poly, j.limb)[i] = v;
+    else out.at(j.poly - ndig_polys, j.limb)[i] = v;
+  }
+};
+
+// Key inner product for relinearization, rotations and the multiplication:
+// out_part[j] = add_part[j] + sum_d D[d][j] * key_part[d][j] (mod q_j), with
+// D and the keys canonical, so each product is below 2^124 and up to 15
+// products are summed exactly before a Barrett reduction.
+__global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const uint64_t* k1,
+                          const uint64_t* add0, uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1,
+                          uint64_t add1_stride, uint64_t* out, uint64_t out_stride, uint32_t ndig, uint32_t lk,
+                          uint32_t logn, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
@@ -139,42 +142,23 @@ __global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0,
   uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
   if (add0) lo0 = add0[b * add0_stride + ((uint64_t)j << logn) + (add0_e ? gather_index(i, add0_e, logn) : i)];
   if (add1) lo1 = add1[b * add1_stride + ((uint64_t)j << logn) + i];
+  const uint64_t kstride = (uint64_t)lk << logn;
+  const uint64_t* kp0 = k0 + ((uint64_t)j << logn) + i;
+  const uint64_t* kp1 = k1 + ((uint64_t)j << logn) + i;
   for (uint32_t d = 0; d < ndig; d++) {
     const uint64_t x = D.at(b * ndig + d, j)[i];
-    const uint64_t off = (((uint64_t)d * lk + j) << logn) + i;
-    const uint64_t t0 = mul_shoup_lazy(x, __ldg(k0 + off), __ldg(k0s + off), pr.p);
-    const uint64_t t1 = mul_shoup_lazy(x, __ldg(k1 + off), __ldg(k1s + off), pr.p);
-    lo0 += t0;
-    hi0 += lo0 < t0;
-    lo1 += t1;
-    hi1 += lo1 < t1;
+    mac128(hi0, lo0, x, __ldg(kp0 + d * kstride));
+    mac128(hi1, lo1, x, __ldg(kp1 + d * kstride));
+    if (d % 15 == 14) {
+      lo0 = reduce128(hi0, lo0, pr);
+      hi0 = 0;
+      lo1 = reduce128(hi1, lo1, pr);
+      hi1 = 0;
+    }
   }
   uint64_t* o = out + b * out_stride + ((uint64_t)j << logn) + i;
   o[0] = reduce128(hi0, lo0, pr);
-  o[(uint64_t)lk << logn] = reduce128(hi1, lo1, pr);
-}
-
-// Shoup companions floor(v * 2^64 / p) of key values (zq/mod.rs:195-199).
-__global__ void k_shoup(const DevPrime* primes, const uint64_t* v, uint64_t* out, uint32_t limbs, uint32_t logn,
-                        uint64_t total) {
-  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const uint32_t limb = (gid >> logn) % limbs;
-  const DevPrime pr = primes[limb];
-  const uint64_t x = v[gid];
-  // Estimate with the Barrett constant, then correct (at most a few steps).
-  uint64_t q = x * pr.bhi + __umul64hi(x, pr.blo);
-  uint64_t plo = q * pr.p, phi = __umul64hi(q, pr.p);
-  // r = x * 2^64 - q * p (128-bit, small and non-negative when q <= true q)
-  uint64_t rlo = 0 - plo;
-  uint64_t rhi = x - phi - (plo != 0);
-  for (int it = 0; it < 4 && (rhi != 0 || rlo >= pr.p); it++) {
-    const uint64_t nlo = rlo - pr.p;
-    rhi -= (rlo < pr.p);
-    rlo = nlo;
-    q++;
-  }
-  out[gid] = q;
+  o[kstride] = reduce128(hi1, lo1, pr);
 }
 
 // ---------------------------------------------------------------------------
@@ -188,21 +172,13 @@ void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* ad
   const uint32_t logn = kc.logn;
   PolyRef dref = plain_ref(D, Lk, logn);
   NttGeom g{kc.primes_dev(), (uint32_t)Lk, 0};
-  // F1: every digit in every key modulus, lazy output (rq/mod.rs:518-540).
-  ntt_forward_any<false>(logn, g, batch * nd, SrcDigit{digits, (uint32_t)nd}, DstPoly{dref}, st);
+  // Every digit in every key modulus (rq/mod.rs:518-540), reduced output.
+  ntt_forward_any<true>(logn, g, batch * nd, SrcDigit{digits, (uint32_t)nd}, DstPoly{dref}, st);
   const uint64_t total = batch * Lk << logn;
-  k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(kc.primes_dev(), dref, k.values(0), k.shoup(0), k.values(1),
-                                                 k.shoup(1), add0, add0_poly_stride, add0_exponent, add1,
-                                                 add1_poly_stride, out, out_poly_stride, (uint32_t)nd, (uint32_t)Lk,
-                                                 logn, total);
+  k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(kc.primes_dev(), dref, k.values(0), k.values(1), add0,
+                                                 add0_poly_stride, add0_exponent, add1, add1_poly_stride, out,
+                                                 out_poly_stride, (uint32_t)nd, (uint32_t)Lk, logn, total);
   after_launch("k_key_mac");
-}
-
-void compute_shoup(const Context& c, const uint64_t* vals, uint64_t* out, uint64_t polys, cudaStream_t st) {
-  const uint64_t total = polys * c.L() << c.logn;
-  if (total == 0) return;
-  k_shoup<<<nblocks(total, 256), 256, 0, st>>>(c.primes_dev(), vals, out, (uint32_t)c.L(), c.logn, total);
-  after_launch("k_shoup");
 }
 
 static void require_same_level_key(const Ksk& k) {
@@ -381,37 +357,27 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st);
   NttGeom gb{bc.primes_dev(), (uint32_t)L, 0};
   if (rk) {
-    // F1: digits of c2 in every key modulus.
     const Context& kc = *rk->ctx_ksk;
     PolyRef dref = plain_ref(D, Lk, logn);
     PolyRef c2 = sub_ref(dn, L, logn, 3, 2, 1);
-    NttGeom gk{kc.primes_dev(), (uint32_t)Lk, 0};
-    ntt_forward_any<false>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L}, DstPoly{dref}, st);
-    // F2: forward NTT of c0, c1 with the key inner product in the epilogue.
     PolyRef c01 = sub_ref(dn, L, logn, 3, 0, 2);
-    DstMac mac;
-    mac.D = dref;
-    mac.k[0] = rk->values(0);
-    mac.k[1] = rk->values(1);
-    mac.ks[0] = rk->shoup(0);
-    mac.ks[1] = rk->shoup(1);
-    mac.out = plain_ref(dest, L, logn);
-    mac.ndig = (uint32_t)L;
-    mac.lk = (uint32_t)Lk;
-    mac.logn = logn;
+    PolyRef oref = plain_ref(dest, L, logn);
+    NttGeom gk{kc.primes_dev(), (uint32_t)Lk, 0};
     if (logn <= kMaxSmemLogN) {
-      ntt_fwd_single<true>(logn, gb, 2 * count, SrcPoly{c01}, mac, st);
+      // F: digit NTTs and the c0 / c1 NTTs in one launch (Lk == L).
+      const uint32_t ndp = (uint32_t)(count * L);
+      ntt_fwd_single<true>(logn, gk, count * L + 2 * count, SrcKsF{c2, c01, (uint32_t)L, ndp},
+                           DstKsF{dref, oref, ndp}, st);
     } else {
-      // Two-pass sizes: forward into the output, then apply the inner product.
-      PolyRef o = plain_ref(dest, L, logn);
-      ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{o}, st);
-      const uint64_t total = count * L << logn;
-      k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(bc.primes_dev(), dref, rk->values(0), rk->shoup(0),
-                                                     rk->values(1), rk->shoup(1), dest, 2 * L * N, 0, dest + L * N,
-                                                     2 * L * N, dest, 2 * L * N, (uint32_t)L, (uint32_t)Lk, logn,
-                                                     total);
-      after_launch("k_key_mac");
+      ntt_forward_any<true>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L}, DstPoly{dref}, st);
+      ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st);
     }
+    // G: key inner product added to c0, c1 in place.
+    const uint64_t total = count * L << logn;
+    k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest,
+                                                   2 * L * N, 0, dest + L * N, 2 * L * N, dest, 2 * L * N,
+                                                   (uint32_t)L, (uint32_t)Lk, logn, total);
+    after_launch("k_key_mac");
   } else {
     PolyRef o = plain_ref(dest, L, logn);
     ntt_forward_any<true>(logn, gb, 3 * count, SrcPoly{dnref}, DstPoly{o}, st);

@@ -22,10 +22,11 @@ struct DevPrime {
   uint64_t bhi, blo;    // floor(2^128 / p), the Barrett constant of zq/mod.rs:83-98
   uint64_t ninv;        // N^-1 mod p
   uint64_t ninv_shoup;  // Shoup companion of ninv
-  const uint64_t* w;    // omegas (bit-reversed powers of the 2N-th root), native.rs:51-56
-  const uint64_t* ws;   // Shoup companions of w
-  const uint64_t* zi;   // zetas_inv
-  const uint64_t* zis;  // Shoup companions of zi
+  // Twiddle tables of native.rs:35-73, each entry paired with its Shoup
+  // companion so one 16-byte load fetches both: tw[i] = (omegas[i],
+  // omegas_shoup[i]), itw[i] = (zetas_inv[i], zetas_inv_shoup[i]).
+  const ulonglong2* tw;
+  const ulonglong2* itw;
 };
 
 // Counts every kernel launch issued by the library (reported by benchmarks).
@@ -82,13 +83,120 @@ inline PolyRef sub_ref(uint64_t* base, size_t limbs, uint32_t logn, uint32_t grp
 // ---------------------------------------------------------------------------
 // Device arithmetic
 
-// zq/mod.rs:224-234 `lazy_mul_shoup`: a * b mod p in [0, 2p) for any a < 2^64.
+// zq/mod.rs:224-234 `lazy_mul_shoup`: a * b mod p in [0, 2p) for any a < 2^64,
+// with b_shoup = floor(b * 2^64 / p). (Measured against hand-written 32-bit
+// PTX sequences on GB300, this form issues the fewest instructions.)
 __device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t a, uint64_t b, uint64_t b_shoup, uint64_t p) {
-  uint64_t q = __umul64hi(a, b_shoup);
-  return a * b - q * p;
+  return a * b - __umul64hi(a, b_shoup) * p;
 }
 
-__device__ __forceinline__ uint64_t reduce_once(uint64_t x, uint64_t p) { return x >= p ? x - p : x; }
+// Exact multiply-accumulate into a 128-bit accumulator (hi:lo) += a * b.
+// The caller guarantees the sum stays below 2^128.
+__device__ __forceinline__ void mac128(uint64_t& hi, uint64_t& lo, uint64_t a, uint64_t b) {
+  asm("{\n\t"
+      ".reg .u32 a0, a1, b0, b1, w0, w1, w2, w3;\n\t"
+      "mov.b64 {a0, a1}, %2;\n\t"
+      "mov.b64 {b0, b1}, %3;\n\t"
+      "mov.b64 {w0, w1}, %1;\n\t"
+      "mov.b64 {w2, w3}, %0;\n\t"
+      "mad.lo.cc.u32 w0, a0, b0, w0;\n\t"
+      "madc.hi.cc.u32 w1, a0, b0, w1;\n\t"
+      "madc.lo.cc.u32 w2, a1, b1, w2;\n\t"
+      "madc.hi.u32 w3, a1, b1, w3;\n\t"
+      "mad.lo.cc.u32 w1, a0, b1, w1;\n\t"
+      "madc.hi.cc.u32 w2, a0, b1, w2;\n\t"
+      "addc.u32 w3, w3, 0;\n\t"
+      "mad.lo.cc.u32 w1, a1, b0, w1;\n\t"
+      "madc.hi.cc.u32 w2, a1, b0, w2;\n\t"
+      "addc.u32 w3, w3, 0;\n\t"
+      "mov.b64 %1, {w0, w1};\n\t"
+      "mov.b64 %0, {w2, w3};\n\t"
+      "}"
+      : "+l"(hi), "+l"(lo)
+      : "l"(a), "l"(b));
+}
+
+// w[0..6) (192 bits, 32-bit words) += x * (bhi:blo) for x < 2^64, b < 2^128.
+// The caller guarantees the sum stays below 2^192.
+__device__ __forceinline__ void mac192(uint32_t* w, uint64_t x, uint64_t blo, uint64_t bhi) {
+  asm("{\n\t"
+      ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
+      "mov.b64 {x0, x1}, %6;\n\t"
+      "mov.b64 {b0, b1}, %7;\n\t"
+      "mov.b64 {b2, b3}, %8;\n\t"
+      "mad.lo.cc.u32 %0, x0, b0, %0;\n\t"
+      "madc.lo.cc.u32 %1, x0, b1, %1;\n\t"
+      "madc.lo.cc.u32 %2, x0, b2, %2;\n\t"
+      "madc.lo.cc.u32 %3, x0, b3, %3;\n\t"
+      "addc.cc.u32 %4, %4, 0;\n\t"
+      "addc.u32 %5, %5, 0;\n\t"
+      "mad.hi.cc.u32 %1, x0, b0, %1;\n\t"
+      "madc.hi.cc.u32 %2, x0, b1, %2;\n\t"
+      "madc.hi.cc.u32 %3, x0, b2, %3;\n\t"
+      "madc.hi.cc.u32 %4, x0, b3, %4;\n\t"
+      "addc.u32 %5, %5, 0;\n\t"
+      "mad.lo.cc.u32 %1, x1, b0, %1;\n\t"
+      "madc.lo.cc.u32 %2, x1, b1, %2;\n\t"
+      "madc.lo.cc.u32 %3, x1, b2, %3;\n\t"
+      "madc.lo.cc.u32 %4, x1, b3, %4;\n\t"
+      "addc.u32 %5, %5, 0;\n\t"
+      "mad.hi.cc.u32 %2, x1, b0, %2;\n\t"
+      "madc.hi.cc.u32 %3, x1, b1, %3;\n\t"
+      "madc.hi.cc.u32 %4, x1, b2, %4;\n\t"
+      "madc.hi.u32 %5, x1, b3, %5;\n\t"
+      "}"
+      : "+r"(w[0]), "+r"(w[1]), "+r"(w[2]), "+r"(w[3]), "+r"(w[4]), "+r"(w[5])
+      : "l"(x), "l"(blo), "l"(bhi));
+}
+
+// w[0..8) (256 bits, 32-bit words) += x * (bhi:blo) for x < 2^64, b < 2^128,
+// wrapping modulo 2^256.
+__device__ __forceinline__ void mac256(uint32_t* w, uint64_t x, uint64_t blo, uint64_t bhi) {
+  asm("{\n\t"
+      ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
+      "mov.b64 {x0, x1}, %8;\n\t"
+      "mov.b64 {b0, b1}, %9;\n\t"
+      "mov.b64 {b2, b3}, %10;\n\t"
+      "mad.lo.cc.u32 %0, x0, b0, %0;\n\t"
+      "madc.lo.cc.u32 %1, x0, b1, %1;\n\t"
+      "madc.lo.cc.u32 %2, x0, b2, %2;\n\t"
+      "madc.lo.cc.u32 %3, x0, b3, %3;\n\t"
+      "addc.cc.u32 %4, %4, 0;\n\t"
+      "addc.cc.u32 %5, %5, 0;\n\t"
+      "addc.cc.u32 %6, %6, 0;\n\t"
+      "addc.u32 %7, %7, 0;\n\t"
+      "mad.hi.cc.u32 %1, x0, b0, %1;\n\t"
+      "madc.hi.cc.u32 %2, x0, b1, %2;\n\t"
+      "madc.hi.cc.u32 %3, x0, b2, %3;\n\t"
+      "madc.hi.cc.u32 %4, x0, b3, %4;\n\t"
+      "addc.cc.u32 %5, %5, 0;\n\t"
+      "addc.cc.u32 %6, %6, 0;\n\t"
+      "addc.u32 %7, %7, 0;\n\t"
+      "mad.lo.cc.u32 %1, x1, b0, %1;\n\t"
+      "madc.lo.cc.u32 %2, x1, b1, %2;\n\t"
+      "madc.lo.cc.u32 %3, x1, b2, %3;\n\t"
+      "madc.lo.cc.u32 %4, x1, b3, %4;\n\t"
+      "addc.cc.u32 %5, %5, 0;\n\t"
+      "addc.cc.u32 %6, %6, 0;\n\t"
+      "addc.u32 %7, %7, 0;\n\t"
+      "mad.hi.cc.u32 %2, x1, b0, %2;\n\t"
+      "madc.hi.cc.u32 %3, x1, b1, %3;\n\t"
+      "madc.hi.cc.u32 %4, x1, b2, %4;\n\t"
+      "madc.hi.cc.u32 %5, x1, b3, %5;\n\t"
+      "addc.cc.u32 %6, %6, 0;\n\t"
+      "addc.u32 %7, %7, 0;\n\t"
+      "}"
+      : "+r"(w[0]), "+r"(w[1]), "+r"(w[2]), "+r"(w[3]), "+r"(w[4]), "+r"(w[5]), "+r"(w[6]), "+r"(w[7])
+      : "l"(x), "l"(blo), "l"(bhi));
+}
+
+// x >= m ? x - m : x with a predicated subtraction.
+__device__ __forceinline__ uint64_t csub(uint64_t x, uint64_t m) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ge.u64 q, %0, %1;\n\t@q sub.u64 %0, %0, %1;\n\t}" : "+l"(x) : "l"(m));
+  return x;
+}
+
+__device__ __forceinline__ uint64_t reduce_once(uint64_t x, uint64_t p) { return csub(x, p); }
 
 __device__ __forceinline__ uint64_t mul_shoup(uint64_t a, uint64_t b, uint64_t b_shoup, uint64_t p) {
   return reduce_once(mul_shoup_lazy(a, b, b_shoup, p), p);
@@ -135,8 +243,8 @@ __device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uint64_t p) 
 // Harvey forward butterfly (native.rs:256-269): x, y in [0, 4p) -> [0, 4p).
 __device__ __forceinline__ void fwd_bfly(uint64_t& x, uint64_t& y, uint64_t w, uint64_t ws, uint64_t p,
                                          uint64_t p2) {
-  uint64_t a = x >= p2 ? x - p2 : x;
-  uint64_t t = mul_shoup_lazy(y, w, ws, p);
+  const uint64_t a = csub(x, p2);
+  const uint64_t t = mul_shoup_lazy(y, w, ws, p);
   x = a + t;
   y = a + p2 - t;
 }
@@ -144,16 +252,12 @@ __device__ __forceinline__ void fwd_bfly(uint64_t& x, uint64_t& y, uint64_t w, u
 // Gentleman-Sande inverse butterfly (native.rs:288-300): x, y in [0, 2p).
 __device__ __forceinline__ void inv_bfly(uint64_t& x, uint64_t& y, uint64_t z, uint64_t zs, uint64_t p,
                                          uint64_t p2) {
-  uint64_t t = x;
-  uint64_t s = x + y;
-  x = s >= p2 ? s - p2 : s;
+  const uint64_t t = x;
+  x = csub(x + y, p2);
   y = mul_shoup_lazy(t + p2 - y, z, zs, p);
 }
 
 // native.rs:238-243 `reduce3`: [0, 4p) -> [0, p).
-__device__ __forceinline__ uint64_t reduce4(uint64_t x, uint64_t p, uint64_t p2) {
-  x = x >= p2 ? x - p2 : x;
-  return x >= p ? x - p : x;
-}
+__device__ __forceinline__ uint64_t reduce4(uint64_t x, uint64_t p, uint64_t p2) { return csub(csub(x, p2), p); }
 
 }  // namespace fheg

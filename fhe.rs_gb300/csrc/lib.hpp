@@ -48,7 +48,7 @@ void set_last_error(const std::string& msg);
 // every context that uses the prime (registry keyed by device, p, n, root).
 struct PrimeTables {
   NttTablesHost host;
-  DevBuf tables;  // 4 * n words: omegas, omegas_shoup, zetas_inv, zetas_inv_shoup
+  DevBuf tables;  // 4 * n words: (omega, shoup) pairs, then (zeta_inv, shoup) pairs
   DevPrime dev;
 };
 std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t root);
@@ -90,6 +90,7 @@ struct ScalerDev {
   const uint64_t* to_sign;      // theta_omega sign [from]
   const uint64_t* tgar_lo;      // theta_garner lo [from]
   const uint64_t* tgar_hi;      // theta_garner hi [from]
+  const uint64_t* gamma_neg;    // (q_j - gamma_j) mod q_j [to]
   const DevPrime* to_primes;    // [to]
 };
 
@@ -153,13 +154,10 @@ struct Ksk {
   size_t ciphertext_level = 0, ksk_level = 0;
   std::shared_ptr<Context> ctx_ct, ctx_ksk;
   size_t count = 0;  // digits = moduli of the ciphertext context
-  // [2 parts][count][Lk][N] values, then the same layout of Shoup companions.
+  // [2 parts][count][Lk][N] values (canonical, Ntt representation).
   DevBuf keys;
   mutable Workspace ws;  // scratch of relinearize / galois_relinearize
   uint64_t* values(int part) const { return keys.u64() + (size_t)part * count * ctx_ksk->L() * ctx_ksk->N(); }
-  uint64_t* shoup(int part) const {
-    return keys.u64() + (size_t)(2 + part) * count * ctx_ksk->L() * ctx_ksk->N();
-  }
 };
 
 
@@ -169,8 +167,7 @@ struct Ksk {
 void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* add0, uint64_t add0_poly_stride,
                 uint64_t add0_exponent, const uint64_t* add1, uint64_t add1_poly_stride, uint64_t* out,
                 uint64_t out_poly_stride, uint64_t* D, cudaStream_t st);
-// Shoup companions of the Ntt values of `polys` polynomials over context c.
-void compute_shoup(const Context& c, const uint64_t* vals, uint64_t* out, uint64_t polys, cudaStream_t st);
+
 
 struct Multiplicator {
   const Params* par = nullptr;

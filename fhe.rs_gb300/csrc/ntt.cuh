@@ -52,21 +52,29 @@ __device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
   return j;
 }
 
-// Shared-memory swizzle: XOR bits 4-5 into bits 0-1 and bits 6-7 into bits
-// 2-3 of the word index. Every access pattern of the rounds below then maps
-// the 16 threads of a half warp to 16 distinct 8-byte bank pairs.
-__device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 3) ^ (((i >> 6) & 3) << 2); }
+// Shared-memory swizzle: the low 4 bits of the word index are XORed with
+// bits 4-7 and 5-8. Every access pattern of the rounds below (and of the
+// coalesced staging) then maps the 16 threads of a half warp to 16 distinct
+// 8-byte bank pairs, for every supported size.
+__device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 15) ^ ((i >> 5) & 15); }
 
+// 32 residues per thread (16 for tiny sizes): radix-32 rounds, 512 threads
+// and a 128-register budget at N = 2^14.
 template <int LOGN>
 struct NttShape {
+  static constexpr int LOGE = LOGN < 5 ? LOGN : 5;
+  static constexpr int E = 1 << LOGE;
   static constexpr int N = 1 << LOGN;
-  static constexpr int E = N < 16 ? N : 16;  // residues per thread
-  static constexpr int T = N / E;            // threads per CTA
+  static constexpr int T = N / E;
+  // At least 512 threads' worth of blocks per SM: caps registers at 128.
+  static constexpr int MIN_BLOCKS = T >= 512 ? 1 : (512 / T > 32 ? 32 : 512 / T);
 };
 
 // One forward round: global stages S0 .. S0+K-1 of a transform of size 2^LOGN
 // held as E residues per thread (E / 2^K groups of 2^K). Group g holds
-// elements c * 2^(LOGN-S0) + b + t * 2^(LOGN-S0-K) for t < 2^K.
+// elements c * 2^(LOGN-S0) + b + t * 2^(LOGN-S0-K) for t < 2^K. The stage
+// with 2^s chunks uses omegas[2^s * tw_mult + chunk] (tw_mult = 1 for a whole
+// transform); the 2^r twiddles a group needs at round stage r are contiguous.
 template <int LOGN, int S0, int K>
 __device__ __forceinline__ void fwd_round(uint64_t* x, uint32_t tid, const DevPrime& pr, uint32_t tw_mult) {
   constexpr int E = NttShape<LOGN>::E;
@@ -81,16 +89,13 @@ __device__ __forceinline__ void fwd_round(uint64_t* x, uint32_t tid, const DevPr
 #pragma unroll
     for (int r = 0; r < K; r++) {
       const int half = 1 << (K - 1 - r);
+      const ulonglong2* twr = pr.tw + (1u << (S0 + r)) * tw_mult + (c << r);
+      // Constant trip counts at every level keep x[] in registers.
 #pragma unroll
-      for (int k = 0; k < (1 << r); k++) {
-        const uint32_t idx = (1u << (S0 + r)) * tw_mult + (c << r) + k;
-        const uint64_t w = __ldg(pr.w + idx);
-        const uint64_t ws = __ldg(pr.ws + idx);
-#pragma unroll
-        for (int u = 0; u < half; u++) {
-          const int t = (k << (K - r)) + u;
-          fwd_bfly(xx[t], xx[t + half], w, ws, pr.p, pr.p2);
-        }
+      for (int t = 0; t < (1 << K); t++) {
+        if (t & half) continue;
+        const ulonglong2 w = __ldg(twr + (t >> (K - r)));
+        fwd_bfly(xx[t], xx[t + half], w.x, w.y, pr.p, pr.p2);
       }
     }
   }
@@ -121,14 +126,15 @@ __device__ __forceinline__ void fwd_from_smem(uint64_t* x, const uint64_t* sm, u
   for (int e = 0; e < E; e++) x[e] = sm[swz(fwd_index<LOGN, S0, K>(tid, e >> K, e & ((1 << K) - 1)))];
 }
 
-// Applies forward rounds S0, S0+4, ... up to LOGN, exchanging through smem.
+// Applies forward rounds S0, S0+LOGE, ... up to LOGN, exchanging through smem.
 template <int LOGN, int S0>
 __device__ __forceinline__ void fwd_rounds(uint64_t* x, uint64_t* sm, uint32_t tid, const DevPrime& pr,
                                            uint32_t tw_mult) {
-  constexpr int K = (LOGN - S0) < 4 ? (LOGN - S0) : 4;
+  constexpr int LOGE = NttShape<LOGN>::LOGE;
+  constexpr int K = (LOGN - S0) < LOGE ? (LOGN - S0) : LOGE;
   fwd_round<LOGN, S0, K>(x, tid, pr, tw_mult);
   if constexpr (S0 + K < LOGN) {
-    constexpr int K2 = (LOGN - S0 - K) < 4 ? (LOGN - S0 - K) : 4;
+    constexpr int K2 = (LOGN - S0 - K) < LOGE ? (LOGN - S0 - K) : LOGE;
     __syncthreads();
     fwd_to_smem<LOGN, S0, K>(x, sm, tid);
     __syncthreads();
@@ -146,10 +152,9 @@ __device__ __forceinline__ void fwd_rounds(uint64_t* x, uint64_t* sm, uint32_t t
 // `beta` of a transform of size 2^(LOGN + s1) whose first s1 stages already
 // ran (ntt_fwd_top). REDUCE selects reduced ([0, p)) or lazy ([0, 4p)) output.
 template <int LOGN, bool REDUCE, class Src, class Dst>
-__global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_fwd(NttGeom g, Src src, Dst dst) {
+__global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS) k_ntt_fwd(NttGeom g, Src src, Dst dst) {
   constexpr int E = NttShape<LOGN>::E;
   constexpr int T = NttShape<LOGN>::T;
-  constexpr int N = 1 << LOGN;
   extern __shared__ uint64_t sm[];
   const uint32_t tid = threadIdx.x;
   const NttJob jb = decode_job(g);
@@ -167,7 +172,6 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_fwd(NttGeom g, Src sr
     if (REDUCE) v = reduce4(v, pr.p, pr.p2);
     dst(jb, pr, base + i, v);
   }
-  (void)N;
 }
 
 // ---------------------------------------------------------------------------
@@ -197,17 +201,13 @@ __device__ __forceinline__ void inv_round(uint64_t* x, uint32_t tid, const DevPr
     for (int r = 0; r < K; r++) {
       // m_local = N_local / (2l) chunks of this block at this stage.
       const uint32_t m_local = 1u << (LOGN - 1 - U0 - r);
-      const uint32_t idx0 = n_total - (m_local << (s1 + 1)) + beta * m_local + (c << (K - 1 - r));
+      const ulonglong2* twr = pr.itw + (n_total - (m_local << (s1 + 1)) + beta * m_local + (c << (K - 1 - r)));
       const int span = 1 << r;
 #pragma unroll
-      for (int k = 0; k < (1 << (K - 1 - r)); k++) {
-        const uint64_t z = __ldg(pr.zi + idx0 + k);
-        const uint64_t zs = __ldg(pr.zis + idx0 + k);
-#pragma unroll
-        for (int u = 0; u < span; u++) {
-          const int t = (k << (r + 1)) + u;
-          inv_bfly(xx[t], xx[t + span], z, zs, pr.p, pr.p2);
-        }
+      for (int t = 0; t < (1 << K); t++) {
+        if (t & span) continue;
+        const ulonglong2 z = __ldg(twr + (t >> (r + 1)));
+        inv_bfly(xx[t], xx[t + span], z.x, z.y, pr.p, pr.p2);
       }
     }
   }
@@ -228,18 +228,20 @@ __device__ __forceinline__ void inv_from_smem(uint64_t* x, const uint64_t* sm, u
 }
 
 // Size of the first inverse round: the remainder, so that later rounds are
-// radix-16 and the last round stores coalesced.
+// full and the last round stores coalesced.
 template <int LOGN>
 struct InvFirst {
-  static constexpr int K = (LOGN % 4) ? (LOGN % 4) : (LOGN < 4 ? LOGN : 4);
+  static constexpr int LOGE = NttShape<LOGN>::LOGE;
+  static constexpr int K = (LOGN % LOGE) ? (LOGN % LOGE) : LOGE;
 };
 
 template <int LOGN, int U0, int K>
 __device__ __forceinline__ void inv_rounds(uint64_t* x, uint64_t* sm, uint32_t tid, const DevPrime& pr,
                                            uint32_t n_total, uint32_t s1, uint32_t beta) {
+  constexpr int LOGE = NttShape<LOGN>::LOGE;
   inv_round<LOGN, U0, K>(x, tid, pr, n_total, s1, beta);
   if constexpr (U0 + K < LOGN) {
-    constexpr int K2 = (LOGN - U0 - K) < 4 ? (LOGN - U0 - K) : 4;
+    constexpr int K2 = (LOGN - U0 - K) < LOGE ? (LOGN - U0 - K) : LOGE;
     __syncthreads();
     inv_to_smem<LOGN, U0, K>(x, sm, tid);
     __syncthreads();
@@ -252,7 +254,7 @@ __device__ __forceinline__ void inv_rounds(uint64_t* x, uint64_t* sm, uint32_t t
 // With g.s1 = 0 this is the whole `backward`, including the N^-1 scaling
 // (FINAL). With g.s1 > 0 the remaining stages run in ntt_inv_top.
 template <int LOGN, bool FINAL, class Src, class Dst>
-__global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_inv(NttGeom g, Src src, Dst dst) {
+__global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS) k_ntt_inv(NttGeom g, Src src, Dst dst) {
   constexpr int E = NttShape<LOGN>::E;
   constexpr int T = NttShape<LOGN>::T;
   constexpr int K0 = InvFirst<LOGN>::K;
@@ -272,14 +274,63 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T) k_ntt_inv(NttGeom g, Src sr
   inv_from_smem<LOGN, 0, K0>(x, sm, tid);
   inv_rounds<LOGN, 0, K0>(x, sm, tid, pr, 1u << (LOGN + g.s1), g.s1, jb.beta);
   // The last round holds elements tid + e*T (b = tid, c = 0): coalesced stores.
-  constexpr int KL = LOGN < 4 ? LOGN : 4;
 #pragma unroll
   for (int e = 0; e < E; e++) {
     uint64_t v = x[e];
     if (FINAL) v = mul_shoup(v, pr.ninv, pr.ninv_shoup, pr.p);
-    const uint32_t i = (LOGN >= 4) ? (tid + e * T) : inv_index<LOGN, 0, KL>(tid, 0, e);
-    dst(jb, pr, base + i, v);
+    dst(jb, pr, base + tid + e * T, v);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Small transforms (N <= 2^11, used by small parameter sets and tests): one
+// CTA per limb, radix-2 stages in shared memory, the size a runtime value.
+// Same butterflies and twiddle indices as above, so the same outputs.
+
+template <bool REDUCE, class Src, class Dst>
+__global__ void __launch_bounds__(1024) k_ntt_fwd_small(NttGeom g, uint32_t logn, Src src, Dst dst) {
+  extern __shared__ uint64_t sm[];
+  const uint32_t n = 1u << logn, tid = threadIdx.x, nt = blockDim.x;
+  const NttJob jb = decode_job(g);
+  const DevPrime pr = g.primes[jb.limb];
+  for (uint32_t i = tid; i < n; i += nt) sm[i] = src(jb, pr, i);
+  __syncthreads();
+  for (uint32_t s = 0; s < logn; s++) {
+    const uint32_t l = n >> (s + 1);
+    for (uint32_t b = tid; b < n / 2; b += nt) {
+      const uint32_t chunk = b / l, j = chunk * 2 * l + (b % l);
+      const ulonglong2 w = __ldg(pr.tw + (1u << s) + chunk);
+      uint64_t x = sm[j], y = sm[j + l];
+      fwd_bfly(x, y, w.x, w.y, pr.p, pr.p2);
+      sm[j] = x;
+      sm[j + l] = y;
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = tid; i < n; i += nt) dst(jb, pr, i, REDUCE ? reduce4(sm[i], pr.p, pr.p2) : sm[i]);
+}
+
+template <class Src, class Dst>
+__global__ void __launch_bounds__(1024) k_ntt_inv_small(NttGeom g, uint32_t logn, Src src, Dst dst) {
+  extern __shared__ uint64_t sm[];
+  const uint32_t n = 1u << logn, tid = threadIdx.x, nt = blockDim.x;
+  const NttJob jb = decode_job(g);
+  const DevPrime pr = g.primes[jb.limb];
+  for (uint32_t i = tid; i < n; i += nt) sm[i] = src(jb, pr, i);
+  __syncthreads();
+  for (uint32_t l = 1; l < n; l <<= 1) {
+    const uint32_t m = n / (2 * l);
+    for (uint32_t b = tid; b < n / 2; b += nt) {
+      const uint32_t chunk = b / l, j = chunk * 2 * l + (b % l);
+      const ulonglong2 z = __ldg(pr.itw + (n - 2 * m + chunk));
+      uint64_t x = sm[j], y = sm[j + l];
+      inv_bfly(x, y, z.x, z.y, pr.p, pr.p2);
+      sm[j] = x;
+      sm[j + l] = y;
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = tid; i < n; i += nt) dst(jb, pr, i, mul_shoup(sm[i], pr.ninv, pr.ninv_shoup, pr.p));
 }
 
 // ---------------------------------------------------------------------------
@@ -307,8 +358,8 @@ __global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, u
     const int half = 1 << (S1 - 1 - s);
 #pragma unroll
     for (int k = 0; k < (1 << s); k++) {
-      const uint32_t idx = (1u << s) + k;
-      const uint64_t w = __ldg(pr.w + idx), ws = __ldg(pr.ws + idx);
+      const ulonglong2 wp = __ldg(pr.tw + (1u << s) + k);
+      const uint64_t w = wp.x, ws = wp.y;
 #pragma unroll
       for (int u = 0; u < half; u++) {
         const int t = (k << (S1 - s)) + u;
@@ -342,8 +393,8 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
     const uint32_t m = 1u << (S1 - 1 - r);  // chunks at this stage
 #pragma unroll
     for (int k = 0; k < (1 << (S1 - 1 - r)); k++) {
-      const uint32_t idx = n_total - 2 * m + k;
-      const uint64_t z = __ldg(pr.zi + idx), zs = __ldg(pr.zis + idx);
+      const ulonglong2 zp = __ldg(pr.itw + (n_total - 2 * m + k));
+      const uint64_t z = zp.x, zs = zp.y;
 #pragma unroll
       for (int u = 0; u < span; u++) {
         const int t = (k << (r + 1)) + u;
@@ -415,41 +466,37 @@ void launch_inv_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t 
 }
 
 // Dispatch over log2(N) for a single-pass transform (3 <= logn <= 14).
+constexpr uint32_t kMinUnrolledLogN = 12;
+
 template <bool REDUCE, class Src, class Dst>
 void ntt_fwd_single(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
   switch (logn) {
-    case 3: launch_fwd_block<3, REDUCE>(g, polys, src, dst, st); break;
-    case 4: launch_fwd_block<4, REDUCE>(g, polys, src, dst, st); break;
-    case 5: launch_fwd_block<5, REDUCE>(g, polys, src, dst, st); break;
-    case 6: launch_fwd_block<6, REDUCE>(g, polys, src, dst, st); break;
-    case 7: launch_fwd_block<7, REDUCE>(g, polys, src, dst, st); break;
-    case 8: launch_fwd_block<8, REDUCE>(g, polys, src, dst, st); break;
-    case 9: launch_fwd_block<9, REDUCE>(g, polys, src, dst, st); break;
-    case 10: launch_fwd_block<10, REDUCE>(g, polys, src, dst, st); break;
-    case 11: launch_fwd_block<11, REDUCE>(g, polys, src, dst, st); break;
     case 12: launch_fwd_block<12, REDUCE>(g, polys, src, dst, st); break;
     case 13: launch_fwd_block<13, REDUCE>(g, polys, src, dst, st); break;
     case 14: launch_fwd_block<14, REDUCE>(g, polys, src, dst, st); break;
-    default: throw Error(12, "unsupported NTT size");
+    default: {
+      if (logn < 3 || logn > 11) throw Error(12, "unsupported NTT size");
+      const uint32_t threads = logn >= 11 ? 1024 : (1u << (logn - 1));
+      const uint64_t blocks = polys * g.limbs;
+      k_ntt_fwd_small<REDUCE><<<(unsigned)blocks, threads, (sizeof(uint64_t) << logn), st>>>(g, logn, src, dst);
+      after_launch("k_ntt_fwd_small");
+    }
   }
 }
 
 template <bool FINAL, class Src, class Dst>
 void ntt_inv_single(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
   switch (logn) {
-    case 3: launch_inv_block<3, FINAL>(g, polys, src, dst, st); break;
-    case 4: launch_inv_block<4, FINAL>(g, polys, src, dst, st); break;
-    case 5: launch_inv_block<5, FINAL>(g, polys, src, dst, st); break;
-    case 6: launch_inv_block<6, FINAL>(g, polys, src, dst, st); break;
-    case 7: launch_inv_block<7, FINAL>(g, polys, src, dst, st); break;
-    case 8: launch_inv_block<8, FINAL>(g, polys, src, dst, st); break;
-    case 9: launch_inv_block<9, FINAL>(g, polys, src, dst, st); break;
-    case 10: launch_inv_block<10, FINAL>(g, polys, src, dst, st); break;
-    case 11: launch_inv_block<11, FINAL>(g, polys, src, dst, st); break;
     case 12: launch_inv_block<12, FINAL>(g, polys, src, dst, st); break;
     case 13: launch_inv_block<13, FINAL>(g, polys, src, dst, st); break;
     case 14: launch_inv_block<14, FINAL>(g, polys, src, dst, st); break;
-    default: throw Error(12, "unsupported NTT size");
+    default: {
+      if (logn < 3 || logn > 11 || !FINAL) throw Error(12, "unsupported NTT size");
+      const uint32_t threads = logn >= 11 ? 1024 : (1u << (logn - 1));
+      const uint64_t blocks = polys * g.limbs;
+      k_ntt_inv_small<<<(unsigned)blocks, threads, (sizeof(uint64_t) << logn), st>>>(g, logn, src, dst);
+      after_launch("k_ntt_inv_small");
+    }
   }
 }
 

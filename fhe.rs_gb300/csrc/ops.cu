@@ -35,21 +35,23 @@ std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t roo
   auto t = std::make_shared<PrimeTables>();
   t->host = make_ntt_tables(p, n, root);
   t->tables.alloc(4 * n * sizeof(uint64_t));
+  std::vector<uint64_t> inter(4 * n);
+  for (size_t i = 0; i < n; i++) {
+    inter[2 * i] = t->host.omegas[i];
+    inter[2 * i + 1] = t->host.omegas_shoup[i];
+    inter[2 * n + 2 * i] = t->host.zetas_inv[i];
+    inter[2 * n + 2 * i + 1] = t->host.zetas_inv_shoup[i];
+  }
   uint64_t* d = t->tables.u64();
-  upload(d, t->host.omegas.data(), n * 8);
-  upload(d + n, t->host.omegas_shoup.data(), n * 8);
-  upload(d + 2 * n, t->host.zetas_inv.data(), n * 8);
-  upload(d + 3 * n, t->host.zetas_inv_shoup.data(), n * 8);
+  upload(d, inter.data(), 4 * n * 8);
   DevPrime& dp = t->dev;
   dp.p = p;
   dp.p2 = 2 * p;
   barrett128(p, &dp.bhi, &dp.blo);
   dp.ninv = t->host.size_inv;
   dp.ninv_shoup = t->host.size_inv_shoup;
-  dp.w = d;
-  dp.ws = d + n;
-  dp.zi = d + 2 * n;
-  dp.zis = d + 3 * n;
+  dp.tw = reinterpret_cast<const ulonglong2*>(d);
+  dp.itw = reinterpret_cast<const ulonglong2*>(d + 2 * n);
   registry[key] = t;
   return t;
 }
@@ -262,74 +264,63 @@ void poly_switch_down_ntt(const Context& ctx, PolyRef in, PolyRef out, uint64_t 
 
 // ---------------------------------------------------------------------------
 // RNS scaling (rns/scaler.rs:249-352), one thread per coefficient.
+//
+// The reference accumulates in wrapping 256-bit integers; the sums here are
+// the same integers accumulated exactly in 32-bit words:
+//   G = sum_k r_k * theta_garner_k           (< 2^192 by the choice of shift)
+//   O = sum_k (+/-) r_k * theta_omega_k - (+/-) v * theta_gamma   (mod 2^256)
+// and each output residue is one exact dot product reduced once:
+//   y_j = sum_k r_k * omega_jk + v_j * (q_j - gamma_j) + w_term  (mod q_j),
+// which equals the reference's lazily reduced sum modulo q_j.
 
-struct U192 {
-  uint64_t w0, w1, w2;
-};
+__device__ __forceinline__ uint64_t join(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
 
-__device__ __forceinline__ void mac_192(U192& acc, uint64_t r, uint64_t lo, uint64_t hi) {
-  // acc += r * (hi:lo), r < 2^64, product < 2^192.
-  const uint64_t p0l = r * lo, p0h = __umul64hi(r, lo);
-  const uint64_t p1l = r * hi, p1h = __umul64hi(r, hi);
-  unsigned __int128 s = (unsigned __int128)acc.w0 + p0l;
-  acc.w0 = (uint64_t)s;
-  s = (s >> 64) + acc.w1 + p0h + (unsigned __int128)p1l;
-  acc.w1 = (uint64_t)s;
-  acc.w2 = acc.w2 + p1h + (uint64_t)(s >> 64);
-}
-
-struct U256d {
-  uint64_t w[4];
-};
-
-__device__ __forceinline__ void add256(U256d& a, const U256d& b) {
-  unsigned __int128 c = 0;
+// Low 128 bits of (w >> s) for an nw-word little-endian value (32-bit words).
+__device__ __forceinline__ void shr_words(const uint32_t* w, int nw, uint32_t s, uint64_t* lo, uint64_t* hi) {
+  uint32_t o[4];
+  const uint32_t ws = s >> 5, bs = s & 31;
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    c += (unsigned __int128)a.w[i] + b.w[i];
-    a.w[i] = (uint64_t)c;
-    c >>= 64;
-  }
-}
-
-__device__ __forceinline__ void sub256(U256d& a, const U256d& b) {
-  uint64_t borrow = 0;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const uint64_t ai = a.w[i], bi = b.w[i];
-    const uint64_t d = ai - bi - borrow;
-    borrow = (ai < bi) || (ai == bi && borrow) ? 1 : 0;
-    a.w[i] = d;
-  }
-}
-
-// r (< 2^128) times (hi:lo) as a full 256-bit product.
-__device__ __forceinline__ U256d mul_128x128(uint64_t a0, uint64_t a1, uint64_t b0, uint64_t b1) {
-  U256d r;
-  unsigned __int128 p00 = (unsigned __int128)a0 * b0, p01 = (unsigned __int128)a0 * b1;
-  unsigned __int128 p10 = (unsigned __int128)a1 * b0, p11 = (unsigned __int128)a1 * b1;
-  r.w[0] = (uint64_t)p00;
-  unsigned __int128 mid = (p00 >> 64) + (uint64_t)p01 + (uint64_t)p10;
-  r.w[1] = (uint64_t)mid;
-  unsigned __int128 hi = (mid >> 64) + (p01 >> 64) + (p10 >> 64) + (uint64_t)p11;
-  r.w[2] = (uint64_t)hi;
-  r.w[3] = (uint64_t)(hi >> 64) + (uint64_t)(p11 >> 64);
-  return r;
-}
-
-// Low 128 bits of (w >> s) for a 4-word value, 0 <= s < 256.
-__device__ __forceinline__ void shr_low128(const uint64_t* w, int nw, uint32_t s, uint64_t* lo, uint64_t* hi) {
-  uint64_t out[2] = {0, 0};
-  const uint32_t ws = s >> 6, bs = s & 63;
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < 4; k++) {
     const uint32_t idx = ws + k;
-    uint64_t v = idx < (uint32_t)nw ? w[idx] : 0;
-    uint64_t nx = (idx + 1) < (uint32_t)nw ? w[idx + 1] : 0;
-    out[k] = bs ? ((v >> bs) | (nx << (64 - bs))) : v;
+    uint32_t a = 0, b = 0;
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+      if (m < nw && (uint32_t)m == idx) a = w[m];
+      if (m < nw && (uint32_t)m == idx + 1) b = w[m];
+    }
+    o[k] = bs ? ((a >> bs) | (b << (32 - bs))) : a;
   }
-  *lo = out[0];
-  *hi = out[1];
+  *lo = join(o[0], o[1]);
+  *hi = join(o[2], o[3]);
+}
+
+// 256-bit a += b, a -= b (32-bit words).
+__device__ __forceinline__ void add256w(uint32_t* a, const uint32_t* b) {
+  asm("add.cc.u32 %0, %0, %8;\n\taddc.cc.u32 %1, %1, %9;\n\taddc.cc.u32 %2, %2, %10;\n\taddc.cc.u32 %3, %3, %11;\n\t"
+      "addc.cc.u32 %4, %4, %12;\n\taddc.cc.u32 %5, %5, %13;\n\taddc.cc.u32 %6, %6, %14;\n\taddc.u32 %7, %7, %15;"
+      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
+      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+}
+
+__device__ __forceinline__ void sub256w(uint32_t* a, const uint32_t* b) {
+  asm("sub.cc.u32 %0, %0, %8;\n\tsubc.cc.u32 %1, %1, %9;\n\tsubc.cc.u32 %2, %2, %10;\n\tsubc.cc.u32 %3, %3, %11;\n\t"
+      "subc.cc.u32 %4, %4, %12;\n\tsubc.cc.u32 %5, %5, %13;\n\tsubc.cc.u32 %6, %6, %14;\n\tsubc.u32 %7, %7, %15;"
+      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
+      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+}
+
+// Full 128 x 128 -> 256-bit product (32-bit words).
+__device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) r[k] = 0;
+  uint32_t t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  mac256(t, alo, blo, bhi);  // alo * b at word 0
+  uint32_t hi6[6] = {0, 0, 0, 0, 0, 0};
+  mac192(hi6, ahi, blo, bhi);  // ahi * b at word 2 (< 2^192)
+  uint32_t u[8] = {0, 0, hi6[0], hi6[1], hi6[2], hi6[3], hi6[4], hi6[5]};
+  add256w(t, u);
+#pragma unroll
+  for (int k = 0; k < 8; k++) r[k] = t[k];
 }
 
 template <int MAXF>
@@ -340,19 +331,19 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
   const uint32_t i = gid & ((1u << logn) - 1);
   const uint32_t poly = (uint32_t)(gid >> logn);
   const uint32_t F = s.from_len;
+  const uint64_t* src = in.at(poly, 0) + i;
   uint64_t r[MAXF];
 #pragma unroll
-  for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? in.at(poly, k)[i] : 0;
+  for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? src[(uint64_t)k << logn] : 0;
 
-  // scaler.rs:260-272: v = ceil((sum r_k theta_garner_k) >> (shift - 1) / 2).
-  U192 g = {0, 0, 0};
+  // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2).
+  uint32_t g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
   for (int k = 0; k < MAXF; k++)
-    if (k < (int)F) mac_192(g, r[k], __ldg(s.tgar_lo + k), __ldg(s.tgar_hi + k));
-  uint64_t gw[3] = {g.w0, g.w1, g.w2};
+    if (k < (int)F) mac192(g, r[k], __ldg(s.tgar_lo + k), __ldg(s.tgar_hi + k));
   uint64_t vlo, vhi;
-  shr_low128(gw, 3, s.shift - 1, &vlo, &vhi);
-  {  // div_ceil(2)
+  shr_words(g, 6, s.shift - 1, &vlo, &vhi);
+  {
     const uint64_t odd = vlo & 1;
     vlo = (vlo >> 1) | (vhi << 63);
     vhi >>= 1;
@@ -364,28 +355,31 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
   bool w_sign = false;
   uint64_t wlo = 0, whi = 0;
   if (!s.is_one) {
-    U256d acc = {{0, 0, 0, 0}};
+    uint32_t pos[8] = {0, 0, 0, 0, 0, 0, 0, 0}, neg[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int k = 0; k < MAXF; k++) {
       if (k < (int)F) {
-        U256d prod = mul_128x128(r[k], 0, __ldg(s.to_lo + k), __ldg(s.to_hi + k));
-        if (__ldg(s.to_sign + k)) sub256(acc, prod);
-        else add256(acc, prod);
+        if (__ldg(s.to_sign + k)) mac256(neg, r[k], __ldg(s.to_lo + k), __ldg(s.to_hi + k));
+        else mac256(pos, r[k], __ldg(s.to_lo + k), __ldg(s.to_hi + k));
       }
     }
-    U256d vt = mul_128x128(vlo, vhi, s.tg_lo, s.tg_hi);
-    if (s.tg_sign) add256(acc, vt);
-    else sub256(acc, vt);
-    w_sign = (acc.w[3] >> 63) != 0;
+    sub256w(pos, neg);
+    uint32_t vt[8];
+    mul128x128w(vt, vlo, vhi, s.tg_lo, s.tg_hi);
+    if (s.tg_sign) add256w(pos, vt);
+    else sub256w(pos, vt);
+    w_sign = (pos[7] >> 31) != 0;
     if (w_sign) {
-      uint64_t nw[4] = {~acc.w[0], ~acc.w[1], ~acc.w[2], ~acc.w[3]};
-      shr_low128(nw, 4, 126, &wlo, &whi);
+      uint32_t nw[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) nw[k] = ~pos[k];
+      shr_words(nw, 8, 126, &wlo, &whi);
       wlo += 1;
       whi += (wlo == 0);
       wlo = (wlo >> 1) | (whi << 63);
       whi >>= 1;
     } else {
-      shr_low128(acc.w, 4, 126, &wlo, &whi);
+      shr_words(pos, 8, 126, &wlo, &whi);
       const uint64_t odd = wlo & 1;
       wlo = (wlo >> 1) | (whi << 63);
       whi >>= 1;
@@ -395,22 +389,29 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
   }
 
   // scaler.rs:316-351.
+  uint64_t* dst = out.at(poly, 0) + i;
   for (uint32_t o = 0; o < out_len; o++) {
     const uint32_t j = start + o;
     const DevPrime pr = s.to_primes[j];
     const uint64_t vj = reduce128(vhi, vlo, pr);
-    unsigned __int128 y =
-        (unsigned __int128)(pr.p2 - mul_shoup_lazy(vj, __ldg(s.gamma + j), __ldg(s.gamma_shoup + j), pr.p));
+    uint64_t lo = 0, hi = 0;
     if (!s.is_one) {
       const uint64_t wj = reduce128_lazy(whi, wlo, pr);
-      y += w_sign ? pr.p2 - wj : wj;
+      lo = w_sign ? pr.p2 - wj : wj;
     }
+    mac128(hi, lo, vj, __ldg(s.gamma_neg + j));
     const uint64_t* om = s.omega + (uint64_t)j * F;
-    const uint64_t* oms = s.omega_shoup + (uint64_t)j * F;
 #pragma unroll
-    for (int k = 0; k < MAXF; k++)
-      if (k < (int)F) y += mul_shoup_lazy(r[k], __ldg(om + k), __ldg(oms + k), pr.p);
-    out.at(poly, o)[i] = reduce128((uint64_t)(y >> 64), (uint64_t)y, pr);
+    for (int k = 0; k < MAXF; k++) {
+      if (k < (int)F) {
+        mac128(hi, lo, r[k], __ldg(om + k));
+        if ((k % 15) == 14) {  // keep the exact sum below 2^128
+          lo = reduce128(hi, lo, pr);
+          hi = 0;
+        }
+      }
+    }
+    dst[(uint64_t)o << logn] = reduce128(hi, lo, pr);
   }
 }
 
@@ -440,6 +441,9 @@ RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& nu
          o_oms = put(host.omega_shoup), o_tol = put(host.theta_omega_lo), o_toh = put(host.theta_omega_hi);
   std::vector<uint64_t> sign(host.theta_omega_sign.begin(), host.theta_omega_sign.end());
   size_t o_tos = put(sign), o_tgl = put(host.theta_garner_lo), o_tgh = put(host.theta_garner_hi);
+  std::vector<uint64_t> gneg(T);
+  for (size_t j = 0; j < T; j++) gneg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
+  size_t o_gneg = put(gneg);
   buf.alloc(std::max<size_t>(flat.size(), 1) * 8);
   upload(buf.ptr, flat.data(), flat.size() * 8);
   uint64_t* b = buf.u64();
@@ -460,6 +464,7 @@ RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& nu
   dev.to_sign = b + o_tos;
   dev.tgar_lo = b + o_tgl;
   dev.tgar_hi = b + o_tgh;
+  dev.gamma_neg = b + o_gneg;
   dev.to_primes = to.primes_dev();
 }
 
