@@ -145,24 +145,25 @@ def run_reference(args, rank: int):
     oracle_build.build()
     par, sk, rk, cts, _, _ = make_inputs(ora, 8, distinct=8)
     cores = os.cpu_count() or 1
+    # One step = the GPU arm's batch of products, spread over every host core.
+    per_thread = -(-args.batch // cores)
     cpu_multiply_rate(ora, rk, cts, 1, 1)  # warm the caches of the oracle
-    rates = []
     for _ in range(max(args.warmup, 0)):
-        cpu_multiply_rate(ora, rk, cts, cores, 1)
+        cpu_multiply_rate(ora, rk, cts, cores, per_thread)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, _ = cpu_multiply_rate(ora, rk, cts, cores, 1)
-        rates.append(r)
+        cpu_multiply_rate(ora, rk, cts, cores, per_thread)
     total = time.perf_counter() - t0
-    value = args.steps * cores / total
+    value = args.steps * cores * per_thread / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": "bfv_mul_relin", "degree": N, "moduli": L, "moduli_bits": 62, "plaintext": T,
-                   "batch_pairs_per_step": cores, "parallelism": "host threads"},
+                   "batch_pairs_per_step": cores * per_thread, "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} products per step (one per host thread) of the CPU restatement of "
+                         "sample": f"{cores * per_thread} products per step ({per_thread} per host thread) of the "
+                                   "CPU restatement of "
                                    "fhe.rs Multiplicator::default().multiply; the Rust reference cannot be built "
                                    "(no Rust toolchain)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -287,8 +288,11 @@ def run_ours(args, rank: int, world: int):
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         cpu_multiply_rate(ora, rk_o, cts, 1, 1)
-        single_thread, st_s = cpu_multiply_rate(ora, rk_o, cts, 1, 2)
-        per_thread = max(1, min(4, int(args.cpu_seconds / max(st_s / 2, 1e-3) / 1)))
+        single_thread, _ = cpu_multiply_rate(ora, rk_o, cts, 1, 2)
+        # Calibrate on one product per core, then size the sample to about
+        # --cpu-seconds of wall time on all cores.
+        rate0, _ = cpu_multiply_rate(ora, rk_o, cts, cores, 1)
+        per_thread = max(1, int(args.cpu_seconds * rate0 / cores))
         rate, dt = cpu_multiply_rate(ora, rk_o, cts, cores, per_thread)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{cores * per_thread} products on {cores} host threads ({dt:.1f} s); single-thread "
@@ -387,6 +391,238 @@ def run_ntt(args):
     print(json.dumps(line), flush=True)
 
 
+def run_rotate(args):
+    """Uneven-level rotation batch: N = 2^15, twelve 62-bit moduli at the top
+    level, 32 ciphertexts each switched to a random level (4 to 12 live
+    moduli) and rotated by a random column step in [1, N/2) with the Galois
+    key of its (step, level); ~1 GB of keys resident. One step = the whole
+    ragged batch in one call (one launch per stage)."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    n, top, count = 1 << 15, 12, args.rot_count
+    rng = np.random.default_rng(15)
+    par_o = ora.BfvParameters(n, T, moduli_sizes=[62] * top)
+    par = fg.BfvParameters(n, par_o.moduli, T)
+    sk = ora.SecretKey.random(par_o, rng)
+    levels = [int(x) for x in rng.integers(0, top - 3, count)]  # 4..12 live moduli
+    steps = [int(x) for x in rng.integers(1, n // 2, count)]
+    keys, gks_o, cts_o, cts_d = [], [], [], []
+    key_bytes = 0
+    for b in range(count):
+        e = ora.rotation_exponent(par_o, steps[b])
+        gk = ora.GaloisKey(sk, e, levels[b], levels[b], rng)
+        gks_o.append(gk)
+        c0, c1 = gk.ksk.c0_array(), gk.ksk.c1_array()
+        key_bytes += c0.nbytes + c1.nbytes
+        keys.append(fg.GaloisKey(par, e, c0, c1, levels[b], levels[b]))
+        v = rng.integers(0, T, n, dtype=np.uint64)
+        ct = sk.encrypt(ora.Plaintext.encode(v, "simd", par_o, levels[b]), rng)
+        cts_o.append(ct)
+        cts_d.append(fg.to_device(ct.to_array()))
+    outs = [fg.empty(c.shape) for c in cts_d]
+    fg.rotate_batch(par, keys, cts_d, outs)
+    torch.cuda.synchronize()
+    for b in (0, count - 1):
+        if not np.array_equal(fg.to_host(outs[b]), gks_o[b].relinearize(cts_o[b]).to_array()):
+            raise SystemExit(f"bench: rotation {b} is not bit-exact with the oracle")
+    for _ in range(args.warmup):
+        fg.rotate_batch(par, keys, cts_d, outs)
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            fg.rotate_batch(par, keys, cts_d, outs)
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = fg.kernel_launch_count() - launches0
+    ms = start.elapsed_time(end) / args.steps
+    # One rotation per call (GaloisKey::relinearize on each ciphertext).
+    start.record(stream)
+    for b in range(count):
+        keys[b].relinearize(cts_d[b][None])
+    end.record(stream)
+    torch.cuda.synchronize()
+    single_ms = start.elapsed_time(end)
+    lv = [top - l for l in levels]
+    line = {"metric": "ragged rotation ct/s N=2^15 L=4..12 (GaloisKey per level)", "value": count / (ms / 1000),
+            "unit": "ct/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
+            "config": {"workload": "rotation_uneven_levels", "degree": n, "top_moduli": top, "count": count,
+                       "live_moduli": lv, "key_bytes_resident": key_bytes},
+            "single": {"value": count / (single_ms / 1000), "unit": "ct/s", "note": "one call per ciphertext"},
+            "batch_vs_single": single_ms / ms, "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+SERVE_SETS = [(1 << 13, 3), (1 << 14, 6), (1 << 15, 12)]
+SERVE_MIX = (("mul", 0.50), ("rot", 0.30), ("add", 0.15), ("down", 0.05))
+
+
+def _serve_setup(fg, ora, torch, n, nm, seed, ring):
+    """Keys, pinned input ciphertexts and pinned output rings of one parameter set."""
+    rng = np.random.default_rng(seed)
+    par_o = ora.BfvParameters(n, T, moduli_sizes=[62] * nm)
+    sk = ora.SecretKey.random(par_o, rng)
+    rk_o = ora.RelinearizationKey(sk, rng)
+    par = fg.BfvParameters(n, par_o.moduli, T)
+    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
+    exps = (2 * n - 1, ora.rotation_exponent(par_o, 1))
+    gks_o = [ora.GaloisKey(sk, e, 0, 0, rng) for e in exps]
+    gks = [fg.GaloisKey(par, e, g.ksk.c0_array(), g.ksk.c1_array()) for e, g in zip(exps, gks_o)]
+    cts_o = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, n, dtype=np.uint64), "simd", par_o), rng)
+             for _ in range(6)]
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+
+    cts = []
+    for c in cts_o:
+        h = pinned((2, nm, n))
+        h[...] = c.to_array()
+        cts.append(h)
+    return {"n": n, "L": nm, "par_o": par_o, "par": par, "rk_o": rk_o, "mult_o": ora.Multiplicator.default(rk_o),
+            "mult": fg.Multiplicator.default(rk), "rk": rk, "gks_o": gks_o, "gks": gks, "cts_o": cts_o, "cts": cts,
+            "out": [pinned((2, nm, n)) for _ in range(ring)], "out_down": [pinned((2, nm - 1, n)) for _ in range(ring)]}
+
+
+def _serve_requests(count, seed):
+    """(set index, kind, operand a, operand b, key index) of each request."""
+    rng = np.random.default_rng(seed)
+    kinds = [k for k, _ in SERVE_MIX]
+    probs = [p for _, p in SERVE_MIX]
+    sets = rng.integers(0, len(SERVE_SETS), count)
+    ks = rng.choice(len(kinds), count, p=probs)
+    a, b, g = rng.integers(0, 6, count), rng.integers(0, 6, count), rng.integers(0, 2, count)
+    return [(int(sets[i]), kinds[ks[i]], int(a[i]), int(b[i]), int(g[i])) for i in range(count)]
+
+
+def _serve_submit(srv, setups, req, slot):
+    si, kind, a, b, g = req
+    s = setups[si]
+    if kind == "mul":
+        return srv.submit_mul_relin(s["mult"], s["cts"][a], s["cts"][b], out=s["out"][slot % len(s["out"])])
+    if kind == "rot":
+        return srv.submit_rotate(s["gks"][g], s["cts"][a], out=s["out"][slot % len(s["out"])])
+    if kind == "add":
+        return srv.submit_add(s["par"], 0, s["cts"][a], s["cts"][b], out=s["out"][slot % len(s["out"])])
+    return srv.submit_switch_down(s["par"], 0, s["cts"][a], out=s["out_down"][slot % len(s["out_down"])])
+
+
+def _serve_run(fg, setups, reqs, budget, streams, max_batch, arrivals=None):
+    """Submits `reqs` (all at once, or at the `arrivals` offsets in seconds)
+    and returns (requests/s, latencies in ms, batches)."""
+    with fg.Server(budget, streams=streams, max_batch=max_batch) as srv:
+        ids = []
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            if arrivals is not None:
+                target = t0 + arrivals[i]
+                while True:
+                    left = target - time.perf_counter()
+                    if left <= 0:
+                        break
+                    if left > 3e-4:
+                        time.sleep(left - 2e-4)
+            ids.append(_serve_submit(srv, setups, r, i))
+        for rid in ids:
+            srv.wait(rid, 600000)
+        times = np.array([srv.times(rid) for rid in ids], dtype=np.int64)
+        batches = srv.stats()["batches"]
+    lat = (times[:, 2] - times[:, 0]) / 1e6
+    span = (times[:, 2].max() - times[:, 0].min()) / 1e9
+    return len(reqs) / span, lat, batches
+
+
+def run_serve(args):
+    """Serving loop: a stream of requests over three parameter sets (N = 2^13
+    with 3 moduli, 2^14 with 6, 2^15 with 12, chosen uniformly), 50% mul+relin,
+    30% rotation, 15% addition and 5% switch-down, keys resident, ciphertexts
+    in pinned host memory. The continuous-batching server (HBM budget, several
+    streams) against the same server restricted to one request at a time:
+    saturation throughput with everything submitted at once, and p50/p99
+    latency under Poisson arrivals at 70% of the one-at-a-time capacity and at
+    70% of the batched capacity."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    ring = 64
+    setups = [_serve_setup(fg, ora, torch, n, nm, 100 + k, ring) for k, (n, nm) in enumerate(SERVE_SETS)]
+    budget = int(args.serve_budget_gb * (1 << 30))
+    # Parity gate: every operation of every set through the server, alone,
+    # against the oracle.
+    with fg.Server(budget, streams=1, max_batch=1) as srv:
+        for si, s in enumerate(setups):
+            co = s["cts_o"]
+            checks = [(("mul", 0, 1, 0), s["mult_o"].multiply(co[0], co[1])),
+                      (("rot", 2, 0, 1), s["gks_o"][1].relinearize(co[2])),
+                      (("add", 3, 4, 0), co[3] + co[4]),
+                      (("down", 5, 0, 0), co[5].copy().switch_down())]
+            for (kind, a, b, g), want in checks:
+                got = srv.wait(_serve_submit(srv, setups, (si, kind, a, b, g), 0), 600000)
+                if not np.array_equal(got, want.to_array()):
+                    raise SystemExit(f"bench: served {kind} at N={s['n']} is not bit-exact with the oracle")
+    reqs = _serve_requests(args.serve_requests, 7)
+    warm = _serve_requests(min(200, args.serve_requests), 8)
+    for _ in range(max(1, args.warmup // 2)):
+        _serve_run(fg, setups, warm, budget, args.serve_streams, args.serve_batch)
+        _serve_run(fg, setups, warm, budget, 1, 1)
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        thr_b, lat_sat_b, batches_b = _serve_run(fg, setups, reqs, budget, args.serve_streams, args.serve_batch)
+    launches = fg.kernel_launch_count() - launches0
+    thr_1, lat_sat_1, _ = _serve_run(fg, setups, reqs, budget, 1, 1)
+    rng = np.random.default_rng(9)
+    gaps = rng.exponential(1.0, len(reqs))
+
+    def poisson(rate, streams, max_batch):
+        _, lat, batches = _serve_run(fg, setups, reqs, budget, streams, max_batch, np.cumsum(gaps) / rate)
+        return {"offered_req_s": rate, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()), "batches": int(batches)}
+
+    low = 0.7 * thr_1
+    at_low_b = poisson(low, args.serve_streams, args.serve_batch)
+    at_low_1 = poisson(low, 1, 1)
+    high = 0.7 * thr_b
+    at_high_b = poisson(high, args.serve_streams, args.serve_batch)
+    h2d = d2h = 0
+    for si, kind, _, _, _ in reqs:
+        s = setups[si]
+        ct_bytes = 2 * s["L"] * s["n"] * 8
+        h2d += ct_bytes * (2 if kind in ("mul", "add") else 1)
+        d2h += ct_bytes if kind != "down" else 2 * (s["L"] - 1) * s["n"] * 8
+    line = {"metric": "BFV serving req/s (mixed N=2^13..2^15), p50/p99 vs one-at-a-time",
+            "value": thr_b, "unit": "req/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
+            "ms_per_step": 1000 * len(reqs) / thr_b, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
+            "config": {"workload": "serve_mixed", "sets": [{"degree": n, "moduli": nm} for n, nm in SERVE_SETS],
+                       "mix": dict(SERVE_MIX), "requests": len(reqs), "hbm_budget_bytes": budget,
+                       "streams": args.serve_streams, "max_batch": args.serve_batch,
+                       "host_buffers": "pinned"},
+            "e2e": {"value": thr_b, "unit": "req/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "one step = all requests, host buffers to host buffers"},
+            "saturation": {"batched_req_s": thr_b, "one_at_a_time_req_s": thr_1, "speedup": thr_b / thr_1,
+                           "batched_batches": int(batches_b)},
+            "poisson_at_70pct_of_one_at_a_time": {"batched": at_low_b, "one_at_a_time": at_low_1},
+            "poisson_at_70pct_of_batched": {"batched": at_high_b},
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -396,13 +632,22 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt"])
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve"])
+    ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-budget-gb", type=float, default=24.0)
+    ap.add_argument("--serve-streams", type=int, default=4)
+    ap.add_argument("--serve-batch", type=int, default=32)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.workload == "ntt":
         run_ntt(args)
+    elif args.workload == "rotate":
+        run_rotate(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

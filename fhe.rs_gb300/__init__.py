@@ -67,6 +67,15 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_size), ("streams", ctypes.c_uint32), ("max_batch", ctypes.c_uint32)]
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int), ("par", c_vp), ("mult", c_vp), ("key", c_vp), ("exponent", c_size),
+                ("level", c_size), ("in0", P_u64), ("in1", P_u64), ("out", P_u64)]
+
+
 def _declare(L):
     i = ctypes.c_int
     sig = {
@@ -112,6 +121,17 @@ def _declare(L):
         "fheg_multiplicator_multiply": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_multiplicator_multiply_host": (i, [c_vp, P_u64, P_u64, P_u64, c_size]),
         "fheg_relinearize_noalloc": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
+                                              ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
+        "fheg_server_create": (i, [ctypes.POINTER(_ServerConfig), ctypes.POINTER(c_vp)]),
+        "fheg_server_destroy": (None, [c_vp]),
+        "fheg_server_submit": (i, [c_vp, ctypes.POINTER(_Request), ctypes.POINTER(c_u64)]),
+        "fheg_server_wait": (i, [c_vp, c_u64, ctypes.c_uint32]),
+        "fheg_server_request_times": (i, [c_vp, c_u64, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+        "fheg_server_release": (i, [c_vp, c_u64]),
+        "fheg_server_stats": (i, [c_vp, ctypes.POINTER(c_u64), ctypes.POINTER(c_u64), ctypes.POINTER(c_u64),
+                                  ctypes.POINTER(c_size)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -463,6 +483,21 @@ class EvaluationKey:
         return self.gk[pow(3, i, 2 * self.par.degree)].relinearize(ct)
 
 
+def rotate_batch(par: BfvParameters, keys: Sequence["GaloisKey"], cts: Sequence, outs: Sequence = None):
+    """A ragged batch of GaloisKey::relinearize calls (one key, exponent and
+    ciphertext per entry; ciphertexts may be at different levels), executed
+    with one launch per stage."""
+    n = len(keys)
+    if outs is None:
+        outs = [empty(c.shape, c.device) for c in cts]
+    kh = (c_vp * n)(*[k._h for k in keys])
+    ex = (c_size * n)(*[k.exponent for k in keys])
+    ci = (c_vp * n)(*[_dp(c) for c in cts])
+    co = (c_vp * n)(*[_dp(o) for o in outs])
+    check(lib().fheg_galois_relinearize_batch(par._h, kh, ex, ci, co, n, _stream()))
+    return outs
+
+
 def ciphertext_switch_down(par: BfvParameters, level: int, ct):
     """Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) on a batch
     [count][parts][L][N]; `ct` is consumed as scratch."""
@@ -550,3 +585,98 @@ class Multiplicator:
         lhs, rhs = np.ascontiguousarray(lhs, dtype=np.uint64), np.ascontiguousarray(rhs, dtype=np.uint64)
         check(lib().fheg_multiplicator_multiply_host(self._h, _ptr(lhs), _ptr(rhs), _ptr(out), count))
         return out
+
+
+# ---------------------------------------------------------------------------
+# Serving runtime (no counterpart in the reference: fhe.rs runs one operation
+# per call on the caller's thread).
+
+OP_MUL_RELIN, OP_ROTATE, OP_ADD, OP_SWITCH_DOWN = 0, 1, 2, 3
+
+
+class Server:
+    """Continuous-batching server over a fixed device-memory budget.
+
+    Requests carry host arrays ([2][L][N] u64 ciphertexts); the scheduler
+    thread of the library batches pending requests of the same operation and
+    parameters, runs them on one of `streams` streams and writes each result
+    into its output array. Pinned host arrays (for instance the numpy view of
+    a pinned torch tensor) are copied directly; pageable ones through pinned
+    staging."""
+
+    def __init__(self, hbm_budget_bytes: int, streams: int = 2, max_batch: int = 64):
+        cfg = _ServerConfig(hbm_budget_bytes, streams, max_batch)
+        h = c_vp()
+        check(lib().fheg_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_server_destroy(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _submit(self, op, par, arrays, out_shape, out=None, mult=None, key=None, exponent=0, level=0) -> int:
+        arrays = [np.ascontiguousarray(a, dtype=np.uint64) for a in arrays]
+        if out is None:
+            out = np.empty(out_shape, dtype=np.uint64)
+        if tuple(out.shape) != tuple(out_shape) or out.dtype != np.uint64 or not out.flags["C_CONTIGUOUS"]:
+            raise FhegError(ERR_INVALID_ARGUMENT, "output array of the wrong shape or type")
+        for a in arrays:
+            if a.shape[0] != 2:
+                raise FhegError(ERR_WRONG_PARTS, "requests take ciphertexts with 2 parts")
+        r = _Request(op, par._h, mult._h if mult is not None else None, key._h if key is not None else None,
+                     exponent, level, _ptr(arrays[0]), _ptr(arrays[1]) if len(arrays) > 1 else None, _ptr(out))
+        rid = c_u64(0)
+        check(lib().fheg_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)))
+        self._live[rid.value] = (arrays, out)
+        return rid.value
+
+    def submit_mul_relin(self, mult: "Multiplicator", lhs, rhs, out=None) -> int:
+        parts, level = mult.output_shape()
+        shape = (parts, len(mult.par.moduli) - level, mult.par.degree)
+        return self._submit(OP_MUL_RELIN, mult.par, [lhs, rhs], shape, out, mult=mult)
+
+    def submit_rotate(self, key: "GaloisKey", ct, out=None) -> int:
+        return self._submit(OP_ROTATE, key.par, [ct], ct.shape, out, key=key, exponent=key.exponent)
+
+    def submit_add(self, par: BfvParameters, level: int, a, b, out=None) -> int:
+        return self._submit(OP_ADD, par, [a, b], a.shape, out, level=level)
+
+    def submit_switch_down(self, par: BfvParameters, level: int, ct, out=None) -> int:
+        shape = (2, ct.shape[1] - 1, ct.shape[2])
+        return self._submit(OP_SWITCH_DOWN, par, [ct], shape, out, level=level)
+
+    def wait(self, rid: int, timeout_ms: int = 60000) -> np.ndarray:
+        """The request's output; raises FhegError on failure or timeout."""
+        st = lib().fheg_server_wait(self._h, rid, timeout_ms)
+        if st == ERR_TIMEOUT:
+            raise FhegError(st, lib().fheg_last_error().decode())
+        _, out = self._live.pop(rid, (None, None))
+        check(st)
+        return out
+
+    def times(self, rid: int):
+        """(submit, start, done) host steady-clock nanoseconds."""
+        a, b, c = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        check(lib().fheg_server_request_times(self._h, rid, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def release(self, rid: int):
+        check(lib().fheg_server_release(self._h, rid))
+        self._live.pop(rid, None)
+
+    def stats(self) -> dict:
+        s, c, b, p = c_u64(0), c_u64(0), c_u64(0), c_size(0)
+        check(lib().fheg_server_stats(self._h, ctypes.byref(s), ctypes.byref(c), ctypes.byref(b), ctypes.byref(p)))
+        return {"submitted": s.value, "completed": c.value, "batches": b.value, "peak_bytes": p.value}

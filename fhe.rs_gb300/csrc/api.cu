@@ -322,6 +322,20 @@ FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const 
   });
 }
 
+FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
+                                           const size_t* exponents, const uint64_t* const* d_cts,
+                                           uint64_t* const* d_outs, size_t count, void* stream) {
+  return guard([&] {
+    need(par && ((keys && exponents && d_cts && d_outs) || !count), "null input");
+    std::vector<RotRequest> req(count);
+    for (size_t b = 0; b < count; b++) {
+      need(keys[b] && d_cts[b] && d_outs[b] && d_cts[b] != d_outs[b], "null or aliased batch entry");
+      req[b] = RotRequest{&keys[b]->k, exponents[b], d_cts[b], d_outs[b]};
+    }
+    galois_relinearize_batch(*par->p, req.data(), count, const_cast<fheg_params*>(par)->ws, as_stream(stream));
+  });
+}
+
 FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts, uint64_t* d_ct,
                                          uint64_t* d_out, size_t count, void* stream) {
   return guard([&] {

@@ -191,7 +191,7 @@ void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t cou
   const Context& c = *rk.ctx_ct;
   const size_t L = c.L(), N = c.N(), Lk = rk.ctx_ksk->L();
   if (count == 0) return;
-  ws.buf.reserve((count * L * N + count * L * Lk * N + 64) * 8);
+  ws.reserve((count * L * N + count * L * Lk * N + 64) * 8);
   size_t off = 0;
   uint64_t* digits = ws.take(count * L * N, &off);
   uint64_t* D = ws.take(count * L * Lk * N, &off);
@@ -225,7 +225,7 @@ void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, ui
   const uint64_t e = exponent % (2 * N);
   if ((e & 1) == 0) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
   if (count == 0) return;
-  ws.buf.reserve((count * L * N + count * L * Lk * N + 64) * 8);
+  ws.reserve((count * L * N + count * L * Lk * N + 64) * 8);
   size_t off = 0;
   uint64_t* digits = ws.take(count * L * N, &off);
   uint64_t* D = ws.take(count * L * Lk * N, &off);
@@ -237,6 +237,179 @@ void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, ui
   ntt_inverse_any(c.logn, g, count, SrcSubst{src, e, c.logn}, DstPoly{dst}, st);
   // galois_key.rs:111-122: key switch, then out0 += substitute(ct[0]).
   key_switch(gk, dst, count, ct, 2 * L * N, e, nullptr, 0, out, 2 * L * N, D, st);
+}
+
+// ---------------------------------------------------------------------------
+// Ragged rotation batch: GaloisKey::relinearize_into (galois_key.rs:90-124)
+// for ciphertexts at different levels, each with its own key and exponent,
+// in one launch per stage. Levels are prefixes of one moduli chain, so limb
+// j of every ciphertext uses modulus j.
+
+struct RotDesc {
+  const uint64_t* ct;  // [2][L][N] Ntt
+  uint64_t* out;       // [2][L][N] Ntt
+  uint64_t* digits;    // [L][N] scratch: substituted c1 in the power basis
+  uint64_t* D;         // [L digits][L limbs][N] scratch: digit NTTs
+  const uint64_t* k0;  // [L][L][N] key values, part 0
+  const uint64_t* k1;  // part 1
+  uint64_t e;          // substitution exponent mod 2N
+  uint32_t L, pad;
+};
+
+// R1: substituted c1, gathered into the inverse NTT (jobs: poly = b, limb = i).
+struct SrcRotSubst {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    const RotDesc& r = d[j.poly];
+    return r.ct[((uint64_t)(r.L + j.limb) << logn) + gather_index(i, r.e, logn)];
+  }
+};
+
+struct DstRotDigits {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    d[j.poly].digits[((uint64_t)j.limb << logn) + i] = v;
+  }
+  __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const {
+    return d[j.poly].digits[((uint64_t)j.limb << logn) + i];
+  }
+};
+
+// F: digit `aux` of ciphertext `poly` in key limb `limb`.
+struct SrcRotDigit {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
+    return reduce64_lazy(d[j.poly].digits[((uint64_t)j.aux << logn) + i], pr);
+  }
+};
+
+struct DstRotD {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t* at(const NttJob& j, uint32_t i) const {
+    const RotDesc& r = d[j.poly];
+    return r.D + ((uint64_t)(j.aux * r.L + j.limb) << logn) + i;
+  }
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    *at(j, i) = v;
+  }
+  __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const { return *at(j, i); }
+};
+
+// G: out0 = substitute(ct0) + sum_d D[d] * k0[d], out1 = sum_d D[d] * k1[d]
+// for row (poly, limb) = rows[blockIdx.y]; exact sums reduced once.
+__global__ void k_rot_mac(const DevPrime* primes, const RotDesc* d, const uint2* rows, uint32_t logn) {
+  const uint2 row = rows[blockIdx.y];
+  const RotDesc& r = d[row.x];
+  const uint32_t j = row.y;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (1u << logn)) return;
+  const DevPrime pr = primes[j];
+  const uint64_t plane = (uint64_t)r.L << logn;
+  uint64_t lo0 = r.ct[((uint64_t)j << logn) + gather_index(i, r.e, logn)], hi0 = 0, lo1 = 0, hi1 = 0;
+  for (uint32_t dd = 0; dd < r.L; dd++) {
+    const uint64_t off = ((uint64_t)(dd * r.L + j) << logn) + i;
+    const uint64_t x = r.D[off];
+    mac128(hi0, lo0, x, __ldg(r.k0 + off));
+    mac128(hi1, lo1, x, __ldg(r.k1 + off));
+    if (dd % 15 == 14) {
+      lo0 = reduce128(hi0, lo0, pr);
+      hi0 = 0;
+      lo1 = reduce128(hi1, lo1, pr);
+      hi1 = 0;
+    }
+  }
+  r.out[((uint64_t)j << logn) + i] = reduce128(hi0, lo0, pr);
+  r.out[plane + ((uint64_t)j << logn) + i] = reduce128(hi1, lo1, pr);
+}
+
+size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count) {
+  size_t words = 0, n_r1 = 0, n_f = 0;
+  for (size_t b = 0; b < count; b++) {
+    const size_t L = req[b].key->ctx_ct->L(), N = req[b].key->ctx_ct->N();
+    words += L * N + L * L * N;
+    n_r1 += L;
+    n_f += L * L;
+  }
+  const size_t table_words = (count * sizeof(RotDesc) + (n_r1 + n_f) * sizeof(uint4) + n_r1 * sizeof(uint2)) / 8 + 8;
+  return (words + table_words + 128 + 3 * 32) * 8;
+}
+
+void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
+                              cudaStream_t st) {
+  if (count == 0) return;
+  const Context& top = *par.ctx(0);
+  const size_t N = top.N();
+  const uint32_t logn = top.logn;
+  // Scratch and tables.
+  size_t digit_words = 0, d_words = 0, n_r1 = 0, n_f = 0;
+  for (size_t b = 0; b < count; b++) {
+    const Ksk& k = *req[b].key;
+    if (k.par != &par) throw Error(FHEG_ERR_KEY_MISMATCH, "all keys of a batch must share the parameters");
+    require_same_level_key(k);
+    if ((req[b].exponent % (2 * N)) % 2 == 0)
+      throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
+    const size_t L = k.ctx_ct->L();
+    digit_words += L * N;
+    d_words += L * L * N;
+    n_r1 += L;
+    n_f += L * L;
+  }
+  std::vector<RotDesc> desc(count);
+  std::vector<uint4> jobs;
+  jobs.reserve(n_r1 + n_f);
+  std::vector<uint2> rows;
+  rows.reserve(n_r1);
+  const size_t table_words = (count * sizeof(RotDesc) + (n_r1 + n_f) * sizeof(uint4) + n_r1 * sizeof(uint2)) / 8 + 8;
+  ws.reserve((digit_words + d_words + table_words + 128) * 8);
+  size_t off = 0;
+  uint64_t* digits = ws.take(digit_words, &off);
+  uint64_t* D = ws.take(d_words, &off);
+  uint64_t* tables = ws.take(table_words, &off);
+  size_t dpos = 0, Dpos = 0;
+  for (size_t b = 0; b < count; b++) {
+    const Ksk& k = *req[b].key;
+    const uint32_t L = (uint32_t)k.ctx_ct->L();
+    RotDesc& r = desc[b];
+    r.ct = req[b].ct;
+    r.out = req[b].out;
+    r.digits = digits + dpos;
+    r.D = D + Dpos;
+    r.k0 = k.values(0);
+    r.k1 = k.values(1);
+    r.e = req[b].exponent % (2 * N);
+    r.L = L;
+    r.pad = 0;
+    dpos += (size_t)L * N;
+    Dpos += (size_t)L * L * N;
+    for (uint32_t i = 0; i < L; i++) jobs.push_back(make_uint4((uint32_t)b, i, 0, 0));
+  }
+  for (size_t b = 0; b < count; b++)
+    for (uint32_t dd = 0; dd < desc[b].L; dd++)
+      for (uint32_t j = 0; j < desc[b].L; j++) jobs.push_back(make_uint4((uint32_t)b, j, dd, 0));
+  for (size_t b = 0; b < count; b++)
+    for (uint32_t j = 0; j < desc[b].L; j++) rows.push_back(make_uint2((uint32_t)b, j));
+  // Upload the tables (pageable source: the copy completes before return).
+  uint8_t* tb = reinterpret_cast<uint8_t*>(tables);
+  RotDesc* d_desc = reinterpret_cast<RotDesc*>(tb);
+  uint4* d_jobs = reinterpret_cast<uint4*>(tb + count * sizeof(RotDesc));
+  uint2* d_rows = reinterpret_cast<uint2*>(tb + count * sizeof(RotDesc) + jobs.size() * sizeof(uint4));
+  check_cuda(cudaMemcpyAsync(d_desc, desc.data(), count * sizeof(RotDesc), cudaMemcpyHostToDevice, st), "H2D");
+  check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(uint4), cudaMemcpyHostToDevice, st), "H2D");
+  check_cuda(cudaMemcpyAsync(d_rows, rows.data(), rows.size() * sizeof(uint2), cudaMemcpyHostToDevice, st), "H2D");
+  // R1: substituted c1 into the power basis.
+  NttGeom g1{top.primes_dev(), 1, 0, d_jobs};
+  ntt_inverse_any(logn, g1, n_r1, SrcRotSubst{d_desc, logn}, DstRotDigits{d_desc, logn}, st);
+  // F: every digit in every key limb.
+  NttGeom g2{top.primes_dev(), 1, 0, d_jobs + n_r1};
+  ntt_forward_any<true>(logn, g2, n_f, SrcRotDigit{d_desc, logn}, DstRotD{d_desc, logn}, st);
+  // G: inner products and the substituted c0.
+  dim3 grid((unsigned)((N + 255) / 256), (unsigned)rows.size());
+  k_rot_mac<<<grid, 256, 0, st>>>(top.primes_dev(), d_desc, d_rows, logn);
+  after_launch("k_rot_mac");
 }
 
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
@@ -294,9 +467,18 @@ std::unique_ptr<Multiplicator> make_default_multiplicator(const Ksk& rk) {
   return m;
 }
 
+size_t Multiplicator::scratch_bytes(uint64_t count) const {
+  const size_t L = base->L(), M = mul->L(), N = base->N();
+  const size_t Lk = rk ? rk->ctx_ksk->L() : 0;
+  const size_t words = count * 4 * L * N + count * 4 * M * N + count * 3 * M * N + count * 3 * L * N +
+                       (rk ? count * L * Lk * N : 0) + (mod_switch ? count * out_parts() * L * N : 0) + 6 * 32;
+  return words * 8;
+}
+
 void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count,
-                             cudaStream_t st) {
+                             cudaStream_t st, Workspace* scratch) {
   if (count == 0) return;
+  Workspace& ws = scratch ? *scratch : this->ws;
   const Context& bc = *base;
   const Context& mc = *mul;
   const size_t L = bc.L(), M = mc.L(), N = bc.N();
@@ -308,7 +490,7 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   const size_t w_pb = count * 4 * L * N, w_ext = count * 4 * M * N, w_prod = count * 3 * M * N,
                w_down = count * 3 * L * N, w_d = rk ? count * L * Lk * N : 0,
                w_tmp = mod_switch ? count * parts * L * N : 0;
-  ws.buf.reserve((w_pb + w_ext + w_prod + w_down + w_d + w_tmp + 6 * 32) * 8);
+  ws.reserve(scratch_bytes(count));
   size_t off = 0;
   uint64_t* pb = ws.take(w_pb, &off);
   uint64_t* ext = ws.take(w_ext, &off);

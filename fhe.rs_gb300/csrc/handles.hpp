@@ -17,6 +17,7 @@ struct fheg_scaler {
 struct fheg_params {
   std::unique_ptr<fheg::Params> p;
   std::vector<fheg_context> level_handles;
+  fheg::Workspace ws;  // scratch of the ragged batch entry points
 };
 struct fheg_ksk {
   fheg::Ksk k;

@@ -140,10 +140,27 @@ struct Params {
   const std::shared_ptr<Context>& ctx(size_t level) const;
 };
 
+// Scratch memory of an operation: either a buffer the workspace owns and
+// grows on demand, or an external region (a slice of the serving arena) of
+// fixed size.
 struct Workspace {
   DevBuf buf;
+  uint64_t* ext = nullptr;
+  size_t ext_bytes = 0;
+  void attach(uint64_t* p, size_t bytes) {
+    ext = p;
+    ext_bytes = bytes;
+  }
+  void reserve(size_t bytes) {
+    if (ext) {
+      if (bytes > ext_bytes) throw Error(FHEG_ERR_BUDGET, "operation scratch exceeds the reserved region");
+      return;
+    }
+    buf.reserve(bytes);
+  }
+  uint64_t* base() const { return ext ? ext : buf.u64(); }
   uint64_t* take(size_t words, size_t* offset) {
-    uint64_t* p = buf.u64() + *offset;
+    uint64_t* p = base() + *offset;
     *offset += (words + 31) & ~(size_t)31;
     return p;
   }
@@ -178,7 +195,10 @@ struct Multiplicator {
   bool mod_switch = false;
   Workspace ws;
   DevBuf staging;  // device copies for the host entry point
-  void multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count, cudaStream_t st);
+  void multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count, cudaStream_t st,
+                Workspace* scratch = nullptr);
+  // Bytes of scratch multiply() needs for `count` pairs.
+  size_t scratch_bytes(uint64_t count) const;
   size_t out_parts() const { return rk ? 2 : 3; }
   size_t out_level() const { return mod_switch ? level + 1 : level; }
 };
@@ -194,6 +214,17 @@ void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint
                          uint64_t* D, cudaStream_t st);
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st);
+// One rotation of a ragged batch: ciphertext `ct` ([2][L][N] at the key's
+// ciphertext level) rotated by `exponent` with `key`, into `out`.
+struct RotRequest {
+  const Ksk* key;
+  uint64_t exponent;
+  const uint64_t* ct;
+  uint64_t* out;
+};
+void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
+                              cudaStream_t st);
+size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
                             uint64_t count, cudaStream_t st);
 

@@ -32,23 +32,42 @@ namespace {
 
 // Job decoding shared by all NTT kernels: blockIdx.x enumerates
 // (poly, limb, block) with block fastest.
+// With `jobs` set, the launch is ragged: unit u is jobs[u] = (poly, limb,
+// aux, -) instead of (u / limbs, u % limbs, 0), so one launch can cover
+// polynomials with different numbers of limbs (ciphertexts at different
+// levels). `limb` always indexes `primes`.
 struct NttGeom {
-  const DevPrime* primes;  // one entry per limb
-  uint32_t limbs;          // limbs per polynomial
+  const DevPrime* primes;  // one entry per limb (modulus index)
+  uint32_t limbs;          // limbs per polynomial (1 for ragged launches)
   uint32_t s1;             // stages handled by the strided pass (0, 1 or 2)
+  const uint4* jobs;       // optional ragged job table
 };
 
 struct NttJob {
-  uint32_t poly, limb, beta;
+  uint32_t poly, limb, beta, aux;
 };
+
+__device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
+  NttJob j;
+  if (g.jobs) {
+    const uint4 t = g.jobs[unit];
+    j.poly = t.x;
+    j.limb = t.y;
+    j.aux = t.z;
+  } else {
+    j.limb = (uint32_t)(unit % g.limbs);
+    j.poly = (uint32_t)(unit / g.limbs);
+    j.aux = 0;
+  }
+  j.beta = 0;
+  return j;
+}
 
 __device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
   uint32_t job = blockIdx.x;
-  NttJob j;
-  j.beta = job & ((1u << g.s1) - 1);
-  job >>= g.s1;
-  j.limb = job % g.limbs;
-  j.poly = job / g.limbs;
+  const uint32_t beta = job & ((1u << g.s1) - 1);
+  NttJob j = unit_job(g, job >> g.s1);
+  j.beta = beta;
   return j;
 }
 
@@ -344,11 +363,7 @@ __global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, u
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t b = gid % groups_per_limb;
-  const uint64_t job = gid / groups_per_limb;
-  NttJob jb;
-  jb.limb = job % g.limbs;
-  jb.poly = job / g.limbs;
-  jb.beta = 0;
+  const NttJob jb = unit_job(g, gid / groups_per_limb);
   const DevPrime pr = g.primes[jb.limb];
   uint64_t x[1 << S1];
 #pragma unroll
@@ -377,11 +392,7 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t b = gid % groups_per_limb;
-  const uint64_t job = gid / groups_per_limb;
-  NttJob jb;
-  jb.limb = job % g.limbs;
-  jb.poly = job / g.limbs;
-  jb.beta = 0;
+  const NttJob jb = unit_job(g, gid / groups_per_limb);
   const DevPrime pr = g.primes[jb.limb];
   const uint32_t n_total = 1u << (logb + S1);
   uint64_t x[1 << S1];
@@ -417,10 +428,21 @@ struct SrcPoly {
   }
 };
 
+// Destinations also provide `reload`, which the two-pass sizes use to read
+// back the intermediate values the first pass stored.
 struct DstPoly {
   PolyRef r;
   __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
     r.at(j.poly, j.limb)[i] = v;
+  }
+  __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const { return r.at(j.poly, j.limb)[i]; }
+};
+
+template <class Dst>
+struct SrcReload {
+  Dst d;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    return d.reload(j, i);
   }
 };
 
@@ -504,10 +526,9 @@ constexpr uint32_t kMaxSmemLogN = 14;
 
 // Full forward NTT, any 3 <= logn <= 16. For logn > 14 the source is read by
 // the strided pass and the result goes through `dst` twice: the strided pass
-// writes its lazy output to dst, and the block pass reads it back from dst
-// (so dst must be a plain polynomial batch: a DstPoly).
-template <bool REDUCE, class Src>
-void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly dst, cudaStream_t st) {
+// writes its lazy output to dst, and the block pass reads it back.
+template <bool REDUCE, class Src, class Dst>
+void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
   if (logn <= kMaxSmemLogN) {
     g.s1 = 0;
     ntt_fwd_single<REDUCE>(logn, g, polys, src, dst, st);
@@ -526,14 +547,13 @@ void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly 
   }
   after_launch("k_ntt_fwd_top");
   g.s1 = s1;
-  SrcPoly mid{dst.r};
-  launch_fwd_block<kMaxSmemLogN, REDUCE>(g, polys, mid, dst, st);
+  launch_fwd_block<kMaxSmemLogN, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st);
 }
 
 // Full inverse NTT, any 3 <= logn <= 16. For logn > 14 the block pass writes
-// to `dst` and the strided pass finishes in place (dst must be a DstPoly).
-template <class Src>
-void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly dst, cudaStream_t st) {
+// to `dst` and the strided pass finishes in place.
+template <class Src, class Dst>
+void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
   if (logn <= kMaxSmemLogN) {
     g.s1 = 0;
     ntt_inv_single<true>(logn, g, polys, src, dst, st);
@@ -545,7 +565,7 @@ void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, DstPoly 
   const uint32_t groups = 1u << kMaxSmemLogN;
   const uint64_t threads = polys * g.limbs * groups;
   g.s1 = 0;
-  SrcPoly mid{dst.r};
+  SrcReload<Dst> mid{dst};
   if (s1 == 1) {
     k_ntt_inv_top<1><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, mid, dst);
   } else if (s1 == 2) {

@@ -192,6 +192,17 @@ FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_
 FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const uint64_t* d_ct,
                                      uint64_t* d_out, size_t count, void* stream);
 
+/* A ragged batch of rotations: ciphertext b (at its key's ciphertext level,
+ * [2][L_b][N] Ntt) is rotated with keys[b] by exponents[b] into d_outs[b],
+ * exactly as GaloisKey::relinearize_into (galois_key.rs:90-124) would one at a
+ * time (EvaluationKey::rotates_columns_by / rotates_rows,
+ * evaluation_key.rs:92-131). Ciphertexts may sit at different levels; all keys
+ * must come from `par`. One launch per stage covers the whole batch. Calls on
+ * the same parameters must not run concurrently (shared scratch). */
+FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
+                                           const size_t* exponents, const uint64_t* const* d_cts,
+                                           uint64_t* const* d_outs, size_t count, void* stream);
+
 /* Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) for ciphertexts
  * at `level` with `parts` polynomials: d_ct [count][parts][L][N] ->
  * d_out [count][parts][L-1][N]. d_ct is used as scratch. */
@@ -250,5 +261,60 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
  * streams, or different threads without ordering) race on it. */
 FHEG_API int fheg_relinearize_noalloc(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
                                       void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Serving runtime                                                            */
+
+/* No counterpart in the reference (fhe.rs evaluates one operation per call on
+ * the caller's thread). A server owns a fixed device-memory budget and a
+ * scheduler thread that batches pending requests with the same operation and
+ * parameters (rotations with any keys, exponents and levels batch together),
+ * admits a batch when one of its streams is free and the batch's inputs,
+ * outputs and scratch fit in the budget, and runs host->device copies, the
+ * batched operation and device->host copies on that stream. Results are
+ * bit-identical to the single-operation entry points. A request that does not
+ * fit in the budget even alone completes with FHEG_ERR_BUDGET. */
+typedef struct fheg_server fheg_server;
+
+typedef struct fheg_server_config {
+  size_t hbm_budget_bytes; /* device arena (inputs, outputs and scratch of running batches) */
+  uint32_t streams;        /* batches in flight at once */
+  uint32_t max_batch;      /* requests per batch */
+} fheg_server_config;
+
+enum fheg_server_op {
+  FHEG_OP_MUL_RELIN = 0,   /* Multiplicator::multiply (fhe/src/bfv/ops/mul.rs:158-227) */
+  FHEG_OP_ROTATE = 1,      /* GaloisKey::relinearize (fhe/src/bfv/keys/galois_key.rs:63-124) */
+  FHEG_OP_ADD = 2,         /* Add<&Ciphertext> (fhe/src/bfv/ops/mod.rs:15-43) */
+  FHEG_OP_SWITCH_DOWN = 3  /* Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) */
+};
+
+typedef struct fheg_request {
+  int op;                          /* enum fheg_server_op */
+  const fheg_params* par;
+  const fheg_multiplicator* mult;  /* FHEG_OP_MUL_RELIN */
+  const fheg_ksk* key;             /* FHEG_OP_ROTATE */
+  size_t exponent;                 /* FHEG_OP_ROTATE */
+  size_t level;                    /* FHEG_OP_ADD, FHEG_OP_SWITCH_DOWN */
+  const uint64_t* in0;             /* host [2][L][N] */
+  const uint64_t* in1;             /* host [2][L][N] (MUL_RELIN, ADD) */
+  uint64_t* out;                   /* host, the shape of the operation's result */
+} fheg_request;
+
+FHEG_API int fheg_server_create(const fheg_server_config* cfg, fheg_server** out);
+/* Finishes every submitted request, then stops the scheduler. */
+FHEG_API void fheg_server_destroy(fheg_server* s);
+/* Validates and queues a request; host buffers must stay valid until it completes. */
+FHEG_API int fheg_server_submit(fheg_server* s, const fheg_request* req, uint64_t* id);
+/* Waits at most timeout_ms for the request; returns its status, or
+ * FHEG_ERR_TIMEOUT when it has not completed yet. */
+FHEG_API int fheg_server_wait(fheg_server* s, uint64_t id, uint32_t timeout_ms);
+/* Host steady-clock times (ns) of submission, batch start and completion. */
+FHEG_API int fheg_server_request_times(fheg_server* s, uint64_t id, int64_t* submit_ns, int64_t* start_ns,
+                                       int64_t* done_ns);
+/* Forgets a completed request. */
+FHEG_API int fheg_server_release(fheg_server* s, uint64_t id);
+FHEG_API int fheg_server_stats(fheg_server* s, uint64_t* submitted, uint64_t* completed, uint64_t* batches,
+                               size_t* peak_bytes);
 
 #endif /* FHEG_H */

@@ -905,25 +905,21 @@ class Switcher:
 
 
 def sample_vec_cbd(size: int, variance: int, rng: np.random.Generator) -> np.ndarray:
-    """fhe-util/src/lib.rs:22-55 `sample_vec_cbd` over a numpy u64 stream."""
+    """fhe-util/src/lib.rs:22-55 `sample_vec_cbd` over a numpy u64 stream.
+
+    The reference keeps a bit pool fed by 64-bit draws (appended above the
+    bits already pooled) and consumes 4*variance bits per sample: the first
+    2*variance are added, the next 2*variance subtracted. That is the same as
+    cutting the concatenated little-endian bit stream of the draws into
+    consecutive 4*variance-bit chunks, which is what this does."""
     if not (1 <= variance <= 16):
         raise ValueError("The variance should be between 1 and 16")
-    number_bits = 4 * variance
-    mask_add = ((M64 >> (64 - number_bits)) >> (2 * variance))
-    mask_sub = mask_add << (2 * variance)
-    draws = rng.integers(0, 1 << 64, size=size + 2, dtype=np.uint64, endpoint=False).tolist()
-    di = 0
-    pool, nbits = 0, 0
-    out = np.zeros(size, dtype=np.int64)
-    for k in range(size):
-        if nbits < number_bits:
-            pool |= int(draws[di]) << nbits
-            di += 1
-            nbits += 64
-        out[k] = bin(pool & mask_add).count("1") - bin(pool & mask_sub).count("1")
-        pool >>= number_bits
-        nbits -= number_bits
-    return out
+    nb = 4 * variance
+    ndraws = (size * nb + 63) // 64 + 2
+    draws = rng.integers(0, 1 << 64, size=ndraws, dtype=np.uint64, endpoint=False)
+    bits = np.unpackbits(draws.view(np.uint8), bitorder="little")[: size * nb].reshape(size, nb)
+    half = 2 * variance
+    return bits[:, :half].sum(axis=1).astype(np.int64) - bits[:, half:].sum(axis=1).astype(np.int64)
 
 
 # ---------------------------------------------------------------------------

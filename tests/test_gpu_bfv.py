@@ -206,3 +206,26 @@ def test_errors(fg, ora, cuda):
     with pytest.raises(fg.FhegError) as e:
         s.par.context_at_level(3)
     assert e.value.code == fg.ERR_INVALID_LEVEL
+
+
+@pytest.mark.parametrize("n,L,count", [(4096, 4, 6), (32768, 5, 4)])
+def test_rotate_ragged_batch(fg, ora, cuda, n, L, count):
+    """Ciphertexts at different levels, each rotated with its own key in one
+    batched call, equal the oracle's one-at-a-time GaloisKey::relinearize."""
+    s = Setup(fg, ora, n, L, 65537, seed=1000 + n + L)
+    rng = np.random.default_rng(77)
+    levels = [int(x) for x in rng.integers(0, L - 1, count)]  # keep >= 2 moduli
+    steps = [int(x) for x in rng.integers(1, n // 2, count)]
+    keys, cts_o, cts_d, want = [], [], [], []
+    for b in range(count):
+        lvl = levels[b]
+        e = ora.rotation_exponent(s.par_o, steps[b]) if b % 3 else 2 * n - 1
+        gk_o = ora.GaloisKey(s.sk, e, lvl, lvl, s.rng)
+        keys.append(fg.GaloisKey(s.par, e, gk_o.ksk.c0_array(), gk_o.ksk.c1_array(), lvl, lvl))
+        _, cts = s.encrypt(1, level=lvl)
+        cts_o.append(cts[0])
+        cts_d.append(fg.to_device(cts[0].to_array()))
+        want.append(gk_o.relinearize(cts[0]).to_array())
+    outs = fg.rotate_batch(s.par, keys, cts_d)
+    for b in range(count):
+        assert np.array_equal(fg.to_host(outs[b]), want[b]), f"entry {b} (level {levels[b]})"
