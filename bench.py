@@ -3,9 +3,11 @@
 Workload (one step): `Multiplicator::multiply` with relinearization on a batch
 of 64 ciphertext pairs at N = 2^14 with six 62-bit moduli, the default
 extension basis of seven 62-bit primes, t = 65537, relinearization key
-resident on the device. Ciphertexts are synthetic: real encryptions made by
-the CPU oracle from a seeded RNG. The metric is ciphertext products per second
-(whole job). Besides the device-resident number the line carries:
+resident on the device, the pipeline recorded once as a CUDA graph and
+replayed. Ciphertexts are synthetic: real encryptions made by the CPU oracle
+from a seeded RNG. The metric is ciphertext products per second (whole job).
+Besides the device-resident number the line carries:
+  direct_calls  the same batch without the graph;
   e2e           the same metric through the host entry point (pinned host
                 buffers, H2D + compute + D2H inside the timed region);
   single        64 one-ciphertext launches (the unbatched GPU path);
@@ -33,10 +35,32 @@ sys.path.insert(0, ROOT)
 N, L, T = 1 << 14, 6, 65537
 METRIC = "BFV mul+relin ct/s N=2^14 L=6, batched vs single, bit-exact; NTT % HBM peak"
 UNIT = "ct/s"
-# DRAM bytes per launch of the forward NTT kernel (k_ntt_fwd<14>) on the
-# bench's 1536-limb batch, from an ncu capture (profiles/ntt_fwd_n16384.md);
-# None until a capture exists.
-NTT_FWD_TRAFFIC_BYTES = None
+# Algorithmic traffic of each stage of one product, in limbs of 8N bytes
+# (L = 6 ciphertext moduli, M = 13 extended, Lk = 6 key moduli): what a stage
+# must read and write at least once; twiddle tables stay in L2.
+STAGE_LIMBS = {
+    "A": 8 * L,                      # read + write the 4 operands
+    "B": 4 * L + 4 * (2 * L + 1 - L),  # read 4L, write 4(M - L)
+    "C": 8 * (2 * L + 1 - L),        # read + write the extension limbs
+    "D": 4 * (2 * L + 1) + 3 * (2 * L + 1),  # read 4M operand limbs, write 3M
+    "E": 3 * (2 * L + 1) + 3 * L,    # read 3M, write 3L
+    "F": 3 * L + L * L + 2 * L,      # read c0, c1, c2; write the digit NTTs and c0, c1
+    "G": L * L + 4 * L,              # read the digit NTTs, read + write c0, c1 (keys added per batch)
+}
+STAGE_KERNELS = {
+    "A": "k_ntt_inv (inverse NTT of the operands)",
+    "B": "k_rns_scale (basis extension 6 -> 7 new moduli)",
+    "C": "k_ntt_fwd (forward NTT of the extension limbs)",
+    "D": "k_ntt_inv<SrcTensor> (tensor product + inverse NTT, 13 moduli)",
+    "E": "k_rns_scale (t/Q scale-down 13 -> 6 moduli)",
+    "F": "k_ntt_fwd (digit NTTs in every key modulus + c0/c1 NTTs)",
+    "G": "k_key_mac (key inner product)",
+}
+# DRAM bytes (read + write) of each stage's kernels for one 64-pair
+# multiplication with the plan A,C,D,F = 14 and F in two launches, from the
+# ncu capture summarised in profiles/stages_mul_relin_n16384_b64.md.
+STAGE_TRAFFIC_BYTES = {"A": 354.8e6, "B": 384.3e6, "C": 442.2e6, "D": 729.1e6, "E": 445.9e6, "F": 484.4e6,
+                       "G": 493.9e6}
 
 
 def _peaks():
@@ -195,6 +219,12 @@ def run_ours(args, rank: int, world: int):
     lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
     out_d = fg.empty((B, 2, L, N))
     stream = torch.cuda.current_stream()
+    logn = N.bit_length() - 1
+    if args.ntt_block == "auto":
+        mult.autotune(B)
+    else:
+        fg.ntt_plan_set(logn, int(args.ntt_block))
+    ntt_block = dict(zip(["A", "C", "D", "F", "F_split"], mult.plan))
 
     # Parity gate: two products of the batch against the oracle.
     mult.multiply(lhs_d, rhs_d, out_d)
@@ -207,9 +237,15 @@ def run_ours(args, rank: int, world: int):
         if not np.array_equal(got[b], mult_o.multiply(lo, ro).to_array()):
             raise SystemExit(f"bench: GPU product {b} is not bit-exact with the oracle")
 
+    # The step: the whole batched pipeline recorded once as a CUDA graph and
+    # replayed (the graph reads lhs_d / rhs_d and writes out_d at replay).
+    graph = mult.capture(lhs_d, rhs_d, out_d)
     for _ in range(args.warmup):
+        graph.launch()
         mult.multiply(lhs_d, rhs_d, out_d)
     torch.cuda.synchronize()
+    if not np.array_equal(fg.to_host(out_d), got):
+        raise SystemExit("bench: graph replay differs from the direct call")
     if dist:
         dist.barrier()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -218,11 +254,18 @@ def run_ours(args, rank: int, world: int):
         torch.cuda.synchronize()
         start.record(stream)
         for _ in range(args.steps):
-            mult.multiply(lhs_d, rhs_d, out_d)
+            graph.launch()
         end.record(stream)
         torch.cuda.synchronize()
     launches = fg.kernel_launch_count() - launches0
     ms = start.elapsed_time(end) / args.steps
+    # The same batch through direct calls (one launch call per kernel).
+    start.record(stream)
+    for _ in range(args.steps):
+        mult.multiply(lhs_d, rhs_d, out_d)
+    end.record(stream)
+    torch.cuda.synchronize()
+    direct_ms = start.elapsed_time(end) / args.steps
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -284,6 +327,16 @@ def run_ours(args, rank: int, world: int):
     inv_gbs = (data_bytes + tw_bytes) / (inv_ms / 1000.0) / 1e9
     peak, peak_kind = _peaks()
 
+    # Stage durations of the batched pipeline (events between stages, the
+    # median of 5 runs) and the dominant stage's roofline.
+    runs = [mult.stage_times(lhs_d, rhs_d, out_d) for _ in range(6)][1:]
+    stage_ms = {k: statistics.median(r[k] for r in runs) for k in runs[0]}
+    limb = 8 * N
+    stage_bytes = {k: B * v * limb for k, v in STAGE_LIMBS.items()}
+    stage_bytes["G"] += 2 * L * L * limb  # the relinearization key, read once per batch
+    dom = max(stage_ms, key=stage_ms.get)
+    dom_gbs = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
@@ -306,16 +359,24 @@ def run_ours(args, rank: int, world: int):
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions by the CPU oracle)",
             "config": {"workload": "bfv_mul_relin_batched", "degree": N, "moduli": L, "moduli_bits": 62,
                        "extension_moduli": 7, "plaintext": T, "batch_pairs": B, "keys": "device resident",
+                       "ntt_block_logn": ntt_block, "step": f"one CUDA graph of {graph.kernels} kernels",
                        "l2": "no flush: each step streams > 1 GB (inputs 201 MB, outputs 100 MB, scratch) through "
                              "the 126 MB L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "single": {"value": single_rate, "unit": UNIT, "note": f"{B} one-ciphertext launches"},
+            "direct_calls": {"value": B / (direct_ms / 1000.0), "unit": UNIT, "ms_per_step": direct_ms,
+                             "note": "the batch without the graph"},
             "batch_vs_single": value / world / single_rate,
             "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
                     "d2h_bytes_per_step": int(h_o.nbytes)},
-            "roofline": {"bound": "hbm", "achieved": fwd_gbs, "peak": peak, "unit": "GB/s", "frac": fwd_gbs / peak,
-                         "traffic": NTT_FWD_TRAFFIC_BYTES, "kernel": "k_ntt_fwd<14> (forward NTT, 1536 limbs)",
-                         "peak_kind": peak_kind, "inverse_achieved": inv_gbs, "inverse_frac": inv_gbs / peak,
-                         "fwd_ms": fwd_ms, "inv_ms": inv_ms},
+            "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
+                         "traffic": STAGE_TRAFFIC_BYTES.get(dom), "kernel": STAGE_KERNELS[dom],
+                         "algorithmic_bytes": stage_bytes[dom], "launch_ms": stage_ms[dom], "peak_kind": peak_kind,
+                         "note": "integer-issue bound: all arithmetic is exact 64-bit residue arithmetic on CUDA cores"},
+            "stages": {k: {"ms": stage_ms[k], "gbs": stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9,
+                           "kernel": STAGE_KERNELS[k]} for k in stage_ms},
+            "ntt": {"kernel": "forward / inverse NTT alone, 256 polys x 6 limbs", "fwd_gbs": fwd_gbs,
+                    "inv_gbs": inv_gbs, "fwd_frac": fwd_gbs / peak, "inv_frac": inv_gbs / peak, "fwd_ms": fwd_ms,
+                    "inv_ms": inv_ms},
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
@@ -326,10 +387,10 @@ def run_ours(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
-def run_ntt(args):
-    """The batched NTT configuration: forward + inverse over `--polys`
-    polynomials of six 62-bit moduli at N = 2^14 (device resident), GB/s of
-    algorithmic traffic against the measured HBM bandwidth."""
+def run_stages(args):
+    """Stage breakdown of the batched multiplication (64 pairs at N = 2^14,
+    L = 6): W warm-up multiplies, then one multiply with events at the stage
+    boundaries. Small enough to run under a profiler (14 launches a multiply)."""
     import torch
 
     import __graft_entry__ as ge
@@ -338,56 +399,99 @@ def run_ntt(args):
     ge.build()
     fg = ge.load_package()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    B = args.batch
+    par_o, sk, rk_o, cts, lhs, rhs = make_inputs(ora, B)
+    par = fg.BfvParameters(N, par_o.moduli, T)
+    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
+    mult = fg.Multiplicator.default(rk)
+    if args.stage_plan:
+        mult.plan = [int(x) for x in args.stage_plan.split(",")]
+    lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
+    out_d = fg.empty((B, 2, L, N))
+    for _ in range(args.warmup):
+        mult.multiply(lhs_d, rhs_d, out_d)
+    ms = mult.stage_times(lhs_d, rhs_d, out_d)
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "stages", "batch_pairs": B, "plan": mult.plan, "stage_ms": ms}), flush=True)
+
+
+def run_ntt(args):
+    """The batched NTT configuration: forward + inverse over `--polys`
+    polynomials of six 62-bit moduli at N = 2^logn (device resident), GB/s of
+    algorithmic traffic against the measured HBM bandwidth. Every valid NTT
+    plan is timed; the line reports the fastest (what fheg_ntt_autotune
+    installs) and lists the others."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    logn = args.logn
+    n = 1 << logn
     moduli, ub = [], 1 << 62
     while len(moduli) < L:
-        ub = ora.generate_prime(62, 2 * N, ub)
+        ub = ora.generate_prime(62, 2 * n, ub)
         moduli.append(ub)
     rng = np.random.default_rng(1)
     polys = args.polys
-    one = np.stack([rng.integers(0, m, N, dtype=np.uint64) for m in moduli])
-    ctx = fg.Context(moduli, N)
+    one = np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli])
+    ctx = fg.Context(moduli, n)
     buf = fg.to_device(np.tile(one[None], (polys, 1, 1)))
     expect = one.copy()
     for i, m in enumerate(moduli):
-        ora.ntt_operator(m, N).forward(expect[i])
-    fg.ntt_forward(ctx, buf)
-    torch.cuda.synchronize()
-    got = fg.to_host(buf[:1])[0]
-    if not np.array_equal(got, expect):
-        raise SystemExit("bench: NTT is not bit-exact with the oracle")
-    fg.ntt_backward(ctx, buf)
-    for _ in range(args.warmup):
-        fg.ntt_forward(ctx, buf)
-        fg.ntt_backward(ctx, buf)
+        ora.ntt_operator(m, n).forward(expect[i])
+    plans = [bl for bl in (12, 13, 14) if bl <= logn and logn - bl <= 4 and (bl < logn or logn <= 14)] or [logn]
+    default = fg.ntt_plan_get(logn)
     stream = torch.cuda.current_stream()
     start, mid, end = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    fwd = inv = 0.0
-    launches0 = fg.kernel_launch_count()
-    with ClockSampler(0) as clocks:
-        for _ in range(args.steps):
-            start.record(stream)
+    nbytes = 2 * 8 * polys * L * n + 2 * 8 * L * n
+    results = {}
+    launches = 0
+    for bl in plans:
+        fg.ntt_plan_set(logn, bl)
+        fg.ntt_forward(ctx, buf)
+        torch.cuda.synchronize()
+        if not np.array_equal(fg.to_host(buf[:1])[0], expect):
+            raise SystemExit(f"bench: NTT (blocks of 2^{bl}) is not bit-exact with the oracle")
+        fg.ntt_backward(ctx, buf)
+        for _ in range(args.warmup):
             fg.ntt_forward(ctx, buf)
-            mid.record(stream)
             fg.ntt_backward(ctx, buf)
-            end.record(stream)
-            torch.cuda.synchronize()
-            fwd += start.elapsed_time(mid)
-            inv += mid.elapsed_time(end)
-    launches = fg.kernel_launch_count() - launches0
-    fwd /= args.steps
-    inv /= args.steps
-    nbytes = 2 * 8 * polys * L * N + 2 * 8 * L * N
+        fwd = inv = 0.0
+        launches0 = fg.kernel_launch_count()
+        with ClockSampler(0) as clocks:
+            for _ in range(args.steps):
+                start.record(stream)
+                fg.ntt_forward(ctx, buf)
+                mid.record(stream)
+                fg.ntt_backward(ctx, buf)
+                end.record(stream)
+                torch.cuda.synchronize()
+                fwd += start.elapsed_time(mid)
+                inv += mid.elapsed_time(end)
+        fwd /= args.steps
+        inv /= args.steps
+        results[bl] = {"fwd_ms": fwd, "inv_ms": inv, "gbs": 2 * nbytes / ((fwd + inv) / 1000.0) / 1e9,
+                       "clocks": clocks.summary(), "launches": fg.kernel_launch_count() - launches0}
+    fg.ntt_plan_set(logn, default)
+    best = max(results, key=lambda k: results[k]["gbs"])
+    r = results[best]
+    fwd, inv, gbs = r["fwd_ms"], r["inv_ms"], r["gbs"]
     peak, kind = _peaks()
-    gbs = 2 * nbytes / ((fwd + inv) / 1000.0) / 1e9
-    line = {"metric": "NTT fwd+inv GB/s N=2^14 L=6", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+    line = {"metric": f"NTT fwd+inv GB/s N=2^{logn} L=6", "value": gbs, "unit": "GB/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": fwd + inv, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": "ntt_batched", "degree": N, "moduli": L, "polys": polys,
-                       "l2": f"buffer {polys * L * N * 8 / 1e6:.0f} MB > L2"},
+            "config": {"workload": "ntt_batched", "degree": n, "moduli": L, "polys": polys, "block_logn": best,
+                       "l2": f"buffer {polys * L * n * 8 / 1e6:.0f} MB > L2"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "traffic": None, "peak_kind": kind, "fwd_ms": fwd, "inv_ms": inv,
                          "fwd_gbs": nbytes / (fwd / 1000) / 1e9, "inv_gbs": nbytes / (inv / 1000) / 1e9},
-            "gpu_launches": int(launches), "clocks": clocks.summary()}
+            "plans": {str(k): {"fwd_ms": v["fwd_ms"], "inv_ms": v["inv_ms"], "gbs": v["gbs"]}
+                      for k, v in results.items()},
+            "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -426,6 +530,10 @@ def run_rotate(args):
         cts_o.append(ct)
         cts_d.append(fg.to_device(ct.to_array()))
     outs = [fg.empty(c.shape) for c in cts_d]
+    if args.ntt_block == "auto":
+        fg.ntt_autotune(par.context_at_level(0), 64)
+    else:
+        fg.ntt_plan_set(15, int(args.ntt_block))
     fg.rotate_batch(par, keys, cts_d, outs)
     torch.cuda.synchronize()
     for b in (0, count - 1):
@@ -458,7 +566,7 @@ def run_rotate(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
             "config": {"workload": "rotation_uneven_levels", "degree": n, "top_moduli": top, "count": count,
-                       "live_moduli": lv, "key_bytes_resident": key_bytes},
+                       "live_moduli": lv, "key_bytes_resident": key_bytes, "ntt_block_logn": fg.ntt_plan_get(15)},
             "single": {"value": count / (single_ms / 1000), "unit": "ct/s", "note": "one call per ciphertext"},
             "batch_vs_single": single_ms / ms, "gpu_launches": int(launches), "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
@@ -469,53 +577,69 @@ SERVE_MIX = (("mul", 0.50), ("rot", 0.30), ("add", 0.15), ("down", 0.05))
 
 
 def _serve_setup(fg, ora, torch, n, nm, seed, ring):
-    """Keys, pinned input ciphertexts and pinned output rings of one parameter set."""
+    """Keys, pinned input ciphertexts and a pinned output ring of one
+    parameter set, at every level with at least two live moduli (relinearization
+    key, multiplicator and two Galois keys per level)."""
     rng = np.random.default_rng(seed)
     par_o = ora.BfvParameters(n, T, moduli_sizes=[62] * nm)
     sk = ora.SecretKey.random(par_o, rng)
-    rk_o = ora.RelinearizationKey(sk, rng)
     par = fg.BfvParameters(n, par_o.moduli, T)
-    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
-    exps = (2 * n - 1, ora.rotation_exponent(par_o, 1))
-    gks_o = [ora.GaloisKey(sk, e, 0, 0, rng) for e in exps]
-    gks = [fg.GaloisKey(par, e, g.ksk.c0_array(), g.ksk.c1_array()) for e, g in zip(exps, gks_o)]
-    cts_o = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, n, dtype=np.uint64), "simd", par_o), rng)
-             for _ in range(6)]
 
     def pinned(shape):
         return torch.empty(shape, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
 
-    cts = []
-    for c in cts_o:
-        h = pinned((2, nm, n))
-        h[...] = c.to_array()
-        cts.append(h)
-    return {"n": n, "L": nm, "par_o": par_o, "par": par, "rk_o": rk_o, "mult_o": ora.Multiplicator.default(rk_o),
-            "mult": fg.Multiplicator.default(rk), "rk": rk, "gks_o": gks_o, "gks": gks, "cts_o": cts_o, "cts": cts,
-            "out": [pinned((2, nm, n)) for _ in range(ring)], "out_down": [pinned((2, nm - 1, n)) for _ in range(ring)]}
+    levels = []
+    for lvl in range(nm - 1):
+        rk_o = ora.RelinearizationKey(sk, rng, lvl, lvl)
+        rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array(), lvl, lvl)
+        exps = (2 * n - 1, ora.rotation_exponent(par_o, 1 + lvl))
+        gks_o = [ora.GaloisKey(sk, e, lvl, lvl, rng) for e in exps]
+        gks = [fg.GaloisKey(par, e, g.ksk.c0_array(), g.ksk.c1_array(), lvl, lvl) for e, g in zip(exps, gks_o)]
+        cts_o = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, n, dtype=np.uint64), "simd", par_o, lvl), rng)
+                 for _ in range(3)]
+        cts = []
+        for c in cts_o:
+            h = pinned((2, nm - lvl, n))
+            h[...] = c.to_array()
+            cts.append(h)
+        levels.append({"rk_o": rk_o, "rk": rk, "mult": fg.Multiplicator.default(rk), "gks_o": gks_o, "gks": gks,
+                       "cts_o": cts_o, "cts": cts})
+    slot_words = 2 * nm * n
+    return {"n": n, "L": nm, "par_o": par_o, "par": par, "levels": levels, "ring": ring,
+            "out_flat": pinned((ring * slot_words,)), "slot_words": slot_words}
 
 
 def _serve_requests(count, seed):
-    """(set index, kind, operand a, operand b, key index) of each request."""
+    """(set index, kind, level, operand a, operand b, key index) of each
+    request: set uniform, kind by the mix, level uniform over the live range."""
     rng = np.random.default_rng(seed)
     kinds = [k for k, _ in SERVE_MIX]
     probs = [p for _, p in SERVE_MIX]
     sets = rng.integers(0, len(SERVE_SETS), count)
     ks = rng.choice(len(kinds), count, p=probs)
-    a, b, g = rng.integers(0, 6, count), rng.integers(0, 6, count), rng.integers(0, 2, count)
-    return [(int(sets[i]), kinds[ks[i]], int(a[i]), int(b[i]), int(g[i])) for i in range(count)]
+    lv = [int(rng.integers(0, SERVE_SETS[si][1] - 1)) for si in sets]
+    a, b, g = rng.integers(0, 3, count), rng.integers(0, 3, count), rng.integers(0, 2, count)
+    return [(int(sets[i]), kinds[ks[i]], lv[i], int(a[i]), int(b[i]), int(g[i])) for i in range(count)]
+
+
+def _serve_out(s, slot, shape):
+    w = int(np.prod(shape))
+    k = slot % s["ring"]
+    return s["out_flat"][k * s["slot_words"]:k * s["slot_words"] + w].reshape(shape)
 
 
 def _serve_submit(srv, setups, req, slot):
-    si, kind, a, b, g = req
+    si, kind, lvl, a, b, g = req
     s = setups[si]
+    lv = s["levels"][lvl]
+    n, live = s["n"], s["L"] - lvl
     if kind == "mul":
-        return srv.submit_mul_relin(s["mult"], s["cts"][a], s["cts"][b], out=s["out"][slot % len(s["out"])])
+        return srv.submit_mul_relin(lv["mult"], lv["cts"][a], lv["cts"][b], out=_serve_out(s, slot, (2, live, n)))
     if kind == "rot":
-        return srv.submit_rotate(s["gks"][g], s["cts"][a], out=s["out"][slot % len(s["out"])])
+        return srv.submit_rotate(lv["gks"][g], lv["cts"][a], out=_serve_out(s, slot, (2, live, n)))
     if kind == "add":
-        return srv.submit_add(s["par"], 0, s["cts"][a], s["cts"][b], out=s["out"][slot % len(s["out"])])
-    return srv.submit_switch_down(s["par"], 0, s["cts"][a], out=s["out_down"][slot % len(s["out_down"])])
+        return srv.submit_add(s["par"], lvl, lv["cts"][a], lv["cts"][b], out=_serve_out(s, slot, (2, live, n)))
+    return srv.submit_switch_down(s["par"], lvl, lv["cts"][a], out=_serve_out(s, slot, (2, live - 1, n)))
 
 
 def _serve_run(fg, setups, reqs, budget, streams, max_batch, arrivals=None):
@@ -563,19 +687,25 @@ def run_serve(args):
     ring = 64
     setups = [_serve_setup(fg, ora, torch, n, nm, 100 + k, ring) for k, (n, nm) in enumerate(SERVE_SETS)]
     budget = int(args.serve_budget_gb * (1 << 30))
-    # Parity gate: every operation of every set through the server, alone,
-    # against the oracle.
+    for s in setups:
+        fg.ntt_autotune(s["par"].context_at_level(0), 32)
+        for lv in s["levels"]:
+            lv["mult"].autotune(8)
+    # Parity gate: every operation of every set, at its top and bottom live
+    # levels, through the server alone, against the oracle.
     with fg.Server(budget, streams=1, max_batch=1) as srv:
         for si, s in enumerate(setups):
-            co = s["cts_o"]
-            checks = [(("mul", 0, 1, 0), s["mult_o"].multiply(co[0], co[1])),
-                      (("rot", 2, 0, 1), s["gks_o"][1].relinearize(co[2])),
-                      (("add", 3, 4, 0), co[3] + co[4]),
-                      (("down", 5, 0, 0), co[5].copy().switch_down())]
-            for (kind, a, b, g), want in checks:
-                got = srv.wait(_serve_submit(srv, setups, (si, kind, a, b, g), 0), 600000)
-                if not np.array_equal(got, want.to_array()):
-                    raise SystemExit(f"bench: served {kind} at N={s['n']} is not bit-exact with the oracle")
+            for lvl in (0, s["L"] - 2):
+                lv = s["levels"][lvl]
+                co = lv["cts_o"]
+                checks = [(("mul", 0, 1, 0), ora.Multiplicator.default(lv["rk_o"]).multiply(co[0], co[1])),
+                          (("rot", 2, 0, 1), lv["gks_o"][1].relinearize(co[2])),
+                          (("add", 1, 2, 0), co[1] + co[2]),
+                          (("down", 0, 0, 0), co[0].copy().switch_down())]
+                for (kind, a, b, g), want in checks:
+                    got = srv.wait(_serve_submit(srv, setups, (si, kind, lvl, a, b, g), 0), 600000).copy()
+                    if not np.array_equal(got, want.to_array()):
+                        raise SystemExit(f"bench: served {kind} at N={s['n']} level {lvl} is not bit-exact")
     reqs = _serve_requests(args.serve_requests, 7)
     warm = _serve_requests(min(200, args.serve_requests), 8)
     for _ in range(max(1, args.warmup // 2)):
@@ -600,18 +730,21 @@ def run_serve(args):
     high = 0.7 * thr_b
     at_high_b = poisson(high, args.serve_streams, args.serve_batch)
     h2d = d2h = 0
-    for si, kind, _, _, _ in reqs:
+    for si, kind, lvl, _, _, _ in reqs:
         s = setups[si]
-        ct_bytes = 2 * s["L"] * s["n"] * 8
+        live = s["L"] - lvl
+        ct_bytes = 2 * live * s["n"] * 8
         h2d += ct_bytes * (2 if kind in ("mul", "add") else 1)
-        d2h += ct_bytes if kind != "down" else 2 * (s["L"] - 1) * s["n"] * 8
+        d2h += ct_bytes if kind != "down" else 2 * (live - 1) * s["n"] * 8
     line = {"metric": "BFV serving req/s (mixed N=2^13..2^15), p50/p99 vs one-at-a-time",
             "value": thr_b, "unit": "req/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
             "ms_per_step": 1000 * len(reqs) / thr_b, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
             "config": {"workload": "serve_mixed", "sets": [{"degree": n, "moduli": nm} for n, nm in SERVE_SETS],
+                       "levels": "uniform over the live range (2 .. L moduli)",
                        "mix": dict(SERVE_MIX), "requests": len(reqs), "hbm_budget_bytes": budget,
                        "streams": args.serve_streams, "max_batch": args.serve_batch,
+                       "ntt_block_logn": {str(n): fg.ntt_plan_get(n.bit_length() - 1) for n, _ in SERVE_SETS},
                        "host_buffers": "pinned"},
             "e2e": {"value": thr_b, "unit": "req/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "note": "one step = all requests, host buffers to host buffers"},
@@ -632,9 +765,12 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve"])
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages"])
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
+    ap.add_argument("--logn", type=int, default=14)
+    ap.add_argument("--stage-plan", default="", help="A,C,D,F,split block log2 of the multiply stages")
+    ap.add_argument("--ntt-block", default="auto", help="NTT plan for the degree: auto (autotune) or a block log2")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-budget-gb", type=float, default=24.0)
     ap.add_argument("--serve-streams", type=int, default=4)
@@ -648,6 +784,8 @@ def main():
         run_rotate(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "stages":
+        run_stages(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

@@ -123,6 +123,17 @@ def _declare(L):
         "fheg_relinearize_noalloc": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
+        "fheg_ntt_plan_set": (i, [ctypes.c_uint32, ctypes.c_uint32]),
+        "fheg_ntt_plan_get": (i, [ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_ntt_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_multiplicator_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_multiplicator_get_plan": (i, [c_vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_multiplicator_stage_times": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_float)]),
+        "fheg_multiplicator_set_plan": (i, [c_vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_multiplicator_capture": (i, [c_vp, c_vp, c_vp, c_vp, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_graph_launch": (i, [c_vp, c_vp]),
+        "fheg_graph_kernel_count": (i, [c_vp, ctypes.POINTER(c_u64)]),
+        "fheg_graph_destroy": (None, [c_vp]),
         "fheg_server_create": (i, [ctypes.POINTER(_ServerConfig), ctypes.POINTER(c_vp)]),
         "fheg_server_destroy": (None, [c_vp]),
         "fheg_server_submit": (i, [c_vp, ctypes.POINTER(_Request), ctypes.POINTER(c_u64)]),
@@ -320,6 +331,24 @@ def ntt_backward(ctx: Context, t):
     """Poly::into_power_basis on a batch [count][L][N] (in place)."""
     count = t.numel() // (ctx.L * ctx.degree)
     check(lib().fheg_ntt_backward(ctx._h, _dp(t), count, _stream()))
+
+
+def ntt_plan_set(logn: int, block_logn: int):
+    """Runs transforms of 2^logn as blocks of 2^block_logn (see fheg.h)."""
+    check(lib().fheg_ntt_plan_set(logn, block_logn))
+
+
+def ntt_plan_get(logn: int) -> int:
+    out = ctypes.c_uint32(0)
+    check(lib().fheg_ntt_plan_get(logn, ctypes.byref(out)))
+    return out.value
+
+
+def ntt_autotune(ctx: Context, count: int = 64) -> int:
+    """Times the valid plans for the context's degree and installs the fastest."""
+    out = ctypes.c_uint32(0)
+    check(lib().fheg_ntt_autotune(ctx._h, count, _stream(), ctypes.byref(out)))
+    return out.value
 
 
 def poly_op(ctx: Context, op: str, a, b=None):
@@ -575,6 +604,41 @@ class Multiplicator:
                                                 _stream() if stream is None else stream))
         return out
 
+    def autotune(self, count: int) -> list:
+        """Tunes the per-stage NTT plans on `count`-pair multiplications and
+        returns them ([A, C, D, F, F split])."""
+        out = (ctypes.c_uint32 * 5)()
+        check(lib().fheg_multiplicator_autotune(self._h, count, _stream(), out))
+        return list(out)
+
+    STAGES = ("A", "B", "C", "D", "E", "F", "G")
+
+    def stage_times(self, lhs, rhs, out) -> dict:
+        """One multiplication with events at the stage boundaries: ms per stage."""
+        ms = (ctypes.c_float * 7)()
+        check(lib().fheg_multiplicator_stage_times(self._h, _dp(lhs), _dp(rhs), _dp(out), lhs.shape[0], _stream(),
+                                                   ms))
+        return dict(zip(self.STAGES, [float(x) for x in ms]))
+
+    @property
+    def plan(self) -> list:
+        out = (ctypes.c_uint32 * 5)()
+        check(lib().fheg_multiplicator_get_plan(self._h, out))
+        return list(out)
+
+    @plan.setter
+    def plan(self, values):
+        arr = (ctypes.c_uint32 * 5)(*values)
+        check(lib().fheg_multiplicator_set_plan(self._h, arr))
+
+    def capture(self, lhs, rhs, out) -> "MultiplyGraph":
+        """Records multiply(lhs, rhs, out) on these device tensors into a CUDA
+        graph (runs it once first)."""
+        h = c_vp()
+        check(lib().fheg_multiplicator_capture(self._h, _dp(lhs), _dp(rhs), _dp(out), lhs.shape[0],
+                                               ctypes.byref(h)))
+        return MultiplyGraph(h, [self, lhs, rhs, out])
+
     def multiply_host(self, lhs: np.ndarray, rhs: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
         """End to end from host arrays [count][2][L][N] (u64)."""
         parts, level = self.output_shape()
@@ -585,6 +649,29 @@ class Multiplicator:
         lhs, rhs = np.ascontiguousarray(lhs, dtype=np.uint64), np.ascontiguousarray(rhs, dtype=np.uint64)
         check(lib().fheg_multiplicator_multiply_host(self._h, _ptr(lhs), _ptr(rhs), _ptr(out), count))
         return out
+
+
+class MultiplyGraph:
+    """A recorded batched multiplication; launch() replays it on the current
+    stream. Keeps its multiplicator and buffers alive."""
+
+    def __init__(self, handle, keep):
+        self._h = handle
+        self._keep = keep
+
+    def launch(self, stream: Optional[int] = None):
+        check(lib().fheg_graph_launch(self._h, _stream() if stream is None else stream))
+
+    @property
+    def kernels(self) -> int:
+        k = c_u64(0)
+        check(lib().fheg_graph_kernel_count(self._h, ctypes.byref(k)))
+        return k.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_graph_destroy(self._h)
+            self._h = None
 
 
 # ---------------------------------------------------------------------------

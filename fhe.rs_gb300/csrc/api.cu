@@ -1,7 +1,9 @@
 // C ABI of libfheg (declarations and reference mapping in include/fheg.h).
 
+#include <algorithm>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "fheg.h"
 #include "handles.hpp"
@@ -170,6 +172,198 @@ FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_
     need(ctx && (d_polys || !count), "null input");
     PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
     ntt_backward(*ctx->c, r, r, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_ntt_plan_set(uint32_t logn, uint32_t block_logn) {
+  return guard([&] { set_ntt_block_logn(logn, block_logn); });
+}
+
+FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
+  return guard([&] {
+    need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");
+    *block_logn = ntt_block_logn(logn);
+  });
+}
+
+// Times `run` under every valid NTT plan for 2^logn (one warm-up pass, then
+// a timed pass) and installs the fastest.
+template <class F>
+uint32_t autotune_plans(uint32_t logn, cudaStream_t st, F run) {
+  std::vector<uint32_t> plans;
+  for (uint32_t bl = 12; bl <= 14; bl++)
+    if (bl <= logn && logn - bl <= 4 && (bl < logn || logn <= 14)) plans.push_back(bl);
+  const uint32_t before = ntt_block_logn(logn);
+  if (plans.empty()) return before;
+  cudaEvent_t e0, e1;
+  check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+  check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+  float best_ms = 0;
+  uint32_t best = before;
+  try {
+    for (uint32_t bl : plans) {
+      set_ntt_block_logn(logn, bl);
+      for (int rep = 0; rep < 2; rep++) {
+        check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+        run();
+        check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+      }
+      check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+      float ms = 0;
+      check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+      if (best_ms == 0 || ms < best_ms) {
+        best_ms = ms;
+        best = bl;
+      }
+    }
+  } catch (...) {
+    set_ntt_block_logn(logn, before);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  set_ntt_block_logn(logn, best);
+  return best;
+}
+
+FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn) {
+  return guard([&] {
+    need(ctx && count && block_logn, "null input");
+    const Context& c = *ctx->c;
+    cudaStream_t st = as_stream(stream);
+    DevBuf buf(count * c.L() * c.N() * 8);
+    check_cuda(cudaMemsetAsync(buf.ptr, 0, buf.bytes, st), "cudaMemsetAsync");
+    PolyRef r = plain_ref(buf.u64(), c.L(), c.logn);
+    *block_logn = autotune_plans(c.logn, st, [&] {
+      for (int k = 0; k < 3; k++) {
+        ntt_forward(c, r, r, count, false, st);
+        ntt_backward(c, r, r, count, st);
+      }
+    });
+  });
+}
+
+namespace {
+
+// Event time of one call of `run` on `st` after a warm-up call.
+template <class F>
+float time_once(cudaStream_t st, F run) {
+  cudaEvent_t e0, e1;
+  check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+  check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+  float ms = 0;
+  try {
+    run();
+    check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+    run();
+    check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+    check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+void get_mul_plan(const Multiplicator& m, uint32_t* plan) {
+  const uint32_t logn = m.base->logn, dflt = ntt_block_logn(logn);
+  plan[0] = m.plan_a ? m.plan_a : dflt;
+  plan[1] = m.plan_c ? m.plan_c : dflt;
+  plan[2] = m.plan_d ? m.plan_d : dflt;
+  plan[3] = m.plan_f ? m.plan_f : dflt;
+  plan[4] = m.f_split ? 1 : 0;
+}
+
+void set_mul_plan(Multiplicator& m, const uint32_t* plan) {
+  const uint32_t logn = m.base->logn;
+  for (int k = 0; k < 4; k++)
+    if (!ntt_plan_valid(logn, plan[k])) throw Error(FHEG_ERR_INVALID_ARGUMENT, "unsupported NTT plan");
+  m.plan_a = plan[0];
+  m.plan_c = plan[1];
+  m.plan_d = plan[2];
+  m.plan_f = plan[3];
+  m.f_split = plan[4] != 0;
+}
+
+}  // namespace
+
+FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
+                                            uint64_t* d_out, size_t count, void* stream, float* ms) {
+  return guard([&] {
+    need(m && d_lhs && d_rhs && d_out && count && ms, "null input");
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t ev[8] = {};
+    try {
+      for (auto& e : ev) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+      m->m->multiply(d_lhs, d_rhs, d_out, count, st, nullptr, ev);
+      check_cuda(cudaEventSynchronize(ev[7]), "cudaEventSynchronize");
+      for (int k = 0; k < 7; k++) check_cuda(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]), "cudaEventElapsedTime");
+    } catch (...) {
+      for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+      throw;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+  });
+}
+
+FHEG_API int fheg_multiplicator_get_plan(const fheg_multiplicator* m, uint32_t* plan) {
+  return guard([&] {
+    need(m && plan, "null input");
+    get_mul_plan(*m->m, plan);
+  });
+}
+
+FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* plan) {
+  return guard([&] {
+    need(m && plan, "null input");
+    set_mul_plan(*m->m, plan);
+  });
+}
+
+FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan) {
+  return guard([&] {
+    need(m && count, "null input");
+    Multiplicator& mult = *m->m;
+    const Context& bc = *mult.base;
+    cudaStream_t st = as_stream(stream);
+    const size_t in_words = count * 2 * bc.L() * bc.N();
+    const size_t out_words = count * mult.out_parts() * mult.par->ctx(mult.out_level())->L() * bc.N();
+    DevBuf buf((2 * in_words + out_words) * 8);
+    check_cuda(cudaMemsetAsync(buf.ptr, 0, buf.bytes, st), "cudaMemsetAsync");
+    uint64_t* lhs = buf.u64();
+    auto run = [&] { mult.multiply(lhs, lhs + in_words, lhs + 2 * in_words, count, st); };
+    // Coordinate descent over the stages, starting from the current plan.
+    uint32_t cur[5];
+    get_mul_plan(mult, cur);
+    set_mul_plan(mult, cur);
+    float best = time_once(st, run);
+    const std::vector<uint32_t> plans = ntt_plans(bc.logn);
+    for (int k = 0; k < 4; k++) {
+      for (uint32_t bl : plans) {
+        for (uint32_t split = 0; split < (k == 3 && bl >= bc.logn ? 2u : 1u); split++) {
+          uint32_t cand[5];
+          std::copy(cur, cur + 5, cand);
+          cand[k] = bl;
+          if (k == 3) cand[4] = split;
+          if (std::equal(cand, cand + 5, cur)) continue;
+          set_mul_plan(mult, cand);
+          const float ms = time_once(st, run);
+          if (ms < best) {
+            best = ms;
+            std::copy(cand, cand + 5, cur);
+          }
+        }
+      }
+    }
+    set_mul_plan(mult, cur);
+    if (plan) std::copy(cur, cur + 5, plan);
   });
 }
 

@@ -49,8 +49,12 @@ struct SrcPair {
 };
 
 // Tensor product (mul.rs:181-185) at limb j of the extended basis: operand
-// limbs below ncm come from the inputs, the others from the extension.
+// limbs below ncm come from the inputs, the others from the extension. The
+// products are Montgomery reductions (value * 2^-64 mod q_j, in [0, 2q_j));
+// the inverse NTT that consumes them scales by N^-1 * 2^64 instead of N^-1,
+// so its output is the canonical INTT of the exact products.
 struct SrcTensor {
+  static constexpr bool kMontgomery = true;
   PolyRef lhs, rhs;  // inputs [B][2][L][N], Ntt
   PolyRef ext;       // [B][4][M][N], Ntt (limbs >= ncm of each operand)
   uint32_t ncm_l, ncm_r;
@@ -61,16 +65,17 @@ struct SrcTensor {
   }
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     const uint32_t b = j.poly / 3, part = j.poly % 3;
-    if (part == 0) return mul_mod(op(b, 0, j.limb, i), op(b, 2, j.limb, i), pr);
-    if (part == 2) return mul_mod(op(b, 1, j.limb, i), op(b, 3, j.limb, i), pr);
+    if (part != 1) {
+      const uint64_t x = op(b, part >> 1, j.limb, i), y = op(b, 2 + (part >> 1), j.limb, i);
+      return mont_reduce(__umul64hi(x, y), x * y, pr);
+    }
     const uint64_t a0 = op(b, 0, j.limb, i), a1 = op(b, 1, j.limb, i);
     const uint64_t b0 = op(b, 2, j.limb, i), b1 = op(b, 3, j.limb, i);
-    // a0*b1 + a1*b0 < 2^125: one reduction of the exact sum.
-    const uint64_t lo1 = a0 * b1, hi1 = __umul64hi(a0, b1);
-    const uint64_t lo2 = a1 * b0, hi2 = __umul64hi(a1, b0);
-    const uint64_t lo = lo1 + lo2;
-    const uint64_t hi = hi1 + hi2 + (lo < lo1);
-    return reduce128(hi, lo, pr);
+    // a0*b1 + a1*b0 < 2 q_j^2 < q_j * 2^64: one reduction of the exact sum.
+    uint64_t hi = 0, lo = 0;
+    mac128(hi, lo, a0, b1);
+    mac128(hi, lo, a1, b0);
+    return mont_reduce(hi, lo, pr);
   }
 };
 
@@ -476,8 +481,11 @@ size_t Multiplicator::scratch_bytes(uint64_t count) const {
 }
 
 void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count,
-                             cudaStream_t st, Workspace* scratch) {
+                             cudaStream_t st, Workspace* scratch, cudaEvent_t* marks) {
   if (count == 0) return;
+  auto mark = [&](int k) {
+    if (marks) check_cuda(cudaEventRecord(marks[k], st), "cudaEventRecord");
+  };
   Workspace& ws = scratch ? *scratch : this->ws;
   const Context& bc = *base;
   const Context& mc = *mul;
@@ -506,10 +514,12 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   PolyRef extref = plain_ref(ext, M, logn);
 
   // A: inverse NTT of the four operands.
+  mark(0);
   {
     NttGeom g{bc.primes_dev(), (uint32_t)L, 0};
-    ntt_inverse_any(logn, g, 4 * count, SrcPair{lref, rref}, DstPoly{pbref}, st);
+    ntt_inverse_any(logn, g, 4 * count, SrcPair{lref, rref}, DstPoly{pbref}, st, plan_a);
   }
+  mark(1);
   // B + C: extension of each operand and forward NTT of the new limbs.
   const bool same_ext = ncm_l == ncm_r && ext_lhs->num == ext_rhs->num && ext_lhs->den == ext_rhs->den;
   auto extend = [&](const Scaler& s, uint32_t first, uint32_t take) {
@@ -518,8 +528,9 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     PolyRef o = sub_ref(ext, M, logn, 4, first, take);
     o.base += (uint64_t)ncm << logn;
     rns_scale(*s.rns, logn, in, o, (uint32_t)ncm, (uint32_t)(M - ncm), count * take, st);
+    if (first == 0) mark(2);
     NttGeom g{mc.primes_dev() + ncm, (uint32_t)(M - ncm), 0};
-    ntt_forward_any<true>(logn, g, count * take, SrcPoly{o}, DstPoly{o}, st);
+    ntt_forward_any<true>(logn, g, count * take, SrcPoly{o}, DstPoly{o}, st, plan_c);
   };
   if (same_ext) {
     extend(*ext_lhs, 0, 4);
@@ -527,16 +538,19 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     extend(*ext_lhs, 0, 2);
     extend(*ext_rhs, 2, 2);
   }
+  mark(3);
   // D: tensor product fused into the inverse NTT over the extended basis.
   PolyRef prodref = plain_ref(prod, M, logn);
   {
     NttGeom g{mc.primes_dev(), (uint32_t)M, 0};
     ntt_inverse_any(logn, g, 3 * count, SrcTensor{lref, rref, extref, (uint32_t)ncm_l, (uint32_t)ncm_r},
-                    DstPoly{prodref}, st);
+                    DstPoly{prodref}, st, plan_d);
   }
+  mark(4);
   // E: scale down by t/Q into the base context (power basis).
   PolyRef dnref = plain_ref(dn, L, logn);
   rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st);
+  mark(5);
   NttGeom gb{bc.primes_dev(), (uint32_t)L, 0};
   if (rk) {
     const Context& kc = *rk->ctx_ksk;
@@ -545,15 +559,17 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     PolyRef c01 = sub_ref(dn, L, logn, 3, 0, 2);
     PolyRef oref = plain_ref(dest, L, logn);
     NttGeom gk{kc.primes_dev(), (uint32_t)Lk, 0};
-    if (logn <= kMaxSmemLogN) {
+    const uint32_t bf = plan_f ? plan_f : ntt_block_logn(logn);
+    if (bf >= logn && !f_split) {
       // F: digit NTTs and the c0 / c1 NTTs in one launch (Lk == L).
       const uint32_t ndp = (uint32_t)(count * L);
       ntt_fwd_single<true>(logn, gk, count * L + 2 * count, SrcKsF{c2, c01, (uint32_t)L, ndp},
                            DstKsF{dref, oref, ndp}, st);
     } else {
-      ntt_forward_any<true>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L}, DstPoly{dref}, st);
-      ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st);
+      ntt_forward_any<true>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L}, DstPoly{dref}, st, bf);
+      ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st, bf);
     }
+    mark(6);
     // G: key inner product added to c0, c1 in place.
     const uint64_t total = count * L << logn;
     k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest,
@@ -563,12 +579,14 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   } else {
     PolyRef o = plain_ref(dest, L, logn);
     ntt_forward_any<true>(logn, gb, 3 * count, SrcPoly{dnref}, DstPoly{o}, st);
+    mark(6);
   }
   if (mod_switch) {
     PolyRef in = plain_ref(tmp, L, logn);
     PolyRef o = plain_ref(out, L - 1, logn);
     poly_switch_down_ntt(bc, in, o, count * parts, st);
   }
+  mark(7);
 }
 
 }  // namespace fheg

@@ -8,6 +8,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "host_math.hpp"
 #include "fheg.h"
@@ -22,6 +23,9 @@ struct DevPrime {
   uint64_t bhi, blo;    // floor(2^128 / p), the Barrett constant of zq/mod.rs:83-98
   uint64_t ninv;        // N^-1 mod p
   uint64_t ninv_shoup;  // Shoup companion of ninv
+  uint64_t pinv;        // -p^-1 mod 2^64 (Montgomery reduction)
+  uint64_t ninv_mont;   // N^-1 * 2^64 mod p: final scale of an inverse NTT of Montgomery products
+  uint64_t ninv_mont_shoup;
   // Twiddle tables of native.rs:35-73, each entry paired with its Shoup
   // companion so one 16-byte load fetches both: tw[i] = (omegas[i],
   // omegas_shoup[i]), itw[i] = (zetas_inv[i], zetas_inv_shoup[i]).
@@ -31,6 +35,16 @@ struct DevPrime {
 
 // Counts every kernel launch issued by the library (reported by benchmarks).
 extern std::atomic<uint64_t> g_launches;
+
+// NTT plan: the block size (log2) used for transforms of 2^logn residues. A
+// value >= logn runs the single-pass kernel; a smaller one (12, 13 or 14,
+// with logn - bl <= 4) runs a strided pass plus 2^(logn - bl) blocks.
+uint32_t ntt_block_logn(uint32_t logn);
+// Validates and installs a plan entry (FHEG_ERR_INVALID_ARGUMENT otherwise).
+void set_ntt_block_logn(uint32_t logn, uint32_t block_logn);
+bool ntt_plan_valid(uint32_t logn, uint32_t block_logn);
+// The valid block sizes for 2^logn, ascending.
+std::vector<uint32_t> ntt_plans(uint32_t logn);
 
 inline void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw Error(10 /*FHEG_ERR_CUDA*/, std::string(what) + ": " + cudaGetErrorString(e));
@@ -224,6 +238,15 @@ __device__ __forceinline__ uint64_t reduce128(uint64_t hi, uint64_t lo, const De
 // a * b mod p for a, b < 2^64 with a * b < 2^126 (Barrett).
 __device__ __forceinline__ uint64_t mul_mod(uint64_t a, uint64_t b, const DevPrime& pr) {
   return reduce128(__umul64hi(a, b), a * b, pr);
+}
+
+// Montgomery reduction of the 128-bit value hi:lo < p * 2^64: returns
+// hi:lo * 2^-64 mod p in [0, 2p). With m = lo * (-p^-1) mod 2^64 the sum
+// hi:lo + m * p is a multiple of 2^64 whose low word carries exactly when
+// lo != 0.
+__device__ __forceinline__ uint64_t mont_reduce(uint64_t hi, uint64_t lo, const DevPrime& pr) {
+  const uint64_t m = lo * pr.pinv;
+  return hi + __umul64hi(m, pr.p) + (lo != 0);
 }
 
 // Lazy reduction of a single word into [0, 2p) (zq/mod.rs:712-723 `lazy_reduce`).

@@ -76,28 +76,12 @@ struct Context {
   std::shared_ptr<Context> prefix(size_t count) const;
 };
 
-// rns::RnsScaler (fhe-math/src/rns/scaler.rs:51-72) on the device.
-struct ScalerDev {
-  uint32_t from_len, to_len, is_one, shift;
-  uint64_t tg_lo, tg_hi;
-  uint32_t tg_sign, pad;
-  const uint64_t* gamma;        // [to]
-  const uint64_t* gamma_shoup;  // [to]
-  const uint64_t* omega;        // [to][from]
-  const uint64_t* omega_shoup;  // [to][from]
-  const uint64_t* to_lo;        // theta_omega lo [from]
-  const uint64_t* to_hi;        // theta_omega hi [from]
-  const uint64_t* to_sign;      // theta_omega sign [from]
-  const uint64_t* tgar_lo;      // theta_garner lo [from]
-  const uint64_t* tgar_hi;      // theta_garner hi [from]
-  const uint64_t* gamma_neg;    // (q_j - gamma_j) mod q_j [to]
-  const DevPrime* to_primes;    // [to]
-};
-
+// rns::RnsScaler (fhe-math/src/rns/scaler.rs:51-72): the host constants and
+// the per-target-modulus values each launch copies into its parameters.
 struct RnsScalerD {
   RnsScalerHost host;
-  DevBuf buf;
-  ScalerDev dev;
+  std::vector<uint64_t> gamma_neg;  // (q_j - gamma_j) mod q_j
+  std::vector<uint64_t> to_moduli, to_bhi, to_blo;
   RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den);
 };
 
@@ -193,10 +177,18 @@ struct Multiplicator {
   std::unique_ptr<Scaler> ext_lhs, ext_rhs, down;
   const Ksk* rk = nullptr;
   bool mod_switch = false;
+  // NTT block sizes of the stages (0 = the process-wide plan): A inverse of
+  // the operands, C forward of the extension limbs, D tensor + inverse, F
+  // forward of digits and c0 / c1 (f_split: digits and c0 / c1 as two
+  // launches instead of one when F runs single-pass).
+  uint32_t plan_a = 0, plan_c = 0, plan_d = 0, plan_f = 0;
+  bool f_split = false;
   Workspace ws;
   DevBuf staging;  // device copies for the host entry point
+  // `marks` (optional, 8 events) are recorded on `st` at the stage
+  // boundaries: before A, after A, B, C, D, E, F and at the end.
   void multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, uint64_t count, cudaStream_t st,
-                Workspace* scratch = nullptr);
+                Workspace* scratch = nullptr, cudaEvent_t* marks = nullptr);
   // Bytes of scratch multiply() needs for `count` pairs.
   size_t scratch_bytes(uint64_t count) const;
   size_t out_parts() const { return rk ? 2 : 3; }

@@ -8,13 +8,14 @@
 // Residues stay in Harvey's lazy ranges ([0, 4p) forward, [0, 2p) inverse)
 // and are reduced at the end, so outputs are bit-identical to the reference.
 //
-// Layout: one CTA transforms one limb of one polynomial (N <= 2^14 words,
-// resident in shared memory). Each thread keeps 16 residues in registers and
-// runs up to four butterfly stages on them (a radix-16 round); rounds
+// Layout: one CTA transforms one block of 2^bl residues of one limb (bl <= 14,
+// resident in shared memory). Each thread keeps 32 residues in registers and
+// runs up to five butterfly stages on them (a radix-32 round); rounds
 // exchange data through shared memory with an XOR swizzle that keeps 64-bit
-// accesses free of bank conflicts. For N = 2^15 and 2^16 the first (forward)
-// or last (inverse) one or two stages run in a separate pass over strided
-// groups, and the remaining stages run in this kernel over blocks of 2^14.
+// accesses free of bank conflicts. A transform of 2^logn is either one block
+// (bl = logn) or, following the plan of ntt_block_logn(), a strided pass over
+// groups of 2^(logn - bl) elements for the first (forward) or last (inverse)
+// stages plus the block kernel for the others.
 //
 // The kernels are templates over a source functor (produces the input
 // residue of element i; fuses element-wise prologues such as the BFV tensor
@@ -39,9 +40,26 @@ namespace {
 struct NttGeom {
   const DevPrime* primes;  // one entry per limb (modulus index)
   uint32_t limbs;          // limbs per polynomial (1 for ragged launches)
-  uint32_t s1;             // stages handled by the strided pass (0, 1 or 2)
+  uint32_t s1;             // stages handled by the strided pass (0 to 4)
   const uint4* jobs;       // optional ragged job table
+  uint32_t mont;           // inverse transforms: inputs carry a factor 2^-64 (Montgomery products)
 };
+
+// Final scale of an inverse transform: N^-1, or N^-1 * 2^64 when the inputs
+// are Montgomery products (a * b * 2^-64), which cancels their factor.
+__device__ __forceinline__ uint64_t inv_final_scale(const NttGeom& g, const DevPrime& pr, uint64_t v) {
+  return g.mont ? mul_shoup(v, pr.ninv_mont, pr.ninv_mont_shoup, pr.p) : mul_shoup(v, pr.ninv, pr.ninv_shoup, pr.p);
+}
+
+// Sources whose values are Montgomery products declare kMontgomery = true.
+template <class S>
+constexpr auto src_is_montgomery(int) -> decltype(S::kMontgomery) {
+  return S::kMontgomery;
+}
+template <class S>
+constexpr bool src_is_montgomery(long) {
+  return false;
+}
 
 struct NttJob {
   uint32_t poly, limb, beta, aux;
@@ -296,7 +314,7 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
 #pragma unroll
   for (int e = 0; e < E; e++) {
     uint64_t v = x[e];
-    if (FINAL) v = mul_shoup(v, pr.ninv, pr.ninv_shoup, pr.p);
+    if (FINAL) v = inv_final_scale(g, pr, v);
     dst(jb, pr, base + tid + e * T, v);
   }
 }
@@ -349,11 +367,11 @@ __global__ void __launch_bounds__(1024) k_ntt_inv_small(NttGeom g, uint32_t logn
     }
     __syncthreads();
   }
-  for (uint32_t i = tid; i < n; i += nt) dst(jb, pr, i, mul_shoup(sm[i], pr.ninv, pr.ninv_shoup, pr.p));
+  for (uint32_t i = tid; i < n; i += nt) dst(jb, pr, i, inv_final_scale(g, pr, sm[i]));
 }
 
 // ---------------------------------------------------------------------------
-// Strided passes for N = 2^(LOGB + S1) with S1 in {1, 2}: the first S1
+// Strided passes for N = 2^(LOGB + S1) with 1 <= S1 <= 4: the first S1
 // forward stages / the last S1 inverse stages, on groups of 2^S1 elements
 // b + t * 2^LOGB. One thread per group.
 
@@ -415,7 +433,7 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
   }
 #pragma unroll
   for (int t = 0; t < (1 << S1); t++)
-    dst(jb, pr, b + ((uint32_t)t << logb), mul_shoup(x[t], pr.ninv, pr.ninv_shoup, pr.p));
+    dst(jb, pr, b + ((uint32_t)t << logb), inv_final_scale(g, pr, x[t]));
 }
 
 // ---------------------------------------------------------------------------
@@ -522,58 +540,86 @@ void ntt_inv_single(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, 
   }
 }
 
-constexpr uint32_t kMaxSmemLogN = 14;
+// Two-pass transforms: a strided pass runs the first (forward) or last
+// (inverse) s1 stages on groups of 2^s1 elements b + t * 2^bl, and the block
+// kernel runs the other bl stages on 2^s1 blocks of 2^bl elements.
+template <class Src, class Dst>
+void launch_fwd_top(uint32_t s1, NttGeom g, uint32_t bl, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  const uint32_t groups = 1u << bl;
+  const uint64_t threads = polys * g.limbs * groups;
+  const unsigned blocks = (unsigned)((threads + 255) / 256);
+  g.s1 = 0;
+  switch (s1) {
+    case 1: k_ntt_fwd_top<1><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 2: k_ntt_fwd_top<2><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 3: k_ntt_fwd_top<3><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 4: k_ntt_fwd_top<4><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    default: throw Error(12, "unsupported NTT plan");
+  }
+  after_launch("k_ntt_fwd_top");
+}
 
-// Full forward NTT, any 3 <= logn <= 16. For logn > 14 the source is read by
-// the strided pass and the result goes through `dst` twice: the strided pass
-// writes its lazy output to dst, and the block pass reads it back.
+template <class Src, class Dst>
+void launch_inv_top(uint32_t s1, NttGeom g, uint32_t bl, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  const uint32_t groups = 1u << bl;
+  const uint64_t threads = polys * g.limbs * groups;
+  const unsigned blocks = (unsigned)((threads + 255) / 256);
+  g.s1 = 0;
+  switch (s1) {
+    case 1: k_ntt_inv_top<1><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 2: k_ntt_inv_top<2><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 3: k_ntt_inv_top<3><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    case 4: k_ntt_inv_top<4><<<blocks, 256, 0, st>>>(g, bl, groups, threads, src, dst); break;
+    default: throw Error(12, "unsupported NTT plan");
+  }
+  after_launch("k_ntt_inv_top");
+}
+
+// Full forward NTT, any 3 <= logn <= 16, following the plan of
+// ntt_block_logn(logn): single pass, or a strided pass that reads `src` and
+// writes its lazy output to `dst`, then the block pass that reads it back.
+// `bl` selects the plan explicitly (0 = the process-wide plan of logn).
 template <bool REDUCE, class Src, class Dst>
-void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
-  if (logn <= kMaxSmemLogN) {
+void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st,
+                     uint32_t bl = 0) {
+  if (bl == 0) bl = ntt_block_logn(logn);
+  if (bl >= logn || logn < 13) {
     g.s1 = 0;
     ntt_fwd_single<REDUCE>(logn, g, polys, src, dst, st);
     return;
   }
-  const uint32_t s1 = logn - kMaxSmemLogN;
-  const uint32_t groups = 1u << kMaxSmemLogN;
-  const uint64_t threads = polys * g.limbs * groups;
-  g.s1 = 0;
-  if (s1 == 1) {
-    k_ntt_fwd_top<1><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, src, dst);
-  } else if (s1 == 2) {
-    k_ntt_fwd_top<2><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, src, dst);
-  } else {
-    throw Error(12, "unsupported NTT size");
-  }
-  after_launch("k_ntt_fwd_top");
+  const uint32_t s1 = logn - bl;
+  launch_fwd_top(s1, g, bl, polys, src, dst, st);
   g.s1 = s1;
-  launch_fwd_block<kMaxSmemLogN, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st);
+  switch (bl) {
+    case 12: launch_fwd_block<12, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    case 13: launch_fwd_block<13, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    case 14: launch_fwd_block<14, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    default: throw Error(12, "unsupported NTT plan");
+  }
 }
 
-// Full inverse NTT, any 3 <= logn <= 16. For logn > 14 the block pass writes
-// to `dst` and the strided pass finishes in place.
+// Full inverse NTT, any 3 <= logn <= 16: single pass, or the block pass into
+// `dst` followed by the strided pass in place.
 template <class Src, class Dst>
-void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
-  if (logn <= kMaxSmemLogN) {
+void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st,
+                     uint32_t bl = 0) {
+  g.mont = src_is_montgomery<Src>(0) ? 1u : 0u;
+  if (bl == 0) bl = ntt_block_logn(logn);
+  if (bl >= logn || logn < 13) {
     g.s1 = 0;
     ntt_inv_single<true>(logn, g, polys, src, dst, st);
     return;
   }
-  const uint32_t s1 = logn - kMaxSmemLogN;
+  const uint32_t s1 = logn - bl;
   g.s1 = s1;
-  launch_inv_block<kMaxSmemLogN, false>(g, polys, src, dst, st);
-  const uint32_t groups = 1u << kMaxSmemLogN;
-  const uint64_t threads = polys * g.limbs * groups;
-  g.s1 = 0;
-  SrcReload<Dst> mid{dst};
-  if (s1 == 1) {
-    k_ntt_inv_top<1><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, mid, dst);
-  } else if (s1 == 2) {
-    k_ntt_inv_top<2><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, kMaxSmemLogN, groups, threads, mid, dst);
-  } else {
-    throw Error(12, "unsupported NTT size");
+  switch (bl) {
+    case 12: launch_inv_block<12, false>(g, polys, src, dst, st); break;
+    case 13: launch_inv_block<13, false>(g, polys, src, dst, st); break;
+    case 14: launch_inv_block<14, false>(g, polys, src, dst, st); break;
+    default: throw Error(12, "unsupported NTT plan");
   }
-  after_launch("k_ntt_inv_top");
+  launch_inv_top(s1, g, bl, polys, SrcReload<Dst>{dst}, dst, st);
 }
 
 }  // namespace

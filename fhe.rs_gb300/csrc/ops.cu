@@ -2,6 +2,7 @@
 // modulus switch-down and RNS scaling (fhe-math `rq`, `ntt`, `rns`).
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -12,6 +13,33 @@
 namespace fheg {
 
 std::atomic<uint64_t> g_launches{0};
+
+// Default NTT plan: single pass up to 2^14 (the whole limb in shared memory);
+// 2^15 and 2^16 as strided stages in front of 2^13-residue blocks (measured
+// faster on GB300 than 2^14-residue blocks).
+static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 13, 13};
+
+uint32_t ntt_block_logn(uint32_t logn) { return logn <= 16 ? g_ntt_block[logn].load(std::memory_order_relaxed) : 14; }
+
+bool ntt_plan_valid(uint32_t logn, uint32_t block_logn) {
+  const bool single = block_logn == logn && logn >= 3 && logn <= 14;
+  const bool split = logn >= 13 && logn <= 16 && block_logn >= 12 && block_logn <= 14 && block_logn < logn &&
+                     logn - block_logn <= 4;
+  return single || split;
+}
+
+std::vector<uint32_t> ntt_plans(uint32_t logn) {
+  std::vector<uint32_t> out;
+  for (uint32_t bl = 12; bl <= 14; bl++)
+    if (ntt_plan_valid(logn, bl)) out.push_back(bl);
+  if (out.empty() && ntt_plan_valid(logn, logn)) out.push_back(logn);
+  return out;
+}
+
+void set_ntt_block_logn(uint32_t logn, uint32_t block_logn) {
+  if (!ntt_plan_valid(logn, block_logn)) throw Error(FHEG_ERR_INVALID_ARGUMENT, "unsupported NTT plan");
+  g_ntt_block[logn].store(block_logn, std::memory_order_relaxed);
+}
 
 void upload(void* dst, const void* src, size_t bytes) {
   check_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
@@ -50,6 +78,12 @@ std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t roo
   barrett128(p, &dp.bhi, &dp.blo);
   dp.ninv = t->host.size_inv;
   dp.ninv_shoup = t->host.size_inv_shoup;
+  uint64_t inv = p;  // p^-1 mod 2^64 by Newton's iteration (each step doubles the correct bits)
+  for (int k = 0; k < 6; k++) inv *= 2 - p * inv;
+  dp.pinv = 0 - inv;
+  const uint64_t r_mod_p = (uint64_t)(((unsigned __int128)1 << 64) % p);
+  dp.ninv_mont = (uint64_t)((unsigned __int128)dp.ninv * r_mod_p % p);
+  dp.ninv_mont_shoup = shoup(dp.ninv_mont, p);
   dp.tw = reinterpret_cast<const ulonglong2*>(d);
   dp.itw = reinterpret_cast<const ulonglong2*>(d + 2 * n);
   registry[key] = t;
@@ -323,9 +357,26 @@ __device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t 
   for (int k = 0; k < 8; k++) r[k] = t[k];
 }
 
-template <int MAXF>
-__global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, PolyRef in, PolyRef out,
-                                                   uint32_t start, uint32_t out_len, uint64_t total) {
+// All constants of one launch travel in the kernel's parameter space, so
+// every multiply-add reads its constant operand straight from the constant
+// bank (fully unrolled loops give compile-time offsets). Outputs are limbs
+// start .. start + out_len of the target; the rows of omega, gamma and the
+// primes are pre-sliced on the host so output o uses row o.
+template <int MAXF, int MAXT>
+struct RnsLaunch {
+  uint32_t from_len, out_len, is_one, shift;
+  uint32_t tg_sign, to_sign;  // to_sign: bit k = sign of theta_omega_k
+  uint64_t tg_lo, tg_hi;
+  uint64_t tgar_lo[MAXF], tgar_hi[MAXF];
+  uint64_t to_lo[MAXF], to_hi[MAXF];
+  uint64_t omega[MAXT][MAXF];
+  uint64_t gamma_neg[MAXT];  // (q_j - gamma_j) mod q_j
+  uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
+};
+
+template <int MAXF, int MAXT>
+__global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
+                                                   PolyRef in, PolyRef out, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
@@ -340,7 +391,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
   uint32_t g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
   for (int k = 0; k < MAXF; k++)
-    if (k < (int)F) mac192(g, r[k], __ldg(s.tgar_lo + k), __ldg(s.tgar_hi + k));
+    if (k < (int)F) mac192(g, r[k], s.tgar_lo[k], s.tgar_hi[k]);
   uint64_t vlo, vhi;
   shr_words(g, 6, s.shift - 1, &vlo, &vhi);
   {
@@ -359,8 +410,8 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
 #pragma unroll
     for (int k = 0; k < MAXF; k++) {
       if (k < (int)F) {
-        if (__ldg(s.to_sign + k)) mac256(neg, r[k], __ldg(s.to_lo + k), __ldg(s.to_hi + k));
-        else mac256(pos, r[k], __ldg(s.to_lo + k), __ldg(s.to_hi + k));
+        if ((s.to_sign >> k) & 1) mac256(neg, r[k], s.to_lo[k], s.to_hi[k]);
+        else mac256(pos, r[k], s.to_lo[k], s.to_hi[k]);
       }
     }
     sub256w(pos, neg);
@@ -390,28 +441,72 @@ __global__ void __launch_bounds__(128) k_rns_scale(ScalerDev s, uint32_t logn, P
 
   // scaler.rs:316-351.
   uint64_t* dst = out.at(poly, 0) + i;
-  for (uint32_t o = 0; o < out_len; o++) {
-    const uint32_t j = start + o;
-    const DevPrime pr = s.to_primes[j];
-    const uint64_t vj = reduce128(vhi, vlo, pr);
-    uint64_t lo = 0, hi = 0;
-    if (!s.is_one) {
-      const uint64_t wj = reduce128_lazy(whi, wlo, pr);
-      lo = w_sign ? pr.p2 - wj : wj;
-    }
-    mac128(hi, lo, vj, __ldg(s.gamma_neg + j));
-    const uint64_t* om = s.omega + (uint64_t)j * F;
 #pragma unroll
-    for (int k = 0; k < MAXF; k++) {
-      if (k < (int)F) {
-        mac128(hi, lo, r[k], __ldg(om + k));
-        if ((k % 15) == 14) {  // keep the exact sum below 2^128
-          lo = reduce128(hi, lo, pr);
-          hi = 0;
+  for (int o = 0; o < MAXT; o++) {
+    if (o < (int)s.out_len) {
+      DevPrime pr;
+      pr.p = s.p[o];
+      pr.p2 = 2 * s.p[o];
+      pr.bhi = s.bhi[o];
+      pr.blo = s.blo[o];
+      const uint64_t vj = reduce128(vhi, vlo, pr);
+      uint64_t lo = 0, hi = 0;
+      if (!s.is_one) {
+        const uint64_t wj = reduce128_lazy(whi, wlo, pr);
+        lo = w_sign ? pr.p2 - wj : wj;
+      }
+      mac128(hi, lo, vj, s.gamma_neg[o]);
+#pragma unroll
+      for (int k = 0; k < MAXF; k++) {
+        if (k < (int)F) {
+          mac128(hi, lo, r[k], s.omega[o][k]);
+          if ((k % 15) == 14) {  // keep the exact sum below 2^128
+            lo = reduce128(hi, lo, pr);
+            hi = 0;
+          }
         }
       }
+      dst[(uint64_t)o << logn] = reduce128(hi, lo, pr);
     }
-    dst[(uint64_t)o << logn] = reduce128(hi, lo, pr);
+  }
+}
+
+template <int MAXF, int MAXT>
+void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
+                      uint32_t out_len, uint64_t total, cudaStream_t st) {
+  const RnsScalerHost& h = sc.host;
+  const size_t F = h.from_len;
+  for (uint32_t first = 0; first < out_len; first += MAXT) {
+    const uint32_t n = std::min<uint32_t>(MAXT, out_len - first);
+    RnsLaunch<MAXF, MAXT> s;
+    memset(&s, 0, sizeof(s));
+    s.from_len = (uint32_t)F;
+    s.out_len = n;
+    s.is_one = h.is_one ? 1 : 0;
+    s.shift = (uint32_t)h.theta_garner_shift;
+    s.tg_sign = h.theta_gamma_sign ? 1 : 0;
+    s.tg_lo = h.theta_gamma_lo;
+    s.tg_hi = h.theta_gamma_hi;
+    for (size_t k = 0; k < F; k++) {
+      s.tgar_lo[k] = h.theta_garner_lo[k];
+      s.tgar_hi[k] = h.theta_garner_hi[k];
+      s.to_lo[k] = h.theta_omega_lo[k];
+      s.to_hi[k] = h.theta_omega_hi[k];
+      if (h.theta_omega_sign[k]) s.to_sign |= 1u << k;
+    }
+    for (uint32_t o = 0; o < n; o++) {
+      const size_t j = start + first + o;
+      for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
+      s.gamma_neg[o] = sc.gamma_neg[j];
+      s.p[o] = sc.to_moduli[j];
+      s.bhi[o] = sc.to_bhi[j];
+      s.blo[o] = sc.to_blo[j];
+    }
+    PolyRef o = out;
+    o.base += (uint64_t)first << logn;
+    const unsigned threads = 128;
+    k_rns_scale<MAXF, MAXT><<<blocks_for(total, threads), threads, 0, st>>>(s, logn, in, o, total);
+    after_launch("k_rns_scale");
   }
 }
 
@@ -419,53 +514,25 @@ void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint
                uint64_t polys, cudaStream_t st) {
   const uint64_t total = polys << logn;
   if (total == 0 || out_len == 0) return;
-  const uint32_t F = s.dev.from_len;
-  const unsigned threads = 128;
-  if (F <= 8) k_rns_scale<8><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
-  else if (F <= 16) k_rns_scale<16><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
-  else if (F <= 32) k_rns_scale<32><<<blocks_for(total, threads), threads, 0, st>>>(s.dev, logn, in, out, start, out_len, total);
+  const size_t F = s.host.from_len;
+  if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
+  else if (F <= 16 && out_len <= 8) launch_rns_scale<16, 8>(s, logn, in, out, start, out_len, total, st);
+  else if (F <= 16) launch_rns_scale<16, 16>(s, logn, in, out, start, out_len, total, st);
+  else if (F <= 32) launch_rns_scale<32, 16>(s, logn, in, out, start, out_len, total, st);
   else throw Error(FHEG_ERR_UNSUPPORTED, "RNS scaling from more than 32 moduli is not supported");
-  after_launch("k_rns_scale");
 }
 
 RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den)
     : host(make_rns_scaler(*from.rns, *to.rns, num, den)) {
-  const size_t F = host.from_len, T = host.to_len;
-  std::vector<uint64_t> flat;
-  auto put = [&](const std::vector<uint64_t>& v) {
-    size_t off = flat.size();
-    flat.insert(flat.end(), v.begin(), v.end());
-    return off;
-  };
-  size_t o_gamma = put(host.gamma), o_gs = put(host.gamma_shoup), o_om = put(host.omega),
-         o_oms = put(host.omega_shoup), o_tol = put(host.theta_omega_lo), o_toh = put(host.theta_omega_hi);
-  std::vector<uint64_t> sign(host.theta_omega_sign.begin(), host.theta_omega_sign.end());
-  size_t o_tos = put(sign), o_tgl = put(host.theta_garner_lo), o_tgh = put(host.theta_garner_hi);
-  std::vector<uint64_t> gneg(T);
-  for (size_t j = 0; j < T; j++) gneg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
-  size_t o_gneg = put(gneg);
-  buf.alloc(std::max<size_t>(flat.size(), 1) * 8);
-  upload(buf.ptr, flat.data(), flat.size() * 8);
-  uint64_t* b = buf.u64();
-  dev.from_len = (uint32_t)F;
-  dev.to_len = (uint32_t)T;
-  dev.is_one = host.is_one ? 1 : 0;
-  dev.shift = (uint32_t)host.theta_garner_shift;
-  dev.tg_lo = host.theta_gamma_lo;
-  dev.tg_hi = host.theta_gamma_hi;
-  dev.tg_sign = host.theta_gamma_sign ? 1 : 0;
-  dev.pad = 0;
-  dev.gamma = b + o_gamma;
-  dev.gamma_shoup = b + o_gs;
-  dev.omega = b + o_om;
-  dev.omega_shoup = b + o_oms;
-  dev.to_lo = b + o_tol;
-  dev.to_hi = b + o_toh;
-  dev.to_sign = b + o_tos;
-  dev.tgar_lo = b + o_tgl;
-  dev.tgar_hi = b + o_tgh;
-  dev.gamma_neg = b + o_gneg;
-  dev.to_primes = to.primes_dev();
+  const size_t T = host.to_len;
+  gamma_neg.resize(T);
+  to_moduli = to.moduli;
+  to_bhi.resize(T);
+  to_blo.resize(T);
+  for (size_t j = 0; j < T; j++) {
+    gamma_neg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
+    barrett128(to.moduli[j], &to_bhi[j], &to_blo[j]);
+  }
 }
 
 Scaler::Scaler(std::shared_ptr<Context> f, std::shared_ptr<Context> t, const BigUint& n, const BigUint& d)
@@ -515,11 +582,7 @@ void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t p
   if (ntt) {  // rq/scaler.rs:96-114: forward NTT of the new limbs.
     // The target context restricted to limbs ncm.. : same tables, offset primes.
     NttGeom g{s.to->primes_dev() + ncm, (uint32_t)(Lt - ncm), 0};
-    if (s.to->logn <= kMaxSmemLogN) {
-      ntt_fwd_single<true>(logn, g, polys, SrcPoly{dst}, DstPoly{dst}, st);
-    } else {
-      ntt_forward_any<true>(logn, g, polys, SrcPoly{dst}, DstPoly{dst}, st);
-    }
+    ntt_forward_any<true>(logn, g, polys, SrcPoly{dst}, DstPoly{dst}, st);
   }
 }
 

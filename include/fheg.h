@@ -126,6 +126,17 @@ FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t
                               void* stream);
 FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_t count, void* stream);
 
+/* NTT plan (no counterpart in the reference: it only changes how the GPU
+ * schedules a transform, never its result). Transforms of 2^logn residues run
+ * as one block (block_logn == logn, logn <= 14) or as a strided pass over the
+ * first / last logn - block_logn stages plus blocks of 2^block_logn
+ * (block_logn in 12..14, logn - block_logn <= 4). The plan is process-wide. */
+FHEG_API int fheg_ntt_plan_set(uint32_t logn, uint32_t block_logn);
+FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn);
+/* Times every valid plan for the context's degree on `count` scratch
+ * polynomials (forward + inverse), installs the fastest and returns it. */
+FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn);
+
 /* Coefficient-wise ring operations (fhe-math/src/rq/ops.rs:10-418):
  * op 0 = add, 1 = sub, 2 = mul (both Ntt, `MulAssign<&Poly<Ntt>>`),
  * 3 = neg (b ignored). d_out may alias d_a. */
@@ -236,6 +247,24 @@ FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t
  * d_lhs, d_rhs [count][2][L][N] (Ntt) -> d_out [count][parts][L'][N]. */
 FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                          uint64_t* d_out, size_t count, void* stream);
+/* Runs one multiplication with events at the stage boundaries and returns
+ * the duration of each stage in ms[7]: A inverse NTT of the operands,
+ * B basis extension, C forward NTT of the extension limbs, D tensor product
+ * + inverse NTT, E t/Q scaling, F digit and c0 / c1 NTTs, G key inner product
+ * (and the switch-down when enabled). No counterpart in the reference. */
+FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
+                                            uint64_t* d_out, size_t count, void* stream, float* ms);
+/* Per-stage NTT plans of a multiplicator (no counterpart in the reference:
+ * schedules only, results are unchanged). plan[5] = block log2 of stage A
+ * (inverse NTT of the operands), C (forward NTT of the extension limbs),
+ * D (tensor product + inverse NTT), F (digit and c0 / c1 forward NTTs), and
+ * plan[4] = 1 to run F as two launches when it is single-pass. Block sizes
+ * follow fheg_ntt_plan_set's rules. */
+FHEG_API int fheg_multiplicator_get_plan(const fheg_multiplicator* m, uint32_t* plan);
+FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* plan);
+/* Times the multiplication of `count` pairs while varying one stage's plan
+ * at a time, installs the fastest and returns it in plan[5] (may be NULL). */
+FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
 /* Same, end to end from host buffers: copies the inputs to the device,
  * multiplies, and copies the product back before returning. */
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs,
@@ -261,6 +290,23 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
  * streams, or different threads without ordering) race on it. */
 FHEG_API int fheg_relinearize_noalloc(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
                                       void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* CUDA graphs                                                                */
+
+/* Records Multiplicator::multiply for fixed device buffers (d_lhs, d_rhs:
+ * [count][2][L][N], d_out: the multiplicator's output shape) into a CUDA
+ * graph; each fheg_graph_launch replays the whole pipeline with one call.
+ * The graph owns its scratch. It runs the multiplication once before
+ * recording (so d_out is written). Destroy the graph before the
+ * multiplicator and its key. No counterpart in the reference. */
+typedef struct fheg_graph fheg_graph;
+FHEG_API int fheg_multiplicator_capture(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
+                                        uint64_t* d_out, size_t count, fheg_graph** out);
+FHEG_API int fheg_graph_launch(const fheg_graph* g, void* stream);
+/* Number of kernels one replay launches. */
+FHEG_API int fheg_graph_kernel_count(const fheg_graph* g, uint64_t* kernels);
+FHEG_API void fheg_graph_destroy(fheg_graph* g);
 
 /* ------------------------------------------------------------------------ */
 /* Serving runtime                                                            */

@@ -123,6 +123,31 @@ def test_multiply_at_level(fg, ora, cuda):
     assert list(s.decrypt(out, 1)) == s.product(vals[0], vals[1])
 
 
+def test_graph_replay(fg, ora, cuda):
+    """A captured multiplication replays the pipeline on whatever the input
+    buffers hold at launch time, bit-exact with multiply()."""
+    s = Setup(fg, ora, 16384, 3, 65537, seed=31)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(8)
+    first = [np.stack([c.to_array() for c in cts[k:k + 2]]) for k in (0, 2)]
+    second = [np.stack([c.to_array() for c in cts[k:k + 2]]) for k in (4, 6)]
+    lhs, rhs = fg.to_device(first[0]), fg.to_device(first[1])
+    out = fg.empty((2, 2, 3, 16384))
+    g = m.capture(lhs, rhs, out)
+    assert g.kernels >= 7
+    want1 = fg.to_host(m.multiply(lhs, rhs))
+    assert np.array_equal(fg.to_host(out), want1)
+    lhs.copy_(fg.to_device(second[0]))
+    rhs.copy_(fg.to_device(second[1]))
+    g.launch()
+    cuda.cuda.synchronize()
+    want2 = fg.to_host(m.multiply(lhs, rhs))
+    assert np.array_equal(fg.to_host(out), want2)
+    mo = ora.Multiplicator.default(rk_o)
+    assert np.array_equal(want2[1], mo.multiply(cts[5], cts[7]).to_array())
+
+
 def test_batched_equals_single_and_host(fg, ora, cuda):
     """A batch of 6 equals 6 single launches and the host entry point."""
     s = Setup(fg, ora, 4096, 2, 65537, seed=21)
@@ -229,3 +254,58 @@ def test_rotate_ragged_batch(fg, ora, cuda, n, L, count):
     outs = fg.rotate_batch(s.par, keys, cts_d)
     for b in range(count):
         assert np.array_equal(fg.to_host(outs[b]), want[b]), f"entry {b} (level {levels[b]})"
+
+
+@pytest.mark.parametrize("n,plans", [(16384, [12, 13]), (32768, [12, 13])])
+def test_pipelines_under_every_ntt_plan(fg, ora, cuda, n, plans):
+    """mul+relin, a rotation and a switch-down give the same bytes under every
+    NTT plan of their degree (the plan only changes the GPU schedule)."""
+    s = Setup(fg, ora, n, 3, 65537, seed=n + 3)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    gk_o = ora.GaloisKey(s.sk, 2 * n - 1, 0, 0, s.rng)
+    gk = fg.GaloisKey(s.par, 2 * n - 1, gk_o.ksk.c0_array(), gk_o.ksk.c1_array())
+    _, cts = s.encrypt(2)
+    a, b = fg.to_device(cts[0].to_array()[None]), fg.to_device(cts[1].to_array()[None])
+    logn = n.bit_length() - 1
+
+    def run():
+        return (fg.to_host(m.multiply(a, b)), fg.to_host(gk.relinearize(a)),
+                fg.to_host(fg.ciphertext_switch_down(s.par, 0, a.clone())))
+
+    want = (ora.Multiplicator.default(rk_o).multiply(cts[0], cts[1]).to_array(),
+            gk_o.relinearize(cts[0]).to_array(), cts[0].copy().switch_down().to_array())
+    default = fg.ntt_plan_get(logn)
+    try:
+        for bl in plans + [default]:
+            fg.ntt_plan_set(logn, bl)
+            got = run()
+            for g, w in zip(got, want):
+                assert np.array_equal(g[0], w), f"plan {bl}"
+    finally:
+        fg.ntt_plan_set(logn, default)
+
+
+def test_multiplicator_stage_plans_and_times(fg, ora, cuda):
+    """Per-stage NTT plans (including the two-launch F stage) leave the product
+    unchanged; the autotuner installs a valid plan; stage times are reported."""
+    s = Setup(fg, ora, 16384, 3, 65537, seed=404)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(4)
+    lhs = fg.to_device(np.stack([cts[0].to_array(), cts[1].to_array()]))
+    rhs = fg.to_device(np.stack([cts[2].to_array(), cts[3].to_array()]))
+    mo = ora.Multiplicator.default(rk_o)
+    want = np.stack([mo.multiply(cts[0], cts[2]).to_array(), mo.multiply(cts[1], cts[3]).to_array()])
+    for plan in ([14, 14, 14, 14, 0], [14, 14, 14, 14, 1], [12, 13, 12, 13, 0], [13, 12, 14, 12, 1]):
+        m.plan = plan
+        assert m.plan == plan
+        assert np.array_equal(fg.to_host(m.multiply(lhs, rhs)), want), plan
+    with pytest.raises(fg.FhegError):
+        m.plan = [15, 14, 14, 14, 0]
+    tuned = m.autotune(2)
+    assert all(b in (12, 13, 14) for b in tuned[:4]) and m.plan == tuned
+    out = fg.empty((2, 2, 3, 16384))
+    ms = m.stage_times(lhs, rhs, out)
+    assert list(ms) == list("ABCDEFG") and all(v > 0 for v in ms.values())
+    assert np.array_equal(fg.to_host(out), want)

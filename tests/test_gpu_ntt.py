@@ -41,6 +41,51 @@ def test_ntt_forward_backward_bit_exact(fg, ora, cuda, logn, L, B):
     assert np.array_equal(fg.to_host(t), data)
 
 
+PLANS = [(13, 12), (14, 12), (14, 13), (15, 12), (15, 13), (16, 12), (16, 13)]
+
+
+@pytest.mark.parametrize("logn,bl", PLANS)
+def test_ntt_plans_bit_exact(fg, ora, cuda, logn, bl):
+    """Every two-pass plan (strided pass + blocks of 2^bl) gives the oracle's
+    output, lazy and reduced, and inverts."""
+    n = 1 << logn
+    moduli = _moduli(ora, n, 2)
+    rng = np.random.default_rng(logn * 7 + bl)
+    data = np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli]) for _ in range(2)])
+    expect = data.copy()
+    for b in range(2):
+        for i, m in enumerate(moduli):
+            ora.ntt_operator(m, n).forward(expect[b, i])
+    ctx = fg.Context(moduli, n)
+    default = fg.ntt_plan_get(logn)
+    try:
+        fg.ntt_plan_set(logn, bl)
+        t = fg.to_device(data)
+        fg.ntt_forward(ctx, t)
+        assert np.array_equal(fg.to_host(t), expect)
+        lazy = fg.to_device(data)
+        fg.ntt_forward(ctx, lazy, lazy=True)
+        got = fg.to_host(lazy)
+        for i, m in enumerate(moduli):
+            assert (got[:, i] < np.uint64(4 * m)).all()
+            assert np.array_equal(got[:, i] % np.uint64(m), expect[:, i])
+        fg.ntt_backward(ctx, t)
+        assert np.array_equal(fg.to_host(t), data)
+    finally:
+        fg.ntt_plan_set(logn, default)
+
+
+def test_ntt_autotune_installs_a_valid_plan(fg, ora, cuda):
+    n = 1 << 14
+    ctx = fg.Context(_moduli(ora, n, 2), n)
+    default = fg.ntt_plan_get(14)
+    try:
+        bl = fg.ntt_autotune(ctx, 8)
+        assert bl in (12, 13, 14) and fg.ntt_plan_get(14) == bl
+    finally:
+        fg.ntt_plan_set(14, default)
+
+
 def test_ntt_lazy_inputs(fg, ora, cuda):
     """Forward NTT accepts lazy [0, 4p) inputs like `forward_vt_lazy`."""
     n, p = 1 << 14, 4611686018427322369
