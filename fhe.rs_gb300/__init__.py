@@ -123,6 +123,12 @@ def _declare(L):
         "fheg_relinearize_noalloc": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
+        "fheg_poly_scalar_mul": (i, [c_vp, P_u64, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_ciphertext_switch_to_level": (i, [c_vp, c_size, c_size, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_device_alloc": (i, [c_size, ctypes.POINTER(c_vp)]),
+        "fheg_device_free": (i, [c_vp]),
+        "fheg_copy_to_device": (i, [c_vp, c_vp, c_size, c_vp]),
+        "fheg_copy_to_host": (i, [c_vp, c_vp, c_size, c_vp]),
         "fheg_ntt_plan_set": (i, [ctypes.c_uint32, ctypes.c_uint32]),
         "fheg_ntt_plan_get": (i, [ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_ntt_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
@@ -360,6 +366,15 @@ def poly_op(ctx: Context, op: str, a, b=None):
     return out
 
 
+def scalar_mul(ctx: Context, t, scalar: int):
+    """MulAssign<&BigUint> for Poly (rq/ops.rs:297-352) on a batch [count][L][N]."""
+    out = empty(t.shape, t.device)
+    count = t.numel() // (ctx.L * ctx.degree)
+    w = _words(scalar)
+    check(lib().fheg_poly_scalar_mul(ctx._h, _ptr(w), len(w), _dp(t), _dp(out), count, _stream()))
+    return out
+
+
 def substitute(ctx: Context, t, exponent: int, representation: int):
     """Poly::substitute (rq/mod.rs:319-369) on a batch."""
     out = empty(t.shape, t.device)
@@ -534,6 +549,17 @@ def ciphertext_switch_down(par: BfvParameters, level: int, ct):
     ctx = par.context_at_level(level)
     out = empty((count, parts, ctx.L - 1, ctx.degree), ct.device)
     check(lib().fheg_ciphertext_switch_down(par._h, level, parts, _dp(ct), _dp(out), count, _stream()))
+    return out
+
+
+def ciphertext_switch_to_level(par: BfvParameters, level: int, target_level: int, ct):
+    """Ciphertext::switch_to_level (fhe/src/bfv/ciphertext.rs:100-119) on a
+    batch [count][parts][L][N]; `ct` is consumed as scratch."""
+    count, parts = ct.shape[0], ct.shape[1]
+    ctx = par.context_at_level(target_level) if target_level <= len(par.moduli) - 1 else None
+    out = empty((count, parts, ctx.L if ctx else 1, par.degree), ct.device)
+    check(lib().fheg_ciphertext_switch_to_level(par._h, level, target_level, parts, _dp(ct), _dp(out), count,
+                                                _stream()))
     return out
 
 

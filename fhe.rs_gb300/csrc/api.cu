@@ -367,6 +367,48 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
   });
 }
 
+FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scalar, size_t scalar_words,
+                                  const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream) {
+  return guard([&] {
+    need(ctx && ((d_in && d_out) || !count), "null input");
+    const Context& c = *ctx->c;
+    poly_scalar_mul(c, big(scalar, scalar_words), plain_ref(const_cast<uint64_t*>(d_in), c.L(), c.logn),
+                    plain_ref(d_out, c.L(), c.logn), count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_device_alloc(size_t bytes, void** out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    *out = nullptr;
+    if (bytes) check_cuda(cudaMalloc(out, bytes), "cudaMalloc");
+  });
+}
+
+FHEG_API int fheg_device_free(void* ptr) {
+  return guard([&] {
+    if (ptr) check_cuda(cudaFree(ptr), "cudaFree");
+  });
+}
+
+FHEG_API int fheg_copy_to_device(void* d_dst, const void* h_src, size_t bytes, void* stream) {
+  return guard([&] {
+    need((d_dst && h_src) || !bytes, "null input");
+    if (!bytes) return;
+    check_cuda(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, as_stream(stream)), "H2D");
+  });
+}
+
+FHEG_API int fheg_copy_to_host(void* h_dst, const void* d_src, size_t bytes, void* stream) {
+  return guard([&] {
+    need((h_dst && d_src) || !bytes, "null input");
+    if (!bytes) return;
+    cudaStream_t st = as_stream(stream);
+    check_cuda(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
+}
+
 FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out,
                           size_t count, void* stream) {
   return guard([&] {
@@ -535,6 +577,35 @@ FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, s
   return guard([&] {
     need(par && parts >= 1 && ((d_ct && d_out) || !count), "null input");
     ciphertext_switch_down(*par->p, level, parts, d_ct, d_out, count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t level, size_t target_level,
+                                             size_t parts, uint64_t* d_ct, uint64_t* d_out, size_t count,
+                                             void* stream) {
+  return guard([&] {
+    need(par && ((d_ct && d_out) || !count), "null input");
+    const Params& p = *par->p;
+    if (target_level < level || target_level > p.max_level())
+      throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    cudaStream_t st = as_stream(stream);
+    const size_t N = p.degree;
+    if (target_level == level) {
+      const size_t bytes = count * parts * p.ctx(level)->L() * N * 8;
+      if (bytes) check_cuda(cudaMemcpyAsync(d_out, d_ct, bytes, cudaMemcpyDeviceToDevice, st), "D2D");
+      return;
+    }
+    // ciphertext.rs:100-119: one switch_down per level. Intermediate levels
+    // alternate between a scratch region of the parameters' workspace and
+    // d_ct (consumed as scratch, large enough for every lower level).
+    Workspace& ws = const_cast<fheg_params*>(par)->ws;
+    ws.reserve(count * parts * (p.ctx(level)->L() - 1) * N * 8);
+    uint64_t* src = d_ct;
+    for (size_t l = level; l < target_level; l++) {
+      uint64_t* dst = (l + 1 == target_level) ? d_out : (src == d_ct ? ws.base() : d_ct);
+      ciphertext_switch_down(p, l, parts, src, dst, count, st);
+      src = dst;
+    }
   });
 }
 

@@ -99,6 +99,9 @@ struct Scaler {
 void ntt_forward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, bool lazy, cudaStream_t st);
 void ntt_backward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, cudaStream_t st);
 void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint64_t polys, cudaStream_t st);
+constexpr size_t kMaxScalarLimbs = 64;
+void poly_scalar_mul(const Context& ctx, const BigUint& scalar, PolyRef in, PolyRef out, uint64_t polys,
+                     cudaStream_t st);
 void poly_substitute(const Context& ctx, uint64_t exponent, bool ntt, PolyRef in, PolyRef out, uint64_t polys,
                      cudaStream_t st);
 // Power-basis switch-down: in [L] limbs -> out [L-1] limbs.

@@ -188,6 +188,42 @@ void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint
   after_launch("k_poly_op");
 }
 
+// MulAssign<&BigUint> for Poly (rq/ops.rs:297-352): every limb times the
+// scalar's projection s_j = scalar mod q_j, as zq `scalar_mul_vec`
+// (zq/mod.rs:349-355: Shoup products, reduced). Any representation.
+struct ScalarLimbs {
+  ulonglong2 s[kMaxScalarLimbs];  // (s_j, shoup(s_j))
+};
+
+__global__ void k_poly_scalar_mul(const DevPrime* primes, uint32_t limbs, uint32_t logn,
+                                  const __grid_constant__ ScalarLimbs sc, PolyRef in, PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  const uint32_t limb = job % limbs;
+  const uint32_t poly = job / limbs;
+  const uint64_t p = primes[limb].p;
+  out.at(poly, limb)[i] = mul_shoup(in.at(poly, limb)[i], sc.s[limb].x, sc.s[limb].y, p);
+}
+
+void poly_scalar_mul(const Context& ctx, const BigUint& scalar, PolyRef in, PolyRef out, uint64_t polys,
+                     cudaStream_t st) {
+  if (ctx.L() > kMaxScalarLimbs) throw Error(FHEG_ERR_UNSUPPORTED, "scalar multiplication supports up to 64 moduli");
+  ScalarLimbs sc;
+  memset(&sc, 0, sizeof(sc));
+  for (size_t j = 0; j < ctx.L(); j++) {
+    const uint64_t q = ctx.moduli[j];
+    const uint64_t v = scalar.mod_u64(q);
+    sc.s[j] = make_ulonglong2(v, shoup(v, q));
+  }
+  const uint64_t total = polys * ctx.L() << ctx.logn;
+  if (total == 0) return;
+  k_poly_scalar_mul<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), (uint32_t)ctx.L(), ctx.logn, sc, in,
+                                                            out, total);
+  after_launch("k_poly_scalar_mul");
+}
+
 // Poly::substitute (rq/mod.rs:319-369).
 //  Ntt:        q[bitrev[j]] = p[power_bitrev[j]], power_bitrev[j] =
 //              bitrev(((e-1)/2 + j*e) mod N): output i reads input g(i)

@@ -73,6 +73,14 @@ FHEG_API const char* fheg_last_error(void);
  * Used by benchmarks to report how many of the library's kernels ran. */
 FHEG_API uint64_t fheg_kernel_launch_count(void);
 
+/* Device memory for callers without their own CUDA bindings (a Rust -sys
+ * crate): plain cudaMalloc / cudaFree and stream-ordered copies. The copy to
+ * the host returns after the copy completes. */
+FHEG_API int fheg_device_alloc(size_t bytes, void** out);
+FHEG_API int fheg_device_free(void* ptr);
+FHEG_API int fheg_copy_to_device(void* d_dst, const void* h_src, size_t bytes, void* stream);
+FHEG_API int fheg_copy_to_host(void* h_dst, const void* d_src, size_t bytes, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Host-only number theory (no device work).                                  */
 
@@ -142,6 +150,12 @@ FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stre
  * 3 = neg (b ignored). d_out may alias d_a. */
 FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b,
                           uint64_t* d_out, size_t count, void* stream);
+
+/* MulAssign<&BigUint> for Poly (fhe-math/src/rq/ops.rs:297-352): every limb
+ * times scalar mod q_j (scalar: little-endian u64 words), in either
+ * representation. d_out may alias d_in. */
+FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scalar, size_t scalar_words,
+                                  const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream);
 
 /* Poly::substitute (fhe-math/src/rq/mod.rs:319-369) for an odd exponent,
  * in Ntt (representation 1) or PowerBasis (0). d_out must not alias d_in. */
@@ -219,6 +233,16 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
  * d_out [count][parts][L-1][N]. d_ct is used as scratch. */
 FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts,
                                          uint64_t* d_ct, uint64_t* d_out, size_t count, void* stream);
+
+/* Ciphertext::switch_to_level (fhe/src/bfv/ciphertext.rs:100-119): repeated
+ * switch_down from `level` to `target_level` (level <= target_level <=
+ * max_level, else FHEG_ERR_INVALID_LEVEL). d_ct [count][parts][L][N] is used as
+ * scratch; d_out receives [count][parts][L'][N] at the target level. The
+ * intermediate levels use the parameters' scratch region, so calls on the same
+ * parameters must not overlap. */
+FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t level, size_t target_level,
+                                             size_t parts, uint64_t* d_ct, uint64_t* d_out, size_t count,
+                                             void* stream);
 
 /* Add<&Ciphertext> (fhe/src/bfv/ops/mod.rs:15-43). */
 FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_a,

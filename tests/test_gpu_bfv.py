@@ -309,3 +309,21 @@ def test_multiplicator_stage_plans_and_times(fg, ora, cuda):
     ms = m.stage_times(lhs, rhs, out)
     assert list(ms) == list("ABCDEFG") and all(v > 0 for v in ms.values())
     assert np.array_equal(fg.to_host(out), want)
+
+
+def test_switch_to_level(fg, ora, cuda):
+    """Ciphertext::switch_to_level (ciphertext.rs:100-119) = repeated switch_down."""
+    s = Setup(fg, ora, 4096, 5, 65537, seed=91)
+    vals, cts = s.encrypt(3)
+    arr = np.stack([c.to_array() for c in cts])
+    for target in (0, 1, 3, 4):
+        got = fg.to_host(fg.ciphertext_switch_to_level(s.par, 0, target, fg.to_device(arr)))
+        for b in range(3):
+            c = cts[b].copy()
+            for _ in range(target):
+                c.switch_down()
+            assert np.array_equal(got[b], c.to_array()), (target, b)
+            assert list(s.decrypt(got[b], target)) == [int(v) for v in vals[b]]
+    with pytest.raises(fg.FhegError) as e:
+        fg.ciphertext_switch_to_level(s.par, 2, 1, fg.to_device(arr))
+    assert e.value.code == fg.ERR_INVALID_LEVEL

@@ -107,3 +107,20 @@ def test_mul_scalers(fg, ora, cuda, n, L):
     got = fg.to_host(down.scale(fg.to_device(b), 1))
     for k in range(2):
         assert np.array_equal(got[k], down_o.scale(ora.Poly(mul_o, b[k], ora.NTT)).coefficients)
+
+
+def test_scalar_mul(fg, ora, cuda):
+    """MulAssign<&BigUint> (rq/ops.rs:297-352): limb j times scalar mod q_j."""
+    n = 4096
+    moduli = [ora.generate_prime(62, 2 * n, 1 << 62)]
+    moduli.append(ora.generate_prime(62, 2 * n, moduli[-1]))
+    moduli.append(ora.generate_prime(40, 2 * n, 1 << 40))
+    ctx = fg.Context(moduli, n)
+    rng = np.random.default_rng(8)
+    x = np.stack([np.stack([rng.integers(0, q, n, dtype=np.uint64) for q in moduli]) for _ in range(3)])
+    for scalar in (0, 1, 65537, (1 << 200) + 12345, int(np.prod([float(q) for q in moduli[:1]]))):
+        got = fg.to_host(fg.scalar_mul(ctx, fg.to_device(x), scalar))
+        for j, q in enumerate(moduli):
+            s = scalar % q
+            want = np.array([int(v) * s % q for v in x[:, j].ravel()], dtype=np.uint64).reshape(x[:, j].shape)
+            assert np.array_equal(got[:, j], want), (scalar, j)
