@@ -224,7 +224,7 @@ def run_ours(args, rank: int, world: int):
         mult.autotune(B)
     else:
         fg.ntt_plan_set(logn, int(args.ntt_block))
-    ntt_block = dict(zip(["A", "C", "D", "F", "F_split"], mult.plan))
+    ntt_block = dict(zip(["A", "C", "D", "F", "F_split", "D_split"], mult.plan))
 
     # Parity gate: two products of the batch against the oracle.
     mult.multiply(lhs_d, rhs_d, out_d)
@@ -413,6 +413,71 @@ def run_stages(args):
     ms = mult.stage_times(lhs_d, rhs_d, out_d)
     torch.cuda.synchronize()
     print(json.dumps({"workload": "stages", "batch_pairs": B, "plan": mult.plan, "stage_ms": ms}), flush=True)
+
+
+def run_codec(args):
+    """Plaintext side at N = 2^14, L = 6, 64 vectors: SIMD encoding into the
+    plaintext's Ntt polynomial, ciphertext x plaintext, and decryption with
+    SIMD decoding, each a batched call on device-resident data."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    B = args.batch
+    par_o, sk_o, _, cts, lhs, _ = make_inputs(ora, B)
+    par = fg.BfvParameters(N, par_o.moduli, T)
+    sk = fg.SecretKey(par, sk_o.coeffs)
+    rng = np.random.default_rng(4)
+    vals = rng.integers(0, T, (B, N), dtype=np.uint64)
+    vals_d, ct_d = fg.to_device(vals), fg.to_device(lhs)
+    pt = fg.plaintext_encode(par, 0, vals_d)
+    prod = fg.ciphertext_mul_plain(par, 0, ct_d, pt)
+    dec = sk.decrypt(ct_d)
+    torch.cuda.synchronize()
+    # Parity gate against the oracle on two entries.
+    ctx = par_o.context_at_level(0)
+    for b in (0, B - 1):
+        m = ora.Poly.from_u64(ctx, ora.Plaintext.encode(vals[b], "simd", par_o).value).into_ntt()
+        if not np.array_equal(fg.to_host(pt[b]), m.coefficients):
+            raise SystemExit("bench: encoding is not bit-exact with the oracle")
+        ct_o = ora.Ciphertext.from_array(par_o, lhs[b], 0)
+        want = np.stack([(ct_o[k] * m).coefficients for k in range(2)])
+        if not np.array_equal(fg.to_host(prod[b]), want):
+            raise SystemExit("bench: ciphertext x plaintext is not bit-exact with the oracle")
+        if not np.array_equal(fg.to_host(dec[b]), sk_o.decrypt(ct_o).decode("simd")):
+            raise SystemExit("bench: decryption is not bit-exact with the oracle")
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        enc_ms = timed(lambda: fg.plaintext_encode(par, 0, vals_d))
+        mul_ms = timed(lambda: fg.ciphertext_mul_plain(par, 0, ct_d, pt))
+        dec_ms = timed(lambda: sk.decrypt(ct_d))
+    launches = fg.kernel_launch_count() - launches0
+    line = {"metric": "BFV plaintext side per second N=2^14 L=6 (SIMD encode, ct x pt, decrypt + decode)",
+            "value": B / (dec_ms / 1000.0), "unit": "decryptions/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": enc_ms + mul_ms + dec_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded encryptions by the CPU oracle)",
+            "config": {"workload": "codec", "degree": N, "moduli": L, "plaintext": T, "batch": B},
+            "encode_per_s": B / (enc_ms / 1000.0), "mul_plain_per_s": B / (mul_ms / 1000.0),
+            "decrypt_per_s": B / (dec_ms / 1000.0), "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
 
 
 def run_ntt(args):
@@ -765,11 +830,11 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages"])
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec"])
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
-    ap.add_argument("--stage-plan", default="", help="A,C,D,F,split block log2 of the multiply stages")
+    ap.add_argument("--stage-plan", default="", help="A,C,D,F,F-split,D-split plan of the multiply stages")
     ap.add_argument("--ntt-block", default="auto", help="NTT plan for the degree: auto (autotune) or a block log2")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-budget-gb", type=float, default=24.0)
@@ -786,6 +851,8 @@ def main():
         run_serve(args)
     elif args.workload == "stages":
         run_stages(args)
+    elif args.workload == "codec":
+        run_codec(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

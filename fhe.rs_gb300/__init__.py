@@ -124,6 +124,11 @@ def _declare(L):
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
         "fheg_poly_scalar_mul": (i, [c_vp, P_u64, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_plaintext_encode": (i, [c_vp, c_size, c_vp, i, c_vp, c_size, c_vp]),
+        "fheg_ciphertext_mul_plain": (i, [c_vp, c_size, c_size, c_vp, c_vp, i, c_vp, c_size, c_vp]),
+        "fheg_secret_key_create": (i, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(c_vp)]),
+        "fheg_secret_key_destroy": (None, [c_vp]),
+        "fheg_decrypt": (i, [c_vp, c_size, c_size, c_vp, i, c_vp, c_size, c_vp]),
         "fheg_ciphertext_switch_to_level": (i, [c_vp, c_size, c_size, c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_device_alloc": (i, [c_size, ctypes.POINTER(c_vp)]),
         "fheg_device_free": (i, [c_vp]),
@@ -563,6 +568,51 @@ def ciphertext_switch_to_level(par: BfvParameters, level: int, target_level: int
     return out
 
 
+def plaintext_encode(par: BfvParameters, level: int, values, simd: bool = True):
+    """Plaintext::poly_ntt of each row of `values` [count][N] (< t), device in
+    and out (plaintext_vec.rs:40-100)."""
+    count = values.shape[0]
+    ctx = par.context_at_level(level)
+    out = empty((count, ctx.L, par.degree), values.device)
+    check(lib().fheg_plaintext_encode(par._h, level, _dp(values), int(simd), _dp(out), count, _stream()))
+    return out
+
+
+def ciphertext_mul_plain(par: BfvParameters, level: int, ct, pt_ntt):
+    """MulAssign<&Plaintext> for Ciphertext (ops/mod.rs:229-238) on a batch
+    [count][parts][L][N]; pt_ntt is [L][N] (shared) or [count][L][N]."""
+    out = empty(ct.shape, ct.device)
+    per_ct = int(pt_ntt.dim() == 3)
+    check(lib().fheg_ciphertext_mul_plain(par._h, level, ct.shape[1], _dp(ct), _dp(pt_ntt), per_ct, _dp(out),
+                                          ct.shape[0], _stream()))
+    return out
+
+
+class SecretKey:
+    """SecretKey (fhe/src/bfv/keys/secret_key.rs:24-60) resident on the device."""
+
+    def __init__(self, par: BfvParameters, coeffs):
+        c = np.ascontiguousarray(np.asarray(coeffs, dtype=np.int64))
+        h = c_vp()
+        check(lib().fheg_secret_key_create(par._h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                           ctypes.byref(h)))
+        self._h = h
+        self.par = par
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_secret_key_destroy(self._h)
+            self._h = None
+
+    def decrypt(self, ct, level: int = 0, simd: bool = True):
+        """try_decrypt + decode (secret_key.rs:200-252, plaintext.rs:337-390):
+        [count][parts][L][N] -> [count][N] values mod t."""
+        count = ct.shape[0]
+        out = empty((count, self.par.degree), ct.device)
+        check(lib().fheg_decrypt(self._h, level, ct.shape[1], _dp(ct), int(simd), _dp(out), count, _stream()))
+        return out
+
+
 def ciphertext_add(par: BfvParameters, level: int, a, b):
     """Add<&Ciphertext> (fhe/src/bfv/ops/mod.rs:15-43) on batches."""
     out = empty(a.shape, a.device)
@@ -632,8 +682,8 @@ class Multiplicator:
 
     def autotune(self, count: int) -> list:
         """Tunes the per-stage NTT plans on `count`-pair multiplications and
-        returns them ([A, C, D, F, F split])."""
-        out = (ctypes.c_uint32 * 5)()
+        returns them ([A, C, D, F, F split, tensor split])."""
+        out = (ctypes.c_uint32 * 6)()
         check(lib().fheg_multiplicator_autotune(self._h, count, _stream(), out))
         return list(out)
 
@@ -648,13 +698,14 @@ class Multiplicator:
 
     @property
     def plan(self) -> list:
-        out = (ctypes.c_uint32 * 5)()
+        out = (ctypes.c_uint32 * 6)()
         check(lib().fheg_multiplicator_get_plan(self._h, out))
         return list(out)
 
     @plan.setter
     def plan(self, values):
-        arr = (ctypes.c_uint32 * 5)(*values)
+        values = list(values) + [0] * (6 - len(values))
+        arr = (ctypes.c_uint32 * 6)(*values)
         check(lib().fheg_multiplicator_set_plan(self._h, arr))
 
     def capture(self, lhs, rhs, out) -> "MultiplyGraph":

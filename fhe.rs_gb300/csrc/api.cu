@@ -278,6 +278,7 @@ void get_mul_plan(const Multiplicator& m, uint32_t* plan) {
   plan[2] = m.plan_d ? m.plan_d : dflt;
   plan[3] = m.plan_f ? m.plan_f : dflt;
   plan[4] = m.f_split ? 1 : 0;
+  plan[5] = m.tensor_split ? 1 : 0;
 }
 
 void set_mul_plan(Multiplicator& m, const uint32_t* plan) {
@@ -289,6 +290,7 @@ void set_mul_plan(Multiplicator& m, const uint32_t* plan) {
   m.plan_d = plan[2];
   m.plan_f = plan[3];
   m.f_split = plan[4] != 0;
+  m.tensor_split = plan[5] != 0;
 }
 
 }  // namespace
@@ -340,30 +342,35 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
     uint64_t* lhs = buf.u64();
     auto run = [&] { mult.multiply(lhs, lhs + in_words, lhs + 2 * in_words, count, st); };
     // Coordinate descent over the stages, starting from the current plan.
-    uint32_t cur[5];
+    uint32_t cur[6];
     get_mul_plan(mult, cur);
     set_mul_plan(mult, cur);
     float best = time_once(st, run);
     const std::vector<uint32_t> plans = ntt_plans(bc.logn);
+    auto consider = [&](const uint32_t* cand) {
+      if (std::equal(cand, cand + 6, cur)) return;
+      set_mul_plan(mult, cand);
+      const float ms = time_once(st, run);
+      if (ms < best) {
+        best = ms;
+        std::copy(cand, cand + 6, cur);
+      }
+    };
     for (int k = 0; k < 4; k++) {
       for (uint32_t bl : plans) {
-        for (uint32_t split = 0; split < (k == 3 && bl >= bc.logn ? 2u : 1u); split++) {
-          uint32_t cand[5];
-          std::copy(cur, cur + 5, cand);
+        for (uint32_t split = 0; split < 2u; split++) {
+          if (split && !(k == 3 && bl >= bc.logn) && k != 2) continue;
+          uint32_t cand[6];
+          std::copy(cur, cur + 6, cand);
           cand[k] = bl;
           if (k == 3) cand[4] = split;
-          if (std::equal(cand, cand + 5, cur)) continue;
-          set_mul_plan(mult, cand);
-          const float ms = time_once(st, run);
-          if (ms < best) {
-            best = ms;
-            std::copy(cand, cand + 5, cur);
-          }
+          if (k == 2) cand[5] = split;
+          consider(cand);
         }
       }
     }
     set_mul_plan(mult, cur);
-    if (plan) std::copy(cur, cur + 5, plan);
+    if (plan) std::copy(cur, cur + 6, plan);
   });
 }
 

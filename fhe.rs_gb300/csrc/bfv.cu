@@ -79,6 +79,32 @@ struct SrcTensor {
   }
 };
 
+// Montgomery products already in memory (the split form of stage D).
+struct SrcPolyMont {
+  static constexpr bool kMontgomery = true;
+  PolyRef r;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    return r.at(j.poly, j.limb)[i];
+  }
+};
+
+// The tensor products of SrcTensor as an element-wise kernel: one thread per
+// (product polynomial, limb, coefficient).
+__global__ void k_tensor(const DevPrime* primes, SrcTensor t, PolyRef out, uint32_t limbs, uint32_t logn,
+                         uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t job = gid >> logn;
+  NttJob j;
+  j.limb = (uint32_t)(job % limbs);
+  j.poly = (uint32_t)(job / limbs);
+  j.beta = 0;
+  j.aux = 0;
+  const DevPrime pr = primes[j.limb];
+  out.at(j.poly, j.limb)[i] = t(j, pr, i);
+}
+
 // Digit i of c2 (power basis, mod q_i) lazily reduced modulo key limb j
 // (rq/mod.rs:525-528).
 struct SrcDigit {
@@ -539,12 +565,22 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     extend(*ext_rhs, 2, 2);
   }
   mark(3);
-  // D: tensor product fused into the inverse NTT over the extended basis.
+  // D: tensor product fused into the inverse NTT over the extended basis, or
+  // (tensor_split) an element-wise product kernel followed by the inverse
+  // NTT in place: the separate kernel keeps enough loads in flight to hide
+  // their latency, at the cost of one more pass over the products.
   PolyRef prodref = plain_ref(prod, M, logn);
   {
     NttGeom g{mc.primes_dev(), (uint32_t)M, 0};
-    ntt_inverse_any(logn, g, 3 * count, SrcTensor{lref, rref, extref, (uint32_t)ncm_l, (uint32_t)ncm_r},
-                    DstPoly{prodref}, st, plan_d);
+    const SrcTensor tensor{lref, rref, extref, (uint32_t)ncm_l, (uint32_t)ncm_r};
+    if (tensor_split) {
+      const uint64_t total = 3 * count * M << logn;
+      k_tensor<<<nblocks(total, 256), 256, 0, st>>>(mc.primes_dev(), tensor, prodref, (uint32_t)M, logn, total);
+      after_launch("k_tensor");
+      ntt_inverse_any(logn, g, 3 * count, SrcPolyMont{prodref}, DstPoly{prodref}, st, plan_d);
+    } else {
+      ntt_inverse_any(logn, g, 3 * count, tensor, DstPoly{prodref}, st, plan_d);
+    }
   }
   mark(4);
   // E: scale down by t/Q into the base context (power basis).

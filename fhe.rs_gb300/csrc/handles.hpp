@@ -29,4 +29,7 @@ struct fheg_multiplicator {
     if (copy_stream) cudaStreamDestroy(copy_stream);
   }
 };
-
+struct fheg_secret_key {
+  fheg::SecretKeyDev k;
+  mutable fheg::Workspace ws;  // scratch of fheg_decrypt
+};

@@ -117,6 +117,15 @@ void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t p
                   cudaStream_t st);
 
 // ---- BFV (bfv.cu) ----
+
+// Plaintext side of a parameter set (codec.cu, built on first use).
+struct PlainSide {
+  std::shared_ptr<Context> tctx;       // modulus t, for SIMD (null if t has no NTT of size N)
+  DevBuf maps;                         // u32 [N] matrix_reps_index_map, then u32 [N] its inverse
+  std::shared_ptr<Context> plain_ctx;  // parameters.rs:480-494
+  std::vector<std::unique_ptr<Scaler>> dec;  // per level: cipher context -> plaintext context by t / Q
+};
+
 struct Params {
   size_t degree = 0;
   std::vector<uint64_t> moduli;
@@ -125,6 +134,17 @@ struct Params {
   Params(size_t degree, const std::vector<uint64_t>& moduli, uint64_t plaintext);
   size_t max_level() const { return moduli.size() - 1; }
   const std::shared_ptr<Context>& ctx(size_t level) const;
+  const PlainSide& plain_side() const;
+
+ private:
+  mutable std::mutex plain_mu;
+  mutable std::unique_ptr<PlainSide> plain;
+};
+
+// A secret key on the device: s in Ntt form over the level-0 context.
+struct SecretKeyDev {
+  const Params* par = nullptr;
+  DevBuf s_ntt;  // [L][N]
 };
 
 // Scratch memory of an operation: either a buffer the workspace owns and
@@ -186,6 +206,7 @@ struct Multiplicator {
   // launches instead of one when F runs single-pass).
   uint32_t plan_a = 0, plan_c = 0, plan_d = 0, plan_f = 0;
   bool f_split = false;
+  bool tensor_split = false;  // D as a product kernel plus an in-place inverse NTT
   Workspace ws;
   DevBuf staging;  // device copies for the host entry point
   // `marks` (optional, 8 events) are recorded on `st` at the stage
@@ -222,5 +243,14 @@ void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t c
 size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
                             uint64_t count, cudaStream_t st);
+
+// ---- plaintext side (codec.cu) ----
+void plaintext_encode(const Params& par, size_t level, const uint64_t* values, bool simd, uint64_t* pt_ntt,
+                      uint64_t count, Workspace& ws, cudaStream_t st);
+void ciphertext_mul_plain(const Params& par, size_t level, size_t parts, const uint64_t* ct, const uint64_t* pt,
+                          bool pt_per_ct, uint64_t* out, uint64_t count, cudaStream_t st);
+size_t decrypt_scratch_bytes(const Params& par, size_t level, uint64_t count);
+void decrypt(const SecretKeyDev& sk, size_t level, size_t parts, const uint64_t* ct, bool simd, uint64_t* values,
+             uint64_t count, Workspace& ws, cudaStream_t st);
 
 }  // namespace fheg

@@ -279,15 +279,16 @@ FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* 
 FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                             uint64_t* d_out, size_t count, void* stream, float* ms);
 /* Per-stage NTT plans of a multiplicator (no counterpart in the reference:
- * schedules only, results are unchanged). plan[5] = block log2 of stage A
+ * schedules only, results are unchanged). plan[6] = block log2 of stage A
  * (inverse NTT of the operands), C (forward NTT of the extension limbs),
- * D (tensor product + inverse NTT), F (digit and c0 / c1 forward NTTs), and
- * plan[4] = 1 to run F as two launches when it is single-pass. Block sizes
- * follow fheg_ntt_plan_set's rules. */
+ * D (tensor product + inverse NTT), F (digit and c0 / c1 forward NTTs),
+ * plan[4] = 1 to run F as two launches when it is single-pass, and plan[5] =
+ * 1 to run the tensor product of D as its own kernel before the inverse NTT.
+ * Block sizes follow fheg_ntt_plan_set's rules. */
 FHEG_API int fheg_multiplicator_get_plan(const fheg_multiplicator* m, uint32_t* plan);
 FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* plan);
 /* Times the multiplication of `count` pairs while varying one stage's plan
- * at a time, installs the fastest and returns it in plan[5] (may be NULL). */
+ * at a time, installs the fastest and returns it in plan[6] (may be NULL). */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
 /* Same, end to end from host buffers: copies the inputs to the device,
  * multiplies, and copies the product back before returning. */
@@ -314,6 +315,39 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
  * streams, or different threads without ordering) race on it. */
 FHEG_API int fheg_relinearize_noalloc(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
                                       void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Plaintext side: encoding, ciphertext x plaintext, decryption               */
+
+typedef struct fheg_secret_key fheg_secret_key;
+
+/* The Ntt polynomial a Plaintext carries (`poly_ntt`, plaintext_vec.rs:40-100)
+ * for `count` vectors d_values [count][N] of values below t (pad with zeros):
+ * simd != 0 scatters them by `matrix_reps_index_map` (parameters.rs:616-629)
+ * and applies the inverse NTT mod t; the result is lifted into the context of
+ * `level` and transformed: d_pt_ntt [count][L][N]. Uses the parameters'
+ * scratch region (calls on the same parameters must not overlap). */
+FHEG_API int fheg_plaintext_encode(const fheg_params* par, size_t level, const uint64_t* d_values, int simd,
+                                   uint64_t* d_pt_ntt, size_t count, void* stream);
+
+/* MulAssign<&Plaintext> for Ciphertext (fhe/src/bfv/ops/mod.rs:229-238):
+ * every part of d_ct [count][parts][L][N] times the plaintext polynomial
+ * (d_pt_ntt [L][N] shared, or [count][L][N] with pt_per_ciphertext != 0). */
+FHEG_API int fheg_ciphertext_mul_plain(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_ct,
+                                       const uint64_t* d_pt_ntt, int pt_per_ciphertext, uint64_t* d_out,
+                                       size_t count, void* stream);
+
+/* A secret key (SecretKey::coeffs, secret_key.rs:24-60: N signed
+ * coefficients) resident on the device in Ntt form. */
+FHEG_API int fheg_secret_key_create(const fheg_params* par, const int64_t* coeffs, fheg_secret_key** out);
+FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk);
+
+/* SecretKey::try_decrypt (secret_key.rs:200-252) followed by decoding
+ * (plaintext.rs:337-390): d_ct [count][parts][L][N] at `level` ->
+ * d_values [count][N] mod t (simd != 0: slot order; 0: coefficient order).
+ * Calls on the same key must not overlap (shared scratch). */
+FHEG_API int fheg_decrypt(const fheg_secret_key* sk, size_t level, size_t parts, const uint64_t* d_ct, int simd,
+                          uint64_t* d_values, size_t count, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */

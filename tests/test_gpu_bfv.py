@@ -297,14 +297,14 @@ def test_multiplicator_stage_plans_and_times(fg, ora, cuda):
     rhs = fg.to_device(np.stack([cts[2].to_array(), cts[3].to_array()]))
     mo = ora.Multiplicator.default(rk_o)
     want = np.stack([mo.multiply(cts[0], cts[2]).to_array(), mo.multiply(cts[1], cts[3]).to_array()])
-    for plan in ([14, 14, 14, 14, 0], [14, 14, 14, 14, 1], [12, 13, 12, 13, 0], [13, 12, 14, 12, 1]):
+    for plan in ([14, 14, 14, 14, 0, 0], [14, 14, 14, 14, 1, 1], [12, 13, 12, 13, 0, 1], [13, 12, 14, 12, 1, 0]):
         m.plan = plan
         assert m.plan == plan
         assert np.array_equal(fg.to_host(m.multiply(lhs, rhs)), want), plan
     with pytest.raises(fg.FhegError):
-        m.plan = [15, 14, 14, 14, 0]
+        m.plan = [15, 14, 14, 14, 0, 0]
     tuned = m.autotune(2)
-    assert all(b in (12, 13, 14) for b in tuned[:4]) and m.plan == tuned
+    assert all(b in (12, 13, 14) for b in tuned[:4]) and len(tuned) == 6 and m.plan == tuned
     out = fg.empty((2, 2, 3, 16384))
     ms = m.stage_times(lhs, rhs, out)
     assert list(ms) == list("ABCDEFG") and all(v > 0 for v in ms.values())
