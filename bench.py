@@ -141,6 +141,22 @@ def make_inputs(ora, batch: int, seed: int = 2026, distinct: int = 16):
     return par, sk, rk, cts, lhs, rhs
 
 
+def max_over_ranks(ms: float, dist) -> float:
+    """The slowest rank's step time (replicas: every rank runs its own batch)."""
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(batch: int, ms: float, world: int) -> float:
+    """Whole-job products per second: every rank multiplies `batch` pairs per
+    step of `ms` milliseconds (the slowest rank's)."""
+    return world * batch / (ms / 1000.0)
+
+
 def cpu_multiply_rate(ora, rk, cts, threads: int, per_thread: int):
     """Oracle products per second with `threads` host threads (independent
     ciphertexts, the reference has no internal parallelism)."""
@@ -267,11 +283,9 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.synchronize()
     direct_ms = start.elapsed_time(end) / args.steps
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist)
         dist.barrier()
-    value = world * B / (ms / 1000.0)
+    value = replica_throughput(B, ms, world)
 
     # The unbatched path: 64 one-ciphertext launches.
     one_l, one_r, one_o = lhs_d[:1], rhs_d[:1], out_d[:1]
@@ -834,6 +848,8 @@ def main():
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
+    ap.add_argument("--ntt-prefetch", default="off", choices=["on", "off"],
+                    help="L2 prefetch of the next CTA's NTT input")
     ap.add_argument("--stage-plan", default="", help="A,C,D,F,F-split,D-split plan of the multiply stages")
     ap.add_argument("--ntt-block", default="auto", help="NTT plan for the degree: auto (autotune) or a block log2")
     ap.add_argument("--serve-requests", type=int, default=2000)
@@ -841,6 +857,11 @@ def main():
     ap.add_argument("--serve-streams", type=int, default=4)
     ap.add_argument("--serve-batch", type=int, default=32)
     args = ap.parse_args()
+    if args.ntt_prefetch == "on":
+        import __graft_entry__ as ge
+
+        ge.build()
+        ge.load_package().ntt_prefetch_set(True)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.workload == "ntt":

@@ -135,6 +135,7 @@ def _declare(L):
         "fheg_copy_to_device": (i, [c_vp, c_vp, c_size, c_vp]),
         "fheg_copy_to_host": (i, [c_vp, c_vp, c_size, c_vp]),
         "fheg_ntt_plan_set": (i, [ctypes.c_uint32, ctypes.c_uint32]),
+        "fheg_ntt_prefetch_set": (i, [i]),
         "fheg_ntt_plan_get": (i, [ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_ntt_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_multiplicator_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
@@ -347,6 +348,11 @@ def ntt_backward(ctx: Context, t):
 def ntt_plan_set(logn: int, block_logn: int):
     """Runs transforms of 2^logn as blocks of 2^block_logn (see fheg.h)."""
     check(lib().fheg_ntt_plan_set(logn, block_logn))
+
+
+def ntt_prefetch_set(on: bool):
+    """L2 prefetch of the next CTA's input rows in the NTT kernels (off by default)."""
+    check(lib().fheg_ntt_prefetch_set(int(on)))
 
 
 def ntt_plan_get(logn: int) -> int:

@@ -179,6 +179,10 @@ FHEG_API int fheg_ntt_plan_set(uint32_t logn, uint32_t block_logn) {
   return guard([&] { set_ntt_block_logn(logn, block_logn); });
 }
 
+FHEG_API int fheg_ntt_prefetch_set(int on) {
+  return guard([&] { set_ntt_prefetch(on != 0); });
+}
+
 FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
   return guard([&] {
     need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");
@@ -719,12 +723,25 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     uint64_t* d_lhs = mm.staging.u64();
     uint64_t* d_rhs = d_lhs + in_words;
     uint64_t* d_out = d_rhs + in_words;
-    if (!m->copy_stream) check_cuda(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking), "stream");
-    cudaStream_t st = m->copy_stream;
-    check_cuda(cudaMemcpyAsync(d_lhs, h_lhs, in_words * 8, cudaMemcpyHostToDevice, st), "H2D");
-    check_cuda(cudaMemcpyAsync(d_rhs, h_rhs, in_words * 8, cudaMemcpyHostToDevice, st), "H2D");
-    mm.multiply(d_lhs, d_rhs, d_out, count, st);
-    check_cuda(cudaMemcpyAsync(h_out, d_out, out_words * 8, cudaMemcpyDeviceToHost, st), "D2H");
-    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    for (auto& s : m->pipe)
+      if (!s) check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    // Chunks of at least 16 pairs rotate over the pipeline's streams, so the
+    // copies of one chunk overlap the multiplication of another.
+    const size_t chunk = count >= 32 ? 16 : count;
+    const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * out_L * N;
+    int k = 0;
+    for (size_t first = 0; first < count; first += chunk, k = (k + 1) % fheg_multiplicator::kPipe) {
+      const size_t c = std::min(chunk, count - first);
+      cudaStream_t st = m->pipe[k];
+      check_cuda(cudaMemcpyAsync(d_lhs + first * in_pair, h_lhs + first * in_pair, c * in_pair * 8,
+                                 cudaMemcpyHostToDevice, st), "H2D");
+      check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
+                                 cudaMemcpyHostToDevice, st), "H2D");
+      mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
+                  &m->pipe_ws[k]);
+      check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
+                                 cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    for (auto& s : m->pipe) check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   });
 }

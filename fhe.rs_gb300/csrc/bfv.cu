@@ -46,6 +46,10 @@ struct SrcPair {
     const uint32_t b = j.poly >> 2, w = j.poly & 3;
     return w < 2 ? lhs.at(2 * b + w, j.limb)[i] : rhs.at(2 * b + w - 2, j.limb)[i];
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    const uint32_t b = j.poly >> 2, w = j.poly & 3;
+    prefetch_l2(w < 2 ? lhs.at(2 * b + w, j.limb) + i : rhs.at(2 * b + w - 2, j.limb) + i);
+  }
 };
 
 // Tensor product (mul.rs:181-185) at limb j of the extended basis: operand
@@ -58,10 +62,24 @@ struct SrcTensor {
   PolyRef lhs, rhs;  // inputs [B][2][L][N], Ntt
   PolyRef ext;       // [B][4][M][N], Ntt (limbs >= ncm of each operand)
   uint32_t ncm_l, ncm_r;
-  __device__ __forceinline__ uint64_t op(uint32_t b, uint32_t w, uint32_t limb, uint32_t i) const {
+  __device__ __forceinline__ const uint64_t* row(uint32_t b, uint32_t w, uint32_t limb) const {
     const bool from_input = w < 2 ? limb < ncm_l : limb < ncm_r;
-    if (from_input) return w < 2 ? lhs.at(2 * b + w, limb)[i] : rhs.at(2 * b + w - 2, limb)[i];
-    return ext.at(4 * b + w, limb)[i];
+    if (from_input) return w < 2 ? lhs.at(2 * b + w, limb) : rhs.at(2 * b + w - 2, limb);
+    return ext.at(4 * b + w, limb);
+  }
+  __device__ __forceinline__ uint64_t op(uint32_t b, uint32_t w, uint32_t limb, uint32_t i) const {
+    return row(b, w, limb)[i];
+  }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    const uint32_t b = j.poly / 3, part = j.poly % 3;
+    if (part != 2) {
+      prefetch_l2(row(b, 0, j.limb) + i);
+      prefetch_l2(row(b, 2, j.limb) + i);
+    }
+    if (part != 0) {
+      prefetch_l2(row(b, 1, j.limb) + i);
+      prefetch_l2(row(b, 3, j.limb) + i);
+    }
   }
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     const uint32_t b = j.poly / 3, part = j.poly % 3;
@@ -86,6 +104,7 @@ struct SrcPolyMont {
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return r.at(j.poly, j.limb)[i];
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(r.at(j.poly, j.limb) + i); }
 };
 
 // The tensor products of SrcTensor as an element-wise kernel: one thread per
@@ -114,6 +133,9 @@ struct SrcDigit {
     const uint32_t b = j.poly / ndig, d = j.poly % ndig;
     return reduce64_lazy(digits.at(b, d)[i], pr);
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    prefetch_l2(digits.at(j.poly / ndig, j.poly % ndig) + i);
+  }
 };
 
 // Ntt input gathered through the substitution x -> x^e (rq/mod.rs:324-334).
@@ -130,6 +152,8 @@ struct SrcSubst {
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return in.at(j.poly, j.limb)[gather_index(i, e, logn)];
   }
+  // The gather reads the whole row: hint its lines in order.
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(in.at(j.poly, j.limb) + i); }
 };
 
 // F stage of the multiplication: polynomials [0, B*L) are the digits of c2
@@ -142,6 +166,10 @@ struct SrcKsF {
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     if (j.poly < ndig_polys) return reduce64_lazy(digits.at(j.poly / ndig, j.poly % ndig)[i], pr);
     return c01.at(j.poly - ndig_polys, j.limb)[i];
+  }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    if (j.poly < ndig_polys) prefetch_l2(digits.at(j.poly / ndig, j.poly % ndig) + i);
+    else prefetch_l2(c01.at(j.poly - ndig_polys, j.limb) + i);
   }
 };
 
@@ -295,6 +323,10 @@ struct SrcRotSubst {
     const RotDesc& r = d[j.poly];
     return r.ct[((uint64_t)(r.L + j.limb) << logn) + gather_index(i, r.e, logn)];
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    const RotDesc& r = d[j.poly];
+    prefetch_l2(r.ct + ((uint64_t)(r.L + j.limb) << logn) + i);
+  }
 };
 
 struct DstRotDigits {
@@ -314,6 +346,9 @@ struct SrcRotDigit {
   uint32_t logn;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     return reduce64_lazy(d[j.poly].digits[((uint64_t)j.aux << logn) + i], pr);
+  }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    prefetch_l2(d[j.poly].digits + ((uint64_t)j.aux << logn) + i);
   }
 };
 

@@ -70,6 +70,9 @@ struct SrcPhase {
   PolyRef ct;  // poly b * parts + k
   const uint64_t* s;
   uint32_t parts, logn;
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    for (uint32_t k = 0; k < parts; k++) prefetch_l2(ct.at(j.poly * parts + k, j.limb) + i);
+  }
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     const uint64_t sj = s[((uint64_t)j.limb << logn) + i];
     uint64_t acc = ct.at(j.poly * parts, j.limb)[i];

@@ -43,6 +43,10 @@ uint32_t ntt_block_logn(uint32_t logn);
 // Validates and installs a plan entry (FHEG_ERR_INVALID_ARGUMENT otherwise).
 void set_ntt_block_logn(uint32_t logn, uint32_t block_logn);
 bool ntt_plan_valid(uint32_t logn, uint32_t block_logn);
+// Whether the block kernels prefetch the next CTA's input into L2
+// (fheg_ntt_prefetch_set; on by default).
+bool ntt_prefetch_enabled();
+void set_ntt_prefetch(bool on);
 // The valid block sizes for 2^logn, ascending.
 std::vector<uint32_t> ntt_plans(uint32_t logn);
 

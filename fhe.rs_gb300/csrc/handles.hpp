@@ -23,10 +23,13 @@ struct fheg_ksk {
   fheg::Ksk k;
 };
 struct fheg_multiplicator {
+  static constexpr int kPipe = 3;  // streams of the host entry point's copy / compute pipeline
   std::unique_ptr<fheg::Multiplicator> m;
-  cudaStream_t copy_stream = nullptr;
+  cudaStream_t pipe[kPipe] = {};
+  fheg::Workspace pipe_ws[kPipe];
   ~fheg_multiplicator() {
-    if (copy_stream) cudaStreamDestroy(copy_stream);
+    for (auto& s : pipe)
+      if (s) cudaStreamDestroy(s);
   }
 };
 struct fheg_secret_key {

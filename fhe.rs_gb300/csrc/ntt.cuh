@@ -23,6 +23,8 @@
 // such as the key-switching inner product).
 #pragma once
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace fheg {
@@ -43,7 +45,9 @@ struct NttGeom {
   uint32_t s1;             // stages handled by the strided pass (0 to 4)
   const uint4* jobs;       // optional ragged job table
   uint32_t mont;           // inverse transforms: inputs carry a factor 2^-64 (Montgomery products)
+  uint32_t pf_stride;      // > 0: each CTA prefetches into L2 the input of CTA blockIdx.x + pf_stride
 };
+
 
 // Final scale of an inverse transform: N^-1, or N^-1 * 2^64 when the inputs
 // are Montgomery products (a * b * 2^-64), which cancels their factor.
@@ -65,6 +69,19 @@ struct NttJob {
   uint32_t poly, limb, beta, aux;
 };
 
+// L2 prefetch hint (no fault, no register result).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Sources that can name the addresses they will read declare
+// prefetch(job, i): a hint for element i of that job.
+template <class S>
+__device__ __forceinline__ auto src_prefetch(const S& s, const NttJob& j, uint32_t i, int)
+    -> decltype(s.prefetch(j, i), void()) {
+  s.prefetch(j, i);
+}
+template <class S>
+__device__ __forceinline__ void src_prefetch(const S&, const NttJob&, uint32_t, long) {}
+
 __device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
   NttJob j;
   if (g.jobs) {
@@ -79,6 +96,27 @@ __device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
   }
   j.beta = 0;
   return j;
+}
+
+__device__ __forceinline__ NttJob decode_job_at(const NttGeom& g, uint32_t block) {
+  uint32_t job = block;
+  const uint32_t beta = job & ((1u << g.s1) - 1);
+  NttJob j = unit_job(g, job >> g.s1);
+  j.beta = beta;
+  return j;
+}
+
+// Block-pass kernels: while this CTA works, the CTA that will take its place
+// on the SM (about pf_stride blocks later) gets its input rows pulled into L2,
+// one hint per 128-byte line, so its load phase hits L2 instead of DRAM.
+template <int LOGN, int T, class Src>
+__device__ __forceinline__ void prefetch_next(const NttGeom& g, const Src& src, uint32_t tid) {
+  if (!g.pf_stride) return;
+  const uint32_t nb = blockIdx.x + g.pf_stride;
+  if (nb >= gridDim.x) return;
+  const NttJob jn = decode_job_at(g, nb);
+  const uint32_t base = jn.beta << LOGN;
+  for (uint32_t k = tid * 16; k < (1u << LOGN); k += T * 16) src_prefetch(src, jn, base + k, 0);
 }
 
 __device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
@@ -197,6 +235,7 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
   const NttJob jb = decode_job(g);
   const DevPrime pr = g.primes[jb.limb];
   const uint32_t base = jb.beta << LOGN;
+  prefetch_next<LOGN, T>(g, src, tid);
   uint64_t x[E];
   // Round 0 holds elements tid + e*T: coalesced loads.
 #pragma unroll
@@ -300,6 +339,7 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
   const NttJob jb = decode_job(g);
   const DevPrime pr = g.primes[jb.limb];
   const uint32_t base = jb.beta << LOGN;
+  prefetch_next<LOGN, T>(g, src, tid);
   uint64_t x[E];
   // Coalesced loads, then regroup through shared memory for the first round.
 #pragma unroll
@@ -444,6 +484,7 @@ struct SrcPoly {
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return r.at(j.poly, j.limb)[i];
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(r.at(j.poly, j.limb) + i); }
 };
 
 // Destinations also provide `reload`, which the two-pass sizes use to read
@@ -454,6 +495,7 @@ struct DstPoly {
     r.at(j.poly, j.limb)[i] = v;
   }
   __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const { return r.at(j.poly, j.limb)[i]; }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(r.at(j.poly, j.limb) + i); }
 };
 
 template <class Dst>
@@ -462,6 +504,7 @@ struct SrcReload {
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return d.reload(j, i);
   }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { src_prefetch(d, j, i, 0); }
 };
 
 // ---------------------------------------------------------------------------
@@ -483,12 +526,28 @@ inline void set_smem(K kernel, size_t bytes, bool* done) {
   }
 }
 
+// CTAs resident on the whole GPU at once for a kernel (the distance to the
+// CTA that takes a finished one's place), computed once per kernel.
+template <class K>
+inline uint32_t resident_ctas(K kernel, int threads, size_t smem, uint32_t* cache) {
+  if (*cache == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem), "occupancy");
+    *cache = (uint32_t)std::max(1, sms * std::max(per_sm, 1));
+  }
+  return *cache;
+}
+
 template <int LOGN, bool REDUCE, class Src, class Dst>
 void launch_fwd_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
   auto kern = k_ntt_fwd<LOGN, REDUCE, Src, Dst>;
   const size_t smem = ntt_smem_bytes<LOGN>();
   static bool done = false;
   set_smem(kern, smem, &done);
+  static uint32_t resident = 0;
+  g.pf_stride = ntt_prefetch_enabled() ? resident_ctas(kern, NttShape<LOGN>::T, smem, &resident) : 0;
   const uint64_t blocks = polys * g.limbs << g.s1;
   kern<<<(unsigned)blocks, NttShape<LOGN>::T, smem, st>>>(g, src, dst);
   after_launch("k_ntt_fwd");
@@ -500,6 +559,8 @@ void launch_inv_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t 
   const size_t smem = ntt_smem_bytes<LOGN>();
   static bool done = false;
   set_smem(kern, smem, &done);
+  static uint32_t resident = 0;
+  g.pf_stride = ntt_prefetch_enabled() ? resident_ctas(kern, NttShape<LOGN>::T, smem, &resident) : 0;
   const uint64_t blocks = polys * g.limbs << g.s1;
   kern<<<(unsigned)blocks, NttShape<LOGN>::T, smem, st>>>(g, src, dst);
   after_launch("k_ntt_inv");

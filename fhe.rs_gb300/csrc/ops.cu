@@ -21,6 +21,12 @@ static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
 
 uint32_t ntt_block_logn(uint32_t logn) { return logn <= 16 ? g_ntt_block[logn].load(std::memory_order_relaxed) : 14; }
 
+// Off by default: on GB300 the hint made the fused tensor NTT 8% slower and
+// left the other stages unchanged.
+static std::atomic<bool> g_ntt_prefetch{false};
+bool ntt_prefetch_enabled() { return g_ntt_prefetch.load(std::memory_order_relaxed); }
+void set_ntt_prefetch(bool on) { g_ntt_prefetch.store(on, std::memory_order_relaxed); }
+
 bool ntt_plan_valid(uint32_t logn, uint32_t block_logn) {
   const bool single = block_logn == logn && logn >= 3 && logn <= 14;
   const bool split = logn >= 13 && logn <= 16 && block_logn >= 12 && block_logn <= 14 && block_logn < logn &&
@@ -321,6 +327,10 @@ struct SrcSwitchDown {
   SwitchConsts c;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     return switch_down_value(c, j.limb, pr, pb.at(j.poly, j.limb)[i], pb.at(j.poly, c.lm1)[i]);
+  }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    prefetch_l2(pb.at(j.poly, j.limb) + i);
+    prefetch_l2(pb.at(j.poly, c.lm1) + i);
   }
 };
 

@@ -141,6 +141,9 @@ FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_
  * (block_logn in 12..14, logn - block_logn <= 4). The plan is process-wide. */
 FHEG_API int fheg_ntt_plan_set(uint32_t logn, uint32_t block_logn);
 FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn);
+/* Whether NTT kernels hint the next CTA's input rows into L2 while they
+ * work (off by default; schedules only). */
+FHEG_API int fheg_ntt_prefetch_set(int on);
 /* Times every valid plan for the context's degree on `count` scratch
  * polynomials (forward + inverse), installs the fastest and returns it. */
 FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn);
