@@ -494,6 +494,86 @@ def run_codec(args):
     print(json.dumps(line), flush=True)
 
 
+def run_compose(args):
+    """Compositions at N = 2^14, L = 6: inner sum of 16 ciphertexts (13 column
+    rotations and the row rotation each), oblivious expansion of one
+    ciphertext into 64, and 4 dot products over 64 ciphertext-plaintext pairs."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    rng = np.random.default_rng(33)
+    par_o = ora.BfvParameters(N, T, moduli_sizes=[62] * L)
+    sk = ora.SecretKey.random(par_o, rng)
+    par = fg.BfvParameters(N, par_o.moduli, T)
+
+    # One key per exponent: the inner sum's column rotation by N/4 uses
+    # exponent 3^(N/4) = N + 1 mod 2N, the first expansion exponent.
+    made = {}
+
+    def keys(exps):
+        for e in exps:
+            if e not in made:
+                g = ora.GaloisKey(sk, e, 0, 0, rng)
+                made[e] = (g, fg.GaloisKey(par, e, g.ksk.c0_array(), g.ksk.c1_array()))
+        return [made[e][0] for e in exps], [made[e][1] for e in exps]
+
+    sum_exps = ora.EvaluationKey.inner_sum_exponents(par_o)
+    exp_exps = ora.EvaluationKey.expansion_exponents(par_o, 6)
+    sum_o, sum_k = keys(sum_exps)
+    exp_o, exp_k = keys(exp_exps)
+    cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, N, dtype=np.uint64), "simd", par_o), rng)
+           for _ in range(16)]
+    arr = fg.to_device(np.stack([c.to_array() for c in cts]))
+    ek = ora.EvaluationKey(sk, rng)
+    ek.gk = dict(zip(sum_exps + exp_exps, sum_o + exp_o))
+    # Parity gate.
+    got = fg.to_host(fg.inner_sum(par, sum_k, arr[:1]))[0]
+    if not np.array_equal(got, ek.computes_inner_sum(cts[0]).to_array()):
+        raise SystemExit("bench: inner sum is not bit-exact with the oracle")
+    got = fg.to_host(fg.expand(par, exp_k, arr[0], 4))
+    want = ek.expands(cts[0], 4)
+    if not all(np.array_equal(got[i], want[i].to_array()) for i in range(4)):
+        raise SystemExit("bench: expansion is not bit-exact with the oracle")
+    groups, count = 4, 64
+    db = fg.plaintext_encode(par, 0, fg.to_device(rng.integers(0, T, (count, N), dtype=np.uint64)))
+    q = arr[torch.arange(groups * count, device=arr.device) % 16].reshape(groups, count, 2, L, N).contiguous()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        sum_ms = timed(lambda: fg.inner_sum(par, sum_k, arr))
+        exp_ms = timed(lambda: fg.expand(par, exp_k, arr[0], 64))
+        dot_ms = timed(lambda: fg.dot_product_scalar(par, 0, q, db))
+    launches = fg.kernel_launch_count() - launches0
+    line = {"metric": "BFV compositions N=2^14 L=6 (inner sum, expansion, dot product)",
+            "value": 16 / (sum_ms / 1000.0), "unit": "inner sums/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum_ms + exp_ms + dot_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
+            "config": {"workload": "compose", "degree": N, "moduli": L, "inner_sum_batch": 16,
+                       "expansion_size": 64, "dot_products": groups, "dot_product_terms": count},
+            "inner_sum_ms": sum_ms, "expansion_64_ms": exp_ms, "dot_products_ms": dot_ms,
+            "rotations_per_s": 16 * len(sum_exps) / (sum_ms / 1000.0),
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_ntt(args):
     """The batched NTT configuration: forward + inverse over `--polys`
     polynomials of six 62-bit moduli at N = 2^logn (device resident), GB/s of
@@ -844,7 +924,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec"])
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec", "compose"])
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
@@ -874,6 +954,8 @@ def main():
         run_stages(args)
     elif args.workload == "codec":
         run_codec(args)
+    elif args.workload == "compose":
+        run_compose(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

@@ -124,6 +124,9 @@ def _declare(L):
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
         "fheg_poly_scalar_mul": (i, [c_vp, P_u64, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_dot_product_scalar": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_size, c_size, c_vp, c_vp]),
+        "fheg_inner_sum": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_expand": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_size, c_vp, c_vp, c_vp]),
         "fheg_plaintext_encode": (i, [c_vp, c_size, c_vp, i, c_vp, c_size, c_vp]),
         "fheg_ciphertext_mul_plain": (i, [c_vp, c_size, c_size, c_vp, c_vp, i, c_vp, c_size, c_vp]),
         "fheg_secret_key_create": (i, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(c_vp)]),
@@ -591,6 +594,42 @@ def ciphertext_mul_plain(par: BfvParameters, level: int, ct, pt_ntt):
     per_ct = int(pt_ntt.dim() == 3)
     check(lib().fheg_ciphertext_mul_plain(par._h, level, ct.shape[1], _dp(ct), _dp(pt_ntt), per_ct, _dp(out),
                                           ct.shape[0], _stream()))
+    return out
+
+
+def dot_product_scalar(par: BfvParameters, level: int, cts, pts):
+    """ops/dot_product.rs:56-140: sum_c cts[g][c] * pts[c] for every group g.
+    cts [groups][count][parts][L][N] (or [count][parts][L][N] for one group),
+    pts [count][L][N] (plaintext Ntt polynomials)."""
+    single = cts.dim() == 4
+    if single:
+        cts = cts[None]
+    groups, count, parts = cts.shape[0], cts.shape[1], cts.shape[2]
+    out = empty((groups, parts, cts.shape[3], cts.shape[4]), cts.device)
+    check(lib().fheg_dot_product_scalar(par._h, level, parts, _dp(cts.contiguous()), _dp(pts), count, groups,
+                                        _dp(out), _stream()))
+    return out[0] if single else out
+
+
+def _keys(keys):
+    n = len(keys)
+    return (c_vp * n)(*[k._h for k in keys]), (c_size * n)(*[k.exponent for k in keys]), n
+
+
+def inner_sum(par: BfvParameters, keys: Sequence["GaloisKey"], ct):
+    """EvaluationKey::computes_inner_sum (evaluation_key.rs:56-83) on a batch
+    [count][2][L][N]; keys in the order of ora.EvaluationKey.inner_sum_exponents."""
+    kh, ex, n = _keys(keys)
+    out = empty(ct.shape, ct.device)
+    check(lib().fheg_inner_sum(par._h, kh, ex, n, _dp(ct), _dp(out), ct.shape[0], _stream()))
+    return out
+
+
+def expand(par: BfvParameters, keys: Sequence["GaloisKey"], ct, size: int):
+    """EvaluationKey::expands (evaluation_key.rs:148-193): [2][L][N] -> [size][2][L][N]."""
+    kh, ex, n = _keys(keys)
+    out = empty((size,) + tuple(ct.shape), ct.device)
+    check(lib().fheg_expand(par._h, kh, ex, n, size, _dp(ct), _dp(out), _stream()))
     return out
 
 

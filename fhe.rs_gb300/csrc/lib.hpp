@@ -244,6 +244,14 @@ size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
                             uint64_t count, cudaStream_t st);
 
+// ---- compositions (compose.cu) ----
+void dot_product_scalar(const Params& par, size_t level, size_t parts, const uint64_t* cts, const uint64_t* pts,
+                        uint64_t count, uint64_t groups, uint64_t* out, cudaStream_t st);
+void inner_sum(const Params& par, const Ksk* const* keys, const uint64_t* exponents, size_t nkeys,
+               const uint64_t* ct, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st);
+void expand(const Params& par, const Ksk* const* keys, const uint64_t* exponents, size_t nlevels, size_t size,
+            const uint64_t* ct, uint64_t* out, Workspace& ws, cudaStream_t st);
+
 // ---- plaintext side (codec.cu) ----
 void plaintext_encode(const Params& par, size_t level, const uint64_t* values, bool simd, uint64_t* pt_ntt,
                       uint64_t count, Workspace& ws, cudaStream_t st);

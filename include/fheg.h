@@ -352,6 +352,29 @@ FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk);
 FHEG_API int fheg_decrypt(const fheg_secret_key* sk, size_t level, size_t parts, const uint64_t* d_ct, int simd,
                           uint64_t* d_values, size_t count, void* stream);
 
+/* dot_product_scalar (fhe/src/bfv/ops/dot_product.rs:56-140) for `groups`
+ * independent dot products over the same `count` plaintexts:
+ * d_out[g] = sum_c d_cts[g][c] * d_pts[c], with d_cts
+ * [groups][count][parts][L][N], d_pts [count][L][N] (Ntt polynomials of the
+ * plaintexts, fheg_plaintext_encode) and d_out [groups][parts][L][N]. */
+FHEG_API int fheg_dot_product_scalar(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_cts,
+                                     const uint64_t* d_pts, size_t count, size_t groups, uint64_t* d_out,
+                                     void* stream);
+
+/* EvaluationKey::computes_inner_sum (fhe/src/bfv/keys/evaluation_key.rs:56-83)
+ * on d_ct [count][2][L][N]: keys / exponents in the reference's order (column
+ * rotations by 1, 2, 4, ... < N/2 as exponents 3^i mod 2N, then the row
+ * rotation 2N - 1), all at the ciphertext's level. Uses the parameters'
+ * scratch region (calls on the same parameters must not overlap). */
+FHEG_API int fheg_inner_sum(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
+                            size_t nkeys, const uint64_t* d_ct, uint64_t* d_out, size_t count, void* stream);
+
+/* EvaluationKey::expands (evaluation_key.rs:148-193): the oblivious expansion
+ * of one ciphertext d_ct [2][L][N] into d_out [size][2][L][N]; keys[l] is the
+ * Galois key of exponent (N >> l) + 1, for l < ceil(log2(size)) <= nlevels. */
+FHEG_API int fheg_expand(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
+                         size_t nlevels, size_t size, const uint64_t* d_ct, uint64_t* d_out, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */
 

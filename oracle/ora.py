@@ -1375,6 +1375,57 @@ class EvaluationKey:
     def rotates_rows(self, ct: Ciphertext) -> Ciphertext:
         return self.gk[2 * self.par.degree - 1].relinearize(ct)
 
+    @staticmethod
+    def inner_sum_exponents(par: BfvParameters) -> List[int]:
+        """evaluation_key.rs:56-83: the column rotations by 1, 2, 4, ... < N/2,
+        then the row rotation, in the order computes_inner_sum applies them."""
+        out, i = [], 1
+        while i < par.degree // 2:
+            out.append(rotation_exponent(par, i))
+            i *= 2
+        return out + [2 * par.degree - 1]
+
+    @staticmethod
+    def expansion_exponents(par: BfvParameters, level: int) -> List[int]:
+        """evaluation_key.rs:349-351: (N >> l) + 1 for l < level."""
+        return [(par.degree >> l) + 1 for l in range(level)]
+
+    def add_keys(self, sk: SecretKey, exponents: Sequence[int], rng: np.random.Generator):
+        for e in exponents:
+            if e not in self.gk:
+                self.gk[e] = GaloisKey(sk, e, self.ciphertext_level, self.evaluation_key_level, rng)
+
+    def computes_inner_sum(self, ct: Ciphertext) -> Ciphertext:
+        """evaluation_key.rs:56-83."""
+        out = ct.copy()
+        for e in self.inner_sum_exponents(self.par):
+            out = out + self.gk[e].relinearize(out)
+        return out
+
+    def monomial(self, l: int) -> Poly:
+        """evaluation_key.rs:355-363: -x^(N - 2^l) in the ciphertext context, Ntt."""
+        n = self.par.degree
+        v = np.zeros(n, dtype=np.int64)
+        v[n - (1 << l)] = -1
+        return Poly.from_i64(self.par.context_at_level(self.ciphertext_level), v).into_ntt()
+
+    def expands(self, ct: Ciphertext, size: int) -> List[Ciphertext]:
+        """evaluation_key.rs:148-193 (oblivious expansion, eprint 2019/1483)."""
+        level = max(size - 1, 0).bit_length()
+        out = [ct.copy()] + [None] * ((1 << level) - 1)
+        for l in range(level):
+            mono = self.monomial(l)
+            gk = self.gk[(self.par.degree >> l) + 1]
+            step = 1 << l
+            for i in range(step):
+                sub = gk.relinearize(out[i])
+                j = step | i
+                if j < size:
+                    t = Ciphertext(self.par, [a - b for a, b in zip(out[i].c, sub.c)], out[i].level)
+                    out[j] = Ciphertext(self.par, [c * mono for c in t.c], t.level)
+                out[i] = out[i] + sub
+        return out[:size]
+
     def rotates_columns_by(self, ct: Ciphertext, i: int) -> Ciphertext:
         return self.gk[self.rot_to_gk_exponent[i]].relinearize(ct)
 
@@ -1456,3 +1507,19 @@ class Multiplicator:
         if self.mod_switch:
             out.switch_down()
         return out
+
+
+def dot_product_scalar(cts: Sequence[Ciphertext], pts: Sequence[Poly]) -> Ciphertext:
+    """ops/dot_product.rs:56-140: sum_i ct_i * pt_i (pt_i the plaintexts' Ntt
+    polynomials), accumulated exactly and reduced once per coefficient."""
+    first = cts[0]
+    parts = []
+    for k in range(len(first)):
+        acc = None
+        for ct, pt in zip(cts, pts):
+            prod = ct[k].coefficients.astype(object) * pt.coefficients.astype(object)
+            acc = prod if acc is None else acc + prod
+        q = np.array(first[k].ctx.moduli, dtype=object)[:, None]
+        c = (acc % q).astype(np.uint64)
+        parts.append(Poly(first[k].ctx, c, NTT))
+    return Ciphertext(first.par, parts, first.level)
