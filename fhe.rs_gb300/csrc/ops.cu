@@ -485,9 +485,14 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     }
   }
 
-  // scaler.rs:316-351.
+  // scaler.rs:316-351. From 16 source moduli on, the output loop stays
+  // rolled: unrolling it as well made the kernel body overflow the
+  // instruction cache (ncu: a third of the stall cycles waiting for
+  // instructions); its constants are then read with an indexed constant-bank
+  // load per term. Smaller bodies run faster unrolled.
+  constexpr int kOutUnroll = MAXF >= 16 ? 1 : MAXT;
   uint64_t* dst = out.at(poly, 0) + i;
-#pragma unroll
+#pragma unroll kOutUnroll
   for (int o = 0; o < MAXT; o++) {
     if (o < (int)s.out_len) {
       DevPrime pr;
