@@ -574,6 +574,73 @@ def run_compose(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serialize(args):
+    """Wire format: the Rq coefficient payload of 128 polynomials (64
+    ciphertexts) at N = 2^14 with six 62-bit moduli, packed and unpacked on
+    the device, in the power basis (pure bit packing, HBM-bound) and from the
+    Ntt representation (with the NTTs the conversion needs)."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    moduli, ub = [], 1 << 62
+    while len(moduli) < L:
+        ub = ora.generate_prime(62, 2 * N, ub)
+        moduli.append(ub)
+    ctx = fg.Context(moduli, N)
+    octx = ora.Context(moduli, N)
+    rng = np.random.default_rng(5)
+    polys = 128
+    x = np.stack([rng.integers(0, m, N, dtype=np.uint64) for m in moduli])
+    xd = fg.to_device(np.tile(x[None], (polys, 1, 1)))
+    payload = fg.serialize(ctx, xd, 0)
+    if bytes(payload[0].cpu().numpy().tobytes()) != ora.rq_payload(ora.Poly(octx, x.copy(), ora.POWER_BASIS)):
+        raise SystemExit("bench: serialization is not byte-exact with the oracle")
+    if not np.array_equal(fg.to_host(fg.deserialize(ctx, payload, 0)[:1])[0], x):
+        raise SystemExit("bench: deserialization does not invert serialization")
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    out = fg.empty((polys, L, N))
+    launches0 = fg.kernel_launch_count()
+    with ClockSampler(0) as clocks:
+        pack_ms = timed(lambda: fg.serialize(ctx, xd, 0))
+        unpack_ms = timed(lambda: fg.deserialize(ctx, payload, 0))
+        pack_ntt_ms = timed(lambda: fg.serialize(ctx, xd, 1))
+        unpack_ntt_ms = timed(lambda: fg.deserialize(ctx, payload, 1))
+    launches = fg.kernel_launch_count() - launches0
+    words = polys * L * N * 8
+    pb = payload.numel()
+    pack_gbs = (words + pb) / (pack_ms / 1000) / 1e9
+    unpack_gbs = (words + pb) / (unpack_ms / 1000) / 1e9
+    peak, kind = _peaks()
+    line = {"metric": "Rq payload pack/unpack GB/s N=2^14 L=6 (power basis)", "value": pack_gbs, "unit": "GB/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": pack_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic", "config": {"workload": "serialize", "degree": N, "moduli": L, "polys": polys,
+                                            "payload_bytes_per_poly": pb // polys},
+            "roofline": {"bound": "hbm", "achieved": pack_gbs, "peak": peak, "unit": "GB/s", "frac": pack_gbs / peak,
+                         "traffic": None, "kernel": "k_pack", "peak_kind": kind},
+            "unpack_gbs": unpack_gbs, "pack_ms": pack_ms, "unpack_ms": unpack_ms,
+            "pack_from_ntt_ms": pack_ntt_ms, "unpack_to_ntt_ms": unpack_ntt_ms,
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_ntt(args):
     """The batched NTT configuration: forward + inverse over `--polys`
     polynomials of six 62-bit moduli at N = 2^logn (device resident), GB/s of
@@ -924,7 +991,8 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec", "compose"])
+    ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec", "compose",
+                                                             "serialize"])
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
@@ -956,6 +1024,8 @@ def main():
         run_codec(args)
     elif args.workload == "compose":
         run_compose(args)
+    elif args.workload == "serialize":
+        run_serialize(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

@@ -124,6 +124,9 @@ def _declare(L):
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
         "fheg_poly_scalar_mul": (i, [c_vp, P_u64, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_serialized_size": (i, [c_vp, ctypes.POINTER(c_size)]),
+        "fheg_poly_serialize": (i, [c_vp, i, c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_deserialize": (i, [c_vp, i, c_vp, c_vp, c_size, c_vp]),
         "fheg_dot_product_scalar": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_size, c_size, c_vp, c_vp]),
         "fheg_inner_sum": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_expand": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_size, c_vp, c_vp, c_vp]),
@@ -377,6 +380,30 @@ def poly_op(ctx: Context, op: str, a, b=None):
     out = empty(a.shape, a.device)
     count = a.numel() // (ctx.L * ctx.degree)
     check(lib().fheg_poly_op(ctx._h, code, _dp(a), _dp(b) if b is not None else None, _dp(out), count, _stream()))
+    return out
+
+
+def serialized_size(ctx: Context) -> int:
+    out = c_size(0)
+    check(lib().fheg_poly_serialized_size(ctx._h, ctypes.byref(out)))
+    return out.value
+
+
+def serialize(ctx: Context, t, representation: int):
+    """Rq coefficient payloads (rq/convert.rs:17-42) of a batch [count][L][N]:
+    a uint8 device tensor [count][bytes]."""
+    torch = _torch()
+    count = t.numel() // (ctx.L * ctx.degree)
+    out = torch.empty((count, serialized_size(ctx)), dtype=torch.uint8, device=t.device)
+    check(lib().fheg_poly_serialize(ctx._h, representation, _dp(t), out.data_ptr(), count, _stream()))
+    return out
+
+
+def deserialize(ctx: Context, payload, representation: int):
+    """Inverse of serialize (rq/convert.rs:44-93): [count][bytes] -> [count][L][N]."""
+    count = payload.shape[0]
+    out = empty((count, ctx.L, ctx.degree), payload.device)
+    check(lib().fheg_poly_deserialize(ctx._h, representation, payload.data_ptr(), _dp(out), count, _stream()))
     return out
 
 

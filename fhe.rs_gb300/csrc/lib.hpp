@@ -244,6 +244,13 @@ size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
                             uint64_t count, cudaStream_t st);
 
+// ---- wire format (serialize.cu) ----
+size_t poly_serialized_bytes(const Context& c);
+void poly_serialize(const Context& c, int representation, const uint64_t* polys, uint8_t* bytes, uint64_t count,
+                    DevBuf& scratch, cudaStream_t st);
+void poly_deserialize(const Context& c, int representation, const uint8_t* bytes, uint64_t* polys, uint64_t count,
+                      cudaStream_t st);
+
 // ---- compositions (compose.cu) ----
 void dot_product_scalar(const Params& par, size_t level, size_t parts, const uint64_t* cts, const uint64_t* pts,
                         uint64_t count, uint64_t groups, uint64_t* out, cudaStream_t st);

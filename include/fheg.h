@@ -154,6 +154,20 @@ FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stre
 FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b,
                           uint64_t* d_out, size_t count, void* stream);
 
+/* The coefficient payload of the reference's `Rq` message
+ * (fhe-math/src/rq/convert.rs:17-93): the power-basis coefficients of every
+ * limb bit-packed little-endian with bitlen(q_j - 1) bits each
+ * (zq/mod.rs:783-793, fhe-util/src/lib.rs:57-135), limbs concatenated.
+ * representation 1 (Ntt) goes through the power basis as the reference does.
+ * d_bytes holds count * fheg_poly_serialized_size bytes. Unpacked values are
+ * reduced modulo their limb's modulus. The protobuf framing (representation,
+ * degree, the bytes field) stays with the caller. */
+FHEG_API int fheg_poly_serialized_size(const fheg_context* ctx, size_t* bytes);
+FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, const uint64_t* d_polys,
+                                 uint8_t* d_bytes, size_t count, void* stream);
+FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, const uint8_t* d_bytes,
+                                   uint64_t* d_polys, size_t count, void* stream);
+
 /* MulAssign<&BigUint> for Poly (fhe-math/src/rq/ops.rs:297-352): every limb
  * times scalar mod q_j (scalar: little-endian u64 words), in either
  * representation. d_out may alias d_in. */

@@ -1523,3 +1523,73 @@ def dot_product_scalar(cts: Sequence[Ciphertext], pts: Sequence[Poly]) -> Cipher
         c = (acc % q).astype(np.uint64)
         parts.append(Poly(first[k].ctx, c, NTT))
     return Ciphertext(first.par, parts, first.level)
+
+
+# ---------------------------------------------------------------------------
+# fhe-util/src/lib.rs:57-135 transcoding and the Rq coefficient payload
+# (fhe-math/src/rq/convert.rs:17-42, 44-93; zq/mod.rs:783-793).
+
+
+def transcode_to_bytes(a: Sequence[int], nbits: int) -> bytes:
+    """lib.rs:57-95: little-endian bit packing of nbits-bit values."""
+    assert 0 < nbits <= 64
+    mask = (1 << nbits) - 1
+    acc, acc_bits, out = 0, 0, bytearray()
+    for v in a:
+        acc |= (int(v) & mask) << acc_bits
+        acc_bits += nbits
+        while acc_bits >= 8:
+            out.append(acc & 0xFF)
+            acc >>= 8
+            acc_bits -= 8
+    if acc_bits > 0:
+        out.append(acc & 0xFF)
+    return bytes(out)
+
+
+def transcode_from_bytes(b: bytes, nbits: int) -> List[int]:
+    """lib.rs:97-135."""
+    assert 0 < nbits <= 64
+    mask = (1 << nbits) - 1
+    acc, acc_bits, out = 0, 0, []
+    for byte in b:
+        acc |= int(byte) << acc_bits
+        acc_bits += 8
+        while acc_bits >= nbits:
+            out.append(acc & mask)
+            acc >>= nbits
+            acc_bits -= nbits
+    if acc_bits > 0:
+        out.append(acc)
+    return out
+
+
+def modulus_nbits(p: int) -> int:
+    """zq/mod.rs:783-786: bits of p - 1."""
+    return (p - 1).bit_length()
+
+
+def rq_payload(p: "Poly") -> bytes:
+    """convert.rs:17-42: power-basis coefficients of every limb, each packed
+    with the bit length of its modulus, concatenated."""
+    q = p.copy()
+    if q.representation != POWER_BASIS:
+        q.into_power_basis()
+    return b"".join(transcode_to_bytes(q.coefficients[i].tolist(), modulus_nbits(m))
+                    for i, m in enumerate(q.ctx.moduli))
+
+
+def rq_from_payload(ctx: Context, payload: bytes, representation: str) -> "Poly":
+    """convert.rs:44-93 + TryConvertFrom<&Rq>: unpack every limb (values
+    reduced modulo the limb's modulus), then back to `representation`."""
+    n = ctx.degree
+    rows, index = [], 0
+    for m in ctx.moduli:
+        size = (n * modulus_nbits(m) + 7) // 8
+        vals = transcode_from_bytes(payload[index:index + size], modulus_nbits(m))[:n]
+        rows.append(np.array([v % m for v in vals], dtype=np.uint64))
+        index += size
+    p = Poly(ctx, np.stack(rows), POWER_BASIS)
+    if representation != POWER_BASIS:
+        p.into_ntt()
+    return p

@@ -124,3 +124,29 @@ def test_scalar_mul(fg, ora, cuda):
             s = scalar % q
             want = np.array([int(v) * s % q for v in x[:, j].ravel()], dtype=np.uint64).reshape(x[:, j].shape)
             assert np.array_equal(got[:, j], want), (scalar, j)
+
+
+@pytest.mark.parametrize("n,bits", [(16, [62, 62, 40]), (4096, [62, 50]), (16384, [62] * 6)])
+def test_serialize_matches_oracle(fg, ora, cuda, n, bits):
+    """The Rq coefficient payload (rq/convert.rs:17-93) byte for byte, both
+    representations, and back."""
+    moduli = []
+    for b in bits:
+        ub = 1 << b
+        while True:
+            ub = ora.generate_prime(b, 2 * n, ub)
+            if ub not in moduli:
+                moduli.append(ub)
+                break
+    ctx = fg.Context(moduli, n)
+    octx = ora.Context(moduli, n)
+    rng = np.random.default_rng(n)
+    x = np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli]) for _ in range(3)])
+    for rep, orep in ((0, ora.POWER_BASIS), (1, ora.NTT)):
+        got = fg.serialize(ctx, fg.to_device(x), rep).cpu().numpy()
+        assert got.shape == (3, fg.serialized_size(ctx))
+        for b in range(3):
+            want = ora.rq_payload(ora.Poly(octx, x[b].copy(), orep))
+            assert bytes(got[b].tobytes()) == want, (rep, b)
+        back = fg.to_host(fg.deserialize(ctx, fg.serialize(ctx, fg.to_device(x), rep), rep))
+        assert np.array_equal(back, x), rep

@@ -244,3 +244,33 @@ def test_rotations_decrypt(ora):
         assert np.array_equal(got, want)
     got = sk.decrypt(ek.rotates_rows(ct)).decode("simd")
     assert np.array_equal(got, np.concatenate([values[half:], values[:half]]))
+
+
+def test_transcode_known_and_roundtrip(ora):
+    """fhe-util/src/lib.rs:255-304: the known round trip, the empty case and
+    self-consistency for every width."""
+    b = ora.transcode_to_bytes([1, 2, 3, 4], 4)
+    assert b == bytes([0x21, 0x43])
+    assert ora.transcode_from_bytes(b, 4)[:4] == [1, 2, 3, 4]
+    assert ora.transcode_to_bytes([], 8) == b"" and ora.transcode_from_bytes(b"", 8) == []
+    rng = np.random.default_rng(3)
+    for size in (1, 7, 33):
+        vals = [int(x) for x in rng.integers(0, 2**63, size, dtype=np.uint64)]
+        for nbits in (1, 5, 17, 31, 62, 63):
+            masked = [v & ((1 << nbits) - 1) for v in vals]
+            bb = ora.transcode_to_bytes(masked, nbits)
+            assert len(bb) == (size * nbits + 7) // 8
+            assert ora.transcode_from_bytes(bb, nbits)[:size] == masked
+
+
+def test_rq_payload_roundtrip(ora):
+    """rq/serialize.rs tests: power basis and Ntt survive the payload."""
+    rng = np.random.default_rng(4)
+    moduli = [4611686018282684417, 4611686018326724609, 4611686018309947393]
+    ctx = ora.Context(moduli, 16)
+    c = np.stack([rng.integers(0, m, 16, dtype=np.uint64) for m in moduli])
+    for rep in (ora.POWER_BASIS, ora.NTT):
+        p = ora.Poly(ctx, c.copy(), rep)
+        payload = ora.rq_payload(p)
+        assert len(payload) == 3 * 16 * 62 // 8
+        assert np.array_equal(ora.rq_from_payload(ctx, payload, rep).coefficients, c)
