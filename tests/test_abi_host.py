@@ -105,3 +105,18 @@ def test_ntt_plan_validation(fg):
     assert fg.ntt_plan_get(14) == 12
     fg.ntt_plan_set(14, 14)
     assert fg.ntt_plan_get(14) == 14
+
+
+def test_no_device_fails_loudly(fg):
+    """Without a CUDA device every entry point that needs one returns a CUDA
+    error status (no silent host fallback)."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(fg.FhegError) as e:
+        fg.Context([4611686018427322369], 4096)
+    assert e.value.code == fg.ERR_CUDA
+    ptr = ctypes.c_void_p()
+    assert fg.lib().fheg_device_alloc(1 << 20, ctypes.byref(ptr)) == fg.ERR_CUDA
+    fg.ntt_prefetch_set(False)  # host-only settings still work

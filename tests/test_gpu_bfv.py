@@ -327,3 +327,33 @@ def test_switch_to_level(fg, ora, cuda):
     with pytest.raises(fg.FhegError) as e:
         fg.ciphertext_switch_to_level(s.par, 2, 1, fg.to_device(arr))
     assert e.value.code == fg.ERR_INVALID_LEVEL
+
+
+def test_errors_of_the_wider_api(fg, ora, cuda):
+    """Error statuses of the plaintext side, compositions and wire format."""
+    s = Setup(fg, ora, 16, 3, 1153, seed=99)
+    _, cts = s.encrypt(2)
+    ct = fg.to_device(np.stack([c.to_array() for c in cts]))
+    ctx = s.par.context_at_level(0)
+    with pytest.raises(fg.FhegError) as e:  # representation 2 (NttShoup) has no payload form here
+        fg.check(fg.lib().fheg_poly_serialize(ctx._h, 2, None, None, 0, None))
+    assert e.value.code == fg.ERR_INVALID_ARGUMENT
+    sk = fg.SecretKey(s.par, s.sk.coeffs)
+    with pytest.raises(fg.FhegError) as e:
+        sk.decrypt(ct[:, :1].contiguous())
+    assert e.value.code == fg.ERR_WRONG_PARTS
+    with pytest.raises(fg.FhegError) as e:
+        fg.dot_product_scalar(s.par, 0, ct[:0], fg.empty((0, 3, 16)))
+    assert e.value.code == fg.ERR_INVALID_ARGUMENT
+    gk_o = ora.GaloisKey(s.sk, 17, 1, 1, s.rng)
+    gk1 = fg.GaloisKey(s.par, 17, gk_o.ksk.c0_array(), gk_o.ksk.c1_array(), 1, 1)
+    with pytest.raises(fg.FhegError) as e:
+        fg.expand(s.par, [gk1], ct[0], 4)  # two levels need two keys
+    assert e.value.code == fg.ERR_INVALID_ARGUMENT
+    # SIMD needs t = 1 mod 2N
+    par2_o = ora.BfvParameters(16, 1031, moduli_sizes=[62] * 2)
+    par2 = fg.BfvParameters(16, par2_o.moduli, 1031)
+    with pytest.raises(fg.FhegError) as e:
+        fg.plaintext_encode(par2, 0, fg.to_device(np.zeros((1, 16), dtype=np.uint64)))
+    assert e.value.code == fg.ERR_UNSUPPORTED
+    fg.plaintext_encode(par2, 0, fg.to_device(np.zeros((1, 16), dtype=np.uint64)), simd=False)
