@@ -146,6 +146,7 @@ def _declare(L):
         "fheg_ntt_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_multiplicator_autotune": (i, [c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_multiplicator_get_plan": (i, [c_vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "fheg_multiplicator_set_small_plan": (i, [c_vp, c_size, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_multiplicator_stage_times": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp, ctypes.POINTER(ctypes.c_float)]),
         "fheg_multiplicator_set_plan": (i, [c_vp, ctypes.POINTER(ctypes.c_uint32)]),
         "fheg_multiplicator_capture": (i, [c_vp, c_vp, c_vp, c_vp, c_size, ctypes.POINTER(c_vp)]),
@@ -767,6 +768,11 @@ class Multiplicator:
         check(lib().fheg_multiplicator_stage_times(self._h, _dp(lhs), _dp(rhs), _dp(out), lhs.shape[0], _stream(),
                                                    ms))
         return dict(zip(self.STAGES, [float(x) for x in ms]))
+
+    def set_small_plan(self, max_count: int, plan=None):
+        """Plan of batches of at most max_count pairs (0 turns it off)."""
+        arr = (ctypes.c_uint32 * 6)(*(list(plan or [12, 12, 12, 12, 1, 0]) + [0] * 6)[:6])
+        check(lib().fheg_multiplicator_set_small_plan(self._h, max_count, arr))
 
     @property
     def plan(self) -> list:

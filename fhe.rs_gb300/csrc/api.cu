@@ -251,7 +251,8 @@ FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stre
 
 namespace {
 
-// Event time of one call of `run` on `st` after a warm-up call.
+// Event time of `run` on `st`: the fastest of three calls after a warm-up
+// call (one call alone flips close choices on run-to-run noise).
 template <class F>
 float time_once(cudaStream_t st, F run) {
   cudaEvent_t e0, e1;
@@ -260,11 +261,15 @@ float time_once(cudaStream_t st, F run) {
   float ms = 0;
   try {
     run();
-    check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
-    run();
-    check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
-    check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
-    check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    for (int k = 0; k < 3; k++) {
+      check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+      run();
+      check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+      check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+      float t = 0;
+      check_cuda(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime");
+      if (k == 0 || t < ms) ms = t;
+    }
   } catch (...) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -316,6 +321,19 @@ FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_
       throw;
     }
     for (auto& e : ev) cudaEventDestroy(e);
+  });
+}
+
+FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max_count, const uint32_t* plan) {
+  return guard([&] {
+    need(m && (plan || !max_count), "null input");
+    Multiplicator& mm = *m->m;
+    if (max_count) {
+      for (int k = 0; k < 4; k++)
+        if (!ntt_plan_valid(mm.base->logn, plan[k])) throw Error(FHEG_ERR_INVALID_ARGUMENT, "unsupported NTT plan");
+      std::copy(plan, plan + 6, mm.small_plan);
+    }
+    mm.small_count = max_count;
   });
 }
 

@@ -569,6 +569,19 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   uint64_t* tmp = ws.take(w_tmp, &off);
   uint64_t* dest = mod_switch ? tmp : out;
 
+  // Stage plans: the small-batch plan when it applies.
+  uint32_t plan_a = this->plan_a, plan_c = this->plan_c, plan_d = this->plan_d, plan_f = this->plan_f;
+  bool f_split = this->f_split, tensor_split = this->tensor_split;
+  if (count <= small_count && ntt_plan_valid(logn, small_plan[0]) && ntt_plan_valid(logn, small_plan[1]) &&
+      ntt_plan_valid(logn, small_plan[2]) && ntt_plan_valid(logn, small_plan[3])) {
+    plan_a = small_plan[0];
+    plan_c = small_plan[1];
+    plan_d = small_plan[2];
+    plan_f = small_plan[3];
+    f_split = small_plan[4] != 0;
+    tensor_split = small_plan[5] != 0;
+  }
+
   PolyRef lref = plain_ref(const_cast<uint64_t*>(lhs), L, logn);
   PolyRef rref = plain_ref(const_cast<uint64_t*>(rhs), L, logn);
   PolyRef pbref = plain_ref(pb, L, logn);

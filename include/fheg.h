@@ -304,6 +304,11 @@ FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_
  * Block sizes follow fheg_ntt_plan_set's rules. */
 FHEG_API int fheg_multiplicator_get_plan(const fheg_multiplicator* m, uint32_t* plan);
 FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* plan);
+/* Plan for small batches: multiplications of at most max_count pairs use
+ * plan[6] instead (default: 8 pairs, blocks of 2^12 with F in two launches,
+ * which cuts the one-pair latency by about 30% at N = 2^14). max_count = 0
+ * turns it off. */
+FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max_count, const uint32_t* plan);
 /* Times the multiplication of `count` pairs while varying one stage's plan
  * at a time, installs the fastest and returns it in plan[6] (may be NULL). */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);

@@ -263,6 +263,7 @@ def test_pipelines_under_every_ntt_plan(fg, ora, cuda, n, plans):
     s = Setup(fg, ora, n, 3, 65537, seed=n + 3)
     rk_o, rk = s.rk()
     m = fg.Multiplicator.default(rk)
+    m.set_small_plan(0)
     gk_o = ora.GaloisKey(s.sk, 2 * n - 1, 0, 0, s.rng)
     gk = fg.GaloisKey(s.par, 2 * n - 1, gk_o.ksk.c0_array(), gk_o.ksk.c1_array())
     _, cts = s.encrypt(2)
@@ -292,6 +293,7 @@ def test_multiplicator_stage_plans_and_times(fg, ora, cuda):
     s = Setup(fg, ora, 16384, 3, 65537, seed=404)
     rk_o, rk = s.rk()
     m = fg.Multiplicator.default(rk)
+    m.set_small_plan(0)  # two pairs would otherwise run with the small-batch plan
     _, cts = s.encrypt(4)
     lhs = fg.to_device(np.stack([cts[0].to_array(), cts[1].to_array()]))
     rhs = fg.to_device(np.stack([cts[2].to_array(), cts[3].to_array()]))
@@ -357,3 +359,21 @@ def test_errors_of_the_wider_api(fg, ora, cuda):
         fg.plaintext_encode(par2, 0, fg.to_device(np.zeros((1, 16), dtype=np.uint64)))
     assert e.value.code == fg.ERR_UNSUPPORTED
     fg.plaintext_encode(par2, 0, fg.to_device(np.zeros((1, 16), dtype=np.uint64)), simd=False)
+
+
+def test_small_batch_plan(fg, ora, cuda):
+    """Batches up to the small-batch threshold use their own plan; results
+    are the same with it, without it and with a custom one."""
+    s = Setup(fg, ora, 16384, 3, 65537, seed=405)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(2)
+    a, b = fg.to_device(cts[0].to_array()[None]), fg.to_device(cts[1].to_array()[None])
+    want = ora.Multiplicator.default(rk_o).multiply(cts[0], cts[1]).to_array()
+    assert np.array_equal(fg.to_host(m.multiply(a, b))[0], want)  # default small plan
+    m.set_small_plan(0)
+    assert np.array_equal(fg.to_host(m.multiply(a, b))[0], want)
+    m.set_small_plan(4, [13, 12, 13, 12, 0, 1])
+    assert np.array_equal(fg.to_host(m.multiply(a, b))[0], want)
+    with pytest.raises(fg.FhegError):
+        m.set_small_plan(4, [11, 12, 12, 12, 0, 0])
