@@ -916,7 +916,8 @@ def run_serve(args):
     for s in setups:
         fg.ntt_autotune(s["par"].context_at_level(0), 32)
         for lv in s["levels"]:
-            lv["mult"].autotune(8)
+            lv["mult"].autotune(4)   # the small-batch plan
+            lv["mult"].autotune(32)  # the plan of full batches
     # Parity gate: every operation of every set, at its top and bottom live
     # levels, through the server alone, against the oracle.
     with fg.Server(budget, streams=1, max_batch=1) as srv:

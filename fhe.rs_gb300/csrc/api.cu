@@ -363,15 +363,26 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
     check_cuda(cudaMemsetAsync(buf.ptr, 0, buf.bytes, st), "cudaMemsetAsync");
     uint64_t* lhs = buf.u64();
     auto run = [&] { mult.multiply(lhs, lhs + in_words, lhs + 2 * in_words, count, st); };
+    // Batches the small-batch plan covers tune that plan; others the main one.
+    bool small = count <= mult.small_count;
+    for (int k = 0; k < 4; k++) small = small && ntt_plan_valid(bc.logn, mult.small_plan[k]);
+    auto get = [&](uint32_t* p) {
+      if (small) std::copy(mult.small_plan, mult.small_plan + 6, p);
+      else get_mul_plan(mult, p);
+    };
+    auto set = [&](const uint32_t* p) {
+      if (small) std::copy(p, p + 6, mult.small_plan);
+      else set_mul_plan(mult, p);
+    };
     // Coordinate descent over the stages, starting from the current plan.
     uint32_t cur[6];
-    get_mul_plan(mult, cur);
-    set_mul_plan(mult, cur);
+    get(cur);
+    set(cur);
     float best = time_once(st, run);
     const std::vector<uint32_t> plans = ntt_plans(bc.logn);
     auto consider = [&](const uint32_t* cand) {
       if (std::equal(cand, cand + 6, cur)) return;
-      set_mul_plan(mult, cand);
+      set(cand);
       const float ms = time_once(st, run);
       if (ms < best) {
         best = ms;
@@ -391,7 +402,7 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
         }
       }
     }
-    set_mul_plan(mult, cur);
+    set(cur);
     if (plan) std::copy(cur, cur + 6, plan);
   });
 }

@@ -310,7 +310,8 @@ FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* 
  * turns it off. */
 FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max_count, const uint32_t* plan);
 /* Times the multiplication of `count` pairs while varying one stage's plan
- * at a time, installs the fastest and returns it in plan[6] (may be NULL). */
+ * at a time, installs the fastest and returns it in plan[6] (may be NULL).
+ * A count within the small-batch threshold tunes the small-batch plan. */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
 /* Same, end to end from host buffers: copies the inputs to the device,
  * multiplies, and copies the product back before returning. */

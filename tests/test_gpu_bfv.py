@@ -377,3 +377,7 @@ def test_small_batch_plan(fg, ora, cuda):
     assert np.array_equal(fg.to_host(m.multiply(a, b))[0], want)
     with pytest.raises(fg.FhegError):
         m.set_small_plan(4, [11, 12, 12, 12, 0, 0])
+    big = m.plan
+    tuned = m.autotune(2)  # within the threshold: tunes the small-batch plan only
+    assert m.plan == big and all(b in (12, 13, 14) for b in tuned[:4])
+    assert np.array_equal(fg.to_host(m.multiply(a, b))[0], want)
