@@ -135,6 +135,7 @@ def _declare(L):
         "fheg_secret_key_create": (i, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(c_vp)]),
         "fheg_secret_key_destroy": (None, [c_vp]),
         "fheg_decrypt": (i, [c_vp, c_size, c_size, c_vp, i, c_vp, c_size, c_vp]),
+        "fheg_encrypt": (i, [c_vp, c_size, c_vp, i, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_ciphertext_switch_to_level": (i, [c_vp, c_size, c_size, c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_device_alloc": (i, [c_size, ctypes.POINTER(c_vp)]),
         "fheg_device_free": (i, [c_vp]),
@@ -676,6 +677,16 @@ class SecretKey:
         if getattr(self, "_h", None) is not None and _lib is not None:
             _lib.fheg_secret_key_destroy(self._h)
             self._h = None
+
+    def encrypt(self, values, a_ntt, e, level: int = 0, simd: bool = True):
+        """try_encrypt with the caller's randomness (secret_key.rs:102-138):
+        values [count][N] (< t), a_ntt [count][L][N], e [count][N] (int64)."""
+        count = values.shape[0]
+        ctx = self.par.context_at_level(level)
+        out = empty((count, 2, ctx.L, self.par.degree), values.device)
+        check(lib().fheg_encrypt(self._h, level, _dp(values), int(simd), _dp(a_ntt), _dp(e), _dp(out), count,
+                                 _stream()))
+        return out
 
     def decrypt(self, ct, level: int = 0, simd: bool = True):
         """try_decrypt + decode (secret_key.rs:200-252, plaintext.rs:337-390):

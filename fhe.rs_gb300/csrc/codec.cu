@@ -114,6 +114,43 @@ struct DstSlots {
   }
 };
 
+// Encryption source (secret_key.rs:102-123 with plaintext.rs:71-98): the
+// power-basis element e_i + Delta_j * ((v_i * (Q mod t)) mod t) of limb j,
+// whose forward NTT is e_ntt + m_poly by linearity (Delta is a constant
+// polynomial: Delta_j = (-t)^-1 mod q_j, parameters.rs:509-559).
+struct SrcEncrypt {
+  const int64_t* e;   // [count][N]
+  const uint64_t* v;  // [count][N], < t
+  const ulonglong2* delta;  // (Delta_j, Shoup) per limb
+  uint64_t t, q_mod_t;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
+    const uint64_t k = ((uint64_t)j.poly << logn) + i;
+    const uint64_t m = (uint64_t)(((unsigned __int128)v[k] * q_mod_t) % t);
+    const int64_t ei = e[k];
+    const uint64_t ev = ei >= 0 ? (uint64_t)ei % pr.p : (pr.p - (uint64_t)(-(ei + 1)) % pr.p - 1);
+    const ulonglong2 d = delta[j.limb];
+    return add_mod(ev, mul_shoup(m % pr.p, d.x, d.y, pr.p), pr.p);
+  }
+};
+
+// b -= a s and the copy of a: ciphertext (b, a), one thread per residue.
+__global__ void k_encrypt_finish(const DevPrime* primes, uint64_t* out, const uint64_t* a, const uint64_t* s,
+                                 uint32_t limbs, uint32_t logn, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint64_t row = gid >> logn;  // poly * limbs + limb
+  const uint32_t limb = (uint32_t)(row % limbs);
+  const uint64_t poly = row / limbs;
+  const DevPrime pr = primes[limb];
+  const uint64_t ai = a[gid];
+  const uint64_t as = mul_mod(ai, s[((uint64_t)limb << logn) + i], pr);
+  uint64_t* o = out + ((poly * 2 * limbs + limb) << logn) + i;
+  o[0] = sub_mod(o[0], as, pr.p);
+  o[(uint64_t)limbs << logn] = ai;
+}
+
 __global__ void k_finish(SrcFinish f, uint64_t* out, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
@@ -204,6 +241,47 @@ void ciphertext_mul_plain(const Params& par, size_t level, size_t parts, const u
                                                 plain_ref(out, c.L(), c.logn), (uint32_t)parts, (uint32_t)c.L(),
                                                 c.logn, pt_per_ct ? 1u : 0u, total);
   after_launch("k_mul_plain");
+}
+
+void encrypt(const SecretKeyDev& sk, size_t level, const uint64_t* values, bool simd, const uint64_t* a,
+             const int64_t* e, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st) {
+  if (count == 0) return;
+  const Params& par = *sk.par;
+  const PlainSide& ps = par.plain_side();
+  const Context& c = *par.ctx(level);
+  const uint32_t logn = c.logn;
+  const uint64_t t = par.plaintext;
+  const size_t L = c.L();
+  // Delta_j = (-t)^-1 mod q_j and Q mod t of this level (parameters.rs:509-559).
+  std::vector<uint64_t> dh(2 * L);
+  for (size_t j = 0; j < L; j++) {
+    const uint64_t q = c.moduli[j];
+    const uint64_t neg_t = (q - t % q) % q;
+    dh[2 * j] = invmod(neg_t, q);
+    dh[2 * j + 1] = shoup(dh[2 * j], q);
+  }
+  const uint64_t q_mod_t = c.rns->product.mod_u64(t);
+  ws.reserve((count * c.N() + 2 * L) * 8 + 512);
+  size_t off = 0;
+  uint64_t* vbuf = ws.take(count * c.N(), &off);
+  uint64_t* dbuf = ws.take(2 * L, &off);
+  check_cuda(cudaMemcpyAsync(dbuf, dh.data(), dh.size() * 8, cudaMemcpyHostToDevice, st), "H2D");
+  const uint64_t* v = values;
+  if (simd) {
+    if (!ps.tctx) throw Error(FHEG_ERR_UNSUPPORTED, "the plaintext modulus does not support SIMD encoding");
+    const uint32_t* inv = static_cast<const uint32_t*>(ps.maps.ptr) + c.N();
+    NttGeom gt{ps.tctx->primes_dev(), 1, 0};
+    ntt_inverse_any(logn, gt, count, SrcValues{values, inv, logn}, DstPoly{plain_ref(vbuf, 1, logn)}, st);
+    v = vbuf;
+  }
+  NttGeom g{c.primes_dev(), (uint32_t)L, 0};
+  ntt_forward_any<true>(logn, g, count,
+                        SrcEncrypt{e, v, reinterpret_cast<const ulonglong2*>(dbuf), t, q_mod_t, logn},
+                        DstPoly{sub_ref(out, L, logn, 2, 0, 1)}, st);
+  const uint64_t total = count * L << logn;
+  k_encrypt_finish<<<nblk(total, 256), 256, 0, st>>>(c.primes_dev(), out, a, sk.s_ntt.u64(), (uint32_t)L, logn,
+                                                     total);
+  after_launch("k_encrypt_finish");
 }
 
 size_t decrypt_scratch_bytes(const Params& par, size_t level, uint64_t count) {
@@ -319,6 +397,14 @@ FHEG_API int fheg_secret_key_create(const fheg_params* par, const int64_t* coeff
 }
 
 FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk) { delete sk; }
+
+FHEG_API int fheg_encrypt(const fheg_secret_key* sk, size_t level, const uint64_t* d_values, int simd,
+                          const uint64_t* d_a, const int64_t* d_e, uint64_t* d_ct, size_t count, void* stream) {
+  return guarded([&] {
+    need(sk && ((d_values && d_a && d_e && d_ct) || !count), "null input");
+    encrypt(sk->k, level, d_values, simd != 0, d_a, d_e, d_ct, count, sk->ws, static_cast<cudaStream_t>(stream));
+  });
+}
 
 FHEG_API int fheg_decrypt(const fheg_secret_key* sk, size_t level, size_t parts, const uint64_t* d_ct, int simd,
                           uint64_t* d_values, size_t count, void* stream) {

@@ -270,6 +270,8 @@ void plaintext_encode(const Params& par, size_t level, const uint64_t* values, b
                       uint64_t count, Workspace& ws, cudaStream_t st);
 void ciphertext_mul_plain(const Params& par, size_t level, size_t parts, const uint64_t* ct, const uint64_t* pt,
                           bool pt_per_ct, uint64_t* out, uint64_t count, cudaStream_t st);
+void encrypt(const SecretKeyDev& sk, size_t level, const uint64_t* values, bool simd, const uint64_t* a,
+             const int64_t* e, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st);
 size_t decrypt_scratch_bytes(const Params& par, size_t level, uint64_t count);
 void decrypt(const SecretKeyDev& sk, size_t level, size_t parts, const uint64_t* ct, bool simd, uint64_t* values,
              uint64_t count, Workspace& ws, cudaStream_t st);

@@ -365,6 +365,15 @@ FHEG_API int fheg_ciphertext_mul_plain(const fheg_params* par, size_t level, siz
 FHEG_API int fheg_secret_key_create(const fheg_params* par, const int64_t* coeffs, fheg_secret_key** out);
 FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk);
 
+/* SecretKey::try_encrypt (secret_key.rs:102-138, 186-194) with its
+ * randomness supplied by the caller: d_a [count][L][N] the uniform Ntt
+ * polynomial a (Poly::random_from_seed in the reference), d_e [count][N] the
+ * small error coefficients (Poly::small). d_values [count][N] (< t) are the
+ * plaintext slots (simd != 0) or coefficients. d_ct [count][2][L][N] receives
+ * (e - a s + m, a). Calls on the same key must not overlap. */
+FHEG_API int fheg_encrypt(const fheg_secret_key* sk, size_t level, const uint64_t* d_values, int simd,
+                          const uint64_t* d_a, const int64_t* d_e, uint64_t* d_ct, size_t count, void* stream);
+
 /* SecretKey::try_decrypt (secret_key.rs:200-252) followed by decoding
  * (plaintext.rs:337-390): d_ct [count][parts][L][N] at `level` ->
  * d_values [count][N] mod t (simd != 0: slot order; 0: coefficient order).

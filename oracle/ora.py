@@ -1171,6 +1171,17 @@ class SecretKey:
     def encrypt(self, pt: Plaintext, rng: np.random.Generator) -> Ciphertext:
         return self.encrypt_poly(pt.to_poly(), rng)
 
+    def encrypt_with(self, pt: Plaintext, a_ntt: np.ndarray, e: np.ndarray) -> Ciphertext:
+        """secret_key.rs:102-138 with the randomness given: a (uniform, Ntt)
+        and the small error coefficients e; b = e - a s + m."""
+        m = pt.to_poly()
+        s = self.s_ntt(m.ctx)
+        a = Poly(m.ctx, np.array(a_ntt, dtype=np.uint64), NTT)
+        b = Poly.from_i64(m.ctx, np.asarray(e, dtype=np.int64)).into_ntt()
+        b -= a * s
+        b += m
+        return Ciphertext(self.par, [b, a], self.par.level_of_context(m.ctx))
+
     def decrypt(self, ct: Ciphertext) -> Plaintext:
         """secret_key.rs:200-280."""
         ctx = ct[0].ctx

@@ -71,3 +71,25 @@ def test_mul_plain(fg, ora, cuda, n, L):
         assert np.array_equal(got[b], want)
         assert list(s.decrypt(got[b], 0)) == s.product(vals[b], pv[b])
         assert list(s.decrypt(shared[b], 0)) == s.product(vals[b], pv[0])
+
+
+@pytest.mark.parametrize("n,L,t", [(16, 3, 1153), (4096, 3, 65537), (16384, 6, 65537)])
+def test_encrypt_matches_oracle(fg, ora, cuda, n, L, t):
+    """try_encrypt with the randomness given (secret_key.rs:102-138): the
+    device ciphertext equals the oracle's for the same a and e, and decrypts."""
+    s = Setup(fg, ora, n, L, t, seed=13 * n + L)
+    sk = fg.SecretKey(s.par, s.sk.coeffs)
+    for level in (0, L - 1):
+        ctx = s.par_o.context_at_level(level)
+        vals = s.rng.integers(0, t, (3, n), dtype=np.uint64)
+        a = np.stack([ora.Poly.random(ctx, ora.NTT, s.rng).coefficients for _ in range(3)])
+        e = np.stack([ora.sample_vec_cbd(n, s.par_o.variance, s.rng) for _ in range(3)]).astype(np.int64)
+        for enc in ("simd", "poly"):
+            got = fg.to_host(sk.encrypt(fg.to_device(vals), fg.to_device(a), fg.to_device(e.view(np.uint64)),
+                                        level, simd=enc == "simd"))
+            for b in range(3):
+                pt = ora.Plaintext.encode(vals[b], enc, s.par_o, level)
+                want = s.sk.encrypt_with(pt, a[b], e[b])
+                assert np.array_equal(got[b], want.to_array()), (level, enc, b)
+            dec = fg.to_host(sk.decrypt(fg.to_device(got), level, simd=enc == "simd"))
+            assert np.array_equal(dec, vals), (level, enc)
