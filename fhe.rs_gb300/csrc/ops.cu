@@ -420,14 +420,17 @@ struct RnsLaunch {
   uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
 };
 
-template <int MAXF, int MAXT>
+// EXACT: the source count is MAXF itself (a compile-time constant), so the
+// unrolled loops carry no predicated-off terms; used for the counts the
+// default multiplications produce (L and 2L + 1 source moduli).
+template <int MAXF, int MAXT, bool EXACT>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
                                                    PolyRef in, PolyRef out, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
   const uint32_t poly = (uint32_t)(gid >> logn);
-  const uint32_t F = s.from_len;
+  const uint32_t F = EXACT ? (uint32_t)MAXF : s.from_len;
   const uint64_t* src = in.at(poly, 0) + i;
   uint64_t r[MAXF];
 #pragma unroll
@@ -485,12 +488,12 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     }
   }
 
-  // scaler.rs:316-351. From 16 source moduli on, the output loop stays
+  // scaler.rs:316-351. Above 8 source moduli the output loop stays
   // rolled: unrolling it as well made the kernel body overflow the
   // instruction cache (ncu: a third of the stall cycles waiting for
   // instructions); its constants are then read with an indexed constant-bank
   // load per term. Smaller bodies run faster unrolled.
-  constexpr int kOutUnroll = MAXF >= 16 ? 1 : MAXT;
+  constexpr int kOutUnroll = MAXF > 8 ? 1 : MAXT;
   uint64_t* dst = out.at(poly, 0) + i;
 #pragma unroll kOutUnroll
   for (int o = 0; o < MAXT; o++) {
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   }
 }
 
-template <int MAXF, int MAXT>
+template <int MAXF, int MAXT, bool EXACT = false>
 void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
                       uint32_t out_len, uint64_t total, cudaStream_t st) {
   const RnsScalerHost& h = sc.host;
@@ -556,7 +559,7 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     PolyRef o = out;
     o.base += (uint64_t)first << logn;
     const unsigned threads = 128;
-    k_rns_scale<MAXF, MAXT><<<blocks_for(total, threads), threads, 0, st>>>(s, logn, in, o, total);
+    k_rns_scale<MAXF, MAXT, EXACT><<<blocks_for(total, threads), threads, 0, st>>>(s, logn, in, o, total);
     after_launch("k_rns_scale");
   }
 }
@@ -566,7 +569,15 @@ void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint
   const uint64_t total = polys << logn;
   if (total == 0 || out_len == 0) return;
   const size_t F = s.host.from_len;
-  if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
+  // Exact source counts of the default multiplications at L = 3, 6, 12
+  // (extension from L, scale-down from 2L + 1).
+  if (F == 6 && out_len <= 8) launch_rns_scale<6, 8, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F == 13 && out_len <= 8) launch_rns_scale<13, 8, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F == 3 && out_len <= 8) launch_rns_scale<3, 8, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F == 7 && out_len <= 8) launch_rns_scale<7, 8, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F == 12 && out_len <= 16) launch_rns_scale<12, 16, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F == 25 && out_len <= 16) launch_rns_scale<25, 16, true>(s, logn, in, out, start, out_len, total, st);
+  else if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
   else if (F <= 16 && out_len <= 8) launch_rns_scale<16, 8>(s, logn, in, out, start, out_len, total, st);
   else if (F <= 16) launch_rns_scale<16, 16>(s, logn, in, out, start, out_len, total, st);
   else if (F <= 32) launch_rns_scale<32, 16>(s, logn, in, out, start, out_len, total, st);
