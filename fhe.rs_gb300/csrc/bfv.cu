@@ -126,12 +126,17 @@ __global__ void k_tensor(const DevPrime* primes, SrcTensor t, PolyRef out, uint3
 
 // Digit i of c2 (power basis, mod q_i) lazily reduced modulo key limb j
 // (rq/mod.rs:525-528).
+// With `raw` set every digit modulus is below 4 q_j, so the digit already
+// lies in the forward NTT's input range [0, 4 q_j) and needs no reduction
+// (the transform is the same modulo q_j).
 struct SrcDigit {
   PolyRef digits;  // poly b * ndig + i -> row (b, i): stored as poly b, limb i
   uint32_t ndig;
+  uint32_t raw;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
     const uint32_t b = j.poly / ndig, d = j.poly % ndig;
-    return reduce64_lazy(digits.at(b, d)[i], pr);
+    const uint64_t x = digits.at(b, d)[i];
+    return raw ? x : reduce64_lazy(x, pr);
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     prefetch_l2(digits.at(j.poly / ndig, j.poly % ndig) + i);
@@ -186,38 +191,88 @@ struct DstKsF {
 // Key inner product for relinearization, rotations and the multiplication:
 // out_part[j] = add_part[j] + sum_d D[d][j] * key_part[d][j] (mod q_j), with
 // D and the keys canonical, so each product is below 2^124 and up to 15
-// products are summed exactly before a Barrett reduction.
+// products are summed exactly before a Barrett reduction. A thread handles
+// one residue of limb j for KB ciphertexts of the batch (each key residue is
+// then read once per KB ciphertexts).
+template <int KB>
 __global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const uint64_t* k1,
                           const uint64_t* add0, uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1,
                           uint64_t add1_stride, uint64_t* out, uint64_t out_stride, uint32_t ndig, uint32_t lk,
-                          uint32_t logn, uint64_t total) {
+                          uint32_t logn, uint64_t batch, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
   const uint64_t job = gid >> logn;
   const uint32_t j = job % lk;
-  const uint32_t b = job / lk;
+  const uint64_t b0 = (job / lk) * KB;
   const DevPrime pr = primes[j];
-  uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
-  if (add0) lo0 = add0[b * add0_stride + ((uint64_t)j << logn) + (add0_e ? gather_index(i, add0_e, logn) : i)];
-  if (add1) lo1 = add1[b * add1_stride + ((uint64_t)j << logn) + i];
+  uint64_t lo0[KB], hi0[KB], lo1[KB], hi1[KB];
+  const uint32_t gi = add0_e ? gather_index(i, add0_e, logn) : i;
+#pragma unroll
+  for (int u = 0; u < KB; u++) {
+    const uint64_t b = b0 + u;
+    lo0[u] = hi0[u] = lo1[u] = hi1[u] = 0;
+    if (b < batch) {
+      if (add0) lo0[u] = add0[b * add0_stride + ((uint64_t)j << logn) + gi];
+      if (add1) lo1[u] = add1[b * add1_stride + ((uint64_t)j << logn) + i];
+    }
+  }
   const uint64_t kstride = (uint64_t)lk << logn;
   const uint64_t* kp0 = k0 + ((uint64_t)j << logn) + i;
   const uint64_t* kp1 = k1 + ((uint64_t)j << logn) + i;
   for (uint32_t d = 0; d < ndig; d++) {
-    const uint64_t x = D.at(b * ndig + d, j)[i];
-    mac128(hi0, lo0, x, __ldg(kp0 + d * kstride));
-    mac128(hi1, lo1, x, __ldg(kp1 + d * kstride));
+    const uint64_t w0 = __ldg(kp0 + d * kstride), w1 = __ldg(kp1 + d * kstride);
+#pragma unroll
+    for (int u = 0; u < KB; u++) {
+      const uint64_t b = b0 + u;
+      if (b < batch) {
+        const uint64_t x = D.at(b * ndig + d, j)[i];
+        mac128(hi0[u], lo0[u], x, w0);
+        mac128(hi1[u], lo1[u], x, w1);
+      }
+    }
     if (d % 15 == 14) {
-      lo0 = reduce128(hi0, lo0, pr);
-      hi0 = 0;
-      lo1 = reduce128(hi1, lo1, pr);
-      hi1 = 0;
+#pragma unroll
+      for (int u = 0; u < KB; u++) {
+        lo0[u] = reduce128(hi0[u], lo0[u], pr);
+        hi0[u] = 0;
+        lo1[u] = reduce128(hi1[u], lo1[u], pr);
+        hi1[u] = 0;
+      }
     }
   }
-  uint64_t* o = out + b * out_stride + ((uint64_t)j << logn) + i;
-  o[0] = reduce128(hi0, lo0, pr);
-  o[kstride] = reduce128(hi1, lo1, pr);
+#pragma unroll
+  for (int u = 0; u < KB; u++) {
+    const uint64_t b = b0 + u;
+    if (b < batch) {
+      uint64_t* o = out + b * out_stride + ((uint64_t)j << logn) + i;
+      o[0] = reduce128(hi0[u], lo0[u], pr);
+      o[kstride] = reduce128(hi1[u], lo1[u], pr);
+    }
+  }
+}
+
+// Launches k_key_mac over `batch` ciphertexts, one per thread: sharing the
+// key loads among 4 ciphertexts per thread measured 60% slower on GB300 at 64
+// pairs (fewer threads left too little parallelism to cover the loads of D).
+void launch_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const uint64_t* k1, const uint64_t* add0,
+                    uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1, uint64_t add1_stride, uint64_t* out,
+                    uint64_t out_stride, uint32_t ndig, uint32_t lk, uint32_t logn, uint64_t batch, cudaStream_t st) {
+  if (batch == 0) return;
+  const uint64_t total = batch * lk << logn;
+  k_key_mac<1><<<nblocks(total, 256), 256, 0, st>>>(primes, D, k0, k1, add0, add0_stride, add0_e, add1, add1_stride,
+                                                    out, out_stride, ndig, lk, logn, batch, total);
+  after_launch("k_key_mac");
+}
+
+// Whether digits of `digit_moduli` can enter NTTs modulo `key_moduli`
+// unreduced: every digit is below four times every key modulus (moduli are
+// below 2^62, so 4 q does not overflow).
+static uint32_t digits_fit(const std::vector<uint64_t>& digit_moduli, const std::vector<uint64_t>& key_moduli) {
+  uint64_t dmax = 0, kmin = ~0ull;
+  for (uint64_t q : digit_moduli) dmax = std::max(dmax, q);
+  for (uint64_t q : key_moduli) kmin = std::min(kmin, q);
+  return dmax <= 4 * kmin ? 1u : 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -232,12 +287,10 @@ void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* ad
   PolyRef dref = plain_ref(D, Lk, logn);
   NttGeom g{kc.primes_dev(), (uint32_t)Lk, 0};
   // Every digit in every key modulus (rq/mod.rs:518-540), reduced output.
-  ntt_forward_any<true>(logn, g, batch * nd, SrcDigit{digits, (uint32_t)nd}, DstPoly{dref}, st);
-  const uint64_t total = batch * Lk << logn;
-  k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(kc.primes_dev(), dref, k.values(0), k.values(1), add0,
-                                                 add0_poly_stride, add0_exponent, add1, add1_poly_stride, out,
-                                                 out_poly_stride, (uint32_t)nd, (uint32_t)Lk, logn, total);
-  after_launch("k_key_mac");
+  ntt_forward_any<true>(logn, g, batch * nd,
+                        SrcDigit{digits, (uint32_t)nd, digits_fit(k.ctx_ct->moduli, kc.moduli)}, DstPoly{dref}, st);
+  launch_key_mac(kc.primes_dev(), dref, k.values(0), k.values(1), add0, add0_poly_stride, add0_exponent, add1,
+                 add1_poly_stride, out, out_poly_stride, (uint32_t)nd, (uint32_t)Lk, logn, batch, st);
 }
 
 static void require_same_level_key(const Ksk& k) {
@@ -650,16 +703,14 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
       ntt_fwd_single<true>(logn, gk, count * L + 2 * count, SrcKsF{c2, c01, (uint32_t)L, ndp},
                            DstKsF{dref, oref, ndp}, st);
     } else {
-      ntt_forward_any<true>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L}, DstPoly{dref}, st, bf);
+      ntt_forward_any<true>(logn, gk, count * L, SrcDigit{c2, (uint32_t)L, digits_fit(bc.moduli, kc.moduli)},
+                            DstPoly{dref}, st, bf);
       ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st, bf);
     }
     mark(6);
     // G: key inner product added to c0, c1 in place.
-    const uint64_t total = count * L << logn;
-    k_key_mac<<<nblocks(total, 256), 256, 0, st>>>(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest,
-                                                   2 * L * N, 0, dest + L * N, 2 * L * N, dest, 2 * L * N,
-                                                   (uint32_t)L, (uint32_t)Lk, logn, total);
-    after_launch("k_key_mac");
+    launch_key_mac(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest, 2 * L * N, 0, dest + L * N,
+                   2 * L * N, dest, 2 * L * N, (uint32_t)L, (uint32_t)Lk, logn, count, st);
   } else {
     PolyRef o = plain_ref(dest, L, logn);
     ntt_forward_any<true>(logn, gb, 3 * count, SrcPoly{dnref}, DstPoly{o}, st);
