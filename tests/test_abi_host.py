@@ -120,3 +120,25 @@ def test_no_device_fails_loudly(fg):
     ptr = ctypes.c_void_p()
     assert fg.lib().fheg_device_alloc(1 << 20, ctypes.byref(ptr)) == fg.ERR_CUDA
     fg.ntt_prefetch_set(False)  # host-only settings still work
+
+
+def test_c_client_compiles_and_links(fg, tmp_path):
+    """include/fheg.h is valid C99 (what a cgo / bindgen / ctypes binding
+    parses) and a C program links against libfheg.so and calls it."""
+    import os
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib_dir = os.path.dirname(fg.build())
+    exe = str(tmp_path / "abi_client")
+    cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(root, "include"),
+           os.path.join(root, "tests", "c", "abi_client.c"), "-L", lib_dir, "-lfheg", "-Wl,-rpath," + lib_dir,
+           "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("ok 4611686018427322369")
