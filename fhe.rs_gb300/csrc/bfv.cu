@@ -41,11 +41,17 @@ const std::shared_ptr<Context>& Params::ctx(size_t level) const {
 
 // Four operands of a pair (lhs0, lhs1, rhs0, rhs1) as polynomials 4b .. 4b+3.
 struct SrcPair {
+  static constexpr bool kRowStaged = true;
   PolyRef lhs, rhs;  // [B][2][L][N]
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     const uint32_t b = j.poly >> 2, w = j.poly & 3;
     return w < 2 ? lhs.at(2 * b + w, j.limb)[i] : rhs.at(2 * b + w - 2, j.limb)[i];
   }
+  __device__ __forceinline__ const uint64_t* row_ptr(const NttJob& j) const {
+    const uint32_t b = j.poly >> 2, w = j.poly & 3;
+    return w < 2 ? lhs.at(2 * b + w, j.limb) : rhs.at(2 * b + w - 2, j.limb);
+  }
+  __device__ __forceinline__ uint64_t xform(const NttJob&, const DevPrime&, uint64_t v) const { return v; }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     const uint32_t b = j.poly >> 2, w = j.poly & 3;
     prefetch_l2(w < 2 ? lhs.at(2 * b + w, j.limb) + i : rhs.at(2 * b + w - 2, j.limb) + i);
@@ -59,6 +65,7 @@ struct SrcPair {
 // so its output is the canonical INTT of the exact products.
 struct SrcTensor {
   static constexpr bool kMontgomery = true;
+  static constexpr bool kStaged = true;
   PolyRef lhs, rhs;  // inputs [B][2][L][N], Ntt
   PolyRef ext;       // [B][4][M][N], Ntt (limbs >= ncm of each operand)
   uint32_t ncm_l, ncm_r;
@@ -69,6 +76,46 @@ struct SrcTensor {
   }
   __device__ __forceinline__ uint64_t op(uint32_t b, uint32_t w, uint32_t limb, uint32_t i) const {
     return row(b, w, limb)[i];
+  }
+  // Staged load for the inverse NTT (k_ntt_inv): the operand rows stream
+  // into shared memory with asynchronous copies, half a block at a time (the
+  // two operands of a product fill the buffer), so every load of the phase is
+  // in flight at once instead of what the registers can hold; the products of
+  // the cross term are Montgomery-reduced separately and added (both carry
+  // the factor 2^-64).
+  template <int LOGN, int T, int E>
+  __device__ __forceinline__ void stage(const NttJob& j, const DevPrime& pr, uint32_t base, uint64_t* sm,
+                                        uint32_t tid, uint64_t* x) const {
+    constexpr uint32_t HALF = 1u << (LOGN - 1);
+    const uint32_t b = j.poly / 3, part = j.poly % 3;
+    const int npairs = part == 1 ? 2 : 1;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        if (q < npairs) {
+          // part 0: l0 r0; part 2: l1 r1; part 1: l0 r1 + l1 r0.
+          const uint32_t wa = part == 0 ? 0 : (part == 2 ? 1 : (uint32_t)q);
+          const uint32_t wb = part == 0 ? 2 : (part == 2 ? 3 : (q == 0 ? 3u : 2u));
+          const uint64_t* ra = row(b, wa, j.limb) + base + h * HALF;
+          const uint64_t* rb = row(b, wb, j.limb) + base + h * HALF;
+          for (uint32_t c = tid; c < HALF / 2; c += T) {
+            cp_async16(sm + 2 * c, ra + 2 * c);
+            cp_async16(sm + HALF + 2 * c, rb + 2 * c);
+          }
+          cp_async_wait_all();
+          __syncthreads();
+#pragma unroll
+          for (int e = 0; e < E / 2; e++) {
+            const uint32_t idx = tid + e * T;
+            const uint64_t u = sm[idx], v = sm[HALF + idx];
+            const uint64_t m = mont_reduce(__umul64hi(u, v), u * v, pr);
+            x[h * (E / 2) + e] = q == 0 ? m : csub(x[h * (E / 2) + e] + m, pr.p2);
+          }
+          __syncthreads();
+        }
+      }
+    }
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     const uint32_t b = j.poly / 3, part = j.poly % 3;
@@ -130,6 +177,7 @@ __global__ void k_tensor(const DevPrime* primes, SrcTensor t, PolyRef out, uint3
 // lies in the forward NTT's input range [0, 4 q_j) and needs no reduction
 // (the transform is the same modulo q_j).
 struct SrcDigit {
+  static constexpr bool kRowStaged = true;
   PolyRef digits;  // poly b * ndig + i -> row (b, i): stored as poly b, limb i
   uint32_t ndig;
   uint32_t raw;
@@ -137,6 +185,12 @@ struct SrcDigit {
     const uint32_t b = j.poly / ndig, d = j.poly % ndig;
     const uint64_t x = digits.at(b, d)[i];
     return raw ? x : reduce64_lazy(x, pr);
+  }
+  __device__ __forceinline__ const uint64_t* row_ptr(const NttJob& j) const {
+    return digits.at(j.poly / ndig, j.poly % ndig);
+  }
+  __device__ __forceinline__ uint64_t xform(const NttJob&, const DevPrime& pr, uint64_t v) const {
+    return raw ? v : reduce64_lazy(v, pr);
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     prefetch_l2(digits.at(j.poly / ndig, j.poly % ndig) + i);

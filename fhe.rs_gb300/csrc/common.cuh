@@ -244,6 +244,17 @@ __device__ __forceinline__ uint64_t mul_mod(uint64_t a, uint64_t b, const DevPri
   return reduce128(__umul64hi(a, b), a * b, pr);
 }
 
+// Asynchronous 16-byte copy global -> shared (no register round trip); the
+// copies of a thread complete at cp_async_wait_all (a hardware wait, no
+// spinning).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Montgomery reduction of the 128-bit value hi:lo < p * 2^64: returns
 // hi:lo * 2^-64 mod p in [0, 2p). With m = lo * (-p^-1) mod 2^64 the sum
 // hi:lo + m * p is a multiple of 2^64 whose low word carries exactly when
