@@ -41,17 +41,11 @@ const std::shared_ptr<Context>& Params::ctx(size_t level) const {
 
 // Four operands of a pair (lhs0, lhs1, rhs0, rhs1) as polynomials 4b .. 4b+3.
 struct SrcPair {
-  static constexpr bool kRowStaged = true;
   PolyRef lhs, rhs;  // [B][2][L][N]
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     const uint32_t b = j.poly >> 2, w = j.poly & 3;
     return w < 2 ? lhs.at(2 * b + w, j.limb)[i] : rhs.at(2 * b + w - 2, j.limb)[i];
   }
-  __device__ __forceinline__ const uint64_t* row_ptr(const NttJob& j) const {
-    const uint32_t b = j.poly >> 2, w = j.poly & 3;
-    return w < 2 ? lhs.at(2 * b + w, j.limb) : rhs.at(2 * b + w - 2, j.limb);
-  }
-  __device__ __forceinline__ uint64_t xform(const NttJob&, const DevPrime&, uint64_t v) const { return v; }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     const uint32_t b = j.poly >> 2, w = j.poly & 3;
     prefetch_l2(w < 2 ? lhs.at(2 * b + w, j.limb) + i : rhs.at(2 * b + w - 2, j.limb) + i);
@@ -177,7 +171,6 @@ __global__ void k_tensor(const DevPrime* primes, SrcTensor t, PolyRef out, uint3
 // lies in the forward NTT's input range [0, 4 q_j) and needs no reduction
 // (the transform is the same modulo q_j).
 struct SrcDigit {
-  static constexpr bool kRowStaged = true;
   PolyRef digits;  // poly b * ndig + i -> row (b, i): stored as poly b, limb i
   uint32_t ndig;
   uint32_t raw;
@@ -186,12 +179,7 @@ struct SrcDigit {
     const uint64_t x = digits.at(b, d)[i];
     return raw ? x : reduce64_lazy(x, pr);
   }
-  __device__ __forceinline__ const uint64_t* row_ptr(const NttJob& j) const {
-    return digits.at(j.poly / ndig, j.poly % ndig);
-  }
-  __device__ __forceinline__ uint64_t xform(const NttJob&, const DevPrime& pr, uint64_t v) const {
-    return raw ? v : reduce64_lazy(v, pr);
-  }
+
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     prefetch_l2(digits.at(j.poly / ndig, j.poly % ndig) + i);
   }

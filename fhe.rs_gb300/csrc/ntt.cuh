@@ -68,19 +68,6 @@ constexpr bool src_is_staged(long) {
   return false;
 }
 
-// Single-row sources (element i of a job is xform(row[i])) declare
-// kRowStaged = true with row_ptr(job) and xform(job, prime, v); the block
-// kernels then stream the row into shared memory with asynchronous copies
-// (every load of the phase in flight at once) when it is 16-byte aligned.
-template <class S>
-constexpr auto src_is_row_staged(int) -> decltype(S::kRowStaged) {
-  return S::kRowStaged;
-}
-template <class S>
-constexpr bool src_is_row_staged(long) {
-  return false;
-}
-
 // Sources whose values are Montgomery products declare kMontgomery = true.
 template <class S>
 constexpr auto src_is_montgomery(int) -> decltype(S::kMontgomery) {
@@ -108,22 +95,6 @@ __device__ __forceinline__ auto src_prefetch(const S& s, const NttJob& j, uint32
 template <class S>
 __device__ __forceinline__ void src_prefetch(const S&, const NttJob&, uint32_t, long) {}
 
-// Fills x[e] with element base + tid + e * T of a row-staged source through
-// the shared buffer; returns false (nothing done) if the row is not 16-byte
-// aligned. Ends with the buffer free.
-template <int LOGN, int T, int E, class Src>
-__device__ __forceinline__ bool stage_row(const Src& src, const NttJob& jb, const DevPrime& pr, uint32_t base,
-                                          uint64_t* sm, uint32_t tid, uint64_t* x) {
-  const uint64_t* r = src.row_ptr(jb) + base;
-  if ((reinterpret_cast<uintptr_t>(r) & 15) != 0) return false;
-  for (uint32_t c = tid; c < (1u << LOGN) / 2; c += T) cp_async16(sm + 2 * c, r + 2 * c);
-  cp_async_wait_all();
-  __syncthreads();
-#pragma unroll
-  for (int e = 0; e < E; e++) x[e] = src.xform(jb, pr, sm[tid + e * T]);
-  __syncthreads();
-  return true;
-}
 
 
 __device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
@@ -282,12 +253,8 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
   prefetch_next<LOGN, T>(g, src, tid);
   uint64_t x[E];
   // Round 0 holds elements tid + e*T: coalesced loads.
-  bool staged = false;
-  if constexpr (src_is_row_staged<Src>(0)) staged = stage_row<LOGN, T, E>(src, jb, pr, base, sm, tid, x);
-  if (!staged) {
 #pragma unroll
-    for (int e = 0; e < E; e++) x[e] = src(jb, pr, base + tid + e * T);
-  }
+  for (int e = 0; e < E; e++) x[e] = src(jb, pr, base + tid + e * T);
   fwd_rounds<LOGN, 0>(x, sm, tid, pr, (1u << g.s1) + jb.beta);
 #pragma unroll
   for (int e = 0; e < E; e++) {
@@ -390,14 +357,10 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
   prefetch_next<LOGN, T>(g, src, tid);
   uint64_t x[E];
   // Coalesced loads, then regroup through shared memory for the first round.
-  bool staged = false;
+  // (Staging a single row the same way measured slower: the extra shared-
+  // memory round trip costs more than the load latency it hides.)
   if constexpr (src_is_staged<Src>(0)) {
     src.template stage<LOGN, T, E>(jb, pr, base, sm, tid, x);
-    staged = true;
-  } else if constexpr (src_is_row_staged<Src>(0)) {
-    staged = stage_row<LOGN, T, E>(src, jb, pr, base, sm, tid, x);
-  }
-  if (staged) {
 #pragma unroll
     for (int e = 0; e < E; e++) sm[swz(tid + e * T)] = x[e];
   } else {
@@ -540,13 +503,10 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
 // Basic source / destination functors.
 
 struct SrcPoly {
-  static constexpr bool kRowStaged = true;
   PolyRef r;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return r.at(j.poly, j.limb)[i];
   }
-  __device__ __forceinline__ const uint64_t* row_ptr(const NttJob& j) const { return r.at(j.poly, j.limb); }
-  __device__ __forceinline__ uint64_t xform(const NttJob&, const DevPrime&, uint64_t v) const { return v; }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(r.at(j.poly, j.limb) + i); }
 };
 
