@@ -83,6 +83,8 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.first = 0  # index of the first sample taken once the region started
+        self._got = threading.Event()
 
     def __enter__(self):
         try:
@@ -91,6 +93,10 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            # nvidia-smi takes a few hundred ms to start: wait (bounded) for
+            # its first sample so that short timed regions are covered.
+            self._got.wait(timeout=3.0)
+            self.first = len(self.lines)
         except Exception:
             self.proc = None
         return self
@@ -98,9 +104,15 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self._got.set()
 
     def __exit__(self, *a):
         if self.proc is not None:
+            # A region shorter than the sampling period still gets the sample
+            # that follows it (at most one period later).
+            deadline = time.time() + 0.5
+            while len(self.lines) <= self.first and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -110,7 +122,9 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        for ln in self.lines[self.first:] or self.lines[-1:]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -123,7 +137,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi sample"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 

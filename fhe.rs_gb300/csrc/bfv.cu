@@ -192,12 +192,38 @@ __device__ __forceinline__ uint32_t gather_index(uint32_t i, uint64_t e, uint32_
   return brev_n((uint32_t)((((e - 1) >> 1) + (uint64_t)brev_n(i, logn) * e) & mask), logn);
 }
 
+// Staged gather: when the block is the whole row (single-pass transforms),
+// the row streams into shared memory with asynchronous copies and the
+// permutation reads it there instead of scattering 8-byte reads over DRAM;
+// otherwise the elements are gathered from global memory.
+template <int LOGN, int T, int E>
+__device__ __forceinline__ void stage_gather(const uint64_t* row, uint64_t e, uint32_t logn, uint32_t base,
+                                             uint64_t* sm, uint32_t tid, uint64_t* x) {
+  if (logn != (uint32_t)LOGN || (reinterpret_cast<uintptr_t>(row) & 15) != 0) {
+#pragma unroll
+    for (int k = 0; k < E; k++) x[k] = row[gather_index(base + tid + k * T, e, logn)];
+    return;
+  }
+  for (uint32_t c = tid; c < (1u << LOGN) / 2; c += T) cp_async16(sm + 2 * c, row + 2 * c);
+  cp_async_wait_all();
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < E; k++) x[k] = sm[gather_index(tid + k * T, e, logn)];
+  __syncthreads();
+}
+
 struct SrcSubst {
+  static constexpr bool kStaged = true;
   PolyRef in;
   uint64_t e;
   uint32_t logn;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     return in.at(j.poly, j.limb)[gather_index(i, e, logn)];
+  }
+  template <int LOGN, int T, int E>
+  __device__ __forceinline__ void stage(const NttJob& j, const DevPrime&, uint32_t base, uint64_t* sm, uint32_t tid,
+                                        uint64_t* x) const {
+    stage_gather<LOGN, T, E>(in.at(j.poly, j.limb), e, logn, base, sm, tid, x);
   }
   // The gather reads the whole row: hint its lines in order.
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const { prefetch_l2(in.at(j.poly, j.limb) + i); }
@@ -412,11 +438,18 @@ struct RotDesc {
 
 // R1: substituted c1, gathered into the inverse NTT (jobs: poly = b, limb = i).
 struct SrcRotSubst {
+  static constexpr bool kStaged = true;
   const RotDesc* d;
   uint32_t logn;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
     const RotDesc& r = d[j.poly];
     return r.ct[((uint64_t)(r.L + j.limb) << logn) + gather_index(i, r.e, logn)];
+  }
+  template <int LOGN, int T, int E>
+  __device__ __forceinline__ void stage(const NttJob& j, const DevPrime&, uint32_t base, uint64_t* sm, uint32_t tid,
+                                        uint64_t* x) const {
+    const RotDesc& r = d[j.poly];
+    stage_gather<LOGN, T, E>(r.ct + ((uint64_t)(r.L + j.limb) << logn), r.e, logn, base, sm, tid, x);
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     const RotDesc& r = d[j.poly];
