@@ -511,7 +511,8 @@ def run_codec(args):
 def run_compose(args):
     """Compositions at N = 2^14, L = 6: inner sum of 16 ciphertexts (13 column
     rotations and the row rotation each), oblivious expansion of one
-    ciphertext into 64, and 4 dot products over 64 ciphertext-plaintext pairs."""
+    ciphertext into 64, 4 dot products over 64 ciphertext-plaintext pairs, and
+    the RGSW external product of 16 ciphertexts."""
     import torch
 
     import __graft_entry__ as ge
@@ -553,6 +554,13 @@ def run_compose(args):
     want = ek.expands(cts[0], 4)
     if not all(np.array_equal(got[i], want[i].to_array()) for i in range(4)):
         raise SystemExit("bench: expansion is not bit-exact with the oracle")
+    # RGSW external product (rgsw_ciphertext.rs:123-153) of the 16 ciphertexts.
+    rg_o = ora.RGSWCiphertext(sk, ora.Plaintext.encode(rng.integers(0, T, N, dtype=np.uint64), "simd", par_o), rng)
+    rg = fg.RGSWCiphertext(par, rg_o.ksk0.c0_array(), rg_o.ksk0.c1_array(), rg_o.ksk1.c0_array(),
+                           rg_o.ksk1.c1_array())
+    if not np.array_equal(fg.to_host(rg.external_product(arr[:1]))[0], rg_o.external_product(cts[0]).to_array()):
+        raise SystemExit("bench: external product is not bit-exact with the oracle")
+    ext_out = torch.empty_like(arr)
     groups, count = 4, 64
     db = fg.plaintext_encode(par, 0, fg.to_device(rng.integers(0, T, (count, N), dtype=np.uint64)))
     q = arr[torch.arange(groups * count, device=arr.device) % 16].reshape(groups, count, 2, L, N).contiguous()
@@ -574,15 +582,18 @@ def run_compose(args):
         sum_ms = timed(lambda: fg.inner_sum(par, sum_k, arr))
         exp_ms = timed(lambda: fg.expand(par, exp_k, arr[0], 64))
         dot_ms = timed(lambda: fg.dot_product_scalar(par, 0, q, db))
+        ext_ms = timed(lambda: rg.external_product(arr, out=ext_out))
     launches = fg.kernel_launch_count() - launches0
-    line = {"metric": "BFV compositions N=2^14 L=6 (inner sum, expansion, dot product)",
+    line = {"metric": "BFV compositions N=2^14 L=6 (inner sum, expansion, dot product, RGSW product)",
             "value": 16 / (sum_ms / 1000.0), "unit": "inner sums/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sum_ms + exp_ms + dot_ms, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": sum_ms + exp_ms + dot_ms + ext_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
             "config": {"workload": "compose", "degree": N, "moduli": L, "inner_sum_batch": 16,
-                       "expansion_size": 64, "dot_products": groups, "dot_product_terms": count},
+                       "expansion_size": 64, "dot_products": groups, "dot_product_terms": count,
+                       "external_products": 16},
             "inner_sum_ms": sum_ms, "expansion_64_ms": exp_ms, "dot_products_ms": dot_ms,
+            "external_products_16_ms": ext_ms, "external_products_per_s": 16 / (ext_ms / 1000.0),
             "rotations_per_s": 16 * len(sum_exps) / (sum_ms / 1000.0),
             "gpu_launches": int(launches), "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)

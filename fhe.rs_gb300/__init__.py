@@ -109,6 +109,9 @@ def _declare(L):
         "fheg_ksk_destroy": (None, [c_vp]),
         "fheg_relinearize": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize": (i, [c_vp, c_size, c_vp, c_vp, c_size, c_vp]),
+        "fheg_rgsw_create": (i, [c_vp, c_size, P_u64, P_u64, P_u64, P_u64, ctypes.POINTER(c_vp)]),
+        "fheg_rgsw_destroy": (None, [c_vp]),
+        "fheg_external_product": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_ciphertext_switch_down": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_ciphertext_add": (i, [c_vp, c_size, c_size, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_multiplicator_create_default": (i, [c_vp, ctypes.POINTER(c_vp)]),
@@ -554,6 +557,43 @@ class GaloisKey(KeySwitchingKey):
         out = empty((count, 2, ctx.L, ctx.degree), ct.device)
         check(lib().fheg_galois_relinearize(self._h, self.exponent, _dp(ct), _dp(out), count, _stream()))
         return out
+
+
+class RGSWCiphertext:
+    """RGSWCiphertext (fhe/src/bfv/rgsw_ciphertext.rs:19-24) resident on the
+    device, from its two key-switching keys' c0 / c1 polynomials ([L][L][N],
+    Ntt values) at `level`."""
+
+    def __init__(self, par: BfvParameters, ksk0_c0, ksk0_c1, ksk1_c0, ksk1_c1, level: int = 0):
+        self.par, self.level = par, level
+        arrs = [_u64(a) for a in (ksk0_c0, ksk0_c1, ksk1_c0, ksk1_c1)]
+        ctx = par.context_at_level(level) if level <= par.max_level() else None
+        if ctx is not None:
+            for a in arrs:
+                if a.shape != (ctx.L, ctx.L, par.degree):
+                    raise FhegError(ERR_INVALID_ARGUMENT, f"key polynomials must be [{ctx.L}][{ctx.L}][{par.degree}]")
+        h = c_vp()
+        check(lib().fheg_rgsw_create(par._h, level, *[_ptr(a) for a in arrs], ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fheg_rgsw_destroy(self._h)
+            self._h = None
+
+    def external_product(self, ct, out=None):
+        """ct x RGSW (rgsw_ciphertext.rs:123-160) on a batch [count][2][L][N]."""
+        ctx = self.par.context_at_level(self.level)
+        if ct.dim() != 4 or ct.shape[1] != 2:
+            raise FhegError(ERR_WRONG_PARTS, "Ciphertext must have two parts")
+        if tuple(ct.shape[2:]) != (ctx.L, ctx.degree):
+            raise FhegError(ERR_INVALID_LEVEL, "Ciphertext and RGSWCiphertext must have the same level")
+        if out is None:
+            out = empty(tuple(ct.shape), ct.device)
+        check(lib().fheg_external_product(self._h, _dp(ct), _dp(out), ct.shape[0], _stream()))
+        return out
+
+    __mul__ = external_product  # Mul<&Ciphertext> for &RGSWCiphertext (rgsw_ciphertext.rs:155-160)
 
 
 class EvaluationKey:

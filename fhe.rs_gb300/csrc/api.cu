@@ -598,6 +598,47 @@ FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const 
   });
 }
 
+FHEG_API int fheg_rgsw_create(const fheg_params* par, size_t level, const uint64_t* h_ksk0_c0,
+                              const uint64_t* h_ksk0_c1, const uint64_t* h_ksk1_c0, const uint64_t* h_ksk1_c1,
+                              fheg_rgsw** out) {
+  return guard([&] {
+    need(par && h_ksk0_c0 && h_ksk0_c1 && h_ksk1_c0 && h_ksk1_c1 && out, "null input");
+    const Params& p = *par->p;
+    if (level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    auto h = new fheg_rgsw();
+    try {
+      Ksk& k = h->k;
+      k.par = &p;
+      k.ciphertext_level = k.ksk_level = level;
+      k.ctx_ct = k.ctx_ksk = p.ctx(level);
+      const size_t L = k.ctx_ct->L();
+      if (L < 2) throw Error(FHEG_ERR_UNSUPPORTED, "These parameters do not support key switching");
+      k.count = 2 * L;
+      // [part][digit][L][N]: digits 0..L-1 from ksk0, L..2L-1 from ksk1.
+      const size_t words = L * L * k.ctx_ct->N();
+      k.keys.alloc(4 * words * 8);
+      upload(k.values(0), h_ksk0_c0, words * 8);
+      upload(k.values(0) + words, h_ksk1_c0, words * 8);
+      upload(k.values(1), h_ksk0_c1, words * 8);
+      upload(k.values(1) + words, h_ksk1_c1, words * 8);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API void fheg_rgsw_destroy(fheg_rgsw* rgsw) { delete rgsw; }
+
+FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, uint64_t* d_out, size_t count,
+                                   void* stream) {
+  return guard([&] {
+    need(rgsw && ((d_ct && d_out) || !count), "null input");
+    external_product(rgsw->k, d_ct, d_out, count, rgsw->k.ws, as_stream(stream));
+  });
+}
+
 FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
                                            const size_t* exponents, const uint64_t* const* d_cts,
                                            uint64_t* const* d_outs, size_t count, void* stream) {

@@ -419,6 +419,28 @@ void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, ui
   key_switch(gk, dst, count, ct, 2 * L * N, e, nullptr, 0, out, 2 * L * N, D, st);
 }
 
+// Mul<&RGSWCiphertext> for &Ciphertext (rgsw_ciphertext.rs:123-153): the
+// reference key-switches ct0 with ksk0 and ct1 with ksk1 and adds the two
+// results. `rgsw` holds both keys as one key of 2L digits per part (ksk0's
+// digits, then ksk1's), so the two key switches and their sum are one
+// digit NTT launch and one key inner product over the 2L rows of
+// (ct0, ct1) in the power basis.
+void external_product(const Ksk& rgsw, const uint64_t* ct, uint64_t* out, uint64_t count, Workspace& ws,
+                      cudaStream_t st) {
+  const Context& c = *rgsw.ctx_ct;
+  const size_t L = c.L(), N = c.N(), Lk = rgsw.ctx_ksk->L();
+  if (rgsw.count != 2 * L || Lk != L) throw Error(FHEG_ERR_INTERNAL, "malformed RGSW key");
+  if (count == 0) return;
+  ws.reserve((count * 2 * L * N + count * 2 * L * Lk * N + 64) * 8);
+  size_t off = 0;
+  uint64_t* digits = ws.take(count * 2 * L * N, &off);
+  uint64_t* D = ws.take(count * 2 * L * Lk * N, &off);
+  // rgsw_ciphertext.rs:137-138: both parts into the power basis.
+  ntt_backward(c, plain_ref(const_cast<uint64_t*>(ct), L, c.logn), plain_ref(digits, L, c.logn), 2 * count, st);
+  // rgsw_ciphertext.rs:140-152: digit i < L is row i of ct0, digit L + i row i of ct1.
+  key_switch(rgsw, plain_ref(digits, 2 * L, c.logn), count, nullptr, 0, 0, nullptr, 0, out, 2 * L * N, D, st);
+}
+
 // ---------------------------------------------------------------------------
 // Ragged rotation batch: GaloisKey::relinearize_into (galois_key.rs:90-124)
 // for ciphertexts at different levels, each with its own key and exponent,

@@ -22,6 +22,9 @@ struct fheg_params {
 struct fheg_ksk {
   fheg::Ksk k;
 };
+struct fheg_rgsw {
+  fheg::Ksk k;  // count = 2L digits: ksk0's, then ksk1's
+};
 struct fheg_multiplicator {
   static constexpr int kPipe = 3;  // streams of the host entry point's copy / compute pipeline
   std::unique_ptr<fheg::Multiplicator> m;

@@ -236,6 +236,10 @@ void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint
                          uint64_t* D, cudaStream_t st);
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st);
+// External product with an RGSW ciphertext held as one key of 2L digits per
+// part (ksk0's digits, then ksk1's): ct [count][2][L][N] -> out, both Ntt.
+void external_product(const Ksk& rgsw, const uint64_t* ct, uint64_t* out, uint64_t count, Workspace& ws,
+                      cudaStream_t st);
 // One rotation of a ragged batch: ciphertext `ct` ([2][L][N] at the key's
 // ciphertext level) rotated by `exponent` with `key`, into `out`.
 struct RotRequest {

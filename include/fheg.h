@@ -404,6 +404,25 @@ FHEG_API int fheg_inner_sum(const fheg_params* par, const fheg_ksk* const* keys,
 FHEG_API int fheg_expand(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
                          size_t nlevels, size_t size, const uint64_t* d_ct, uint64_t* d_out, void* stream);
 
+/* RGSWCiphertext (fhe/src/bfv/rgsw_ciphertext.rs:19-24): the key-switching
+ * keys ksk0 (of m) and ksk1 (of m s), both with ciphertext level = key level
+ * = `level` (the reference rejects other levels, rgsw_ciphertext.rs:59-68).
+ * h_ksk0_c0 .. h_ksk1_c1 are the keys' c0[i] / c1[i] polynomials as
+ * [L][L][N] host arrays (Ntt values, canonical), L = moduli at `level`. */
+typedef struct fheg_rgsw fheg_rgsw;
+FHEG_API int fheg_rgsw_create(const fheg_params* par, size_t level, const uint64_t* h_ksk0_c0,
+                              const uint64_t* h_ksk0_c1, const uint64_t* h_ksk1_c0, const uint64_t* h_ksk1_c1,
+                              fheg_rgsw** out);
+FHEG_API void fheg_rgsw_destroy(fheg_rgsw* rgsw);
+
+/* Mul<&RGSWCiphertext> for &Ciphertext (rgsw_ciphertext.rs:123-160; the
+ * product is commutative): the external product of every ciphertext of
+ * d_ct [count][2][L][N] (Ntt, at the RGSW ciphertext's level) -> d_out
+ * [count][2][L][N] (Ntt). Calls on the same RGSW ciphertext must not overlap
+ * (shared scratch). */
+FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, uint64_t* d_out, size_t count,
+                                   void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */
 

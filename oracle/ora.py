@@ -1364,6 +1364,35 @@ class GaloisKey:
         return Ciphertext(ct.par, [out0, out1], self.ksk.ciphertext_level)
 
 
+class RGSWCiphertext:
+    """bfv/rgsw_ciphertext.rs:19-160: the key-switching keys of m and of m s,
+    m the plaintext's Ntt polynomial (`poly_ntt`, plaintext_vec.rs:76) in the
+    power basis, both at the plaintext's level."""
+
+    def __init__(self, sk: SecretKey, pt: Plaintext, rng: np.random.Generator):
+        # rgsw_ciphertext.rs:101-121 (SecretKey::try_encrypt).
+        level = pt.level
+        ctx = sk.par.context_at_level(level)
+        m_ntt = Poly.from_u64(ctx, pt.value).into_ntt()
+        m = m_ntt.copy().into_power_basis()
+        m_s = Poly.from_i64(ctx, sk.coeffs).into_ntt()
+        m_s.mul_assign(m_ntt)
+        m_s.into_power_basis()
+        self.par, self.level = sk.par, level
+        self.ksk0 = KeySwitchingKey(sk, m, level, level, rng)
+        self.ksk1 = KeySwitchingKey(sk, m_s, level, level, rng)
+
+    def external_product(self, ct: Ciphertext) -> Ciphertext:
+        """rgsw_ciphertext.rs:123-153 (`&ct * &rgsw`)."""
+        assert ct.level == self.level, "Ciphertext and RGSWCiphertext must have the same level"
+        assert len(ct) == 2, "Ciphertext must have two parts"
+        ct0 = ct[0].copy().into_power_basis()
+        ct1 = ct[1].copy().into_power_basis()
+        c0, c1 = self.ksk0.key_switch(ct0)
+        c0p, c1p = self.ksk1.key_switch(ct1)
+        return Ciphertext(self.par, [c0 + c0p, c1 + c1p], self.level)
+
+
 def rotation_exponent(par: BfvParameters, i: int) -> int:
     """evaluation_key.rs:195-204: column rotation by i uses exponent 3^i mod 2N."""
     return pow(3, i, 2 * par.degree)

@@ -228,6 +228,24 @@ def test_multiplicator_decrypts(ora, L):
         assert list(sk.decrypt(ct3).decode("simd")) == list(expected)
 
 
+@pytest.mark.parametrize("L", [2, 8])
+def test_rgsw_external_product_decrypts(ora, L):
+    """rgsw_ciphertext.rs:172-210 (default_arc(2, 16) and (8, 16)): ct1 x
+    RGSW(pt2) decrypts to the same plaintext as the 3-part product ct1 * ct2."""
+    rng = np.random.default_rng(300 + L)
+    par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * L)
+    sk = ora.SecretKey.random(par, rng)
+    v1 = rng.integers(0, 1153, 16, dtype=np.uint64)
+    v2 = rng.integers(0, 1153, 16, dtype=np.uint64)
+    pt1, pt2 = ora.Plaintext.encode(v1, "simd", par), ora.Plaintext.encode(v2, "simd", par)
+    ct1, ct2 = sk.encrypt(pt1, rng), sk.encrypt(pt2, rng)
+    rgsw = ora.RGSWCiphertext(sk, pt2, rng)
+    expected = sk.decrypt(ct1 * ct2).decode("simd")
+    assert list(expected) == [int(a) * int(b) % 1153 for a, b in zip(v1, v2)]
+    ct3 = rgsw.external_product(ct1)
+    assert np.array_equal(sk.decrypt(ct3).decode("simd"), expected)
+
+
 def test_rotations_decrypt(ora):
     """evaluation_key.rs:572-675: row and column rotations."""
     rng = np.random.default_rng(7)
