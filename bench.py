@@ -445,8 +445,9 @@ def run_stages(args):
 
 def run_codec(args):
     """Plaintext side at N = 2^14, L = 6, 64 vectors: SIMD encoding into the
-    plaintext's Ntt polynomial, ciphertext x plaintext, and decryption with
-    SIMD decoding, each a batched call on device-resident data."""
+    plaintext's Ntt polynomial, ciphertext x plaintext, decryption with SIMD
+    decoding, and the expansion of seeded c1 polynomials, each a batched call
+    on device-resident data."""
     import torch
 
     import __graft_entry__ as ge
@@ -478,6 +479,13 @@ def run_codec(args):
             raise SystemExit("bench: ciphertext x plaintext is not bit-exact with the oracle")
         if not np.array_equal(fg.to_host(dec[b]), sk_o.decrypt(ct_o).decode("simd")):
             raise SystemExit("bench: decryption is not bit-exact with the oracle")
+    # c1 of B seeded fresh ciphertexts (Poly::random_from_seed, rq/mod.rs:239-257).
+    seeds = rng.integers(0, 256, (B, 32), dtype=np.uint8)
+    seeds_d = torch.tensor(seeds, device=ct_d.device)
+    ctx_d = par.context_at_level(0)
+    c1 = fg.random_from_seed(ctx_d, seeds_d)
+    if not np.array_equal(fg.to_host(c1[0]), ora.random_from_seed(ctx, bytes(seeds[0]))):
+        raise SystemExit("bench: seeded expansion is not bit-exact with the oracle")
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -496,6 +504,7 @@ def run_codec(args):
         enc_ms = timed(lambda: fg.plaintext_encode(par, 0, vals_d))
         mul_ms = timed(lambda: fg.ciphertext_mul_plain(par, 0, ct_d, pt))
         dec_ms = timed(lambda: sk.decrypt(ct_d))
+        seed_ms = timed(lambda: fg.random_from_seed(ctx_d, seeds_d, out=c1))
     launches = fg.kernel_launch_count() - launches0
     line = {"metric": "BFV plaintext side per second N=2^14 L=6 (SIMD encode, ct x pt, decrypt + decode)",
             "value": B / (dec_ms / 1000.0), "unit": "decryptions/s", "n_gpus": 1, "steps": args.steps,
@@ -504,7 +513,9 @@ def run_codec(args):
             "data": "synthetic (seeded encryptions by the CPU oracle)",
             "config": {"workload": "codec", "degree": N, "moduli": L, "plaintext": T, "batch": B},
             "encode_per_s": B / (enc_ms / 1000.0), "mul_plain_per_s": B / (mul_ms / 1000.0),
-            "decrypt_per_s": B / (dec_ms / 1000.0), "gpu_launches": int(launches), "clocks": clocks.summary()}
+            "decrypt_per_s": B / (dec_ms / 1000.0), "seeded_c1_per_s": B / (seed_ms / 1000.0),
+            "seeded_c1_gbs_written": B * L * N * 8 / (seed_ms * 1e6),
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
 
 

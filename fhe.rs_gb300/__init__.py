@@ -107,6 +107,8 @@ def _declare(L):
         "fheg_params_max_level": (c_size, [c_vp]),
         "fheg_ksk_create": (i, [c_vp, c_size, c_size, P_u64, P_u64, c_size, ctypes.POINTER(c_vp)]),
         "fheg_ksk_destroy": (None, [c_vp]),
+        "fheg_ksk_create_seeded": (i, [c_vp, c_size, c_size, P_u64, ctypes.c_char_p, c_size, ctypes.POINTER(c_vp)]),
+        "fheg_poly_random_from_seed": (i, [c_vp, c_vp, c_vp, c_size, c_size, c_vp]),
         "fheg_relinearize": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize": (i, [c_vp, c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_rgsw_create": (i, [c_vp, c_size, P_u64, P_u64, P_u64, P_u64, ctypes.POINTER(c_vp)]),
@@ -421,6 +423,26 @@ def scalar_mul(ctx: Context, t, scalar: int):
     return out
 
 
+def random_from_seed(ctx: Context, seeds, out=None, poly_stride: int = 0):
+    """Poly::random_from_seed (rq/mod.rs:239-257) for a uint8 device tensor of
+    seeds [count][32]: a new [count][L][N] tensor, or polynomial b written at
+    out.data_ptr() + 8 * b * poly_stride (poly_stride in words; 2*L*N with
+    out = ct[:, 1] fills the c1 of seeded ciphertexts [count][2][L][N])."""
+    torch = _torch()
+    if seeds.dtype != torch.uint8 or seeds.dim() != 2 or seeds.shape[1] != 32 or not seeds.is_cuda:
+        raise FhegError(ERR_INVALID_ARGUMENT, "seeds must be a uint8 device tensor [count][32]")
+    seeds = seeds.contiguous()
+    count = seeds.shape[0]
+    if out is None:
+        out = empty((count, ctx.L, ctx.degree), seeds.device)
+        ptr = _dp(out)
+    else:
+        assert out.is_cuda and out.dtype == torch.int64
+        ptr = out.data_ptr()
+    check(lib().fheg_poly_random_from_seed(ctx._h, seeds.data_ptr(), ptr, poly_stride, count, _stream()))
+    return out
+
+
 def substitute(ctx: Context, t, exponent: int, representation: int):
     """Poly::substitute (rq/mod.rs:319-369) on a batch."""
     out = empty(t.shape, t.device)
@@ -523,6 +545,25 @@ class KeySwitchingKey:
                                     ctypes.byref(h)))
         self._h = h
 
+    @classmethod
+    def from_seed(cls, par: BfvParameters, c0: np.ndarray, seed: bytes, ciphertext_level: int = 0,
+                  ksk_level: int = 0, **kw):
+        """A key from its c0 polynomials and the 32-byte seed of its c1
+        (key_switching_key.rs:108-123, 383-406); c1 is expanded on the device."""
+        if len(seed) != 32:
+            raise FhegError(ERR_INVALID_ARGUMENT, "Invalid seed")
+        k = cls.__new__(cls)
+        k.par = par
+        k.ciphertext_level, k.ksk_level = ciphertext_level, ksk_level
+        for name, v in kw.items():
+            setattr(k, name, v)
+        c0 = _u64(c0)
+        h = c_vp()
+        check(lib().fheg_ksk_create_seeded(par._h, ciphertext_level, ksk_level, _ptr(c0), bytes(seed), c0.shape[0],
+                                           ctypes.byref(h)))
+        k._h = h
+        return k
+
     def __del__(self):
         if getattr(self, "_h", None) is not None and _lib is not None:
             _lib.fheg_ksk_destroy(self._h)
@@ -549,6 +590,11 @@ class GaloisKey(KeySwitchingKey):
     def __init__(self, par, exponent: int, c0, c1, ciphertext_level: int = 0, ksk_level: int = 0):
         super().__init__(par, c0, c1, ciphertext_level, ksk_level)
         self.exponent = exponent % (2 * par.degree)
+
+    @classmethod
+    def from_seed(cls, par, exponent: int, c0, seed: bytes, ciphertext_level: int = 0, ksk_level: int = 0):
+        """A Galois key from its c0 polynomials and the seed of its c1."""
+        return super().from_seed(par, c0, seed, ciphertext_level, ksk_level, exponent=exponent % (2 * par.degree))
 
     def relinearize(self, ct):
         """galois_key.rs:63-124 on a batch [count][2][L][N]."""

@@ -550,28 +550,64 @@ FHEG_API int fheg_params_context_at_level(const fheg_params* par, size_t level, 
 
 FHEG_API size_t fheg_params_max_level(const fheg_params* par) { return par ? par->p->max_level() : 0; }
 
+// A key-switching key with its c0 uploaded and room for c1 (shared by the
+// plain and the seeded constructors).
+static fheg_ksk* new_ksk(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
+                         size_t count) {
+  const Params& p = *par->p;
+  if (ciphertext_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+  if (ksk_level > ciphertext_level) throw Error(FHEG_ERR_INVALID_LEVEL, "Unexpected levels");
+  auto h = new fheg_ksk();
+  try {
+    Ksk& k = h->k;
+    k.par = &p;
+    k.ciphertext_level = ciphertext_level;
+    k.ksk_level = ksk_level;
+    k.ctx_ct = p.ctx(ciphertext_level);
+    k.ctx_ksk = p.ctx(ksk_level);
+    if (k.ctx_ksk->L() < 2) throw Error(FHEG_ERR_UNSUPPORTED, "These parameters do not support key switching");
+    if (count != k.ctx_ct->L()) throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
+    k.count = count;
+    const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
+    k.keys.alloc(2 * words * 8);
+    upload(k.values(0), h_c0, words * 8);
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  return h;
+}
+
 FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
                              const uint64_t* h_c1, size_t count, fheg_ksk** out) {
   return guard([&] {
     need(par && h_c0 && h_c1 && out, "null input");
-    const Params& p = *par->p;
-    if (ciphertext_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
-    if (ksk_level > ciphertext_level) throw Error(FHEG_ERR_INVALID_LEVEL, "Unexpected levels");
-    auto h = new fheg_ksk();
+    fheg_ksk* h = new_ksk(par, ciphertext_level, ksk_level, h_c0, count);
     try {
-      Ksk& k = h->k;
-      k.par = &p;
-      k.ciphertext_level = ciphertext_level;
-      k.ksk_level = ksk_level;
-      k.ctx_ct = p.ctx(ciphertext_level);
-      k.ctx_ksk = p.ctx(ksk_level);
-      if (k.ctx_ksk->L() < 2) throw Error(FHEG_ERR_UNSUPPORTED, "These parameters do not support key switching");
-      if (count != k.ctx_ct->L()) throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
-      k.count = count;
-      const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
-      k.keys.alloc(2 * words * 8);
-      upload(k.values(0), h_c0, words * 8);
-      upload(k.values(1), h_c1, words * 8);
+      const Ksk& k = h->k;
+      upload(k.values(1), h_c1, count * k.ctx_ksk->L() * k.ctx_ksk->N() * 8);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
+                                    const uint64_t* h_c0, const uint8_t* seed, size_t count, fheg_ksk** out) {
+  return guard([&] {
+    need(par && h_c0 && seed && out, "null input");
+    fheg_ksk* h = new_ksk(par, ciphertext_level, ksk_level, h_c0, count);
+    try {
+      const Ksk& k = h->k;
+      const std::vector<uint8_t> seeds = ksk_c1_seeds(seed, count);
+      DevBuf d_seeds(seeds.size());
+      upload(d_seeds.ptr, seeds.data(), seeds.size());
+      Workspace ws;
+      poly_random_from_seed(*k.ctx_ksk, static_cast<const uint8_t*>(d_seeds.ptr), k.values(1),
+                            k.ctx_ksk->L() * k.ctx_ksk->N(), count, ws, nullptr);
+      check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
     } catch (...) {
       delete h;
       throw;

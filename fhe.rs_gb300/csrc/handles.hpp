@@ -9,6 +9,8 @@
 
 struct fheg_context {
   std::shared_ptr<fheg::Context> c;
+  // Scratch of fheg_poly_random_from_seed (calls on one context must not overlap).
+  std::shared_ptr<fheg::Workspace> ws = std::make_shared<fheg::Workspace>();
 };
 struct fheg_scaler {
   std::unique_ptr<fheg::Scaler> s;

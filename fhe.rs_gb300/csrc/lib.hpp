@@ -236,6 +236,14 @@ void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint
                          uint64_t* D, cudaStream_t st);
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st);
+// Poly::random_from_seed for `count` 32-byte device seeds: polynomial b
+// ([L][N], the same values in every representation) at out + b * stride.
+void poly_random_from_seed(const Context& c, const uint8_t* seeds, uint64_t* out, uint64_t stride, uint64_t count,
+                           Workspace& ws, cudaStream_t st);
+// The seeds of c1[0 .. count) of a key-switching key with seed `seed` (32
+// bytes): 32 * count bytes (key_switching_key.rs:108-123).
+std::vector<uint8_t> ksk_c1_seeds(const uint8_t* seed, size_t count);
+
 // External product with an RGSW ciphertext held as one key of 2L digits per
 // part (ksk0's digits, then ksk1's): ct [count][2][L][N] -> out, both Ntt.
 void external_product(const Ksk& rgsw, const uint64_t* ct, uint64_t* out, uint64_t count, Workspace& ws,

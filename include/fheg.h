@@ -199,6 +199,17 @@ FHEG_API void fheg_scaler_destroy(fheg_scaler* s);
 FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const uint64_t* d_in,
                                uint64_t* d_out, size_t count, void* stream);
 
+/* Poly::random_from_seed (fhe-math/src/rq/mod.rs:239-257) for `count`
+ * 32-byte seeds d_seeds [count][32] (device): polynomial b ([L][N], uniform
+ * residues; the same values serve every representation) is written at
+ * d_out + b * poly_stride words (poly_stride 0 = L*N; 2*L*N writes the c1 of
+ * [count][2][L][N] ciphertexts, as a seeded Ciphertext is read,
+ * fhe/src/bfv/ciphertext.rs:220-237). SHA-256 of the seed keys ChaCha8; each
+ * limb takes N samples of Uniform[0, q_j) in turn. Calls on the same context
+ * must not overlap (shared scratch). */
+FHEG_API int fheg_poly_random_from_seed(const fheg_context* ctx, const uint8_t* d_seeds, uint64_t* d_out,
+                                        size_t poly_stride, size_t count, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* BFV (crate fhe).                                                           */
 
@@ -220,6 +231,13 @@ FHEG_API size_t fheg_params_max_level(const fheg_params* par);
  * the Shoup companions are computed here. */
 FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
                              const uint64_t* h_c0, const uint64_t* h_c1, size_t count, fheg_ksk** out);
+/* A key-switching key from its c0[i] polynomials and the 32-byte seed the
+ * reference stores instead of c1 (`KeySwitchingKey::seed`,
+ * key_switching_key.rs:67-68; c1 regenerated as generate_c1 does,
+ * key_switching_key.rs:108-123, 383-406): c1[i] = Poly::random_from_seed of
+ * the i-th 32 bytes of ChaCha8Rng::from_seed(seed), expanded on the device. */
+FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
+                                    const uint64_t* h_c0, const uint8_t* seed, size_t count, fheg_ksk** out);
 FHEG_API void fheg_ksk_destroy(fheg_ksk* k);
 
 /* RelinearizationKey::relinearizes (fhe/src/bfv/keys/relinearization_key.rs:71-98):

@@ -27,6 +27,7 @@ Parity pins:
 from __future__ import annotations
 
 import ctypes
+import hashlib
 import math
 import os
 from dataclasses import dataclass, field
@@ -259,6 +260,22 @@ class ChaChaRng:
         hi = self.next_u32()
         return lo | (hi << 32)
 
+    @staticmethod
+    def from_seed(seed: bytes, rounds: int = 8) -> "ChaChaRng":
+        """rand_chacha 0.9.0 `SeedableRng::from_seed`: the 32 seed bytes are
+        the key as little-endian words; counter and stream start at zero."""
+        assert len(seed) == 32
+        return ChaChaRng([int.from_bytes(seed[4 * i:4 * i + 4], "little") for i in range(8)], rounds)
+
+    def fill_bytes(self, n: int) -> bytes:
+        """rand_core 0.9.3 `BlockRng::fill_bytes` (`Rng::fill` of a byte
+        array): whole words, little-endian; the rest of a last partial word is
+        dropped."""
+        out = bytearray()
+        while len(out) < n:
+            out += self.next_u32().to_bytes(4, "little")
+        return bytes(out[:n])
+
     def random_range_u64(self, low: int, high: int) -> int:
         """rand 0.9.2 `random_range(low..high)` for u64 (Canon's method with
         one extra sample to reduce bias)."""
@@ -273,6 +290,99 @@ class ChaChaRng:
             if lo_order + new_hi > M64:
                 result += 1
         return (low + result) & M64
+
+
+def chacha_blocks(key_words: Sequence[int], counters: np.ndarray, rounds: int = 8, stream: int = 0) -> np.ndarray:
+    """The block function of `ChaChaRng._block`, vectorised over block
+    counters: [len(counters), 16] uint32 keystream words."""
+    ctr = np.asarray(counters, dtype=np.uint64)
+    n = ctr.shape[0]
+    st = np.zeros((16, n), dtype=np.uint32)
+    st[0:4] = np.array([0x61707865, 0x3320646E, 0x79622D32, 0x6B206574], dtype=np.uint32)[:, None]
+    st[4:12] = np.array([w & 0xFFFFFFFF for w in key_words], dtype=np.uint32)[:, None]
+    st[12] = (ctr & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    st[13] = (ctr >> np.uint64(32)).astype(np.uint32)
+    st[14] = stream & 0xFFFFFFFF
+    st[15] = (stream >> 32) & 0xFFFFFFFF
+    x = st.copy()
+
+    def rotl(v, r):
+        return (v << np.uint32(r)) | (v >> np.uint32(32 - r))
+
+    def qr(a, b, c, d):
+        x[a] += x[b]
+        x[d] = rotl(x[d] ^ x[a], 16)
+        x[c] += x[d]
+        x[b] = rotl(x[b] ^ x[c], 12)
+        x[a] += x[b]
+        x[d] = rotl(x[d] ^ x[a], 8)
+        x[c] += x[d]
+        x[b] = rotl(x[b] ^ x[c], 7)
+
+    for _ in range(rounds // 2):
+        qr(0, 4, 8, 12)
+        qr(1, 5, 9, 13)
+        qr(2, 6, 10, 14)
+        qr(3, 7, 11, 15)
+        qr(0, 5, 10, 15)
+        qr(1, 6, 11, 12)
+        qr(2, 7, 8, 13)
+        qr(3, 4, 9, 14)
+    return (x + st).T.copy()
+
+
+def chacha_u64_draws(key_words: Sequence[int], first: int, count: int, rounds: int = 8) -> np.ndarray:
+    """Draws first .. first+count-1 of `next_u64` on a fresh generator: draw
+    k joins words 2k (low) and 2k+1 (high) of the keystream."""
+    b0, b1 = first // 8, (first + count + 7) // 8
+    w = chacha_blocks(key_words, np.arange(b0, b1, dtype=np.uint64), rounds).reshape(-1).astype(np.uint64)
+    d = w[0::2] | (w[1::2] << np.uint64(32))
+    return d[first - 8 * b0:first - 8 * b0 + count]
+
+
+def uniform_u64_threshold(q: int) -> int:
+    """rand 0.9.2 `UniformInt<u64>` for the range [0, q): a draw x gives the
+    high word of x q unless the low word is below (2^64 - q) mod q, in which
+    case it is redrawn (Lemire's widening multiply with rejection). The
+    rejection rule is restated from the published method; no reference test
+    pins it."""
+    return ((1 << 64) - q) % q
+
+
+def random_from_seed(ctx: "Context", seed: bytes) -> np.ndarray:
+    """rq/mod.rs:239-257 `Poly::random_from_seed`: SHA-256 of the seed is the
+    key of a ChaCha8 generator, and each limb takes `degree` samples of
+    Uniform[0, q_j) in turn (`Modulus::random_vec`, zq/mod.rs:765-767).
+    Returns the [L][N] coefficients (used as is in every representation)."""
+    digest = hashlib.sha256(bytes(seed)).digest()
+    key = [int.from_bytes(digest[4 * i:4 * i + 4], "little") for i in range(8)]
+    n = ctx.degree
+    out = np.zeros((len(ctx.moduli), n), dtype=np.uint64)
+    pos = 0
+    for j, q in enumerate(ctx.moduli):
+        thresh = uniform_u64_threshold(q)
+        vals: List[int] = []
+        while len(vals) < n:
+            want = n - len(vals)
+            draws = chacha_u64_draws(key, pos, want + 8).astype(object)
+            prod = draws * q
+            for k in range(want + 8):
+                if int(prod[k]) & M64 >= thresh:
+                    vals.append(int(prod[k]) >> 64)
+                    if len(vals) == n:
+                        pos += k + 1
+                        break
+            else:
+                pos += want + 8
+        out[j] = np.array(vals, dtype=np.uint64)
+    return out
+
+
+def ksk_c1_seeds(seed: bytes, size: int) -> List[bytes]:
+    """key_switching_key.rs:108-123 `generate_c1`: seed i of c1[i] is the
+    next 32 bytes of a ChaCha8 generator keyed with the key's seed."""
+    rng = ChaChaRng.from_seed(bytes(seed))
+    return [rng.fill_bytes(32) for _ in range(size)]
 
 
 # ---------------------------------------------------------------------------
@@ -672,6 +782,14 @@ class Poly:
         """rq/mod.rs:226-237 (numpy stream in place of the caller's RNG)."""
         c = np.stack([rng.integers(0, m, ctx.degree, dtype=np.uint64) for m in ctx.moduli])
         return Poly(ctx, c, representation)
+
+    @staticmethod
+    def random_from_seed(ctx: Context, seed: bytes, representation: str = NTT) -> "Poly":
+        """rq/mod.rs:239-257."""
+        p = Poly(ctx, random_from_seed(ctx, seed), representation)
+        if representation == NTT_SHOUP:
+            p.compute_coefficients_shoup()
+        return p
 
     @staticmethod
     def small(ctx: Context, representation: str, variance: int, rng: np.random.Generator) -> "Poly":
@@ -1223,7 +1341,7 @@ class KeySwitchingKey:
     at least two moduli)."""
 
     def __init__(self, sk: SecretKey, frm: Poly, ciphertext_level: int, ksk_level: int,
-                 rng: np.random.Generator):
+                 rng: np.random.Generator, seed: Optional[bytes] = None):
         par = sk.par
         self.par = par
         self.ctx_ksk = par.context_at_level(ksk_level)
@@ -1234,8 +1352,14 @@ class KeySwitchingKey:
         if len(self.ctx_ksk.moduli) == 1:
             raise NotImplementedError("bit decomposition keys (single-modulus key context)")
         size = len(self.ctx_ciphertext.moduli)
-        # generate_c1 (108-123): uniform NttShoup polys.
-        self.c1 = [Poly.random(self.ctx_ksk, NTT_SHOUP, rng) for _ in range(size)]
+        # generate_c1 (108-123): uniform NttShoup polys, from the key's seed
+        # when one is given (as the reference always does), else drawn from
+        # the numpy generator.
+        self.seed = None if seed is None else bytes(seed)
+        if seed is None:
+            self.c1 = [Poly.random(self.ctx_ksk, NTT_SHOUP, rng) for _ in range(size)]
+        else:
+            self.c1 = [Poly.random_from_seed(self.ctx_ksk, s, NTT_SHOUP) for s in ksk_c1_seeds(seed, size)]
         # generate_c0 (126-169)
         s = sk.s_ntt(self.ctx_ksk)
         rns = RnsContext(par.moduli[:size])
@@ -1293,7 +1417,8 @@ class KeySwitchingKey:
 class RelinearizationKey:
     """keys/relinearization_key.rs:22-106."""
 
-    def __init__(self, sk: SecretKey, rng: np.random.Generator, ciphertext_level: int = 0, key_level: int = 0):
+    def __init__(self, sk: SecretKey, rng: np.random.Generator, ciphertext_level: int = 0, key_level: int = 0,
+                 seed: Optional[bytes] = None):
         par = sk.par
         ctx_rk = par.context_at_level(key_level)
         ctx_ct = par.context_at_level(ciphertext_level)
@@ -1302,7 +1427,7 @@ class RelinearizationKey:
         s = sk.s_ntt(ctx_ct)
         s2 = (s * s).into_power_basis()
         s2_up = Switcher(ctx_ct, ctx_rk).switch(s2)
-        self.ksk = KeySwitchingKey(sk, s2_up, ciphertext_level, key_level, rng)
+        self.ksk = KeySwitchingKey(sk, s2_up, ciphertext_level, key_level, rng, seed)
 
     @staticmethod
     def from_ksk(ksk: KeySwitchingKey) -> "RelinearizationKey":
@@ -1335,7 +1460,7 @@ class GaloisKey:
     """keys/galois_key.rs:18-124."""
 
     def __init__(self, sk: SecretKey, exponent: int, ciphertext_level: int, galois_key_level: int,
-                 rng: np.random.Generator):
+                 rng: np.random.Generator, seed: Optional[bytes] = None):
         par = sk.par
         ctx_gk = par.context_at_level(galois_key_level)
         ctx_ct = par.context_at_level(ciphertext_level)
@@ -1343,7 +1468,7 @@ class GaloisKey:
         s = Poly.from_i64(ctx_ct, sk.coeffs)
         s_sub = s.substitute(self.element)
         s_sub_up = Switcher(ctx_ct, ctx_gk).switch(s_sub)
-        self.ksk = KeySwitchingKey(sk, s_sub_up, ciphertext_level, galois_key_level, rng)
+        self.ksk = KeySwitchingKey(sk, s_sub_up, ciphertext_level, galois_key_level, rng, seed)
 
     @staticmethod
     def from_ksk(exponent: int, ksk: KeySwitchingKey) -> "GaloisKey":

@@ -292,3 +292,67 @@ def test_rq_payload_roundtrip(ora):
         payload = ora.rq_payload(p)
         assert len(payload) == 3 * 16 * 62 // 8
         assert np.array_equal(ora.rq_from_payload(ctx, payload, rep).coefficients, c)
+
+
+def test_chacha_block_function(ora):
+    """The vectorised block function equals the scalar generator's stream, and
+    at 20 rounds equals ChaCha20 of the `cryptography` package (OpenSSL) with
+    the 16-byte counter-and-nonce block set to (64-bit counter, 64-bit stream),
+    the rand_chacha state layout."""
+    key = [(0x01234567 * (i + 1)) & 0xFFFFFFFF for i in range(8)]
+    rng = ora.ChaChaRng(key)
+    words = [rng.next_u32() for _ in range(16 * 5)]
+    assert list(ora.chacha_blocks(key, np.arange(5)).reshape(-1)) == words
+    draws = ora.chacha_u64_draws(key, 3, 30)
+    rng = ora.ChaChaRng(key)
+    ref = [rng.next_u64() for _ in range(33)][3:]
+    assert [int(x) for x in draws] == ref
+    ciphers = pytest.importorskip("cryptography.hazmat.primitives.ciphers")
+    kb = b"".join(w.to_bytes(4, "little") for w in key)
+    for counter, stream in [(0, 0), (7, 0), (3, 0x1122334455667788)]:
+        nonce = counter.to_bytes(8, "little") + stream.to_bytes(8, "little")
+        enc = ciphers.Cipher(ciphers.algorithms.ChaCha20(kb, nonce), mode=None).encryptor()
+        ks = enc.update(bytes(64 * 2))
+        got = ora.chacha_blocks(key, np.array([counter, counter + 1]), rounds=20, stream=stream)
+        assert got.astype("<u4").tobytes() == ks
+
+
+def test_random_from_seed(ora):
+    """rq/mod.rs:239-257 and key_switching_key.rs:108-123: deterministic in
+    the seed, uniform residues, seeds of c1 drawn 32 bytes at a time, and the
+    exact rejection walk (a modulus just above 2^61 rejects about one draw in
+    eight, and every limb then starts after the last accepted draw)."""
+    ctx = ora.Context(ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3).moduli, 16)
+    seed = bytes(range(32))
+    a = ora.random_from_seed(ctx, seed)
+    assert np.array_equal(a, ora.random_from_seed(ctx, seed))
+    assert not np.array_equal(a, ora.random_from_seed(ctx, bytes(32)))
+    for j, q in enumerate(ctx.moduli):
+        assert int(a[j].max()) < q
+    digest = __import__("hashlib").sha256(seed).digest()
+    key = [int.from_bytes(digest[4 * i:4 * i + 4], "little") for i in range(8)]
+    # Near-2^62 moduli reject with probability ~2^-46: no rejections here.
+    draws = ora.chacha_u64_draws(key, 0, 48)
+    want = [(int(x) * ctx.moduli[k // 16]) >> 64 for k, x in enumerate(draws)]
+    assert [int(v) for v in a.reshape(-1)] == want
+    # generate_c1: seed i = bytes 32 i .. 32 i + 31 of the key seed's stream.
+    rng = ora.ChaChaRng.from_seed(seed)
+    stream = rng.fill_bytes(96)
+    assert ora.ksk_c1_seeds(seed, 3) == [stream[0:32], stream[32:64], stream[64:96]]
+    # A modulus just above 2^61 (threshold ~ 2^61 - 7 delta): sequential walk.
+    q = ora.generate_prime(62, 32, (1 << 61) + (1 << 45))
+    assert q is not None and q > (1 << 61)
+    ctx2 = ora.Context([q, ctx.moduli[0]], 16)
+    b = ora.random_from_seed(ctx2, seed)
+    thresh = ora.uniform_u64_threshold(q)
+    draws = [int(x) for x in ora.chacha_u64_draws(key, 0, 200)]
+    vals, pos = [], 0
+    while len(vals) < 16:
+        prod = draws[pos] * q
+        pos += 1
+        if prod & ora.M64 >= thresh:
+            vals.append(prod >> 64)
+    assert pos > 16, "expected at least one rejection"
+    assert [int(v) for v in b[0]] == vals
+    vals = [(draws[pos + k] * ctx.moduli[0]) >> 64 for k in range(16)]
+    assert [int(v) for v in b[1]] == vals
