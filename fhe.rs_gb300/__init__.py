@@ -109,6 +109,12 @@ def _declare(L):
         "fheg_ksk_destroy": (None, [c_vp]),
         "fheg_ksk_create_seeded": (i, [c_vp, c_size, c_size, P_u64, ctypes.c_char_p, c_size, ctypes.POINTER(c_vp)]),
         "fheg_poly_random_from_seed": (i, [c_vp, c_vp, c_vp, c_size, c_size, c_vp]),
+        "fheg_ciphertext_serialized_size": (i, [c_vp, c_size, c_size, i, i, ctypes.POINTER(c_size)]),
+        "fheg_ciphertext_to_bytes": (i, [c_vp, c_size, c_size, c_vp, c_size, ctypes.c_char_p, i, c_vp, c_size, c_vp]),
+        "fheg_ciphertext_peek": (i, [c_vp, ctypes.c_char_p, c_size, ctypes.POINTER(c_size), ctypes.POINTER(c_size),
+                                     ctypes.POINTER(i)]),
+        "fheg_ciphertext_from_bytes": (i, [c_vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), c_size,
+                                           c_size, c_size, c_vp, c_vp]),
         "fheg_relinearize": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize": (i, [c_vp, c_size, c_vp, c_vp, c_size, c_vp]),
         "fheg_rgsw_create": (i, [c_vp, c_size, P_u64, P_u64, P_u64, P_u64, ctypes.POINTER(c_vp)]),
@@ -440,6 +446,52 @@ def random_from_seed(ctx: Context, seeds, out=None, poly_stride: int = 0):
         assert out.is_cuda and out.dtype == torch.int64
         ptr = out.data_ptr()
     check(lib().fheg_poly_random_from_seed(ctx._h, seeds.data_ptr(), ptr, poly_stride, count, _stream()))
+    return out
+
+
+def ciphertext_serialized_size(par: BfvParameters, level: int, parts: int = 2, seeded: bool = False,
+                               allow_variable_time: bool = False) -> int:
+    out = c_size(0)
+    check(lib().fheg_ciphertext_serialized_size(par._h, level, parts, int(seeded), int(allow_variable_time),
+                                                ctypes.byref(out)))
+    return out.value
+
+
+def ciphertext_to_bytes(par: BfvParameters, level: int, ct, seeds: Optional[Sequence[bytes]] = None,
+                        allow_variable_time: bool = False) -> List[bytes]:
+    """Ciphertext::to_bytes (fhe/src/bfv/ciphertext.rs:164-191) of a batch
+    [count][parts][L][N]; `seeds` (one 32-byte seed per ciphertext) replace
+    the last parts."""
+    count, parts = ct.shape[0], ct.shape[1]
+    one = ciphertext_serialized_size(par, level, parts, seeds is not None, allow_variable_time)
+    buf = ctypes.create_string_buffer(max(1, count * one))
+    sd = b"".join(bytes(x) for x in seeds) if seeds is not None else None
+    if sd is not None and len(sd) != 32 * count:
+        raise FhegError(ERR_INVALID_ARGUMENT, "one 32-byte seed per ciphertext")
+    check(lib().fheg_ciphertext_to_bytes(par._h, level, parts, _dp(ct), count, sd, int(allow_variable_time),
+                                         ctypes.cast(buf, c_vp), count * one, _stream()))
+    raw = buf.raw
+    return [raw[b * one:(b + 1) * one] for b in range(count)]
+
+
+def ciphertext_peek(par: BfvParameters, msg: bytes):
+    """(level, parts, seeded) of a serialized Ciphertext."""
+    level, parts, seeded = c_size(0), c_size(0), ctypes.c_int(0)
+    check(lib().fheg_ciphertext_peek(par._h, bytes(msg), len(msg), ctypes.byref(level), ctypes.byref(parts),
+                                     ctypes.byref(seeded)))
+    return level.value, parts.value, bool(seeded.value)
+
+
+def ciphertext_from_bytes(par: BfvParameters, msgs: Sequence[bytes], device="cuda"):
+    """Ciphertext::from_bytes (ciphertext.rs:195-240) of messages of one
+    level, part count and seededness: [count][parts][L][N] on the device."""
+    level, parts, _ = ciphertext_peek(par, msgs[0])
+    n = len(msgs)
+    ctx = par.context_at_level(level)
+    out = empty((n, parts, ctx.L, ctx.degree), device)
+    arr = (ctypes.c_char_p * n)(*[bytes(m) for m in msgs])
+    lens = (c_size * n)(*[len(m) for m in msgs])
+    check(lib().fheg_ciphertext_from_bytes(par._h, arr, lens, n, level, parts, _dp(out), _stream()))
     return out
 
 

@@ -6,6 +6,8 @@
 // (inverse NTT before packing, forward NTT after unpacking), as the
 // reference's conversion does.
 
+#include <cstring>
+#include <string>
 #include <vector>
 
 #include "fheg.h"
@@ -56,7 +58,7 @@ PackLayout make_layout(const Context& c) {
 // gathered from the (at most 64 / nb + 2) coefficients they overlap, stored
 // as one word when the destination is aligned, else byte by byte (a limb's
 // last chunk may be short).
-__global__ void k_pack(const __grid_constant__ PackLayout lay, const uint64_t* in, uint8_t* out, uint64_t total) {
+__global__ void k_pack(const __grid_constant__ PackLayout lay, const PolyRef in, uint8_t* out, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint64_t poly = gid / lay.poly_chunks;
@@ -67,7 +69,7 @@ __global__ void k_pack(const __grid_constant__ PackLayout lay, const uint64_t* i
   const uint64_t n = 1ull << lay.logn;
   const uint32_t nb = lay.nbits[j];
   const uint64_t mask = nb == 64 ? ~0ull : ((1ull << nb) - 1);
-  const uint64_t* row = in + (poly * lay.limbs + j) * n;
+  const uint64_t* row = in.at((uint32_t)poly, j);
   const uint64_t bit0 = c * 64;
   uint64_t word = 0;
   for (uint64_t k = bit0 / nb; k < n && k * nb < bit0 + 64; k++) {
@@ -88,7 +90,7 @@ __global__ void k_pack(const __grid_constant__ PackLayout lay, const uint64_t* i
 
 // One coefficient per thread: bits [k nb, k nb + nb) of the limb's stream
 // (at most 9 bytes), reduced once modulo q_j.
-__global__ void k_unpack(const __grid_constant__ PackLayout lay, const uint8_t* in, uint64_t* out, uint64_t total) {
+__global__ void k_unpack(const __grid_constant__ PackLayout lay, const uint8_t* in, const PolyRef out, uint64_t total) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint64_t n = 1ull << lay.logn;
@@ -109,7 +111,7 @@ __global__ void k_unpack(const __grid_constant__ PackLayout lay, const uint8_t* 
   if (b0 + 8 < limb_bytes) hi = p[b0 + 8];
   uint64_t v = (lo >> s) | (s ? hi << (64 - s) : 0);
   if (nb < 64) v &= (1ull << nb) - 1;
-  out[gid] = v >= lay.q[j] ? v - lay.q[j] : v;
+  out.at((uint32_t)poly, j)[k] = v >= lay.q[j] ? v - lay.q[j] : v;
 }
 
 unsigned nblk(uint64_t total, unsigned threads) { return (unsigned)((total + threads - 1) / threads); }
@@ -118,34 +120,304 @@ unsigned nblk(uint64_t total, unsigned threads) { return (unsigned)((total + thr
 
 size_t poly_serialized_bytes(const Context& c) { return make_layout(c).poly_bytes; }
 
-void poly_serialize(const Context& c, int representation, const uint64_t* polys, uint8_t* bytes, uint64_t count,
-                    DevBuf& scratch, cudaStream_t st) {
+// Payloads of `count` polynomials read through `in` (Ntt polynomials go
+// through `tmp`, count * L * N words, in the power basis) into `bytes`.
+void pack_polys(const Context& c, int representation, PolyRef in, uint8_t* bytes, uint64_t count, uint64_t* tmp,
+                cudaStream_t st) {
   if (count == 0) return;
   const PackLayout lay = make_layout(c);
-  const uint64_t* src = polys;
+  PolyRef src = in;
   if (representation == 1) {
-    const size_t words = count * c.L() * c.N();
-    scratch.reserve(words * 8);
-    PolyRef in = plain_ref(const_cast<uint64_t*>(polys), c.L(), c.logn), tmp = plain_ref(scratch.u64(), c.L(), c.logn);
-    ntt_backward(c, in, tmp, count, st);
-    src = scratch.u64();
+    src = plain_ref(tmp, c.L(), c.logn);
+    ntt_backward(c, in, src, count, st);
   }
   const uint64_t total = count * lay.poly_chunks;
   k_pack<<<nblk(total, 256), 256, 0, st>>>(lay, src, bytes, total);
   after_launch("k_pack");
 }
 
-void poly_deserialize(const Context& c, int representation, const uint8_t* bytes, uint64_t* polys, uint64_t count,
-                      cudaStream_t st) {
+// Payloads back into `count` polynomials written through `out`.
+void unpack_polys(const Context& c, int representation, const uint8_t* bytes, PolyRef out, uint64_t count,
+                  cudaStream_t st) {
   if (count == 0) return;
   const PackLayout lay = make_layout(c);
   const uint64_t total = count * c.L() << c.logn;
-  k_unpack<<<nblk(total, 256), 256, 0, st>>>(lay, bytes, polys, total);
+  k_unpack<<<nblk(total, 256), 256, 0, st>>>(lay, bytes, out, total);
   after_launch("k_unpack");
-  if (representation == 1) {
-    PolyRef r = plain_ref(polys, c.L(), c.logn);
-    ntt_forward(c, r, r, count, false, st);
+  if (representation == 1) ntt_forward(c, out, out, count, false, st);
+}
+
+void poly_serialize(const Context& c, int representation, const uint64_t* polys, uint8_t* bytes, uint64_t count,
+                    DevBuf& scratch, cudaStream_t st) {
+  if (count == 0) return;
+  if (representation == 1) scratch.reserve(count * c.L() * c.N() * 8);
+  pack_polys(c, representation, plain_ref(const_cast<uint64_t*>(polys), c.L(), c.logn), bytes, count,
+             representation == 1 ? scratch.u64() : nullptr, st);
+}
+
+void poly_deserialize(const Context& c, int representation, const uint8_t* bytes, uint64_t* polys, uint64_t count,
+                      cudaStream_t st) {
+  unpack_polys(c, representation, bytes, plain_ref(polys, c.L(), c.logn), count, st);
+}
+
+// ---------------------------------------------------------------------------
+// Protobuf framing of `Rq` and `Ciphertext` messages (rq.proto, bfv.proto)
+// as the reference writes them with prost: fields in tag order, proto3
+// defaults (0, false, empty) left out, every element of a repeated field
+// written; readers take fields in any order, the last value of a scalar
+// wins, and unknown fields are skipped.
+
+namespace {
+
+constexpr uint64_t kReprCode[2] = {1, 2};  // fheg representation -> rq.proto Representation
+
+size_t varint_len(uint64_t v) {
+  size_t n = 1;
+  while (v >= 0x80) {
+    v >>= 7;
+    n++;
   }
+  return n;
+}
+
+uint8_t* put_varint(uint8_t* p, uint64_t v) {
+  while (v >= 0x80) {
+    *p++ = (uint8_t)(v | 0x80);
+    v >>= 7;
+  }
+  *p++ = (uint8_t)v;
+  return p;
+}
+
+struct Span {
+  const uint8_t* p = nullptr;
+  size_t n = 0;
+};
+
+struct Field {
+  uint32_t num, type;
+  uint64_t value;  // varints
+  Span bytes;      // length-delimited fields
+};
+
+// Iterates over the fields of one message.
+struct Reader {
+  const uint8_t* p;
+  const uint8_t* end;
+  const char* what;
+  void fail(const char* why) const {
+    throw Error(FHEG_ERR_INVALID_ARGUMENT, std::string(what) + " decode: " + why);
+  }
+  uint64_t varint() {
+    uint64_t v = 0;
+    for (int shift = 0; shift < 70; shift += 7) {
+      if (p >= end) fail("truncated varint");
+      const uint8_t c = *p++;
+      if (shift == 63 && (c & 0x7e)) fail("varint overflow");
+      v |= (uint64_t)(c & 0x7f) << shift;
+      if (!(c & 0x80)) return v;
+    }
+    fail("varint too long");
+    return 0;
+  }
+  bool next(Field& f) {
+    if (p >= end) return false;
+    const uint64_t key = varint();
+    f.num = (uint32_t)(key >> 3);
+    f.type = (uint32_t)(key & 7);
+    if (f.num == 0) fail("field number 0");
+    switch (f.type) {
+      case 0: f.value = varint(); break;
+      case 1:
+        if (end - p < 8) fail("truncated fixed64");
+        p += 8;
+        break;
+      case 2: {
+        const uint64_t n = varint();
+        if (n > (uint64_t)(end - p)) fail("truncated field");
+        f.bytes = Span{p, (size_t)n};
+        p += n;
+        break;
+      }
+      case 5:
+        if (end - p < 4) fail("truncated fixed32");
+        p += 4;
+        break;
+      default: fail("unsupported wire type");
+    }
+    return true;
+  }
+  void expect(const Field& f, uint32_t type) const {
+    if (f.type != type) fail("invalid wire type");
+  }
+};
+
+// Length of one encoded Rq message of a polynomial over `c`.
+size_t rq_message_len(const Context& c, bool avt) {
+  const size_t payload = poly_serialized_bytes(c);
+  return 2 + 1 + varint_len(c.N()) + 1 + varint_len(payload) + payload + (avt ? 2 : 0);
+}
+
+// Writes the Rq message of one packed payload; returns the end.
+uint8_t* put_rq(uint8_t* o, const Context& c, int representation, const uint8_t* payload, bool avt) {
+  const size_t n = poly_serialized_bytes(c);
+  *o++ = 0x08;  // representation
+  o = put_varint(o, kReprCode[representation]);
+  *o++ = 0x10;  // degree
+  o = put_varint(o, c.N());
+  *o++ = 0x1a;  // coefficients
+  o = put_varint(o, n);
+  std::memcpy(o, payload, n);
+  o += n;
+  if (avt) {
+    *o++ = 0x20;  // allow_variable_time
+    *o++ = 1;
+  }
+  return o;
+}
+
+// The payload of one Rq message for a polynomial over `c` in `representation`
+// (convert.rs:44-135, parse_proto and TryConvertFrom<&Rq>).
+Span parse_rq(Span m, const Context& c, int representation) {
+  Reader r{m.p, m.p + m.n, "Rq"};
+  uint64_t repr = 0, degree = 0;
+  Span coeffs;
+  Field f;
+  while (r.next(f)) {
+    if (f.num == 1) r.expect(f, 0), repr = f.value;
+    else if (f.num == 2) r.expect(f, 0), degree = f.value & 0xffffffffu;
+    else if (f.num == 3) r.expect(f, 2), coeffs = f.bytes;
+    else if (f.num == 4) r.expect(f, 0);
+  }
+  const int32_t rep = (int32_t)(uint32_t)repr;
+  if (rep < 0 || rep > 3) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid representation");
+  if (rep == 0) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Unknown representation");
+  if ((uint64_t)rep != kReprCode[representation])
+    throw Error(FHEG_ERR_INVALID_ARGUMENT,
+                "The representation asked for does not match the representation in the serialization");
+  if (degree % 8 != 0 || degree < 8) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid degree");
+  if (degree != c.N()) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid degree: not the context's degree");
+  if (coeffs.n != poly_serialized_bytes(c)) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid coefficients");
+  return coeffs;
+}
+
+struct CtMessage {
+  std::vector<Span> c;
+  Span seed;
+  uint64_t level = 0;
+};
+
+CtMessage parse_ct(const uint8_t* msg, size_t len) {
+  Reader r{msg, msg + len, "Ciphertext"};
+  CtMessage m;
+  Field f;
+  while (r.next(f)) {
+    if (f.num == 1) r.expect(f, 2), m.c.push_back(f.bytes);
+    else if (f.num == 2) r.expect(f, 2), m.seed = f.bytes;
+    else if (f.num == 3) r.expect(f, 0), m.level = f.value & 0xffffffffu;
+  }
+  return m;
+}
+
+// ciphertext.rs:196-216: part count and level checks.
+void check_ct(const Params& par, const CtMessage& m) {
+  if (m.c.empty() || (m.c.size() == 1 && m.seed.n == 0))
+    throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
+  if (m.level > par.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+  if (m.seed.n != 0 && m.seed.n != 32) throw Error(FHEG_ERR_INVALID_ARGUMENT, "InvalidSeedSize");
+}
+
+}  // namespace
+
+size_t ciphertext_message_len(const Params& par, size_t level, size_t parts, bool seeded, bool avt) {
+  const Context& c = *par.ctx(level);
+  const size_t rq = rq_message_len(c, avt);
+  const size_t stored = parts - (seeded ? 1 : 0);
+  return stored * (1 + varint_len(rq) + rq) + (seeded ? 34 : 0) + (level ? 1 + varint_len(level) : 0);
+}
+
+void ciphertext_to_bytes(const Params& par, size_t level, size_t parts, const uint64_t* ct, uint64_t count,
+                         const uint8_t* seeds, bool avt, uint8_t* out, Workspace& ws, cudaStream_t st) {
+  if (parts < 1 || (seeds && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
+  if (count == 0) return;
+  const Context& c = *par.ctx(level);
+  const size_t L = c.L(), N = c.N(), stored = parts - (seeds ? 1 : 0);
+  const size_t payload = poly_serialized_bytes(c);
+  const size_t polys = count * stored;
+  ws.reserve((polys * L * N + (polys * payload + 7) / 8 + 64) * 8);
+  size_t off = 0;
+  uint64_t* tmp = ws.take(polys * L * N, &off);
+  uint8_t* packed = reinterpret_cast<uint8_t*>(ws.take((polys * payload + 7) / 8, &off));
+  pack_polys(c, 1, sub_ref(const_cast<uint64_t*>(ct), L, c.logn, (uint32_t)parts, 0, (uint32_t)stored), packed,
+             polys, tmp, st);
+  std::vector<uint8_t> h(polys * payload);
+  check_cuda(cudaMemcpyAsync(h.data(), packed, h.size(), cudaMemcpyDeviceToHost, st), "D2H");
+  check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  const size_t rq = rq_message_len(c, avt);
+  uint8_t* o = out;
+  for (uint64_t b = 0; b < count; b++) {
+    for (size_t k = 0; k < stored; k++) {
+      *o++ = 0x0a;  // c
+      o = put_varint(o, rq);
+      o = put_rq(o, c, 1, h.data() + (b * stored + k) * payload, avt);
+    }
+    if (seeds) {
+      *o++ = 0x12;  // seed
+      *o++ = 32;
+      std::memcpy(o, seeds + 32 * b, 32);
+      o += 32;
+    }
+    if (level) {
+      *o++ = 0x18;  // level
+      o = put_varint(o, level);
+    }
+  }
+}
+
+void ciphertext_peek(const Params& par, const uint8_t* msg, size_t len, size_t* level, size_t* parts, int* seeded) {
+  const CtMessage m = parse_ct(msg, len);
+  check_ct(par, m);
+  *level = (size_t)m.level;
+  *parts = m.c.size() + (m.seed.n ? 1 : 0);
+  *seeded = m.seed.n ? 1 : 0;
+}
+
+void ciphertext_from_bytes(const Params& par, const uint8_t* const* msgs, const size_t* lens, uint64_t count,
+                           size_t level, size_t parts, uint64_t* out, Workspace& ws, Workspace& seed_ws,
+                           cudaStream_t st) {
+  if (count == 0) return;
+  const Context& c = *par.ctx(level);
+  const size_t L = c.L(), N = c.N(), payload = poly_serialized_bytes(c);
+  std::vector<CtMessage> m(count);
+  for (uint64_t b = 0; b < count; b++) {
+    if (!msgs[b]) throw Error(FHEG_ERR_INVALID_ARGUMENT, "null message");
+    m[b] = parse_ct(msgs[b], lens[b]);
+    check_ct(par, m[b]);
+    if (m[b].level != level || m[b].c.size() + (m[b].seed.n ? 1 : 0) != parts)
+      throw Error(FHEG_ERR_INVALID_ARGUMENT, "message of another level or part count than the batch");
+    if ((m[b].seed.n != 0) != (m[0].seed.n != 0))
+      throw Error(FHEG_ERR_INVALID_ARGUMENT, "a batch mixes seeded and unseeded ciphertexts");
+  }
+  const bool seeded = m[0].seed.n != 0;
+  const size_t stored = parts - (seeded ? 1 : 0);
+  std::vector<uint8_t> h(count * stored * payload + (seeded ? 32 * count : 0));
+  for (uint64_t b = 0; b < count; b++) {
+    for (size_t k = 0; k < stored; k++) {
+      const Span pl = parse_rq(m[b].c[k], c, 1);
+      std::memcpy(h.data() + (b * stored + k) * payload, pl.p, payload);
+    }
+    if (seeded) std::memcpy(h.data() + count * stored * payload + 32 * b, m[b].seed.p, 32);
+  }
+  ws.reserve((h.size() + 7) / 8 * 8 + 512);
+  size_t off = 0;
+  uint8_t* d = reinterpret_cast<uint8_t*>(ws.take((h.size() + 7) / 8, &off));
+  check_cuda(cudaMemcpyAsync(d, h.data(), h.size(), cudaMemcpyHostToDevice, st), "H2D");
+  unpack_polys(c, 1, d, sub_ref(out, L, c.logn, (uint32_t)parts, 0, (uint32_t)stored), count * stored, st);
+  if (seeded)
+    poly_random_from_seed(c, d + count * stored * payload, out + (parts - 1) * L * N, parts * L * N, count, seed_ws,
+                          st);
+  // The pageable source buffer must outlive the copy.
+  check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
 }
 
 }  // namespace fheg
@@ -199,5 +471,49 @@ FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, 
     need(ctx && (representation == 0 || representation == 1), "bad context or representation");
     need((d_polys && d_bytes) || !count, "null input");
     poly_deserialize(*ctx->c, representation, d_bytes, d_polys, count, static_cast<cudaStream_t>(stream));
+  });
+}
+
+FHEG_API int fheg_ciphertext_serialized_size(const fheg_params* par, size_t level, size_t parts, int seeded,
+                                             int allow_variable_time, size_t* bytes) {
+  return guarded([&] {
+    need(par && bytes, "null input");
+    if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    if (parts < 1 || (seeded && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
+    *bytes = ciphertext_message_len(*par->p, level, parts, seeded != 0, allow_variable_time != 0);
+  });
+}
+
+FHEG_API int fheg_ciphertext_to_bytes(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_ct,
+                                      size_t count, const uint8_t* h_seeds, int allow_variable_time, uint8_t* h_out,
+                                      size_t out_capacity, void* stream) {
+  return guarded([&] {
+    need(par && ((d_ct && h_out) || !count), "null input");
+    if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    if (parts < 1 || (h_seeds && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
+    const size_t one = ciphertext_message_len(*par->p, level, parts, h_seeds != nullptr, allow_variable_time != 0);
+    need(out_capacity >= count * one, "output buffer too small");
+    ciphertext_to_bytes(*par->p, level, parts, d_ct, count, h_seeds, allow_variable_time != 0, h_out,
+                        const_cast<fheg_params*>(par)->ws, static_cast<cudaStream_t>(stream));
+  });
+}
+
+FHEG_API int fheg_ciphertext_peek(const fheg_params* par, const uint8_t* h_msg, size_t len, size_t* level,
+                                  size_t* parts, int* seeded) {
+  return guarded([&] {
+    need(par && h_msg && level && parts && seeded, "null input");
+    ciphertext_peek(*par->p, h_msg, len, level, parts, seeded);
+  });
+}
+
+FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* const* h_msgs, const size_t* lens,
+                                        size_t count, size_t level, size_t parts, uint64_t* d_out, void* stream) {
+  return guarded([&] {
+    need(par && ((h_msgs && lens && d_out) || !count), "null input");
+    if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+    if (parts < 2) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
+    fheg_params* p = const_cast<fheg_params*>(par);
+    ciphertext_from_bytes(*p->p, h_msgs, lens, count, level, parts, d_out, p->ws, *p->level_handles[level].ws,
+                          static_cast<cudaStream_t>(stream));
   });
 }

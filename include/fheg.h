@@ -442,6 +442,42 @@ FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, 
                                    void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Ciphertext messages (bfv.proto `Ciphertext` holding rq.proto `Rq` parts,   */
+/* encoded as the reference's prost encoding does: fields in tag order,       */
+/* proto3 defaults left out).                                                 */
+
+/* Bytes of one message from fheg_ciphertext_to_bytes: `parts` polynomials at
+ * `level`; seeded != 0 when the last part is replaced by its 32-byte seed;
+ * allow_variable_time is the Rq flag written for every part. */
+FHEG_API int fheg_ciphertext_serialized_size(const fheg_params* par, size_t level, size_t parts, int seeded,
+                                             int allow_variable_time, size_t* bytes);
+/* Ciphertext::to_bytes (fhe/src/bfv/ciphertext.rs:164-191,
+ * fhe-math/src/rq/convert.rs:17-42) for d_ct [count][parts][L][N] (Ntt):
+ * h_out receives `count` messages of fheg_ciphertext_serialized_size bytes,
+ * back to back. h_seeds (nullable) [count][32] are the seeds of the last
+ * parts (Ciphertext::seed), written in place of those parts. Returns once
+ * h_out is written. Uses the parameters' scratch region. */
+FHEG_API int fheg_ciphertext_to_bytes(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_ct,
+                                      size_t count, const uint8_t* h_seeds, int allow_variable_time,
+                                      uint8_t* h_out, size_t out_capacity, void* stream);
+/* Level, number of parts and seededness of one message, with the
+ * reference's checks (ciphertext.rs:196-216: "Not enough polynomials" ->
+ * FHEG_ERR_WRONG_PARTS, a level above the maximum -> FHEG_ERR_INVALID_LEVEL,
+ * a seed of another length than 32 bytes). No device work. */
+FHEG_API int fheg_ciphertext_peek(const fheg_params* par, const uint8_t* h_msg, size_t len, size_t* level,
+                                  size_t* parts, int* seeded);
+/* Ciphertext::from_bytes (ciphertext.rs:195-240, rq/convert.rs:44-135) for
+ * `count` messages h_msgs[b] of lens[b] bytes that all decode to `level` and
+ * `parts` and are all seeded or all unseeded (fheg_ciphertext_peek tells):
+ * d_out [count][parts][L][N] (Ntt). Payloads are unpacked and transformed on
+ * the device and seeded last parts expanded there (Poly::random_from_seed).
+ * Rq errors: representation other than Ntt, degree not a multiple of 8 or
+ * not the context's, payload of the wrong length -> FHEG_ERR_INVALID_ARGUMENT.
+ * Returns once the messages may be freed. Uses the parameters' scratch. */
+FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* const* h_msgs, const size_t* lens,
+                                        size_t count, size_t level, size_t parts, uint64_t* d_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */
 
 /* Records Multiplicator::multiply for fixed device buffers (d_lhs, d_rhs:

@@ -1758,3 +1758,128 @@ def rq_from_payload(ctx: Context, payload: bytes, representation: str) -> "Poly"
     if representation != POWER_BASIS:
         p.into_ntt()
     return p
+
+
+# ---------------------------------------------------------------------------
+# Protobuf framing (prost 0.14 encoding of rq.proto / bfv.proto): fields in
+# tag order, proto3 defaults (0, false, empty) omitted, every element of a
+# repeated bytes field written. Restated from the published wire format:
+# varints of 7 bits per byte (low groups first), keys (field << 3) | type,
+# type 0 = varint, 2 = length-delimited.
+
+REPRESENTATION_CODE = {POWER_BASIS: 1, NTT: 2, NTT_SHOUP: 3}
+
+
+def _varint(v: int) -> bytes:
+    out = bytearray()
+    while True:
+        b = v & 0x7F
+        v >>= 7
+        if v:
+            out.append(b | 0x80)
+        else:
+            out.append(b)
+            return bytes(out)
+
+
+def _pb_varint(field: int, v: int) -> bytes:
+    return b"" if v == 0 else _varint(field << 3) + _varint(v)
+
+
+def _pb_bytes(field: int, b: bytes, repeated: bool = False) -> bytes:
+    if not b and not repeated:
+        return b""
+    return _varint((field << 3) | 2) + _varint(len(b)) + bytes(b)
+
+
+def rq_message(p: "Poly", allow_variable_time: bool = False) -> bytes:
+    """rq/convert.rs:17-42 (`Rq::from(&Poly)`) then `encode_to_vec`."""
+    return (_pb_varint(1, REPRESENTATION_CODE[p.representation]) + _pb_varint(2, p.ctx.degree) +
+            _pb_bytes(3, rq_payload(p)) + _pb_varint(4, int(allow_variable_time)))
+
+
+def ciphertext_message(ct: "Ciphertext", seed: Optional[bytes] = None, allow_variable_time: bool = False) -> bytes:
+    """fhe/src/bfv/ciphertext.rs:164-191: every part but the last as an Rq
+    message, the last one too unless the ciphertext carries its seed."""
+    polys = ct.c[:-1] if seed else ct.c
+    out = b"".join(_pb_bytes(1, rq_message(p, allow_variable_time), repeated=True) for p in polys)
+    if seed:
+        out += _pb_bytes(2, seed)
+    return out + _pb_varint(3, ct.level)
+
+
+def parse_fields(b: bytes) -> List[tuple]:
+    """(field, wire type, value) of a message: ints for varints, bytes for
+    length-delimited fields (fixed32 / fixed64 values as bytes)."""
+    out, i = [], 0
+
+    def varint():
+        nonlocal i
+        v, shift = 0, 0
+        while True:
+            if i >= len(b) or shift > 63:
+                raise ValueError("truncated varint")
+            c = b[i]
+            i += 1
+            v |= (c & 0x7F) << shift
+            shift += 7
+            if not c & 0x80:
+                return v
+
+    while i < len(b):
+        key = varint()
+        field, wt = key >> 3, key & 7
+        if wt == 0:
+            out.append((field, wt, varint()))
+        elif wt == 2:
+            n = varint()
+            if i + n > len(b):
+                raise ValueError("truncated field")
+            out.append((field, wt, bytes(b[i:i + n])))
+            i += n
+        elif wt == 1:
+            out.append((field, wt, bytes(b[i:i + 8])))
+            i += 8
+        elif wt == 5:
+            out.append((field, wt, bytes(b[i:i + 4])))
+            i += 4
+        else:
+            raise ValueError("unsupported wire type")
+    return out
+
+
+def ciphertext_from_message(par: "BfvParameters", b: bytes) -> "Ciphertext":
+    """fhe/src/bfv/ciphertext.rs:195-240 `TryConvertFrom<&CiphertextProto>`."""
+    cs, seed, level = [], b"", 0
+    for f, wt, v in parse_fields(b):
+        if f == 1 and wt == 2:
+            cs.append(v)
+        elif f == 2 and wt == 2:
+            seed = v
+        elif f == 3 and wt == 0:
+            level = v & 0xFFFFFFFF
+    if not cs or (len(cs) == 1 and not seed):
+        raise ValueError("Not enough polynomials")
+    if level > par.max_level():
+        raise ValueError("InvalidLevel")
+    ctx = par.context_at_level(level)
+    polys = []
+    for m in cs:
+        rep, degree, coeffs = 0, 0, b""
+        for f, wt, v in parse_fields(m):
+            if f == 1 and wt == 0:
+                rep = v
+            elif f == 2 and wt == 0:
+                degree = v
+            elif f == 3 and wt == 2:
+                coeffs = v
+        if rep != REPRESENTATION_CODE[NTT]:
+            raise ValueError("representation")
+        if degree != ctx.degree or len(coeffs) != sum((degree * modulus_nbits(q) + 7) // 8 for q in ctx.moduli):
+            raise ValueError("Invalid coefficients")
+        polys.append(rq_from_payload(ctx, coeffs, NTT))
+    if seed:
+        if len(seed) != 32:
+            raise ValueError("InvalidSeedSize")
+        polys.append(Poly(ctx, random_from_seed(ctx, seed), NTT))
+    return Ciphertext(par, polys, level)

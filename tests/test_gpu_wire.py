@@ -1,0 +1,87 @@
+"""Ciphertext messages on the GPU path (bfv.proto Ciphertext of rq.proto Rq
+parts, fhe/src/bfv/ciphertext.rs:164-240, fhe-math/src/rq/convert.rs:17-135):
+the bytes equal the oracle's prost-equivalent encoding, decoding gives the
+oracle's polynomials, seeded messages expand their last part on the device,
+and malformed messages fail with the reference's error kinds."""
+
+import numpy as np
+import pytest
+
+from test_gpu_bfv import Setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,L,t", [(16, 3, 1153), (4096, 3, 65537), (16384, 6, 65537)])
+def test_ciphertext_bytes_match_oracle(fg, ora, cuda, n, L, t):
+    s = Setup(fg, ora, n, L, t, seed=3 * n + L)
+    for level in (0, 1):
+        ctx = s.par_o.context_at_level(level)
+        _, cts = s.encrypt(3, level=level)
+        seeds = [bytes(s.rng.integers(0, 256, 32, dtype=np.uint8)) for _ in cts]
+        for b, sd in enumerate(seeds):
+            cts[b].c[1] = ora.Poly(ctx, ora.random_from_seed(ctx, sd), ora.NTT)
+        dev = fg.to_device(np.stack([c.to_array() for c in cts]))
+        for seeded in (False, True):
+            for avt in (False, True):
+                got = fg.ciphertext_to_bytes(s.par, level, dev, seeds if seeded else None, avt)
+                for b, c in enumerate(cts):
+                    assert got[b] == ora.ciphertext_message(c, seeds[b] if seeded else None, avt), (level, b)
+                assert fg.ciphertext_peek(s.par, got[0]) == (level, 2, seeded)
+                back = fg.to_host(fg.ciphertext_from_bytes(s.par, got))
+                assert np.array_equal(back, fg.to_host(dev)), (level, seeded, avt)
+
+
+def test_three_part_and_oracle_messages(fg, ora, cuda):
+    """Messages written by the oracle decode on the device, including a 3-part
+    (unrelinearized) product at level 1."""
+    s = Setup(fg, ora, 4096, 3, 65537, seed=77)
+    vals, cts = s.encrypt(2, level=1)
+    ext = ora.Multiplicator.default_extended_basis(s.par_o, 1)
+    q = s.par_o.context_at_level(1).modulus()
+    mo3 = ora.Multiplicator(ora.ScalingFactor.one(), ora.ScalingFactor.one(), ext, ora.ScalingFactor(65537, q), 1,
+                            s.par_o)
+    prod = mo3.multiply(cts[0], cts[1])
+    msg = ora.ciphertext_message(prod)
+    assert fg.ciphertext_peek(s.par, msg) == (1, 3, False)
+    got = fg.to_host(fg.ciphertext_from_bytes(s.par, [msg, msg]))
+    assert np.array_equal(got[1], prod.to_array())
+    assert fg.ciphertext_to_bytes(s.par, 1, fg.to_device(prod.to_array()[None]))[0] == msg
+    # Unknown fields are skipped, fields may come in any order.
+    reordered = ora._pb_varint(3, 1) + ora._pb_varint(9, 5) + msg[:msg.rfind(b"\x18")]
+    assert np.array_equal(fg.to_host(fg.ciphertext_from_bytes(s.par, [reordered]))[0], prod.to_array())
+
+
+def test_ciphertext_bytes_errors(fg, ora, cuda):
+    s = Setup(fg, ora, 16, 3, 1153, seed=5)
+    _, cts = s.encrypt(1)
+    ct = cts[0]
+    good = ora.ciphertext_message(ct)
+
+    def code(msg, batch=None):
+        with pytest.raises(fg.FhegError) as e:
+            if batch is None:
+                fg.ciphertext_peek(s.par, msg)
+                fg.ciphertext_from_bytes(s.par, [msg])
+            else:
+                fg.ciphertext_from_bytes(s.par, batch)
+        return e.value.code
+
+    rq = ora.rq_message(ct[0])
+    assert code(ora._pb_bytes(1, rq, repeated=True)) == fg.ERR_WRONG_PARTS  # one part, no seed
+    assert code(b"") == fg.ERR_WRONG_PARTS
+    assert code(good + ora._pb_varint(3, 7)) == fg.ERR_INVALID_LEVEL
+    assert code(ora._pb_bytes(1, rq, repeated=True) + ora._pb_bytes(2, bytes(31))) == fg.ERR_INVALID_ARGUMENT
+    assert code(good[:-3]) == fg.ERR_INVALID_ARGUMENT  # truncated
+    pb = ct[0].copy().into_power_basis()
+    bad_rep = ora._pb_bytes(1, ora.rq_message(pb), repeated=True) * 2
+    assert code(bad_rep) == fg.ERR_INVALID_ARGUMENT
+    no_rep = ora._pb_bytes(1, rq[2:], repeated=True) * 2  # representation field dropped: Unknown
+    assert code(no_rep) == fg.ERR_INVALID_ARGUMENT
+    bad_deg = ora._pb_bytes(1, b"\x08\x02\x10\x20" + rq[4:], repeated=True) * 2  # degree 32
+    assert code(bad_deg) == fg.ERR_INVALID_ARGUMENT
+    short = ora._pb_bytes(1, ora._pb_varint(1, 2) + ora._pb_varint(2, 16) + ora._pb_bytes(3, bytes(10)),
+                          repeated=True) * 2
+    assert code(short) == fg.ERR_INVALID_ARGUMENT
+    seeded = ora.ciphertext_message(ct, bytes(32))
+    assert code(None, batch=[good, seeded]) == fg.ERR_INVALID_ARGUMENT  # mixed batch

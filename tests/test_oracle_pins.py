@@ -356,3 +356,58 @@ def test_random_from_seed(ora):
     assert [int(v) for v in b[0]] == vals
     vals = [(draws[pos + k] * ctx.moduli[0]) >> 64 for k in range(16)]
     assert [int(v) for v in b[1]] == vals
+
+
+def _proto_classes():
+    """rq.proto Rq and bfv.proto Ciphertext as dynamic message classes of the
+    `protobuf` package (no protoc needed)."""
+    descriptor_pb2 = pytest.importorskip("google.protobuf.descriptor_pb2")
+    from google.protobuf import descriptor_pool, message_factory
+    F = descriptor_pb2.FieldDescriptorProto
+    fd = descriptor_pb2.FileDescriptorProto(name="fheg_wire_pin.proto", package="pin", syntax="proto3")
+    enum = fd.enum_type.add(name="Representation")
+    for name, num in [("UNKNOWN", 0), ("POWERBASIS", 1), ("NTT", 2), ("NTTSHOUP", 3)]:
+        enum.value.add(name=name, number=num)
+    rq = fd.message_type.add(name="Rq")
+    rq.field.add(name="representation", number=1, type=F.TYPE_ENUM, type_name=".pin.Representation",
+                 label=F.LABEL_OPTIONAL)
+    rq.field.add(name="degree", number=2, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    rq.field.add(name="coefficients", number=3, type=F.TYPE_BYTES, label=F.LABEL_OPTIONAL)
+    rq.field.add(name="allow_variable_time", number=4, type=F.TYPE_BOOL, label=F.LABEL_OPTIONAL)
+    ct = fd.message_type.add(name="Ciphertext")
+    ct.field.add(name="c", number=1, type=F.TYPE_BYTES, label=F.LABEL_REPEATED)
+    ct.field.add(name="seed", number=2, type=F.TYPE_BYTES, label=F.LABEL_OPTIONAL)
+    ct.field.add(name="level", number=3, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    pool = descriptor_pool.DescriptorPool()
+    pool.Add(fd)
+    get = message_factory.GetMessageClass
+    return get(pool.FindMessageTypeByName("pin.Rq")), get(pool.FindMessageTypeByName("pin.Ciphertext"))
+
+
+def test_protobuf_framing_pinned(ora):
+    """The oracle's Rq / Ciphertext encoding equals the protobuf package's for
+    the same field values (seeded and unseeded, levels 0 and 1, the variable
+    time flag), and its decoder inverts it."""
+    Rq, Ct = _proto_classes()
+    rng = np.random.default_rng(41)
+    par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3)
+    sk = ora.SecretKey.random(par, rng)
+    for level in (0, 1):
+        ctx = par.context_at_level(level)
+        pt = ora.Plaintext.encode(rng.integers(0, 1153, 16, dtype=np.uint64), "simd", par, level)
+        ct = sk.encrypt(pt, rng)
+        for seed in (None, bytes(range(32))):
+            if seed:
+                ct.c[1] = ora.Poly(ctx, ora.random_from_seed(ctx, seed), ora.NTT)
+            for avt in (False, True):
+                got = ora.ciphertext_message(ct, seed, avt)
+                want = Ct(c=[Rq(representation=2, degree=16, coefficients=ora.rq_payload(p),
+                                allow_variable_time=avt).SerializeToString() for p in (ct.c[:1] if seed else ct.c)],
+                          seed=seed or b"", level=level).SerializeToString()
+                assert got == want, (level, seed is not None, avt)
+                back = ora.ciphertext_from_message(par, got)
+                assert back.level == level and np.array_equal(back.to_array(), ct.to_array())
+    # Multi-byte varints: a degree of 2^14 and payloads over 127 bytes.
+    assert ora._varint(16384) == b"\x80\x80\x01" and ora._varint(300) == b"\xac\x02"
+    with pytest.raises(ValueError):
+        ora.ciphertext_from_message(par, ora._pb_bytes(1, b"\x08\x02", repeated=True))
