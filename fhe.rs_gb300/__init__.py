@@ -109,6 +109,8 @@ def _declare(L):
         "fheg_ksk_destroy": (None, [c_vp]),
         "fheg_ksk_create_seeded": (i, [c_vp, c_size, c_size, P_u64, ctypes.c_char_p, c_size, ctypes.POINTER(c_vp)]),
         "fheg_poly_random_from_seed": (i, [c_vp, c_vp, c_vp, c_size, c_size, c_vp]),
+        "fheg_ksk_from_bytes": (i, [c_vp, ctypes.c_char_p, c_size, i, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
+                                    ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
         "fheg_ciphertext_serialized_size": (i, [c_vp, c_size, c_size, i, i, ctypes.POINTER(c_size)]),
         "fheg_ciphertext_to_bytes": (i, [c_vp, c_size, c_size, c_vp, c_size, ctypes.c_char_p, i, c_vp, c_size, c_vp]),
         "fheg_ciphertext_peek": (i, [c_vp, ctypes.c_char_p, c_size, ctypes.POINTER(c_size), ctypes.POINTER(c_size),
@@ -597,6 +599,22 @@ class KeySwitchingKey:
                                     ctypes.byref(h)))
         self._h = h
 
+    KIND = 0  # message kind of fheg_ksk_from_bytes
+
+    @classmethod
+    def from_bytes(cls, par: BfvParameters, msg: bytes):
+        """KeySwitchingKey / RelinearizationKey / GaloisKey::from_bytes
+        (key_switching_key.rs:354-420): the key as the reference serialized it."""
+        h, e, cl, kl = c_vp(), c_size(0), c_size(0), c_size(0)
+        check(lib().fheg_ksk_from_bytes(par._h, bytes(msg), len(msg), cls.KIND, ctypes.byref(h), ctypes.byref(e),
+                                        ctypes.byref(cl), ctypes.byref(kl)))
+        k = cls.__new__(cls)
+        k.par, k._h = par, h
+        k.ciphertext_level, k.ksk_level = cl.value, kl.value
+        if cls.KIND == 2:
+            k.exponent = e.value
+        return k
+
     @classmethod
     def from_seed(cls, par: BfvParameters, c0: np.ndarray, seed: bytes, ciphertext_level: int = 0,
                   ksk_level: int = 0, **kw):
@@ -625,6 +643,8 @@ class KeySwitchingKey:
 class RelinearizationKey(KeySwitchingKey):
     """bfv::RelinearizationKey (fhe/src/bfv/keys/relinearization_key.rs)."""
 
+    KIND = 1
+
     def relinearizes(self, ct3):
         """relinearization_key.rs:71-98 on a batch [count][3][L][N]."""
         ctx = self.par.context_at_level(self.ciphertext_level)
@@ -638,6 +658,8 @@ class RelinearizationKey(KeySwitchingKey):
 
 class GaloisKey(KeySwitchingKey):
     """GaloisKey (fhe/src/bfv/keys/galois_key.rs) for one exponent."""
+
+    KIND = 2
 
     def __init__(self, par, exponent: int, c0, c1, ciphertext_level: int = 0, ksk_level: int = 0):
         super().__init__(par, c0, c1, ciphertext_level, ksk_level)

@@ -550,9 +550,9 @@ FHEG_API int fheg_params_context_at_level(const fheg_params* par, size_t level, 
 
 FHEG_API size_t fheg_params_max_level(const fheg_params* par) { return par ? par->p->max_level() : 0; }
 
-// A key-switching key with its c0 uploaded and room for c1 (shared by the
-// plain and the seeded constructors).
-static fheg_ksk* new_ksk(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
+// A key-switching key with room for c0 and c1, c0 uploaded from h_c0 unless
+// it is null (shared by the plain, seeded and message constructors).
+fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
                          size_t count) {
   const Params& p = *par->p;
   if (ciphertext_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
@@ -570,7 +570,7 @@ static fheg_ksk* new_ksk(const fheg_params* par, size_t ciphertext_level, size_t
     k.count = count;
     const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
     k.keys.alloc(2 * words * 8);
-    upload(k.values(0), h_c0, words * 8);
+    if (h_c0) upload(k.values(0), h_c0, words * 8);
   } catch (...) {
     delete h;
     throw;
@@ -582,7 +582,7 @@ FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, si
                              const uint64_t* h_c1, size_t count, fheg_ksk** out) {
   return guard([&] {
     need(par && h_c0 && h_c1 && out, "null input");
-    fheg_ksk* h = new_ksk(par, ciphertext_level, ksk_level, h_c0, count);
+    fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
       const Ksk& k = h->k;
       upload(k.values(1), h_c1, count * k.ctx_ksk->L() * k.ctx_ksk->N() * 8);
@@ -598,7 +598,7 @@ FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_le
                                     const uint64_t* h_c0, const uint8_t* seed, size_t count, fheg_ksk** out) {
   return guard([&] {
     need(par && h_c0 && seed && out, "null input");
-    fheg_ksk* h = new_ksk(par, ciphertext_level, ksk_level, h_c0, count);
+    fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
       const Ksk& k = h->k;
       const std::vector<uint8_t> seeds = ksk_c1_seeds(seed, count);

@@ -41,3 +41,8 @@ struct fheg_secret_key {
   fheg::SecretKeyDev k;
   mutable fheg::Workspace ws;  // scratch of fheg_decrypt
 };
+
+// A key-switching key at the given levels with device room for `count`
+// digits; c0 is uploaded from h_c0 unless it is null (api.cu).
+fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
+                         size_t count);

@@ -276,9 +276,10 @@ uint8_t* put_rq(uint8_t* o, const Context& c, int representation, const uint8_t*
   return o;
 }
 
-// The payload of one Rq message for a polynomial over `c` in `representation`
-// (convert.rs:44-135, parse_proto and TryConvertFrom<&Rq>).
-Span parse_rq(Span m, const Context& c, int representation) {
+// The payload of one Rq message for a polynomial over `c` whose rq.proto
+// representation must be `code` (convert.rs:44-135, parse_proto and
+// TryConvertFrom<&Rq>).
+Span parse_rq_code(Span m, const Context& c, uint64_t code) {
   Reader r{m.p, m.p + m.n, "Rq"};
   uint64_t repr = 0, degree = 0;
   Span coeffs;
@@ -292,7 +293,7 @@ Span parse_rq(Span m, const Context& c, int representation) {
   const int32_t rep = (int32_t)(uint32_t)repr;
   if (rep < 0 || rep > 3) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid representation");
   if (rep == 0) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Unknown representation");
-  if ((uint64_t)rep != kReprCode[representation])
+  if ((uint64_t)rep != code)
     throw Error(FHEG_ERR_INVALID_ARGUMENT,
                 "The representation asked for does not match the representation in the serialization");
   if (degree % 8 != 0 || degree < 8) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid degree");
@@ -300,6 +301,8 @@ Span parse_rq(Span m, const Context& c, int representation) {
   if (coeffs.n != poly_serialized_bytes(c)) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid coefficients");
   return coeffs;
 }
+
+Span parse_rq(Span m, const Context& c, int representation) { return parse_rq_code(m, c, kReprCode[representation]); }
 
 struct CtMessage {
   std::vector<Span> c;
@@ -420,6 +423,88 @@ void ciphertext_from_bytes(const Params& par, const uint8_t* const* msgs, const 
   check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
 }
 
+// KeySwitchingKey messages (bfv.proto; key_switching_key.rs:332-420): c0[i]
+// (and c1[i] unless the key carries its seed) as NttShoup Rq messages over the
+// key context, then the levels and the decomposition base. Wrapped in
+// RelinearizationKey { ksk = 1 } or GaloisKey { ksk = 1, exponent = 2 }
+// (relinearization_key.rs:109-127, galois_key.rs:127-149).
+fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t len, int kind, uint64_t* exponent) {
+  const Params& p = *par->p;
+  Span ksk{msg, len};
+  uint64_t exp = 0;
+  if (kind != 0) {
+    Reader r{msg, msg + len, kind == 1 ? "RelinearizationKey" : "GaloisKey"};
+    bool found = false;
+    Field f;
+    while (r.next(f)) {
+      if (f.num == 1) r.expect(f, 2), ksk = f.bytes, found = true;
+      else if (f.num == 2 && kind == 2) r.expect(f, 0), exp = f.value & 0xffffffffu;
+    }
+    if (!found) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid serialization");
+  }
+  std::vector<Span> c0, c1;
+  Span seed;
+  uint64_t ct_level = 0, ksk_level = 0, log_base = 0;
+  {
+    Reader r{ksk.p, ksk.p + ksk.n, "KeySwitchingKey"};
+    Field f;
+    while (r.next(f)) {
+      if (f.num == 1) r.expect(f, 2), c0.push_back(f.bytes);
+      else if (f.num == 2) r.expect(f, 2), c1.push_back(f.bytes);
+      else if (f.num == 3) r.expect(f, 2), seed = f.bytes;
+      else if (f.num == 4) r.expect(f, 0), ct_level = f.value & 0xffffffffu;
+      else if (f.num == 5) r.expect(f, 0), ksk_level = f.value & 0xffffffffu;
+      else if (f.num == 6) r.expect(f, 0), log_base = f.value & 0xffffffffu;
+    }
+  }
+  if (ct_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
+  if (log_base != 0)
+    throw Error(FHEG_ERR_UNSUPPORTED, "keys with a decomposition base (single-modulus key contexts) are not supported");
+  const size_t count = p.ctx(ct_level)->L();
+  if (c0.size() != count) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incorrect number of values in c0");
+  if (seed.n == 0 && c1.size() != count) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incorrect number of values in c1");
+  if (seed.n != 0 && seed.n != 32) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid seed");
+  if (kind == 2) {
+    const uint64_t two_n = 2 * p.ctx(ct_level)->N();
+    if (exp % 2 == 0 || exp >= two_n)
+      throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid exponent");  // SubstitutionExponent::new
+  }
+  fheg_ksk* h = new_ksk_handle(par, ct_level, ksk_level, nullptr, count);
+  try {
+    const Ksk& k = h->k;
+    const Context& kc = *k.ctx_ksk;
+    const size_t payload = poly_serialized_bytes(kc);
+    const bool seeded = seed.n != 0;
+    std::vector<uint8_t> hb((seeded ? 1 : 2) * count * payload);
+    // NttShoup polynomials (representation 3): payloads in the power basis.
+    for (size_t i = 0; i < count; i++) {
+      std::memcpy(hb.data() + i * payload, parse_rq_code(c0[i], kc, 3).p, payload);
+      if (!seeded) std::memcpy(hb.data() + (count + i) * payload, parse_rq_code(c1[i], kc, 3).p, payload);
+    }
+    DevBuf d(hb.size());
+    upload(d.ptr, hb.data(), hb.size());
+    const uint8_t* db = static_cast<const uint8_t*>(d.ptr);
+    unpack_polys(kc, 1, db, plain_ref(k.values(0), kc.L(), kc.logn), count, nullptr);
+    if (seeded) {
+      const std::vector<uint8_t> seeds = ksk_c1_seeds(seed.p, count);
+      DevBuf ds(seeds.size());
+      upload(ds.ptr, seeds.data(), seeds.size());
+      Workspace ws;
+      poly_random_from_seed(kc, static_cast<const uint8_t*>(ds.ptr), k.values(1), kc.L() * kc.N(), count, ws,
+                            nullptr);
+      check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+    } else {
+      unpack_polys(kc, 1, db + count * payload, plain_ref(k.values(1), kc.L(), kc.logn), count, nullptr);
+    }
+    check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  if (exponent) *exponent = exp;
+  return h;
+}
+
 }  // namespace fheg
 
 using namespace fheg;
@@ -515,5 +600,18 @@ FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* c
     fheg_params* p = const_cast<fheg_params*>(par);
     ciphertext_from_bytes(*p->p, h_msgs, lens, count, level, parts, d_out, p->ws, *p->level_handles[level].ws,
                           static_cast<cudaStream_t>(stream));
+  });
+}
+
+FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len, int kind,
+                                 fheg_ksk** out, size_t* exponent, size_t* ciphertext_level, size_t* ksk_level) {
+  return guarded([&] {
+    need(par && h_msg && out && kind >= 0 && kind <= 2, "null input or bad kind");
+    uint64_t e = 0;
+    fheg_ksk* h = ksk_from_message(par, h_msg, len, kind, &e);
+    if (exponent) *exponent = (size_t)e;
+    if (ciphertext_level) *ciphertext_level = h->k.ciphertext_level;
+    if (ksk_level) *ksk_level = h->k.ksk_level;
+    *out = h;
   });
 }

@@ -477,6 +477,20 @@ FHEG_API int fheg_ciphertext_peek(const fheg_params* par, const uint8_t* h_msg, 
 FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* const* h_msgs, const size_t* lens,
                                         size_t count, size_t level, size_t parts, uint64_t* d_out, void* stream);
 
+/* KeySwitchingKey::from_bytes (fhe/src/bfv/keys/key_switching_key.rs:354-420)
+ * of a serialized key: kind 0 a bare KeySwitchingKey message, 1 a
+ * RelinearizationKey (relinearization_key.rs:109-127), 2 a GaloisKey
+ * (galois_key.rs:127-149; *exponent receives its exponent, which must be
+ * odd and below 2N). c0[i] and c1[i] are NttShoup Rq messages over the key
+ * context; a key that carries its seed has its c1 expanded on the device
+ * (generate_c1). Errors as the reference: wrong number of c0 / c1 values or
+ * a seed of another length -> FHEG_ERR_INVALID_ARGUMENT, levels above the
+ * maximum -> FHEG_ERR_INVALID_LEVEL; keys with a decomposition base
+ * (log_base != 0) -> FHEG_ERR_UNSUPPORTED. The key's levels are returned in
+ * *ciphertext_level and *ksk_level (each output nullable). */
+FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len, int kind,
+                                 fheg_ksk** out, size_t* exponent, size_t* ciphertext_level, size_t* ksk_level);
+
 /* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */
 

@@ -1883,3 +1883,26 @@ def ciphertext_from_message(par: "BfvParameters", b: bytes) -> "Ciphertext":
             raise ValueError("InvalidSeedSize")
         polys.append(Poly(ctx, random_from_seed(ctx, seed), NTT))
     return Ciphertext(par, polys, level)
+
+
+def ksk_message(ksk: "KeySwitchingKey", allow_variable_time: bool = True) -> bytes:
+    """fhe/src/bfv/keys/key_switching_key.rs:332-352: c0[i] (and c1[i] unless
+    the key has its seed) as NttShoup Rq messages, the seed, the levels and
+    the decomposition base (0 for RNS-digit keys)."""
+    seed = getattr(ksk, "seed", None)
+    out = b"".join(_pb_bytes(1, rq_message(p, allow_variable_time), repeated=True) for p in ksk.c0)
+    if seed is None:
+        out += b"".join(_pb_bytes(2, rq_message(p, allow_variable_time), repeated=True) for p in ksk.c1)
+    else:
+        out += _pb_bytes(3, seed)
+    return out + _pb_varint(4, ksk.ciphertext_level) + _pb_varint(5, ksk.ksk_level)
+
+
+def relinearization_key_message(rk: "RelinearizationKey") -> bytes:
+    """relinearization_key.rs:109-115: { ksk = 1 }."""
+    return _pb_bytes(1, ksk_message(rk.ksk), repeated=True)
+
+
+def galois_key_message(gk: "GaloisKey") -> bytes:
+    """galois_key.rs:127-134: { ksk = 1, exponent = 2 }."""
+    return _pb_bytes(1, ksk_message(gk.ksk), repeated=True) + _pb_varint(2, gk.element.exponent)

@@ -85,3 +85,54 @@ def test_ciphertext_bytes_errors(fg, ora, cuda):
     assert code(short) == fg.ERR_INVALID_ARGUMENT
     seeded = ora.ciphertext_message(ct, bytes(32))
     assert code(None, batch=[good, seeded]) == fg.ERR_INVALID_ARGUMENT  # mixed batch
+
+
+@pytest.mark.parametrize("n,L", [(16, 3), (4096, 3)])
+def test_key_messages(fg, ora, cuda, n, L):
+    """RelinearizationKey / GaloisKey / KeySwitchingKey::from_bytes
+    (key_switching_key.rs:354-420): keys decoded on the device from the
+    reference's messages, seeded or not, give the oracle's results."""
+    s = Setup(fg, ora, n, L, 65537 if n > 16 else 1153, seed=n + 7)
+    _, cts = s.encrypt(2)
+    lhs, rhs = (fg.to_device(c.to_array()[None]) for c in cts)
+    for seed in (None, bytes(range(5, 37))):
+        rk_o = ora.RelinearizationKey(s.sk, s.rng, seed=seed)
+        rk = fg.RelinearizationKey.from_bytes(s.par, ora.relinearization_key_message(rk_o))
+        assert (rk.ciphertext_level, rk.ksk_level) == (0, 0)
+        want = ora.Multiplicator.default(rk_o).multiply(cts[0], cts[1]).to_array()
+        assert np.array_equal(fg.to_host(fg.Multiplicator.default(rk).multiply(lhs, rhs))[0], want)
+        e = pow(3, 2, 2 * n)
+        gk_o = ora.GaloisKey(s.sk, e, 0, 0, s.rng, seed=seed)
+        gk = fg.GaloisKey.from_bytes(s.par, ora.galois_key_message(gk_o))
+        assert gk.exponent == e
+        got = fg.to_host(gk.relinearize(lhs))[0]
+        assert np.array_equal(got, gk_o.relinearize(cts[0]).to_array())
+        ksk = fg.KeySwitchingKey.from_bytes(s.par, ora.ksk_message(gk_o.ksk))
+        assert (ksk.ciphertext_level, ksk.ksk_level) == (0, 0)
+
+
+def test_key_message_errors(fg, ora, cuda):
+    s = Setup(fg, ora, 16, 3, 1153, seed=8)
+    gk_o = ora.GaloisKey(s.sk, 3, 0, 0, s.rng, seed=bytes(32))
+    k = gk_o.ksk
+    c0 = b"".join(ora._pb_bytes(1, ora.rq_message(p, True), repeated=True) for p in k.c0)
+    tail = ora._pb_bytes(3, bytes(32))
+
+    def code(msg, cls=fg.KeySwitchingKey):
+        with pytest.raises(fg.FhegError) as e:
+            cls.from_bytes(s.par, msg)
+        return e.value.code
+
+    assert code(c0[:len(c0) * 2 // 3] + tail) == fg.ERR_INVALID_ARGUMENT  # too few c0 / truncated
+    assert code(c0 + ora._pb_bytes(3, bytes(31))) == fg.ERR_INVALID_ARGUMENT  # seed length
+    assert code(c0) == fg.ERR_INVALID_ARGUMENT  # no c1 and no seed
+    assert code(c0 + tail + ora._pb_varint(4, 9)) == fg.ERR_INVALID_LEVEL
+    assert code(c0 + tail + ora._pb_varint(6, 30)) == fg.ERR_UNSUPPORTED  # decomposition base
+    ntt = b"".join(ora._pb_bytes(1, ora.rq_message(ora.Poly(p.ctx, p.coefficients, ora.NTT)), repeated=True)
+                   for p in k.c0)
+    assert code(ntt + tail) == fg.ERR_INVALID_ARGUMENT  # Ntt instead of NttShoup
+    assert code(b"", fg.RelinearizationKey) == fg.ERR_INVALID_ARGUMENT  # no ksk field
+    even = ora._pb_bytes(1, ora.ksk_message(k), repeated=True) + ora._pb_varint(2, 4)
+    assert code(even, fg.GaloisKey) == fg.ERR_INVALID_ARGUMENT
+    ok = fg.GaloisKey.from_bytes(s.par, ora.galois_key_message(gk_o))
+    assert ok.exponent == 3

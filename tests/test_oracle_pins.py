@@ -378,17 +378,27 @@ def _proto_classes():
     ct.field.add(name="c", number=1, type=F.TYPE_BYTES, label=F.LABEL_REPEATED)
     ct.field.add(name="seed", number=2, type=F.TYPE_BYTES, label=F.LABEL_OPTIONAL)
     ct.field.add(name="level", number=3, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    ksk = fd.message_type.add(name="KeySwitchingKey")
+    ksk.field.add(name="c0", number=1, type=F.TYPE_BYTES, label=F.LABEL_REPEATED)
+    ksk.field.add(name="c1", number=2, type=F.TYPE_BYTES, label=F.LABEL_REPEATED)
+    ksk.field.add(name="seed", number=3, type=F.TYPE_BYTES, label=F.LABEL_OPTIONAL)
+    for name, num in [("ciphertext_level", 4), ("ksk_level", 5), ("log_base", 6)]:
+        ksk.field.add(name=name, number=num, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    gk = fd.message_type.add(name="GaloisKey")
+    gk.field.add(name="ksk", number=1, type=F.TYPE_MESSAGE, type_name=".pin.KeySwitchingKey", label=F.LABEL_OPTIONAL)
+    gk.field.add(name="exponent", number=2, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
     pool = descriptor_pool.DescriptorPool()
     pool.Add(fd)
     get = message_factory.GetMessageClass
-    return get(pool.FindMessageTypeByName("pin.Rq")), get(pool.FindMessageTypeByName("pin.Ciphertext"))
+    return (get(pool.FindMessageTypeByName("pin.Rq")), get(pool.FindMessageTypeByName("pin.Ciphertext")),
+            get(pool.FindMessageTypeByName("pin.KeySwitchingKey")), get(pool.FindMessageTypeByName("pin.GaloisKey")))
 
 
 def test_protobuf_framing_pinned(ora):
     """The oracle's Rq / Ciphertext encoding equals the protobuf package's for
     the same field values (seeded and unseeded, levels 0 and 1, the variable
     time flag), and its decoder inverts it."""
-    Rq, Ct = _proto_classes()
+    Rq, Ct, _, _ = _proto_classes()
     rng = np.random.default_rng(41)
     par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3)
     sk = ora.SecretKey.random(par, rng)
@@ -411,3 +421,24 @@ def test_protobuf_framing_pinned(ora):
     assert ora._varint(16384) == b"\x80\x80\x01" and ora._varint(300) == b"\xac\x02"
     with pytest.raises(ValueError):
         ora.ciphertext_from_message(par, ora._pb_bytes(1, b"\x08\x02", repeated=True))
+
+
+def test_key_messages_pinned(ora):
+    """KeySwitchingKey / GaloisKey encoding (key_switching_key.rs:332-352,
+    galois_key.rs:127-134) equals the protobuf package's, seeded and not."""
+    Rq, _, Ksk, Gk = _proto_classes()
+    rng = np.random.default_rng(43)
+    par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3)
+    sk = ora.SecretKey.random(par, rng)
+
+    def rq(p):
+        return Rq(representation=3, degree=16, coefficients=ora.rq_payload(p), allow_variable_time=True)
+
+    for seed in (None, bytes(range(32))):
+        gk = ora.GaloisKey(sk, 3, 1, 0, rng, seed=seed)
+        k = gk.ksk
+        want = Ksk(c0=[rq(p).SerializeToString() for p in k.c0],
+                   c1=[] if seed else [rq(p).SerializeToString() for p in k.c1], seed=seed or b"",
+                   ciphertext_level=1, ksk_level=0)
+        assert ora.ksk_message(k) == want.SerializeToString()
+        assert ora.galois_key_message(gk) == Gk(ksk=want, exponent=3).SerializeToString()
