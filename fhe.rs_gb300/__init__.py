@@ -133,6 +133,7 @@ def _declare(L):
         "fheg_multiplicator_output_shape": (i, [c_vp, ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
         "fheg_multiplicator_multiply": (i, [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_multiplicator_multiply_host": (i, [c_vp, P_u64, P_u64, P_u64, c_size]),
+        "fheg_multiplicator_set_host_pipeline": (i, [c_vp, c_size, i]),
         "fheg_relinearize_noalloc": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_galois_relinearize_batch": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                               ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size, c_vp]),
@@ -964,6 +965,10 @@ class Multiplicator:
         check(lib().fheg_multiplicator_capture(self._h, _dp(lhs), _dp(rhs), _dp(out), lhs.shape[0],
                                                ctypes.byref(h)))
         return MultiplyGraph(h, [self, lhs, rhs, out])
+
+    def set_host_pipeline(self, chunk: int = 0, streams: int = 3):
+        """Chunk size (pairs, 0 = automatic) and stream count of multiply_host."""
+        check(lib().fheg_multiplicator_set_host_pipeline(self._h, chunk, streams))
 
     def multiply_host(self, lhs: np.ndarray, rhs: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
         """End to end from host arrays [count][2][L][N] (u64)."""

@@ -815,6 +815,14 @@ FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* 
   });
 }
 
+FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t chunk, int streams) {
+  return guard([&] {
+    need(m && streams >= 1 && streams <= fheg_multiplicator::kPipe, "null multiplicator or streams outside 1..4");
+    m->host_chunk = chunk;
+    m->host_streams = streams;
+  });
+}
+
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs, const uint64_t* h_rhs,
                                               uint64_t* h_out, size_t count) {
   return guard([&] {
@@ -829,25 +837,39 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     uint64_t* d_lhs = mm.staging.u64();
     uint64_t* d_rhs = d_lhs + in_words;
     uint64_t* d_out = d_rhs + in_words;
-    for (auto& s : m->pipe)
-      if (!s) check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
-    // Chunks of at least 16 pairs rotate over the pipeline's streams, so the
-    // copies of one chunk overlap the multiplication of another.
-    const size_t chunk = count >= 32 ? 16 : count;
+    const int ns = m->host_streams;
+    for (int k = 0; k < ns; k++)
+      if (!m->pipe[k]) check_cuda(cudaStreamCreateWithFlags(&m->pipe[k], cudaStreamNonBlocking), "stream");
+    // Chunks rotate over the pipeline's streams, so the copies of one chunk
+    // overlap the multiplication of others. The input copies of chunk i wait
+    // for those of chunk i-1: the host link carries one chunk at a time, and
+    // the first chunk's inputs arrive at full link speed. Small chunks (6
+    // pairs, run with the small-batch plan, three at a time) measured best
+    // on GB300 at 16 to 64 pairs: the fill and drain of the pipeline cost one
+    // small chunk's copies, and concurrent chunks keep the SMs busy.
+    const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 12 ? 6 : count);
+    const size_t nchunks = (count + chunk - 1) / chunk;
+    while (m->copied.size() < nchunks) {
+      cudaEvent_t e;
+      check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+      m->copied.push_back(e);
+    }
     const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * out_L * N;
-    int k = 0;
-    for (size_t first = 0; first < count; first += chunk, k = (k + 1) % fheg_multiplicator::kPipe) {
-      const size_t c = std::min(chunk, count - first);
+    for (size_t i = 0; i < nchunks; i++) {
+      const size_t first = i * chunk, c = std::min(chunk, count - first);
+      const int k = (int)(i % ns);
       cudaStream_t st = m->pipe[k];
+      if (i > 0) check_cuda(cudaStreamWaitEvent(st, m->copied[i - 1], 0), "cudaStreamWaitEvent");
       check_cuda(cudaMemcpyAsync(d_lhs + first * in_pair, h_lhs + first * in_pair, c * in_pair * 8,
                                  cudaMemcpyHostToDevice, st), "H2D");
       check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
                                  cudaMemcpyHostToDevice, st), "H2D");
+      check_cuda(cudaEventRecord(m->copied[i], st), "cudaEventRecord");
       mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
                   &m->pipe_ws[k]);
       check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
                                  cudaMemcpyDeviceToHost, st), "D2H");
     }
-    for (auto& s : m->pipe) check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    for (int k = 0; k < ns; k++) check_cuda(cudaStreamSynchronize(m->pipe[k]), "cudaStreamSynchronize");
   });
 }

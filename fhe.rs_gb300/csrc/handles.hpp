@@ -28,13 +28,17 @@ struct fheg_rgsw {
   fheg::Ksk k;  // count = 2L digits: ksk0's, then ksk1's
 };
 struct fheg_multiplicator {
-  static constexpr int kPipe = 3;  // streams of the host entry point's copy / compute pipeline
+  static constexpr int kPipe = 4;  // most streams of the host entry point's copy / compute pipeline
   std::unique_ptr<fheg::Multiplicator> m;
   cudaStream_t pipe[kPipe] = {};
   fheg::Workspace pipe_ws[kPipe];
+  std::vector<cudaEvent_t> copied;  // end of each chunk's input copies
+  size_t host_chunk = 0;            // pairs per chunk (0 = automatic)
+  int host_streams = 3;
   ~fheg_multiplicator() {
     for (auto& s : pipe)
       if (s) cudaStreamDestroy(s);
+    for (auto& e : copied) cudaEventDestroy(e);
   }
 };
 struct fheg_secret_key {

@@ -331,8 +331,15 @@ FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max
  * at a time, installs the fastest and returns it in plan[6] (may be NULL).
  * A count within the small-batch threshold tunes the small-batch plan. */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
-/* Same, end to end from host buffers: copies the inputs to the device,
- * multiplies, and copies the product back before returning. */
+/* Pipeline of fheg_multiplicator_multiply_host: `chunk` pairs per chunk
+ * (0 = automatic: 6 when count >= 12, else the whole call) rotating over
+ * `streams` streams (1..4, default 3), each with its own scratch. Changes
+ * only the overlap of copies and compute, never the results. No counterpart
+ * in the reference. */
+FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t chunk, int streams);
+/* Multiplicator::multiply end to end from host buffers (h_lhs, h_rhs
+ * [count][2][L][N], h_out the output shape): copies the inputs to the
+ * device, multiplies, and copies the product back before returning. */
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs,
                                               const uint64_t* h_rhs, uint64_t* h_out, size_t count);
 

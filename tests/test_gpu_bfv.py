@@ -161,6 +161,13 @@ def test_batched_equals_single_and_host(fg, ora, cuda):
         single = fg.to_host(m.multiply(fg.to_device(lhs[b:b + 1]), fg.to_device(rhs[b:b + 1])))
         assert np.array_equal(single[0], batched[b])
     assert np.array_equal(m.multiply_host(lhs, rhs), batched)
+    # Every pipeline shape (ragged last chunks, 1 to 4 streams) gives the same product.
+    for chunk, streams in [(1, 1), (2, 4), (4, 3), (5, 2), (0, 3)]:
+        m.set_host_pipeline(chunk, streams)
+        assert np.array_equal(m.multiply_host(lhs, rhs), batched), (chunk, streams)
+    for bad in (0, 5):
+        with pytest.raises(fg.FhegError):
+            m.set_host_pipeline(2, bad)
 
 
 @pytest.mark.parametrize("n,L", [(16, 3), (4096, 2), (32768, 4)])
