@@ -48,19 +48,21 @@ STAGE_LIMBS = {
     "G": L * L + 4 * L,              # read the digit NTTs, read + write c0, c1 (keys added per batch)
 }
 STAGE_KERNELS = {
-    "A": "k_ntt_inv (inverse NTT of the operands)",
+    "A": "k_ntt_inv<12> + k_ntt_inv_top<2> (inverse NTT of the operands)",
     "B": "k_rns_scale (basis extension 6 -> 7 new moduli)",
-    "C": "k_ntt_fwd (forward NTT of the extension limbs)",
-    "D": "k_ntt_inv<SrcTensor> (tensor product + inverse NTT, 13 moduli)",
+    "C": "k_ntt_fwd_top<2> + k_ntt_fwd<12> (forward NTT of the extension limbs)",
+    "D": "k_ntt_inv<12, SrcTensor> + k_ntt_inv_top<2> (tensor product + inverse NTT, 13 moduli)",
     "E": "k_rns_scale (t/Q scale-down 13 -> 6 moduli)",
-    "F": "k_ntt_fwd (digit NTTs in every key modulus + c0/c1 NTTs)",
+    "F": "k_ntt_fwd_top<2> + k_ntt_fwd<12> (digit NTTs in every key modulus, then c0/c1 NTTs)",
     "G": "k_key_mac (key inner product)",
 }
 # DRAM bytes (read + write) of each stage's kernels for one 64-pair
-# multiplication with the plan A,C,D,F = 14 and F in two launches, from the
-# ncu capture summarised in profiles/stages_mul_relin_n16384_b64.md.
-STAGE_TRAFFIC_BYTES = {"A": 354.8e6, "B": 384.3e6, "C": 442.2e6, "D": 729.1e6, "E": 445.9e6, "F": 484.4e6,
-                       "G": 493.9e6}
+# multiplication with the plan A,C,D,F = 12 (2^12-residue blocks after a
+# strided pass over two stages), from the ncu capture summarised in
+# profiles/stages_mul_relin_n16384_b64.md. The two-pass plan writes and
+# re-reads every limb once more than a single pass would.
+STAGE_TRAFFIC_BYTES = {"A": 692.8e6, "B": 384.0e6, "C": 822.9e6, "D": 1319.9e6, "E": 445.7e6, "F": 1138.7e6,
+                       "G": 493.4e6}
 
 
 def _peaks():
@@ -380,6 +382,10 @@ def run_ours(args, rank: int, world: int):
                          f"{single_thread:.2f} ct/s; CPU restatement of fhe.rs Multiplicator::multiply "
                          "(the Rust reference cannot be built here)"}
 
+    # The ncu traffic figures were captured under the 2^12-block plan; a run
+    # whose plan differs reports no traffic rather than a mismatched one.
+    # (A plan entry of 0 means the process-wide plan of the degree.)
+    traffic_plan_matches = all((ntt_block[k] or fg.ntt_plan_get(logn)) == 12 for k in ("A", "C", "D", "F"))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -397,7 +403,8 @@ def run_ours(args, rank: int, world: int):
             "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
                     "d2h_bytes_per_step": int(h_o.nbytes)},
             "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
-                         "traffic": STAGE_TRAFFIC_BYTES.get(dom), "kernel": STAGE_KERNELS[dom],
+                         "traffic": STAGE_TRAFFIC_BYTES.get(dom) if traffic_plan_matches else None,
+                         "traffic_plan": "A,C,D,F = 2^12 blocks", "kernel": STAGE_KERNELS[dom],
                          "algorithmic_bytes": stage_bytes[dom], "launch_ms": stage_ms[dom], "peak_kind": peak_kind,
                          "note": "integer-issue bound: all arithmetic is exact 64-bit residue arithmetic on CUDA cores"},
             "stages": {k: {"ms": stage_ms[k], "gbs": stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9,

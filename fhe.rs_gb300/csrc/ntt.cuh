@@ -9,9 +9,10 @@
 // and are reduced at the end, so outputs are bit-identical to the reference.
 //
 // Layout: one CTA transforms one block of 2^bl residues of one limb (bl <= 14,
-// resident in shared memory). Each thread keeps 32 residues in registers and
-// runs up to five butterfly stages on them (a radix-32 round); rounds
-// exchange data through shared memory with an XOR swizzle that keeps 64-bit
+// resident in shared memory). Each thread keeps 16 residues in registers
+// (32 in blocks below 2^12) and runs up to four (five) butterfly stages on
+// them per round; rounds exchange data through shared memory with an XOR
+// swizzle that keeps 64-bit
 // accesses free of bank conflicts. A transform of 2^logn is either one block
 // (bl = logn) or, following the plan of ntt_block_logn(), a strided pass over
 // groups of 2^(logn - bl) elements for the first (forward) or last (inverse)
@@ -148,16 +149,23 @@ __device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
 // 8-byte bank pairs, for every supported size.
 __device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 15) ^ ((i >> 5) & 15); }
 
-// 32 residues per thread (16 for tiny sizes): radix-32 rounds, 512 threads
-// and a 128-register budget at N = 2^14.
+// Residues per thread: 16 (radix-16 rounds) in blocks of 2^12 to 2^14, 32
+// (radix-32 rounds) in smaller blocks. With 32 residues the 2^12-2^14 kernels
+// spilled 100-470 bytes per thread at their 128-register budget; with 16 they
+// spill nothing at 128. Blocks of 2^12 (256 threads) run three CTAs per SM
+// under an 80-register cap (24 warps, a few words spilled). On GB300 the
+// forward + inverse NTT at N = 2^14 with 2^12 blocks went from 1,064 GB/s
+// (32 residues) to 1,209 GB/s; four CTAs under 64 registers spilled more and
+// reached 1,150.
 template <int LOGN>
 struct NttShape {
-  static constexpr int LOGE = LOGN < 5 ? LOGN : 5;
+  static constexpr int LOGE = LOGN < 5 ? LOGN : (LOGN >= 12 ? 4 : 5);
   static constexpr int E = 1 << LOGE;
   static constexpr int N = 1 << LOGN;
   static constexpr int T = N / E;
-  // At least 512 threads' worth of blocks per SM: caps registers at 128.
-  static constexpr int MIN_BLOCKS = T >= 512 ? 1 : (512 / T > 32 ? 32 : 512 / T);
+  // Blocks per SM the register budget must allow: 3 for 2^12 blocks, else
+  // at least 512 threads' worth (a 128-register budget).
+  static constexpr int MIN_BLOCKS = LOGN == 12 ? 3 : (T >= 512 ? 1 : (512 / T > 32 ? 32 : 512 / T));
 };
 
 // One forward round: global stages S0 .. S0+K-1 of a transform of size 2^LOGN

@@ -14,10 +14,11 @@ namespace fheg {
 
 std::atomic<uint64_t> g_launches{0};
 
-// Default NTT plan: single pass up to 2^14 (the whole limb in shared memory);
-// 2^15 and 2^16 as strided stages in front of 2^13-residue blocks (measured
-// faster on GB300 than 2^14-residue blocks).
-static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 13, 13};
+// Default NTT plan: single pass up to 2^13 (the whole limb in shared memory);
+// 2^14 to 2^16 as strided stages in front of 2^12-residue blocks, which run
+// three CTAs per SM (forward + inverse on GB300 at 256 x 6 limbs: 1,209 GB/s
+// at 2^14 against 1,056 single-pass, 1,215 at 2^15, 1,121 at 2^16).
+static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 12, 12, 12};
 
 uint32_t ntt_block_logn(uint32_t logn) { return logn <= 16 ? g_ntt_block[logn].load(std::memory_order_relaxed) : 14; }
 

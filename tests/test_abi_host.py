@@ -94,17 +94,18 @@ def test_mul_scaler_constants_match_oracle(fg, ora):
 
 
 def test_ntt_plan_validation(fg):
-    """Plan entries are checked on the host: single pass up to 2^14, blocks of
-    2^12..2^14 with at most four strided stages."""
+    """Plan entries are checked on the host: defaults single pass up to 2^13
+    and 2^12 blocks above; blocks of 2^12..2^14 with at most four strided
+    stages."""
     for logn in range(3, 17):
-        assert fg.ntt_plan_get(logn) == (logn if logn <= 14 else 13)
+        assert fg.ntt_plan_get(logn) == (logn if logn <= 13 else 12)
     for logn, bl in [(12, 11), (14, 15), (15, 15), (16, 11), (17, 14), (11, 12)]:
         with pytest.raises(fg.FhegError):
             fg.ntt_plan_set(logn, bl)
-    fg.ntt_plan_set(14, 12)
-    assert fg.ntt_plan_get(14) == 12
     fg.ntt_plan_set(14, 14)
     assert fg.ntt_plan_get(14) == 14
+    fg.ntt_plan_set(14, 12)
+    assert fg.ntt_plan_get(14) == 12
 
 
 def test_no_device_fails_loudly(fg):
