@@ -155,7 +155,7 @@ __global__ void k_tensor(const DevPrime* primes, SrcTensor t, PolyRef out, uint3
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   NttJob j;
   j.limb = (uint32_t)(job % limbs);
   j.poly = (uint32_t)(job / limbs);
@@ -270,9 +270,9 @@ __global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0,
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t j = job % lk;
-  const uint64_t b0 = (job / lk) * KB;
+  const uint64_t b0 = (uint64_t)(job / lk) * KB;
   const DevPrime pr = primes[j];
   uint64_t lo0[KB], hi0[KB], lo1[KB], hi1[KB];
   const uint32_t gi = add0_e ? gather_index(i, add0_e, logn) : i;

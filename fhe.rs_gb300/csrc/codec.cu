@@ -140,8 +140,8 @@ __global__ void k_encrypt_finish(const DevPrime* primes, uint64_t* out, const ui
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t row = gid >> logn;  // poly * limbs + limb
-  const uint32_t limb = (uint32_t)(row % limbs);
+  const uint32_t row = row_of(gid, logn);  // poly * limbs + limb
+  const uint32_t limb = row % limbs;
   const uint64_t poly = row / limbs;
   const DevPrime pr = primes[limb];
   const uint64_t ai = a[gid];
@@ -162,9 +162,9 @@ __global__ void k_mul_plain(const DevPrime* primes, PolyRef ct, PolyRef pt, Poly
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % limbs;
-  const uint32_t poly = (uint32_t)(job / limbs);  // b * parts + k
+  const uint32_t poly = job / limbs;  // b * parts + k
   const uint32_t b = poly / parts;
   const DevPrime pr = primes[limb];
   out.at(poly, limb)[i] = mul_mod(ct.at(poly, limb)[i], pt.at(pt_per_ct ? b : 0, limb)[i], pr);

@@ -75,6 +75,12 @@ struct PolyRef {
   }
 };
 
+// Row (one limb of one polynomial) of element `gid` of a [rows][2^logn]
+// array. Rows fit in 32 bits (2^32 rows of at least 8 residues exceed any
+// device memory), so splitting a row into (polynomial, limb) is a 32-bit
+// division by the limb count rather than a much longer 64-bit one.
+__device__ __forceinline__ uint32_t row_of(uint64_t gid, uint32_t logn) { return (uint32_t)(gid >> logn); }
+
 inline PolyRef plain_ref(uint64_t* base, size_t limbs, uint32_t logn) {
   PolyRef r;
   r.base = base;

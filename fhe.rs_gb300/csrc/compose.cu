@@ -24,10 +24,10 @@ __global__ void k_dot_product(const DevPrime* primes, const uint64_t* ct, const 
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  uint64_t row = gid >> logn;  // (g, k, j)
+  const uint32_t row = row_of(gid, logn);  // (g, k, j)
   const uint32_t j = row % limbs;
   const uint32_t k = (row / limbs) % parts;
-  const uint64_t g = row / ((uint64_t)limbs * parts);
+  const uint64_t g = row / (limbs * parts);
   const DevPrime pr = primes[j];
   const uint64_t plane = (uint64_t)limbs << logn;  // one polynomial
   const uint64_t* c = ct + (g * count * parts + k) * plane + ((uint64_t)j << logn) + i;
@@ -51,9 +51,9 @@ __global__ void k_expand_step(const DevPrime* primes, uint64_t* out, const uint6
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t row = gid >> logn;  // (c, part, limb)
+  const uint32_t row = row_of(gid, logn);  // (c, part, limb)
   const uint32_t j = row % limbs;
-  const uint64_t c = row / (2 * (uint64_t)limbs);
+  const uint64_t c = row / (2 * limbs);
   const uint64_t ct_words = 2 * ((uint64_t)limbs << logn);
   const uint64_t off = gid - c * ct_words;  // within the ciphertext
   const DevPrime pr = primes[j];

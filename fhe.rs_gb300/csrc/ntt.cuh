@@ -98,7 +98,7 @@ __device__ __forceinline__ void src_prefetch(const S&, const NttJob&, uint32_t, 
 
 
 
-__device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
+__device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint32_t unit) {
   NttJob j;
   if (g.jobs) {
     const uint4 t = g.jobs[unit];
@@ -106,8 +106,8 @@ __device__ __forceinline__ NttJob unit_job(const NttGeom& g, uint64_t unit) {
     j.limb = t.y;
     j.aux = t.z;
   } else {
-    j.limb = (uint32_t)(unit % g.limbs);
-    j.poly = (uint32_t)(unit / g.limbs);
+    j.limb = unit % g.limbs;
+    j.poly = unit / g.limbs;
     j.aux = 0;
   }
   j.beta = 0;
@@ -156,7 +156,8 @@ __device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 15)
 // under an 80-register cap (24 warps, a few words spilled). On GB300 the
 // forward + inverse NTT at N = 2^14 with 2^12 blocks went from 1,064 GB/s
 // (32 residues) to 1,209 GB/s; four CTAs under 64 registers spilled more and
-// reached 1,150.
+// reached 1,150, and 8 residues per thread (512 threads, two CTAs, radix-8
+// rounds) 1,131.
 template <int LOGN>
 struct NttShape {
   static constexpr int LOGE = LOGN < 5 ? LOGN : (LOGN >= 12 ? 4 : 5);
@@ -451,8 +452,8 @@ __global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, u
                                                      uint64_t total, Src src, Dst dst) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
-  const uint32_t b = gid % groups_per_limb;
-  const NttJob jb = unit_job(g, gid / groups_per_limb);
+  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
+  const NttJob jb = unit_job(g, row_of(gid, logb));
   const DevPrime pr = g.primes[jb.limb];
   uint64_t x[1 << S1];
 #pragma unroll
@@ -480,8 +481,8 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
                                                      uint64_t total, Src src, Dst dst) {
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
-  const uint32_t b = gid % groups_per_limb;
-  const NttJob jb = unit_job(g, gid / groups_per_limb);
+  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
+  const NttJob jb = unit_job(g, row_of(gid, logb));
   const DevPrime pr = g.primes[jb.limb];
   const uint32_t n_total = 1u << (logb + S1);
   uint64_t x[1 << S1];

@@ -168,7 +168,7 @@ __global__ void k_poly_op(const DevPrime* primes, uint32_t limbs, uint32_t logn,
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % limbs;
   const uint32_t poly = job / limbs;
   const DevPrime pr = primes[limb];
@@ -207,7 +207,7 @@ __global__ void k_poly_scalar_mul(const DevPrime* primes, uint32_t limbs, uint32
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % limbs;
   const uint32_t poly = job / limbs;
   const uint64_t p = primes[limb].p;
@@ -250,7 +250,7 @@ __global__ void k_substitute(const DevPrime* primes, uint32_t limbs, uint32_t lo
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % limbs;
   const uint32_t poly = job / limbs;
   if (ntt) {
@@ -297,7 +297,7 @@ __global__ void k_switch_down_pb(const DevPrime* primes, SwitchConsts c, uint32_
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % c.lm1;
   const uint32_t poly = job / c.lm1;
   const DevPrime pr = primes[limb];
@@ -614,7 +614,7 @@ __global__ void k_copy_limbs(PolyRef in, PolyRef out, uint32_t limbs, uint32_t l
   const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= total) return;
   const uint32_t i = gid & ((1u << logn) - 1);
-  const uint64_t job = gid >> logn;
+  const uint32_t job = row_of(gid, logn);
   const uint32_t limb = job % limbs;
   const uint32_t poly = job / limbs;
   out.at(poly, limb)[i] = in.at(poly, limb)[i];

@@ -95,8 +95,8 @@ __global__ void k_unpack(const __grid_constant__ PackLayout lay, const uint8_t* 
   if (gid >= total) return;
   const uint64_t n = 1ull << lay.logn;
   const uint64_t k = gid & (n - 1);
-  const uint64_t row = gid >> lay.logn;  // poly * limbs + j
-  const uint32_t j = (uint32_t)(row % lay.limbs);
+  const uint32_t row = row_of(gid, lay.logn);  // poly * limbs + j
+  const uint32_t j = row % lay.limbs;
   const uint64_t poly = row / lay.limbs;
   const uint32_t nb = lay.nbits[j];
   const uint8_t* p = in + poly * lay.poly_bytes + lay.offset[j];
