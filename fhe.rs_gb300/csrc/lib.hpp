@@ -80,7 +80,8 @@ struct Context {
 // the per-target-modulus values each launch copies into its parameters.
 struct RnsScalerD {
   RnsScalerHost host;
-  std::vector<uint64_t> gamma_neg;  // (q_j - gamma_j) mod q_j
+  std::vector<uint64_t> gamma_neg;     // (q_j - gamma_j) mod q_j
+  std::vector<uint64_t> gamma_neg_hi;  // gamma_neg * 2^62 mod q_j
   std::vector<uint64_t> to_moduli, to_bhi, to_blo;
   RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den);
 };

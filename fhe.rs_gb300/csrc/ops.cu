@@ -417,7 +417,8 @@ struct RnsLaunch {
   uint64_t tgar_lo[MAXF], tgar_hi[MAXF];
   uint64_t to_lo[MAXF], to_hi[MAXF];
   uint64_t omega[MAXT][MAXF];
-  uint64_t gamma_neg[MAXT];  // (q_j - gamma_j) mod q_j
+  uint64_t gamma_neg[MAXT];     // (q_j - gamma_j) mod q_j
+  uint64_t gamma_neg_hi[MAXT];  // gamma_neg * 2^62 mod q_j
   uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
 };
 
@@ -495,6 +496,13 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   // instructions); its constants are then read with an indexed constant-bank
   // load per term. Smaller bodies run faster unrolled.
   constexpr int kOutUnroll = MAXF > 8 ? 1 : MAXT;
+  // v <= 32 * 2^62 (at most 32 sources, each residue below 2^62), so
+  // v * gamma = (v mod 2^62) * gamma + (v >> 62) * (gamma * 2^62 mod q_j):
+  // two exact terms of the 128-bit sum below, and v needs no reduction
+  // modulo each q_j. The sum then holds at most 15 terms below 2^124 (and a
+  // few small ones) between reductions: below 2^128.
+  const uint64_t v_low = vlo & ((1ull << 62) - 1);
+  const uint64_t v_top = (vlo >> 62) | (vhi << 2);
   uint64_t* dst = out.at(poly, 0) + i;
 #pragma unroll kOutUnroll
   for (int o = 0; o < MAXT; o++) {
@@ -504,18 +512,18 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       pr.p2 = 2 * s.p[o];
       pr.bhi = s.bhi[o];
       pr.blo = s.blo[o];
-      const uint64_t vj = reduce128(vhi, vlo, pr);
       uint64_t lo = 0, hi = 0;
       if (!s.is_one) {
         const uint64_t wj = reduce128_lazy(whi, wlo, pr);
         lo = w_sign ? pr.p2 - wj : wj;
       }
-      mac128(hi, lo, vj, s.gamma_neg[o]);
+      mac128(hi, lo, v_low, s.gamma_neg[o]);
+      mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
 #pragma unroll
       for (int k = 0; k < MAXF; k++) {
         if (k < (int)F) {
           mac128(hi, lo, r[k], s.omega[o][k]);
-          if ((k % 15) == 14) {  // keep the exact sum below 2^128
+          if ((k % 14) == 13) {  // keep the exact sum below 2^128
             lo = reduce128(hi, lo, pr);
             hi = 0;
           }
@@ -553,6 +561,7 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
       const size_t j = start + first + o;
       for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
       s.gamma_neg[o] = sc.gamma_neg[j];
+      s.gamma_neg_hi[o] = sc.gamma_neg_hi[j];
       s.p[o] = sc.to_moduli[j];
       s.bhi[o] = sc.to_bhi[j];
       s.blo[o] = sc.to_blo[j];
@@ -589,11 +598,13 @@ RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& nu
     : host(make_rns_scaler(*from.rns, *to.rns, num, den)) {
   const size_t T = host.to_len;
   gamma_neg.resize(T);
+  gamma_neg_hi.resize(T);
   to_moduli = to.moduli;
   to_bhi.resize(T);
   to_blo.resize(T);
   for (size_t j = 0; j < T; j++) {
     gamma_neg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
+    gamma_neg_hi[j] = mulmod(gamma_neg[j], (1ull << 62) % to.moduli[j], to.moduli[j]);
     barrett128(to.moduli[j], &to_bhi[j], &to_blo[j]);
   }
 }
