@@ -262,8 +262,12 @@ struct DstKsF {
 // products are summed exactly before a Barrett reduction. A thread handles
 // one residue of limb j for KB ciphertexts of the batch (each key residue is
 // then read once per KB ciphertexts).
+// D is a plain array [batch * ndig][lk][N] (digit d of ciphertext b at row
+// b * ndig + d, dstride words apart), addressed directly: a PolyRef lookup
+// per digit would cost a division per residue.
 template <int KB>
-__global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const uint64_t* k1,
+__global__ void k_key_mac(const DevPrime* primes, const uint64_t* D, uint64_t dstride, const uint64_t* k0,
+                          const uint64_t* k1,
                           const uint64_t* add0, uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1,
                           uint64_t add1_stride, uint64_t* out, uint64_t out_stride, uint32_t ndig, uint32_t lk,
                           uint32_t logn, uint64_t batch, uint64_t total) {
@@ -294,7 +298,7 @@ __global__ void k_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0,
     for (int u = 0; u < KB; u++) {
       const uint64_t b = b0 + u;
       if (b < batch) {
-        const uint64_t x = D.at(b * ndig + d, j)[i];
+        const uint64_t x = D[(b * ndig + d) * dstride + ((uint64_t)j << logn) + i];
         mac128(hi0[u], lo0[u], x, w0);
         mac128(hi1[u], lo1[u], x, w1);
       }
@@ -327,9 +331,10 @@ void launch_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const
                     uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1, uint64_t add1_stride, uint64_t* out,
                     uint64_t out_stride, uint32_t ndig, uint32_t lk, uint32_t logn, uint64_t batch, cudaStream_t st) {
   if (batch == 0) return;
+  if (D.grp != 1) throw Error(FHEG_ERR_INTERNAL, "key inner product: digits must be a plain array");
   const uint64_t total = batch * lk << logn;
-  k_key_mac<1><<<nblocks(total, 256), 256, 0, st>>>(primes, D, k0, k1, add0, add0_stride, add0_e, add1, add1_stride,
-                                                    out, out_stride, ndig, lk, logn, batch, total);
+  k_key_mac<1><<<nblocks(total, 256), 256, 0, st>>>(primes, D.base, D.grp_stride, k0, k1, add0, add0_stride, add0_e,
+                                                    add1, add1_stride, out, out_stride, ndig, lk, logn, batch, total);
   after_launch("k_key_mac");
 }
 
