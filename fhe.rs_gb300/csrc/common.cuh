@@ -26,6 +26,11 @@ struct DevPrime {
   uint64_t pinv;        // -p^-1 mod 2^64 (Montgomery reduction)
   uint64_t ninv_mont;   // N^-1 * 2^64 mod p: final scale of an inverse NTT of Montgomery products
   uint64_t ninv_mont_shoup;
+  // The last inverse stage's twiddle zetas_inv[N - 2] times the final scale
+  // (N^-1, or N^-1 * 2^64 for Montgomery inputs), with Shoup companions: the
+  // strided inverse pass folds the scaling into that stage's products.
+  uint64_t zlast_ninv, zlast_ninv_shoup;
+  uint64_t zlast_ninv_mont, zlast_ninv_mont_shoup;
   // Twiddle tables of native.rs:35-73, each entry paired with its Shoup
   // companion so one 16-byte load fetches both: tw[i] = (omegas[i],
   // omegas_shoup[i]), itw[i] = (zetas_inv[i], zetas_inv_shoup[i]).
@@ -299,6 +304,17 @@ __device__ __forceinline__ void inv_bfly(uint64_t& x, uint64_t& y, uint64_t z, u
   const uint64_t t = x;
   x = csub(x + y, p2);
   y = mul_shoup_lazy(t + p2 - y, z, zs, p);
+}
+
+// The last Gentleman-Sande stage followed by the final scale s (N^-1 or its
+// Montgomery form), with zs = z * s precomputed: x, y in [0, 2p) become the
+// canonical ((x + y) s, (x - y) z s) mod p, the values the reference's
+// butterfly and scaling produce, with two products instead of three.
+__device__ __forceinline__ void inv_bfly_final(uint64_t& x, uint64_t& y, uint64_t zs, uint64_t zs_shoup, uint64_t s,
+                                               uint64_t s_shoup, uint64_t p, uint64_t p2) {
+  const uint64_t t = x;
+  x = mul_shoup(x + y, s, s_shoup, p);
+  y = mul_shoup(t + p2 - y, zs, zs_shoup, p);
 }
 
 // native.rs:238-243 `reduce3`: [0, 4p) -> [0, p).

@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
 #pragma unroll
   for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
 #pragma unroll
-  for (int r = 0; r < S1; r++) {
+  for (int r = 0; r < S1 - 1; r++) {
     const int span = 1 << r;
     const uint32_t m = 1u << (S1 - 1 - r);  // chunks at this stage
 #pragma unroll
@@ -503,9 +503,16 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
       }
     }
   }
+  // The last stage (one chunk, twiddle zetas_inv[N - 2]) with the final
+  // scale folded into its products.
+  const uint64_t s = g.mont ? pr.ninv_mont : pr.ninv, s_shoup = g.mont ? pr.ninv_mont_shoup : pr.ninv_shoup;
+  const uint64_t zs = g.mont ? pr.zlast_ninv_mont : pr.zlast_ninv;
+  const uint64_t zs_shoup = g.mont ? pr.zlast_ninv_mont_shoup : pr.zlast_ninv_shoup;
+  constexpr int kHalf = 1 << (S1 - 1);
 #pragma unroll
-  for (int t = 0; t < (1 << S1); t++)
-    dst(jb, pr, b + ((uint32_t)t << logb), inv_final_scale(g, pr, x[t]));
+  for (int u = 0; u < kHalf; u++) inv_bfly_final(x[u], x[u + kHalf], zs, zs_shoup, s, s_shoup, pr.p, pr.p2);
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) dst(jb, pr, b + ((uint32_t)t << logb), x[t]);
 }
 
 // ---------------------------------------------------------------------------

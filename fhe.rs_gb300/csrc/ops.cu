@@ -91,6 +91,11 @@ std::shared_ptr<PrimeTables> get_prime_tables(uint64_t p, size_t n, uint64_t roo
   const uint64_t r_mod_p = (uint64_t)(((unsigned __int128)1 << 64) % p);
   dp.ninv_mont = (uint64_t)((unsigned __int128)dp.ninv * r_mod_p % p);
   dp.ninv_mont_shoup = shoup(dp.ninv_mont, p);
+  const uint64_t zlast = t->host.zetas_inv[n - 2];
+  dp.zlast_ninv = mulmod(zlast, dp.ninv, p);
+  dp.zlast_ninv_shoup = shoup(dp.zlast_ninv, p);
+  dp.zlast_ninv_mont = mulmod(zlast, dp.ninv_mont, p);
+  dp.zlast_ninv_mont_shoup = shoup(dp.zlast_ninv_mont, p);
   dp.tw = reinterpret_cast<const ulonglong2*>(d);
   dp.itw = reinterpret_cast<const ulonglong2*>(d + 2 * n);
   registry[key] = t;
