@@ -742,12 +742,28 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   PolyRef pbref = plain_ref(pb, L, logn);
   PolyRef extref = plain_ref(ext, M, logn);
 
-  // A: inverse NTT of the four operands.
+  // Strided last stages of a two-pass inverse NTT that the RNS scaler after
+  // it can apply while loading (its only consumer): 0 when the plan is single
+  // pass or the scaler cannot.
+  auto top_stages = [&](uint32_t plan, const Scaler& s1c, const Scaler* s2c, uint32_t out_len) -> uint32_t {
+    const uint32_t bl = plan ? plan : ntt_block_logn(logn);
+    if (bl >= logn || logn < 13) return 0;
+    const uint32_t s1 = logn - bl;
+    if (!rns_scale_takes_top(*s1c.rns, logn, out_len, s1)) return 0;
+    if (s2c && !rns_scale_takes_top(*s2c->rns, logn, out_len, s1)) return 0;
+    return s1;
+  };
+
+  // A: inverse NTT of the four operands (without its strided last stages
+  // when B applies them).
   mark(0);
+  const uint32_t top_a = top_stages(plan_a, *ext_lhs, ext_rhs.get(), (uint32_t)(M - std::min(ncm_l, ncm_r)));
   {
     NttGeom g{bc.primes_dev(), (uint32_t)L, 0};
-    ntt_inverse_any(logn, g, 4 * count, SrcPair{lref, rref}, DstPoly{pbref}, st, plan_a);
+    if (top_a) ntt_inverse_blocks(logn, g, 4 * count, SrcPair{lref, rref}, DstPoly{pbref}, st, plan_a);
+    else ntt_inverse_any(logn, g, 4 * count, SrcPair{lref, rref}, DstPoly{pbref}, st, plan_a);
   }
+  const InverseTop top_a_args{top_a, 0u, bc.primes_dev()};
   mark(1);
   // B + C: extension of each operand and forward NTT of the new limbs.
   const bool same_ext = ncm_l == ncm_r && ext_lhs->num == ext_rhs->num && ext_lhs->den == ext_rhs->den;
@@ -756,7 +772,8 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     PolyRef in = sub_ref(pb, L, logn, 4, first, take);
     PolyRef o = sub_ref(ext, M, logn, 4, first, take);
     o.base += (uint64_t)ncm << logn;
-    rns_scale(*s.rns, logn, in, o, (uint32_t)ncm, (uint32_t)(M - ncm), count * take, st);
+    rns_scale(*s.rns, logn, in, o, (uint32_t)ncm, (uint32_t)(M - ncm), count * take, st,
+              top_a ? &top_a_args : nullptr);
     if (first == 0) mark(2);
     NttGeom g{mc.primes_dev() + ncm, (uint32_t)(M - ncm), 0};
     ntt_forward_any<true>(logn, g, count * take, SrcPoly{o}, DstPoly{o}, st, plan_c);
@@ -773,6 +790,7 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   // NTT in place: the separate kernel keeps enough loads in flight to hide
   // their latency, at the cost of one more pass over the products.
   PolyRef prodref = plain_ref(prod, M, logn);
+  const uint32_t top_d = top_stages(plan_d, *down, nullptr, (uint32_t)L);
   {
     NttGeom g{mc.primes_dev(), (uint32_t)M, 0};
     const SrcTensor tensor{lref, rref, extref, (uint32_t)ncm_l, (uint32_t)ncm_r};
@@ -780,15 +798,20 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
       const uint64_t total = 3 * count * M << logn;
       k_tensor<<<nblocks(total, 256), 256, 0, st>>>(mc.primes_dev(), tensor, prodref, (uint32_t)M, logn, total);
       after_launch("k_tensor");
-      ntt_inverse_any(logn, g, 3 * count, SrcPolyMont{prodref}, DstPoly{prodref}, st, plan_d);
+      if (top_d) ntt_inverse_blocks(logn, g, 3 * count, SrcPolyMont{prodref}, DstPoly{prodref}, st, plan_d);
+      else ntt_inverse_any(logn, g, 3 * count, SrcPolyMont{prodref}, DstPoly{prodref}, st, plan_d);
+    } else if (top_d) {
+      ntt_inverse_blocks(logn, g, 3 * count, tensor, DstPoly{prodref}, st, plan_d);
     } else {
       ntt_inverse_any(logn, g, 3 * count, tensor, DstPoly{prodref}, st, plan_d);
     }
   }
   mark(4);
-  // E: scale down by t/Q into the base context (power basis).
+  // E: scale down by t/Q into the base context (power basis), applying the
+  // strided last stages of D's inverse NTT (Montgomery products) on the way.
   PolyRef dnref = plain_ref(dn, L, logn);
-  rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st);
+  const InverseTop top_d_args{top_d, 1u, mc.primes_dev()};
+  rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st, top_d ? &top_d_args : nullptr);
   mark(5);
   NttGeom gb{bc.primes_dev(), (uint32_t)L, 0};
   if (rk) {

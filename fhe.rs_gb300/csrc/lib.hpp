@@ -111,8 +111,19 @@ void poly_switch_down_pb(const Context& ctx, PolyRef in, PolyRef out, uint64_t p
 void poly_switch_down_ntt(const Context& ctx, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st);
 // RnsScaler::scale over all coefficients: `in` power basis [from_len] limbs,
 // `out` limbs k = 0..out_len-1 receive target modulus start + k.
+// The strided last stages of a two-pass inverse NTT left to the consumer:
+// `s1` stages of the source context (`primes`, one DevPrime per source
+// limb), final scale N^-1 * 2^64 when `mont` (Montgomery products), else N^-1.
+struct InverseTop {
+  uint32_t s1;
+  uint32_t mont;
+  const DevPrime* primes;
+};
+// top != nullptr: `in` is the block pass of such a transform, and the scaler
+// applies its last stages while loading (only where rns_scale_takes_top).
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
-               uint64_t polys, cudaStream_t st);
+               uint64_t polys, cudaStream_t st, const InverseTop* top = nullptr);
+bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1);
 // Scaler::scale. `scratch` must hold polys * max(L_from, L_to) * N words.
 void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t polys, uint64_t* scratch,
                   cudaStream_t st);

@@ -476,18 +476,13 @@ __global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, u
   for (int t = 0; t < (1 << S1); t++) dst(jb, pr, b + ((uint32_t)t << logb), x[t]);
 }
 
-template <int S1, class Src, class Dst>
-__global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
-                                                     uint64_t total, Src src, Dst dst) {
-  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
-  const NttJob jb = unit_job(g, row_of(gid, logb));
-  const DevPrime pr = g.primes[jb.limb];
-  const uint32_t n_total = 1u << (logb + S1);
-  uint64_t x[1 << S1];
-#pragma unroll
-  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+// The last S1 inverse stages of a transform of n_total residues and its
+// final scale (N^-1, or N^-1 * 2^64 when `mont`), on the 2^S1 elements
+// x[t] = element b + t * n_total / 2^S1 of one limb: what the strided inverse
+// pass does per thread, also applied by consumers that read the block pass's
+// output directly (the RNS scaler of the multiplication).
+template <int S1>
+__device__ __forceinline__ void inv_top_stages(uint64_t* x, const DevPrime& pr, uint32_t n_total, bool mont) {
 #pragma unroll
   for (int r = 0; r < S1 - 1; r++) {
     const int span = 1 << r;
@@ -505,12 +500,26 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
   }
   // The last stage (one chunk, twiddle zetas_inv[N - 2]) with the final
   // scale folded into its products.
-  const uint64_t s = g.mont ? pr.ninv_mont : pr.ninv, s_shoup = g.mont ? pr.ninv_mont_shoup : pr.ninv_shoup;
-  const uint64_t zs = g.mont ? pr.zlast_ninv_mont : pr.zlast_ninv;
-  const uint64_t zs_shoup = g.mont ? pr.zlast_ninv_mont_shoup : pr.zlast_ninv_shoup;
+  const uint64_t s = mont ? pr.ninv_mont : pr.ninv, s_shoup = mont ? pr.ninv_mont_shoup : pr.ninv_shoup;
+  const uint64_t zs = mont ? pr.zlast_ninv_mont : pr.zlast_ninv;
+  const uint64_t zs_shoup = mont ? pr.zlast_ninv_mont_shoup : pr.zlast_ninv_shoup;
   constexpr int kHalf = 1 << (S1 - 1);
 #pragma unroll
   for (int u = 0; u < kHalf; u++) inv_bfly_final(x[u], x[u + kHalf], zs, zs_shoup, s, s_shoup, pr.p, pr.p2);
+}
+
+template <int S1, class Src, class Dst>
+__global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
+                                                     uint64_t total, Src src, Dst dst) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
+  const NttJob jb = unit_job(g, row_of(gid, logb));
+  const DevPrime pr = g.primes[jb.limb];
+  uint64_t x[1 << S1];
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+  inv_top_stages<S1>(x, pr, 1u << (logb + S1), g.mont != 0);
 #pragma unroll
   for (int t = 0; t < (1 << S1); t++) dst(jb, pr, b + ((uint32_t)t << logb), x[t]);
 }
@@ -720,6 +729,30 @@ void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst,
     default: throw Error(12, "unsupported NTT plan");
   }
   launch_inv_top(s1, g, bl, polys, SrcReload<Dst>{dst}, dst, st);
+}
+
+// The inverse NTT up to its strided last stages: with a two-pass plan only the
+// block pass runs, and the caller's consumer applies the remaining stages
+// (inv_top_stages) as it reads `dst`; returns their number (0: the transform
+// ran whole, single pass).
+template <class Src, class Dst>
+uint32_t ntt_inverse_blocks(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t st,
+                            uint32_t bl = 0) {
+  g.mont = src_is_montgomery<Src>(0) ? 1u : 0u;
+  if (bl == 0) bl = ntt_block_logn(logn);
+  if (bl >= logn || logn < 13) {
+    ntt_inverse_any(logn, g, polys, src, dst, st, bl);
+    return 0;
+  }
+  const uint32_t s1 = logn - bl;
+  g.s1 = s1;
+  switch (bl) {
+    case 12: launch_inv_block<12, false>(g, polys, src, dst, st); break;
+    case 13: launch_inv_block<13, false>(g, polys, src, dst, st); break;
+    case 14: launch_inv_block<14, false>(g, polys, src, dst, st); break;
+    default: throw Error(12, "unsupported NTT plan");
+  }
+  return s1;
 }
 
 }  // namespace

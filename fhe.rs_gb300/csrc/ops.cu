@@ -430,18 +430,53 @@ struct RnsLaunch {
 // EXACT: the source count is MAXF itself (a compile-time constant), so the
 // unrolled loops carry no predicated-off terms; used for the counts the
 // default multiplications produce (L and 2L + 1 source moduli).
-template <int MAXF, int MAXT, bool EXACT>
+//
+// TOP > 0: `in` holds the block pass of a two-pass inverse NTT whose last TOP
+// strided stages and final scale have not run. Each CTA of 128 threads then
+// owns the 128 coefficients b + t * 2^(logn - TOP) of 128 >> TOP groups b
+// (t < 2^TOP); it applies those stages to every source limb of its groups
+// (inv_top_stages, the strided inverse pass's arithmetic) into shared memory,
+// and each thread scales one coefficient from there. The strided pass and
+// its round trip through HBM disappear; the results are the same.
+template <int MAXF, int MAXT, bool EXACT, int TOP>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
-                                                   PolyRef in, PolyRef out, uint64_t total) {
-  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const uint32_t i = gid & ((1u << logn) - 1);
-  const uint32_t poly = (uint32_t)(gid >> logn);
+                                                   PolyRef in, PolyRef out, uint64_t total,
+                                                   const DevPrime* src_primes, uint32_t src_mont) {
   const uint32_t F = EXACT ? (uint32_t)MAXF : s.from_len;
-  const uint64_t* src = in.at(poly, 0) + i;
+  uint32_t i, poly;
   uint64_t r[MAXF];
+  if constexpr (TOP == 0) {
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total) return;
+    i = gid & ((1u << logn) - 1);
+    poly = (uint32_t)(gid >> logn);
+    const uint64_t* src = in.at(poly, 0) + i;
 #pragma unroll
-  for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? src[(uint64_t)k << logn] : 0;
+    for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? src[(uint64_t)k << logn] : 0;
+  } else {
+    // The grid covers whole polynomials (2^logn is a multiple of 128), so
+    // every thread reaches the barrier.
+    constexpr int G = 128 >> TOP;  // groups per CTA
+    __shared__ uint64_t staged[MAXF * 128];
+    poly = blockIdx.x >> (logn - 7);
+    const uint32_t b0 = (blockIdx.x & ((1u << (logn - 7)) - 1)) * G;
+    const uint32_t logb = logn - TOP;
+    for (uint32_t item = threadIdx.x; item < F * G; item += 128) {
+      const uint32_t k = item / G, gi = item % G;
+      const uint64_t* row = in.at(poly, k) + b0 + gi;
+      uint64_t x[1 << TOP];
+#pragma unroll
+      for (int t = 0; t < (1 << TOP); t++) x[t] = row[(uint64_t)t << logb];
+      inv_top_stages<TOP>(x, src_primes[k], 1u << logn, src_mont != 0);
+#pragma unroll
+      for (int t = 0; t < (1 << TOP); t++) staged[(k * (1 << TOP) + t) * G + gi] = x[t];
+    }
+    __syncthreads();
+    const uint32_t t = threadIdx.x / G, gi = threadIdx.x % G;
+    i = b0 + gi + (t << logb);
+#pragma unroll
+    for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? staged[(k * (1 << TOP) + t) * G + gi] : 0;
+  }
 
   // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2).
   uint32_t g[6] = {0, 0, 0, 0, 0, 0};
@@ -539,9 +574,9 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   }
 }
 
-template <int MAXF, int MAXT, bool EXACT = false>
+template <int MAXF, int MAXT, bool EXACT = false, int TOP = 0>
 void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
-                      uint32_t out_len, uint64_t total, cudaStream_t st) {
+                      uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop* top = nullptr) {
   const RnsScalerHost& h = sc.host;
   const size_t F = h.from_len;
   for (uint32_t first = 0; first < out_len; first += MAXT) {
@@ -574,16 +609,45 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     PolyRef o = out;
     o.base += (uint64_t)first << logn;
     const unsigned threads = 128;
-    k_rns_scale<MAXF, MAXT, EXACT><<<blocks_for(total, threads), threads, 0, st>>>(s, logn, in, o, total);
+    k_rns_scale<MAXF, MAXT, EXACT, TOP><<<blocks_for(total, threads), threads, 0, st>>>(
+        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u);
     after_launch("k_rns_scale");
   }
 }
 
+template <int MAXF, int MAXT>
+static void launch_rns_scale_top(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
+                                 uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop& top) {
+  switch (top.s1) {
+    case 1: launch_rns_scale<MAXF, MAXT, true, 1>(s, logn, in, out, start, out_len, total, st, &top); break;
+    case 2: launch_rns_scale<MAXF, MAXT, true, 2>(s, logn, in, out, start, out_len, total, st, &top); break;
+    case 3: launch_rns_scale<MAXF, MAXT, true, 3>(s, logn, in, out, start, out_len, total, st, &top); break;
+    default: throw Error(FHEG_ERR_INTERNAL, "unsupported strided stage count");
+  }
+}
+
+bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1) {
+  const size_t F = s.host.from_len;
+  const bool exact = (F == 6 || F == 13 || F == 3 || F == 7) ? out_len <= 8 : (F == 12 || F == 25) && out_len <= 16;
+  return exact && s1 >= 1 && s1 <= 3 && logn >= 7;
+}
+
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
-               uint64_t polys, cudaStream_t st) {
+               uint64_t polys, cudaStream_t st, const InverseTop* top) {
   const uint64_t total = polys << logn;
   if (total == 0 || out_len == 0) return;
   const size_t F = s.host.from_len;
+  if (top) {
+    if (!rns_scale_takes_top(s, logn, out_len, top->s1))
+      throw Error(FHEG_ERR_INTERNAL, "RNS scaling cannot apply these strided stages");
+    if (F == 6) launch_rns_scale_top<6, 8>(s, logn, in, out, start, out_len, total, st, *top);
+    else if (F == 13) launch_rns_scale_top<13, 8>(s, logn, in, out, start, out_len, total, st, *top);
+    else if (F == 3) launch_rns_scale_top<3, 8>(s, logn, in, out, start, out_len, total, st, *top);
+    else if (F == 7) launch_rns_scale_top<7, 8>(s, logn, in, out, start, out_len, total, st, *top);
+    else if (F == 12) launch_rns_scale_top<12, 16>(s, logn, in, out, start, out_len, total, st, *top);
+    else launch_rns_scale_top<25, 16>(s, logn, in, out, start, out_len, total, st, *top);
+    return;
+  }
   // Exact source counts of the default multiplications at L = 3, 6, 12
   // (extension from L, scale-down from 2L + 1).
   if (F == 6 && out_len <= 8) launch_rns_scale<6, 8, true>(s, logn, in, out, start, out_len, total, st);
