@@ -48,21 +48,23 @@ STAGE_LIMBS = {
     "G": L * L + 4 * L,              # read the digit NTTs, read + write c0, c1 (keys added per batch)
 }
 STAGE_KERNELS = {
-    "A": "k_ntt_inv<12> + k_ntt_inv_top<2> (inverse NTT of the operands)",
-    "B": "k_rns_scale (basis extension 6 -> 7 new moduli)",
+    "A": "k_ntt_inv<12, SrcPair> (inverse NTT of the operands, block pass; its strided last stages run in B)",
+    "B": "k_rns_scale<6, 8> (strided last stages of A, then basis extension 6 -> 7 new moduli)",
     "C": "k_ntt_fwd_top<2> + k_ntt_fwd<12> (forward NTT of the extension limbs)",
-    "D": "k_ntt_inv<12, SrcTensor> + k_ntt_inv_top<2> (tensor product + inverse NTT, 13 moduli)",
-    "E": "k_rns_scale (t/Q scale-down 13 -> 6 moduli)",
-    "F": "k_ntt_fwd_top<2> + k_ntt_fwd<12> (digit NTTs in every key modulus, then c0/c1 NTTs)",
+    "D": "k_ntt_inv<12, SrcTensor> (tensor product + inverse NTT, block pass; its strided last stages run in E)",
+    "E": "k_rns_scale<13, 8> (strided last stages of D, then t/Q scale-down 13 -> 6 moduli)",
+    "F": "k_ntt_fwd_top<2> + k_ntt_fwd<12>, twice (digit NTTs in every key modulus, then c0/c1 NTTs)",
     "G": "k_key_mac (key inner product)",
 }
+# Kernel launches of each stage under the same plan.
+STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 2, "D": 1, "E": 1, "F": 4, "G": 1}
 # DRAM bytes (read + write) of each stage's kernels for one 64-pair
-# multiplication with the plan A,C,D,F = 12 (2^12-residue blocks after a
-# strided pass over two stages), from the ncu capture summarised in
-# profiles/stages_mul_relin_n16384_b64.md. The two-pass plan writes and
-# re-reads every limb once more than a single pass would.
-STAGE_TRAFFIC_BYTES = {"A": 692.8e6, "B": 384.0e6, "C": 822.9e6, "D": 1319.9e6, "E": 445.7e6, "F": 1138.7e6,
-                       "G": 493.4e6}
+# multiplication with the plan A,C,D,F = 12 (2^12-residue blocks; the forward
+# transforms after a strided pass over two stages, the inverse ones with those
+# stages applied by the RNS scaler that reads them), from the ncu capture
+# summarised in profiles/stages_mul_relin_n16384_b64.md.
+STAGE_TRAFFIC_BYTES = {"A": 354.5e6, "B": 384.6e6, "C": 822.3e6, "D": 730.4e6, "E": 446.8e6, "F": 1137.9e6,
+                       "G": 493.3e6}
 
 
 def _peaks():
@@ -364,7 +366,9 @@ def run_ours(args, rank: int, world: int):
     limb = 8 * N
     stage_bytes = {k: B * v * limb for k, v in STAGE_LIMBS.items()}
     stage_bytes["G"] += 2 * L * L * limb  # the relinearization key, read once per batch
-    dom = max(stage_ms, key=stage_ms.get)
+    # The dominant kernel: the stage with the longest launch (per launch, as
+    # stages C and F hold several kernels under the 2^12-block plan).
+    dom = max(stage_ms, key=lambda k: stage_ms[k] / STAGE_LAUNCHES[k])
     dom_gbs = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
 
     cpu = None
