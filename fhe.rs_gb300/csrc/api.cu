@@ -843,11 +843,11 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     // Chunks rotate over the pipeline's streams, so the copies of one chunk
     // overlap the multiplication of others. The input copies of chunk i wait
     // for those of chunk i-1: the host link carries one chunk at a time, and
-    // the first chunk's inputs arrive at full link speed. Small chunks (6
-    // pairs, run with the small-batch plan, three at a time) measured best
-    // on GB300 at 16 to 64 pairs: the fill and drain of the pipeline cost one
+    // the first chunk's inputs arrive at full link speed. Small chunks (4
+    // pairs, run with the small-batch plan, four at a time) measured best
+    // on GB300 at 32 and 64 pairs: the fill and drain of the pipeline cost one
     // small chunk's copies, and concurrent chunks keep the SMs busy.
-    const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 12 ? 6 : count);
+    const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 8 ? 4 : count);
     const size_t nchunks = (count + chunk - 1) / chunk;
     while (m->copied.size() < nchunks) {
       cudaEvent_t e;

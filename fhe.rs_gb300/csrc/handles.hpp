@@ -34,7 +34,7 @@ struct fheg_multiplicator {
   fheg::Workspace pipe_ws[kPipe];
   std::vector<cudaEvent_t> copied;  // end of each chunk's input copies
   size_t host_chunk = 0;            // pairs per chunk (0 = automatic)
-  int host_streams = 3;
+  int host_streams = 4;
   ~fheg_multiplicator() {
     for (auto& s : pipe)
       if (s) cudaStreamDestroy(s);

@@ -332,8 +332,8 @@ FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max
  * A count within the small-batch threshold tunes the small-batch plan. */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
 /* Pipeline of fheg_multiplicator_multiply_host: `chunk` pairs per chunk
- * (0 = automatic: 6 when count >= 12, else the whole call) rotating over
- * `streams` streams (1..4, default 3), each with its own scratch. Changes
+ * (0 = automatic: 4 when count >= 8, else the whole call) rotating over
+ * `streams` streams (1..4, default 4), each with its own scratch. Changes
  * only the overlap of copies and compute, never the results. No counterpart
  * in the reference. */
 FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t chunk, int streams);
