@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "fheg.h"
+#include "abi_call.hpp"
 #include "handles.hpp"
 #include "lib.hpp"
 
@@ -14,28 +15,6 @@ using namespace fheg;
 namespace {
 
 thread_local std::string g_last_error;
-
-template <class F>
-int guard(F&& f) {
-  try {
-    g_last_error.clear();
-    f();
-    return FHEG_OK;
-  } catch (const Error& e) {
-    g_last_error = e.what();
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    g_last_error = "host allocation failed";
-    return FHEG_ERR_BUDGET;
-  } catch (const std::exception& e) {
-    g_last_error = e.what();
-    return FHEG_ERR_INTERNAL;
-  }
-}
-
-void need(bool cond, const char* what) {
-  if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
-}
 
 cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
@@ -76,8 +55,8 @@ FHEG_API uint64_t fheg_kernel_launch_count(void) { return g_launches.load(); }
 // Host-only number theory.
 
 FHEG_API int fheg_generate_prime(uint32_t num_bits, uint64_t modulo, uint64_t upper_bound, uint64_t* out) {
-  return guard([&] {
-    need(out != nullptr && modulo != 0, "null output or zero modulo");
+  return abi_call([&] {
+    abi_need(out != nullptr && modulo != 0, "null output or zero modulo");
     *out = generate_prime(num_bits, modulo, upper_bound);
   });
 }
@@ -88,16 +67,16 @@ FHEG_API int fheg_supports_ntt(uint64_t p, size_t n) {
 }
 
 FHEG_API int fheg_ntt_default_root(uint64_t p, size_t n, uint64_t* out_root) {
-  return guard([&] {
-    need(out_root != nullptr, "null output");
+  return abi_call([&] {
+    abi_need(out_root != nullptr, "null output");
     *out_root = default_ntt_root(p, n);
   });
 }
 
 FHEG_API int fheg_ntt_tables_host(uint64_t p, size_t n, uint64_t root, uint64_t* omegas, uint64_t* omegas_shoup,
                                   uint64_t* zetas_inv, uint64_t* zetas_inv_shoup, uint64_t* out_size_inv) {
-  return guard([&] {
-    need(omegas && omegas_shoup && zetas_inv && zetas_inv_shoup && out_size_inv, "null output");
+  return abi_call([&] {
+    abi_need(omegas && omegas_shoup && zetas_inv && zetas_inv_shoup && out_size_inv, "null output");
     NttTablesHost t = make_ntt_tables(p, n, root);
     std::memcpy(omegas, t.omegas.data(), n * 8);
     std::memcpy(omegas_shoup, t.omegas_shoup.data(), n * 8);
@@ -112,10 +91,10 @@ FHEG_API int fheg_rns_scaler_constants_host(const uint64_t* from_moduli, size_t 
                                             size_t to_len, const uint64_t* num, size_t num_words,
                                             const uint64_t* den, size_t den_words, uint64_t* out,
                                             size_t out_words) {
-  return guard([&] {
-    need(from_moduli && to_moduli && out && from_len && to_len, "null or empty input");
+  return abi_call([&] {
+    abi_need(from_moduli && to_moduli && out && from_len && to_len, "null or empty input");
     const size_t F = from_len, T = to_len;
-    need(out_words >= 5 + 2 * T + 2 * T * F + 5 * F, "output too small");
+    abi_need(out_words >= 5 + 2 * T + 2 * T * F + 5 * F, "output too small");
     RnsContextHost from(std::vector<uint64_t>(from_moduli, from_moduli + F));
     RnsContextHost to(std::vector<uint64_t>(to_moduli, to_moduli + T));
     RnsScalerHost s = make_rns_scaler(from, to, big(num, num_words), big(den, den_words));
@@ -142,8 +121,8 @@ FHEG_API int fheg_rns_scaler_constants_host(const uint64_t* from_moduli, size_t 
 
 FHEG_API int fheg_context_create(const uint64_t* moduli, size_t num_moduli, size_t degree, const uint64_t* roots,
                                  fheg_context** out) {
-  return guard([&] {
-    need(moduli && num_moduli && out, "null or empty input");
+  return abi_call([&] {
+    abi_need(moduli && num_moduli && out, "null or empty input");
     auto h = new fheg_context();
     try {
       h->c = std::make_shared<Context>(std::vector<uint64_t>(moduli, moduli + num_moduli), degree, roots);
@@ -160,32 +139,32 @@ FHEG_API size_t fheg_context_num_moduli(const fheg_context* ctx) { return ctx ? 
 FHEG_API size_t fheg_context_degree(const fheg_context* ctx) { return ctx ? ctx->c->N() : 0; }
 
 FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t count, int lazy, void* stream) {
-  return guard([&] {
-    need(ctx && (d_polys || !count), "null input");
+  return abi_call([&] {
+    abi_need(ctx && (d_polys || !count), "null input");
     PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
     ntt_forward(*ctx->c, r, r, count, lazy != 0, as_stream(stream));
   });
 }
 
 FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_t count, void* stream) {
-  return guard([&] {
-    need(ctx && (d_polys || !count), "null input");
+  return abi_call([&] {
+    abi_need(ctx && (d_polys || !count), "null input");
     PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
     ntt_backward(*ctx->c, r, r, count, as_stream(stream));
   });
 }
 
 FHEG_API int fheg_ntt_plan_set(uint32_t logn, uint32_t block_logn) {
-  return guard([&] { set_ntt_block_logn(logn, block_logn); });
+  return abi_call([&] { set_ntt_block_logn(logn, block_logn); });
 }
 
 FHEG_API int fheg_ntt_prefetch_set(int on) {
-  return guard([&] { set_ntt_prefetch(on != 0); });
+  return abi_call([&] { set_ntt_prefetch(on != 0); });
 }
 
 FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
-  return guard([&] {
-    need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");
+  return abi_call([&] {
+    abi_need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");
     *block_logn = ntt_block_logn(logn);
   });
 }
@@ -233,8 +212,8 @@ uint32_t autotune_plans(uint32_t logn, cudaStream_t st, F run) {
 }
 
 FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn) {
-  return guard([&] {
-    need(ctx && count && block_logn, "null input");
+  return abi_call([&] {
+    abi_need(ctx && count && block_logn, "null input");
     const Context& c = *ctx->c;
     cudaStream_t st = as_stream(stream);
     DevBuf buf(count * c.L() * c.N() * 8);
@@ -306,8 +285,8 @@ void set_mul_plan(Multiplicator& m, const uint32_t* plan) {
 
 FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                             uint64_t* d_out, size_t count, void* stream, float* ms) {
-  return guard([&] {
-    need(m && d_lhs && d_rhs && d_out && count && ms, "null input");
+  return abi_call([&] {
+    abi_need(m && d_lhs && d_rhs && d_out && count && ms, "null input");
     cudaStream_t st = as_stream(stream);
     cudaEvent_t ev[8] = {};
     try {
@@ -325,8 +304,8 @@ FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_
 }
 
 FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max_count, const uint32_t* plan) {
-  return guard([&] {
-    need(m && (plan || !max_count), "null input");
+  return abi_call([&] {
+    abi_need(m && (plan || !max_count), "null input");
     Multiplicator& mm = *m->m;
     if (max_count) {
       for (int k = 0; k < 4; k++)
@@ -338,22 +317,22 @@ FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max
 }
 
 FHEG_API int fheg_multiplicator_get_plan(const fheg_multiplicator* m, uint32_t* plan) {
-  return guard([&] {
-    need(m && plan, "null input");
+  return abi_call([&] {
+    abi_need(m && plan, "null input");
     get_mul_plan(*m->m, plan);
   });
 }
 
 FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* plan) {
-  return guard([&] {
-    need(m && plan, "null input");
+  return abi_call([&] {
+    abi_need(m && plan, "null input");
     set_mul_plan(*m->m, plan);
   });
 }
 
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan) {
-  return guard([&] {
-    need(m && count, "null input");
+  return abi_call([&] {
+    abi_need(m && count, "null input");
     Multiplicator& mult = *m->m;
     const Context& bc = *mult.base;
     cudaStream_t st = as_stream(stream);
@@ -409,8 +388,8 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
 
 FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scalar, size_t scalar_words,
                                   const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(ctx && ((d_in && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(ctx && ((d_in && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     poly_scalar_mul(c, big(scalar, scalar_words), plain_ref(const_cast<uint64_t*>(d_in), c.L(), c.logn),
                     plain_ref(d_out, c.L(), c.logn), count, as_stream(stream));
@@ -418,30 +397,30 @@ FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scala
 }
 
 FHEG_API int fheg_device_alloc(size_t bytes, void** out) {
-  return guard([&] {
-    need(out != nullptr, "null output");
+  return abi_call([&] {
+    abi_need(out != nullptr, "null output");
     *out = nullptr;
     if (bytes) check_cuda(cudaMalloc(out, bytes), "cudaMalloc");
   });
 }
 
 FHEG_API int fheg_device_free(void* ptr) {
-  return guard([&] {
+  return abi_call([&] {
     if (ptr) check_cuda(cudaFree(ptr), "cudaFree");
   });
 }
 
 FHEG_API int fheg_copy_to_device(void* d_dst, const void* h_src, size_t bytes, void* stream) {
-  return guard([&] {
-    need((d_dst && h_src) || !bytes, "null input");
+  return abi_call([&] {
+    abi_need((d_dst && h_src) || !bytes, "null input");
     if (!bytes) return;
     check_cuda(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, as_stream(stream)), "H2D");
   });
 }
 
 FHEG_API int fheg_copy_to_host(void* h_dst, const void* d_src, size_t bytes, void* stream) {
-  return guard([&] {
-    need((h_dst && d_src) || !bytes, "null input");
+  return abi_call([&] {
+    abi_need((h_dst && d_src) || !bytes, "null input");
     if (!bytes) return;
     cudaStream_t st = as_stream(stream);
     check_cuda(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, st), "D2H");
@@ -451,9 +430,9 @@ FHEG_API int fheg_copy_to_host(void* h_dst, const void* d_src, size_t bytes, voi
 
 FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out,
                           size_t count, void* stream) {
-  return guard([&] {
-    need(ctx && op >= 0 && op <= 3, "bad context or op");
-    need((d_a && d_out && (op == 3 || d_b)) || !count, "null input");
+  return abi_call([&] {
+    abi_need(ctx && op >= 0 && op <= 3, "bad context or op");
+    abi_need((d_a && d_out && (op == 3 || d_b)) || !count, "null input");
     const Context& c = *ctx->c;
     PolyRef a = plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn);
     PolyRef b = plain_ref(const_cast<uint64_t*>(d_b ? d_b : d_a), c.L(), c.logn);
@@ -464,9 +443,9 @@ FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, 
 
 FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation, const uint64_t* d_in,
                                   uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(ctx && ((d_in && d_out) || !count), "null input");
-    need(d_in != d_out || !count, "d_out must not alias d_in");
+  return abi_call([&] {
+    abi_need(ctx && ((d_in && d_out) || !count), "null input");
+    abi_need(d_in != d_out || !count, "d_out must not alias d_in");
     const Context& c = *ctx->c;
     PolyRef i = plain_ref(const_cast<uint64_t*>(d_in), c.L(), c.logn);
     PolyRef o = plain_ref(d_out, c.L(), c.logn);
@@ -476,8 +455,8 @@ FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int 
 
 FHEG_API int fheg_poly_switch_down(const fheg_context* ctx, int representation, uint64_t* d_in, uint64_t* d_out,
                                    size_t count, void* stream) {
-  return guard([&] {
-    need(ctx && ((d_in && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(ctx && ((d_in && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     PolyRef i = plain_ref(d_in, c.L(), c.logn);
     PolyRef o = plain_ref(d_out, c.L() - 1, c.logn);
@@ -488,10 +467,10 @@ FHEG_API int fheg_poly_switch_down(const fheg_context* ctx, int representation, 
 
 FHEG_API int fheg_scaler_create(const fheg_context* from, const fheg_context* to, const uint64_t* num,
                                 size_t num_words, const uint64_t* den, size_t den_words, fheg_scaler** out) {
-  return guard([&] {
-    need(from && to && out, "null input");
+  return abi_call([&] {
+    abi_need(from && to && out, "null input");
     BigUint d = big(den, den_words);
-    need(!d.is_zero(), "ScalingFactor denominator is zero");
+    abi_need(!d.is_zero(), "ScalingFactor denominator is zero");
     auto h = new fheg_scaler();
     try {
       h->s.reset(new Scaler(from->c, to->c, big(num, num_words), d));
@@ -507,9 +486,9 @@ FHEG_API void fheg_scaler_destroy(fheg_scaler* s) { delete s; }
 
 FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const uint64_t* d_in, uint64_t* d_out,
                                size_t count, void* stream) {
-  return guard([&] {
-    need(s && ((d_in && d_out) || !count), "null input");
-    need(d_in != d_out || !count, "d_out must not alias d_in");
+  return abi_call([&] {
+    abi_need(s && ((d_in && d_out) || !count), "null input");
+    abi_need(d_in != d_out || !count, "d_out must not alias d_in");
     const Scaler& sc = *s->s;
     PolyRef i = plain_ref(const_cast<uint64_t*>(d_in), sc.from->L(), sc.from->logn);
     PolyRef o = plain_ref(d_out, sc.to->L(), sc.to->logn);
@@ -524,8 +503,8 @@ FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const u
 
 FHEG_API int fheg_params_create(size_t degree, const uint64_t* moduli, size_t num_moduli, uint64_t plaintext,
                                 fheg_params** out) {
-  return guard([&] {
-    need(moduli && num_moduli && out, "null or empty input");
+  return abi_call([&] {
+    abi_need(moduli && num_moduli && out, "null or empty input");
     auto h = new fheg_params();
     try {
       h->p.reset(new Params(degree, std::vector<uint64_t>(moduli, moduli + num_moduli), plaintext));
@@ -541,8 +520,8 @@ FHEG_API int fheg_params_create(size_t degree, const uint64_t* moduli, size_t nu
 FHEG_API void fheg_params_destroy(fheg_params* par) { delete par; }
 
 FHEG_API int fheg_params_context_at_level(const fheg_params* par, size_t level, const fheg_context** out) {
-  return guard([&] {
-    need(par && out, "null input");
+  return abi_call([&] {
+    abi_need(par && out, "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     *out = &par->level_handles[level];
   });
@@ -580,8 +559,8 @@ fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t
 
 FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
                              const uint64_t* h_c1, size_t count, fheg_ksk** out) {
-  return guard([&] {
-    need(par && h_c0 && h_c1 && out, "null input");
+  return abi_call([&] {
+    abi_need(par && h_c0 && h_c1 && out, "null input");
     fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
       const Ksk& k = h->k;
@@ -596,8 +575,8 @@ FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, si
 
 FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
                                     const uint64_t* h_c0, const uint8_t* seed, size_t count, fheg_ksk** out) {
-  return guard([&] {
-    need(par && h_c0 && seed && out, "null input");
+  return abi_call([&] {
+    abi_need(par && h_c0 && seed && out, "null input");
     fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
       const Ksk& k = h->k;
@@ -619,17 +598,17 @@ FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_le
 FHEG_API void fheg_ksk_destroy(fheg_ksk* k) { delete k; }
 
 FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(rk && ((d_ct3 && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(rk && ((d_ct3 && d_out) || !count), "null input");
     relinearize(rk->k, d_ct3, d_out, count, rk->k.ws, as_stream(stream));
   });
 }
 
 FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const uint64_t* d_ct, uint64_t* d_out,
                                      size_t count, void* stream) {
-  return guard([&] {
-    need(gk && ((d_ct && d_out) || !count), "null input");
-    need(d_ct != d_out || !count, "d_out must not alias d_ct");
+  return abi_call([&] {
+    abi_need(gk && ((d_ct && d_out) || !count), "null input");
+    abi_need(d_ct != d_out || !count, "d_out must not alias d_ct");
     galois_relinearize(gk->k, exponent, d_ct, d_out, count, gk->k.ws, as_stream(stream));
   });
 }
@@ -637,8 +616,8 @@ FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const 
 FHEG_API int fheg_rgsw_create(const fheg_params* par, size_t level, const uint64_t* h_ksk0_c0,
                               const uint64_t* h_ksk0_c1, const uint64_t* h_ksk1_c0, const uint64_t* h_ksk1_c1,
                               fheg_rgsw** out) {
-  return guard([&] {
-    need(par && h_ksk0_c0 && h_ksk0_c1 && h_ksk1_c0 && h_ksk1_c1 && out, "null input");
+  return abi_call([&] {
+    abi_need(par && h_ksk0_c0 && h_ksk0_c1 && h_ksk1_c0 && h_ksk1_c1 && out, "null input");
     const Params& p = *par->p;
     if (level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     auto h = new fheg_rgsw();
@@ -669,8 +648,8 @@ FHEG_API void fheg_rgsw_destroy(fheg_rgsw* rgsw) { delete rgsw; }
 
 FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, uint64_t* d_out, size_t count,
                                    void* stream) {
-  return guard([&] {
-    need(rgsw && ((d_ct && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(rgsw && ((d_ct && d_out) || !count), "null input");
     external_product(rgsw->k, d_ct, d_out, count, rgsw->k.ws, as_stream(stream));
   });
 }
@@ -678,11 +657,11 @@ FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, 
 FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
                                            const size_t* exponents, const uint64_t* const* d_cts,
                                            uint64_t* const* d_outs, size_t count, void* stream) {
-  return guard([&] {
-    need(par && ((keys && exponents && d_cts && d_outs) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((keys && exponents && d_cts && d_outs) || !count), "null input");
     std::vector<RotRequest> req(count);
     for (size_t b = 0; b < count; b++) {
-      need(keys[b] && d_cts[b] && d_outs[b] && d_cts[b] != d_outs[b], "null or aliased batch entry");
+      abi_need(keys[b] && d_cts[b] && d_outs[b] && d_cts[b] != d_outs[b], "null or aliased batch entry");
       req[b] = RotRequest{&keys[b]->k, exponents[b], d_cts[b], d_outs[b]};
     }
     galois_relinearize_batch(*par->p, req.data(), count, const_cast<fheg_params*>(par)->ws, as_stream(stream));
@@ -691,8 +670,8 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
 
 FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts, uint64_t* d_ct,
                                          uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(par && parts >= 1 && ((d_ct && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && parts >= 1 && ((d_ct && d_out) || !count), "null input");
     ciphertext_switch_down(*par->p, level, parts, d_ct, d_out, count, as_stream(stream));
   });
 }
@@ -700,8 +679,8 @@ FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, s
 FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t level, size_t target_level,
                                              size_t parts, uint64_t* d_ct, uint64_t* d_out, size_t count,
                                              void* stream) {
-  return guard([&] {
-    need(par && ((d_ct && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((d_ct && d_out) || !count), "null input");
     const Params& p = *par->p;
     if (target_level < level || target_level > p.max_level())
       throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
@@ -728,8 +707,8 @@ FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t leve
 
 FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_a,
                                  const uint64_t* d_b, uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(par && ((d_a && d_b && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((d_a && d_b && d_out) || !count), "null input");
     const Context& c = *par->p->ctx(level);
     PolyRef a = plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn);
     PolyRef b = plain_ref(const_cast<uint64_t*>(d_b), c.L(), c.logn);
@@ -739,8 +718,8 @@ FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t pa
 }
 
 FHEG_API int fheg_multiplicator_create_default(const fheg_ksk* rk, fheg_multiplicator** out) {
-  return guard([&] {
-    need(rk && out, "null input");
+  return abi_call([&] {
+    abi_need(rk && out, "null input");
     auto h = new fheg_multiplicator();
     try {
       h->m = make_default_multiplicator(rk->k);
@@ -758,10 +737,10 @@ FHEG_API int fheg_multiplicator_create(const fheg_params* par, size_t level, con
                                        size_t rhs_den_words, const uint64_t* extended_basis, size_t extended_len,
                                        const uint64_t* post_num, size_t post_num_words, const uint64_t* post_den,
                                        size_t post_den_words, fheg_multiplicator** out) {
-  return guard([&] {
-    need(par && extended_basis && extended_len && out, "null input");
+  return abi_call([&] {
+    abi_need(par && extended_basis && extended_len && out, "null input");
     BigUint ld = big(lhs_den, lhs_den_words), rd = big(rhs_den, rhs_den_words), pd = big(post_den, post_den_words);
-    need(!ld.is_zero() && !rd.is_zero() && !pd.is_zero(), "ScalingFactor denominator is zero");
+    abi_need(!ld.is_zero() && !rd.is_zero() && !pd.is_zero(), "ScalingFactor denominator is zero");
     auto h = new fheg_multiplicator();
     try {
       h->m = make_multiplicator(*par->p, level, big(lhs_num, lhs_num_words), ld, big(rhs_num, rhs_num_words), rd,
@@ -778,8 +757,8 @@ FHEG_API int fheg_multiplicator_create(const fheg_params* par, size_t level, con
 FHEG_API void fheg_multiplicator_destroy(fheg_multiplicator* m) { delete m; }
 
 FHEG_API int fheg_multiplicator_enable_relinearization(fheg_multiplicator* m, const fheg_ksk* rk) {
-  return guard([&] {
-    need(m && rk, "null input");
+  return abi_call([&] {
+    abi_need(m && rk, "null input");
     // mul.rs:133-142
     if (!rk->k.ctx_ct->same_as(*m->m->base) || rk->k.par != m->m->par)
       throw Error(FHEG_ERR_KEY_MISMATCH, "Invalid relinearization key context");
@@ -790,8 +769,8 @@ FHEG_API int fheg_multiplicator_enable_relinearization(fheg_multiplicator* m, co
 }
 
 FHEG_API int fheg_multiplicator_enable_mod_switching(fheg_multiplicator* m) {
-  return guard([&] {
-    need(m != nullptr, "null input");
+  return abi_call([&] {
+    abi_need(m != nullptr, "null input");
     // mul.rs:146-155
     if (m->m->level >= m->m->par->max_level())
       throw Error(FHEG_ERR_NO_MORE_CONTEXT, "Cannot modulo switch as this is already the last level");
@@ -800,8 +779,8 @@ FHEG_API int fheg_multiplicator_enable_mod_switching(fheg_multiplicator* m) {
 }
 
 FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t* parts, size_t* level) {
-  return guard([&] {
-    need(m && parts && level, "null input");
+  return abi_call([&] {
+    abi_need(m && parts && level, "null input");
     *parts = m->m->out_parts();
     *level = m->m->out_level();
   });
@@ -809,15 +788,15 @@ FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t
 
 FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                          uint64_t* d_out, size_t count, void* stream) {
-  return guard([&] {
-    need(m && ((d_lhs && d_rhs && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(m && ((d_lhs && d_rhs && d_out) || !count), "null input");
     m->m->multiply(d_lhs, d_rhs, d_out, count, as_stream(stream));
   });
 }
 
 FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t chunk, int streams) {
-  return guard([&] {
-    need(m && streams >= 1 && streams <= fheg_multiplicator::kPipe, "null multiplicator or streams outside 1..4");
+  return abi_call([&] {
+    abi_need(m && streams >= 1 && streams <= fheg_multiplicator::kPipe, "null multiplicator or streams outside 1..4");
     m->host_chunk = chunk;
     m->host_streams = streams;
   });
@@ -825,8 +804,8 @@ FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t 
 
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs, const uint64_t* h_rhs,
                                               uint64_t* h_out, size_t count) {
-  return guard([&] {
-    need(m && ((h_lhs && h_rhs && h_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(m && ((h_lhs && h_rhs && h_out) || !count), "null input");
     if (!count) return;
     Multiplicator& mm = *m->m;
     const size_t N = mm.base->N(), L = mm.base->L();

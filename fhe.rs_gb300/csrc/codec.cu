@@ -14,6 +14,7 @@
 
 #include "fheg.h"
 #include "handles.hpp"
+#include "abi_call.hpp"
 #include "lib.hpp"
 #include "ntt.cuh"
 
@@ -326,33 +327,10 @@ void decrypt(const SecretKeyDev& sk, size_t level, size_t parts, const uint64_t*
 
 using namespace fheg;
 
-namespace {
-
-template <class F>
-int guarded(F&& f) {
-  try {
-    set_last_error("");
-    f();
-    return FHEG_OK;
-  } catch (const Error& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return FHEG_ERR_INTERNAL;
-  }
-}
-
-void need(bool cond, const char* what) {
-  if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
-}
-
-}  // namespace
-
 FHEG_API int fheg_plaintext_encode(const fheg_params* par, size_t level, const uint64_t* d_values, int simd,
                                    uint64_t* d_pt_ntt, size_t count, void* stream) {
-  return guarded([&] {
-    need(par && ((d_values && d_pt_ntt) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((d_values && d_pt_ntt) || !count), "null input");
     plaintext_encode(*par->p, level, d_values, simd != 0, d_pt_ntt, count, const_cast<fheg_params*>(par)->ws,
                      static_cast<cudaStream_t>(stream));
   });
@@ -361,16 +339,16 @@ FHEG_API int fheg_plaintext_encode(const fheg_params* par, size_t level, const u
 FHEG_API int fheg_ciphertext_mul_plain(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_ct,
                                        const uint64_t* d_pt_ntt, int pt_per_ciphertext, uint64_t* d_out,
                                        size_t count, void* stream) {
-  return guarded([&] {
-    need(par && parts >= 1 && ((d_ct && d_pt_ntt && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && parts >= 1 && ((d_ct && d_pt_ntt && d_out) || !count), "null input");
     ciphertext_mul_plain(*par->p, level, parts, d_ct, d_pt_ntt, pt_per_ciphertext != 0, d_out, count,
                          static_cast<cudaStream_t>(stream));
   });
 }
 
 FHEG_API int fheg_secret_key_create(const fheg_params* par, const int64_t* coeffs, fheg_secret_key** out) {
-  return guarded([&] {
-    need(par && coeffs && out, "null input");
+  return abi_call([&] {
+    abi_need(par && coeffs && out, "null input");
     const Params& p = *par->p;
     const Context& c = *p.ctx(0);
     const size_t L = c.L(), N = c.N();
@@ -400,16 +378,16 @@ FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk) { delete sk; }
 
 FHEG_API int fheg_encrypt(const fheg_secret_key* sk, size_t level, const uint64_t* d_values, int simd,
                           const uint64_t* d_a, const int64_t* d_e, uint64_t* d_ct, size_t count, void* stream) {
-  return guarded([&] {
-    need(sk && ((d_values && d_a && d_e && d_ct) || !count), "null input");
+  return abi_call([&] {
+    abi_need(sk && ((d_values && d_a && d_e && d_ct) || !count), "null input");
     encrypt(sk->k, level, d_values, simd != 0, d_a, d_e, d_ct, count, sk->ws, static_cast<cudaStream_t>(stream));
   });
 }
 
 FHEG_API int fheg_decrypt(const fheg_secret_key* sk, size_t level, size_t parts, const uint64_t* d_ct, int simd,
                           uint64_t* d_values, size_t count, void* stream) {
-  return guarded([&] {
-    need(sk && ((d_ct && d_values) || !count), "null input");
+  return abi_call([&] {
+    abi_need(sk && ((d_ct && d_values) || !count), "null input");
     decrypt(sk->k, level, parts, d_ct, simd != 0, d_values, count, sk->ws, static_cast<cudaStream_t>(stream));
   });
 }

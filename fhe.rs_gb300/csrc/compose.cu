@@ -7,6 +7,7 @@
 
 #include "fheg.h"
 #include "handles.hpp"
+#include "abi_call.hpp"
 #include "lib.hpp"
 
 namespace fheg {
@@ -140,29 +141,11 @@ using namespace fheg;
 
 namespace {
 
-template <class F>
-int guarded(F&& f) {
-  try {
-    set_last_error("");
-    f();
-    return FHEG_OK;
-  } catch (const Error& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return FHEG_ERR_INTERNAL;
-  }
-}
-
-void need(bool cond, const char* what) {
-  if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
-}
 
 std::vector<const Ksk*> key_list(const fheg_ksk* const* keys, size_t n) {
   std::vector<const Ksk*> out(n);
   for (size_t i = 0; i < n; i++) {
-    need(keys[i] != nullptr, "null key");
+    abi_need(keys[i] != nullptr, "null key");
     out[i] = &keys[i]->k;
   }
   return out;
@@ -173,16 +156,16 @@ std::vector<const Ksk*> key_list(const fheg_ksk* const* keys, size_t n) {
 FHEG_API int fheg_dot_product_scalar(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_cts,
                                      const uint64_t* d_pts, size_t count, size_t groups, uint64_t* d_out,
                                      void* stream) {
-  return guarded([&] {
-    need(par && parts >= 1 && ((d_cts && d_pts && d_out) || !groups), "null input");
+  return abi_call([&] {
+    abi_need(par && parts >= 1 && ((d_cts && d_pts && d_out) || !groups), "null input");
     dot_product_scalar(*par->p, level, parts, d_cts, d_pts, count, groups, d_out, static_cast<cudaStream_t>(stream));
   });
 }
 
 FHEG_API int fheg_inner_sum(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
                             size_t nkeys, const uint64_t* d_ct, uint64_t* d_out, size_t count, void* stream) {
-  return guarded([&] {
-    need(par && keys && exponents && nkeys && ((d_ct && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && keys && exponents && nkeys && ((d_ct && d_out) || !count), "null input");
     std::vector<uint64_t> ex(exponents, exponents + nkeys);
     const auto k = key_list(keys, nkeys);
     inner_sum(*par->p, k.data(), ex.data(), nkeys, d_ct, d_out, count, const_cast<fheg_params*>(par)->ws,
@@ -192,8 +175,8 @@ FHEG_API int fheg_inner_sum(const fheg_params* par, const fheg_ksk* const* keys,
 
 FHEG_API int fheg_expand(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
                          size_t nlevels, size_t size, const uint64_t* d_ct, uint64_t* d_out, void* stream) {
-  return guarded([&] {
-    need(par && d_ct && d_out && (nlevels == 0 || (keys && exponents)), "null input");
+  return abi_call([&] {
+    abi_need(par && d_ct && d_out && (nlevels == 0 || (keys && exponents)), "null input");
     std::vector<uint64_t> ex(exponents, exponents + nlevels);
     const auto k = key_list(keys, nlevels);
     expand(*par->p, k.data(), ex.data(), nlevels, size, d_ct, d_out, const_cast<fheg_params*>(par)->ws,

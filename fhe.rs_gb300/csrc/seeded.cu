@@ -22,6 +22,7 @@
 #include <cstring>
 #include <vector>
 
+#include "abi_call.hpp"
 #include "fheg.h"
 #include "handles.hpp"
 #include "lib.hpp"
@@ -304,18 +305,10 @@ using namespace fheg;
 
 FHEG_API int fheg_poly_random_from_seed(const fheg_context* ctx, const uint8_t* d_seeds, uint64_t* d_out,
                                         size_t poly_stride, size_t count, void* stream) {
-  try {
-    set_last_error("");
-    if (!ctx || ((!d_seeds || !d_out) && count)) throw Error(FHEG_ERR_INVALID_ARGUMENT, "null input");
+  return abi_call([&] {
+    abi_need(ctx && ((d_seeds && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     poly_random_from_seed(c, d_seeds, d_out, poly_stride ? poly_stride : c.L() * c.N(), count, *ctx->ws,
                           static_cast<cudaStream_t>(stream));
-    return FHEG_OK;
-  } catch (const Error& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return FHEG_ERR_INTERNAL;
-  }
+  });
 }

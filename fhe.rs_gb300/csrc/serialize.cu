@@ -12,6 +12,7 @@
 
 #include "fheg.h"
 #include "handles.hpp"
+#include "abi_call.hpp"
 #include "lib.hpp"
 
 namespace fheg {
@@ -509,41 +510,18 @@ fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t le
 
 using namespace fheg;
 
-namespace {
-
-template <class F>
-int guarded(F&& f) {
-  try {
-    set_last_error("");
-    f();
-    return FHEG_OK;
-  } catch (const Error& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return FHEG_ERR_INTERNAL;
-  }
-}
-
-void need(bool cond, const char* what) {
-  if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
-}
-
-}  // namespace
-
 FHEG_API int fheg_poly_serialized_size(const fheg_context* ctx, size_t* bytes) {
-  return guarded([&] {
-    need(ctx && bytes, "null input");
+  return abi_call([&] {
+    abi_need(ctx && bytes, "null input");
     *bytes = poly_serialized_bytes(*ctx->c);
   });
 }
 
 FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, const uint64_t* d_polys,
                                  uint8_t* d_bytes, size_t count, void* stream) {
-  return guarded([&] {
-    need(ctx && (representation == 0 || representation == 1), "bad context or representation");
-    need((d_polys && d_bytes) || !count, "null input");
+  return abi_call([&] {
+    abi_need(ctx && (representation == 0 || representation == 1), "bad context or representation");
+    abi_need((d_polys && d_bytes) || !count, "null input");
     DevBuf scratch;
     poly_serialize(*ctx->c, representation, d_polys, d_bytes, count, scratch, static_cast<cudaStream_t>(stream));
     if (scratch.ptr) check_cuda(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
@@ -552,17 +530,17 @@ FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, co
 
 FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, const uint8_t* d_bytes,
                                    uint64_t* d_polys, size_t count, void* stream) {
-  return guarded([&] {
-    need(ctx && (representation == 0 || representation == 1), "bad context or representation");
-    need((d_polys && d_bytes) || !count, "null input");
+  return abi_call([&] {
+    abi_need(ctx && (representation == 0 || representation == 1), "bad context or representation");
+    abi_need((d_polys && d_bytes) || !count, "null input");
     poly_deserialize(*ctx->c, representation, d_bytes, d_polys, count, static_cast<cudaStream_t>(stream));
   });
 }
 
 FHEG_API int fheg_ciphertext_serialized_size(const fheg_params* par, size_t level, size_t parts, int seeded,
                                              int allow_variable_time, size_t* bytes) {
-  return guarded([&] {
-    need(par && bytes, "null input");
+  return abi_call([&] {
+    abi_need(par && bytes, "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     if (parts < 1 || (seeded && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
     *bytes = ciphertext_message_len(*par->p, level, parts, seeded != 0, allow_variable_time != 0);
@@ -572,12 +550,12 @@ FHEG_API int fheg_ciphertext_serialized_size(const fheg_params* par, size_t leve
 FHEG_API int fheg_ciphertext_to_bytes(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_ct,
                                       size_t count, const uint8_t* h_seeds, int allow_variable_time, uint8_t* h_out,
                                       size_t out_capacity, void* stream) {
-  return guarded([&] {
-    need(par && ((d_ct && h_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((d_ct && h_out) || !count), "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     if (parts < 1 || (h_seeds && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
     const size_t one = ciphertext_message_len(*par->p, level, parts, h_seeds != nullptr, allow_variable_time != 0);
-    need(out_capacity >= count * one, "output buffer too small");
+    abi_need(out_capacity >= count * one, "output buffer too small");
     ciphertext_to_bytes(*par->p, level, parts, d_ct, count, h_seeds, allow_variable_time != 0, h_out,
                         const_cast<fheg_params*>(par)->ws, static_cast<cudaStream_t>(stream));
   });
@@ -585,16 +563,16 @@ FHEG_API int fheg_ciphertext_to_bytes(const fheg_params* par, size_t level, size
 
 FHEG_API int fheg_ciphertext_peek(const fheg_params* par, const uint8_t* h_msg, size_t len, size_t* level,
                                   size_t* parts, int* seeded) {
-  return guarded([&] {
-    need(par && h_msg && level && parts && seeded, "null input");
+  return abi_call([&] {
+    abi_need(par && h_msg && level && parts && seeded, "null input");
     ciphertext_peek(*par->p, h_msg, len, level, parts, seeded);
   });
 }
 
 FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* const* h_msgs, const size_t* lens,
                                         size_t count, size_t level, size_t parts, uint64_t* d_out, void* stream) {
-  return guarded([&] {
-    need(par && ((h_msgs && lens && d_out) || !count), "null input");
+  return abi_call([&] {
+    abi_need(par && ((h_msgs && lens && d_out) || !count), "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     if (parts < 2) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
     fheg_params* p = const_cast<fheg_params*>(par);
@@ -605,8 +583,8 @@ FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* c
 
 FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len, int kind,
                                  fheg_ksk** out, size_t* exponent, size_t* ciphertext_level, size_t* ksk_level) {
-  return guarded([&] {
-    need(par && h_msg && out && kind >= 0 && kind <= 2, "null input or bad kind");
+  return abi_call([&] {
+    abi_need(par && h_msg && out && kind >= 0 && kind <= 2, "null input or bad kind");
     uint64_t e = 0;
     fheg_ksk* h = ksk_from_message(par, h_msg, len, kind, &e);
     if (exponent) *exponent = (size_t)e;
