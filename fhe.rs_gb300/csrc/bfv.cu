@@ -767,16 +767,22 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   mark(1);
   // B + C: extension of each operand and forward NTT of the new limbs.
   const bool same_ext = ncm_l == ncm_r && ext_lhs->num == ext_rhs->num && ext_lhs->den == ext_rhs->den;
+  // C's strided first stages run in B's epilogue when both transforms have
+  // the same number of them (B then writes C's block-pass input).
+  const uint32_t bl_c = plan_c ? plan_c : ntt_block_logn(logn);
+  const bool fuse_c = top_a && bl_c < logn && logn - bl_c == top_a;
   auto extend = [&](const Scaler& s, uint32_t first, uint32_t take) {
     const size_t ncm = s.number_common_moduli;
     PolyRef in = sub_ref(pb, L, logn, 4, first, take);
     PolyRef o = sub_ref(ext, M, logn, 4, first, take);
     o.base += (uint64_t)ncm << logn;
+    const ForwardTop fwd{top_a, mc.primes_dev() + ncm};
     rns_scale(*s.rns, logn, in, o, (uint32_t)ncm, (uint32_t)(M - ncm), count * take, st,
-              top_a ? &top_a_args : nullptr);
+              top_a ? &top_a_args : nullptr, fuse_c ? &fwd : nullptr);
     if (first == 0) mark(2);
     NttGeom g{mc.primes_dev() + ncm, (uint32_t)(M - ncm), 0};
-    ntt_forward_any<true>(logn, g, count * take, SrcPoly{o}, DstPoly{o}, st, plan_c);
+    if (fuse_c) ntt_forward_after_top<true>(logn, g, count * take, DstPoly{o}, st, plan_c);
+    else ntt_forward_any<true>(logn, g, count * take, SrcPoly{o}, DstPoly{o}, st, plan_c);
   };
   if (same_ext) {
     extend(*ext_lhs, 0, 4);

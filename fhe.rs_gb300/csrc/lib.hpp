@@ -119,10 +119,18 @@ struct InverseTop {
   uint32_t mont;
   const DevPrime* primes;
 };
+// The strided first stages of a two-pass forward NTT applied by its
+// producer: `s1` stages, `primes` one DevPrime per output limb.
+struct ForwardTop {
+  uint32_t s1;
+  const DevPrime* primes;
+};
 // top != nullptr: `in` is the block pass of such a transform, and the scaler
 // applies its last stages while loading (only where rns_scale_takes_top).
+// fwd != nullptr (with top, the same s1): the outputs are written after the
+// first stages of the forward NTT that consumes them.
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
-               uint64_t polys, cudaStream_t st, const InverseTop* top = nullptr);
+               uint64_t polys, cudaStream_t st, const InverseTop* top = nullptr, const ForwardTop* fwd = nullptr);
 bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1);
 // Scaler::scale. `scratch` must hold polys * max(L_from, L_to) * N words.
 void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t polys, uint64_t* scratch,

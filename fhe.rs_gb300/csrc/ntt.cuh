@@ -447,17 +447,13 @@ __global__ void __launch_bounds__(1024) k_ntt_inv_small(NttGeom g, uint32_t logn
 // forward stages / the last S1 inverse stages, on groups of 2^S1 elements
 // b + t * 2^LOGB. One thread per group.
 
-template <int S1, class Src, class Dst>
-__global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
-                                                     uint64_t total, Src src, Dst dst) {
-  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total) return;
-  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
-  const NttJob jb = unit_job(g, row_of(gid, logb));
-  const DevPrime pr = g.primes[jb.limb];
-  uint64_t x[1 << S1];
-#pragma unroll
-  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+// The first S1 forward stages of a transform on the 2^S1 elements
+// x[t] = element b + t * N / 2^S1 of one limb (inputs below 4p, outputs lazy
+// in [0, 4p)): what the strided forward pass does per thread, also applied
+// by producers that write the block pass's input directly (the RNS scaler of
+// the multiplication).
+template <int S1>
+__device__ __forceinline__ void fwd_top_stages(uint64_t* x, const DevPrime& pr) {
 #pragma unroll
   for (int s = 0; s < S1; s++) {
     const int half = 1 << (S1 - 1 - s);
@@ -472,6 +468,20 @@ __global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, u
       }
     }
   }
+}
+
+template <int S1, class Src, class Dst>
+__global__ void __launch_bounds__(256) k_ntt_fwd_top(NttGeom g, uint32_t logb, uint32_t groups_per_limb,
+                                                     uint64_t total, Src src, Dst dst) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t b = (uint32_t)gid & (groups_per_limb - 1);  // groups_per_limb = 2^logb
+  const NttJob jb = unit_job(g, row_of(gid, logb));
+  const DevPrime pr = g.primes[jb.limb];
+  uint64_t x[1 << S1];
+#pragma unroll
+  for (int t = 0; t < (1 << S1); t++) x[t] = src(jb, pr, b + ((uint32_t)t << logb));
+  fwd_top_stages<S1>(x, pr);
 #pragma unroll
   for (int t = 0; t < (1 << S1); t++) dst(jb, pr, b + ((uint32_t)t << logb), x[t]);
 }
@@ -700,6 +710,22 @@ void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst,
   const uint32_t s1 = logn - bl;
   launch_fwd_top(s1, g, bl, polys, src, dst, st);
   g.s1 = s1;
+  switch (bl) {
+    case 12: launch_fwd_block<12, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    case 13: launch_fwd_block<13, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    case 14: launch_fwd_block<14, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    default: throw Error(12, "unsupported NTT plan");
+  }
+}
+
+// The block pass of a two-pass forward NTT of `dst` in place, for data whose
+// strided first logn - bl stages a producer already applied
+// (fwd_top_stages). Requires a two-pass plan.
+template <bool REDUCE, class Dst>
+void ntt_forward_after_top(uint32_t logn, NttGeom g, uint64_t polys, Dst dst, cudaStream_t st, uint32_t bl = 0) {
+  if (bl == 0) bl = ntt_block_logn(logn);
+  if (bl >= logn || logn < 13) throw Error(12, "the forward NTT plan has no strided stages");
+  g.s1 = logn - bl;
   switch (bl) {
     case 12: launch_fwd_block<12, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
     case 13: launch_fwd_block<13, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;

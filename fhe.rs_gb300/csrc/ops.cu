@@ -438,12 +438,26 @@ struct RnsLaunch {
 // (inv_top_stages, the strided inverse pass's arithmetic) into shared memory,
 // and each thread scales one coefficient from there. The strided pass and
 // its round trip through HBM disappear; the results are the same.
+//
+// With TOP > 0 and fwd_primes set, the outputs are themselves the input of a
+// two-pass forward NTT whose strided first TOP stages this kernel applies
+// (fwd_top_stages, output limb o in fwd_primes[o]): they go through shared
+// memory so that each group's 2^TOP coefficients meet, and leave lazy in
+// [0, 4p) for the block pass.
+template <int WORDS>
+__device__ __forceinline__ uint64_t* rns_stage_buffer() {
+  __shared__ uint64_t buf[WORDS];
+  return buf;
+}
+
 template <int MAXF, int MAXT, bool EXACT, int TOP>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
                                                    PolyRef in, PolyRef out, uint64_t total,
-                                                   const DevPrime* src_primes, uint32_t src_mont) {
+                                                   const DevPrime* src_primes, uint32_t src_mont,
+                                                   const DevPrime* fwd_primes) {
   const uint32_t F = EXACT ? (uint32_t)MAXF : s.from_len;
-  uint32_t i, poly;
+  constexpr int G = 128 >> TOP;  // groups per CTA (TOP > 0)
+  uint32_t i, poly, b0 = 0, logb = 0, t = 0, gi = 0;
   uint64_t r[MAXF];
   if constexpr (TOP == 0) {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -455,12 +469,11 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? src[(uint64_t)k << logn] : 0;
   } else {
     // The grid covers whole polynomials (2^logn is a multiple of 128), so
-    // every thread reaches the barrier.
-    constexpr int G = 128 >> TOP;  // groups per CTA
-    __shared__ uint64_t staged[MAXF * 128];
+    // every thread reaches the barriers.
+    uint64_t* staged = rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>();
     poly = blockIdx.x >> (logn - 7);
-    const uint32_t b0 = (blockIdx.x & ((1u << (logn - 7)) - 1)) * G;
-    const uint32_t logb = logn - TOP;
+    b0 = (blockIdx.x & ((1u << (logn - 7)) - 1)) * G;
+    logb = logn - TOP;
     for (uint32_t item = threadIdx.x; item < F * G; item += 128) {
       const uint32_t k = item / G, gi = item % G;
       const uint64_t* row = in.at(poly, k) + b0 + gi;
@@ -472,10 +485,12 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       for (int t = 0; t < (1 << TOP); t++) staged[(k * (1 << TOP) + t) * G + gi] = x[t];
     }
     __syncthreads();
-    const uint32_t t = threadIdx.x / G, gi = threadIdx.x % G;
+    t = threadIdx.x / G;
+    gi = threadIdx.x % G;
     i = b0 + gi + (t << logb);
 #pragma unroll
     for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? staged[(k * (1 << TOP) + t) * G + gi] : 0;
+    if (fwd_primes) __syncthreads();  // the buffer takes the outputs next
   }
 
   // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2).
@@ -569,14 +584,37 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
           }
         }
       }
-      dst[(uint64_t)o << logn] = reduce128(hi, lo, pr);
+      const uint64_t y = reduce128(hi, lo, pr);
+      if constexpr (TOP > 0) {
+        if (fwd_primes) rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>()[(o * (1 << TOP) + t) * G + gi] = y;
+        else dst[(uint64_t)o << logn] = y;
+      } else {
+        dst[(uint64_t)o << logn] = y;
+      }
+    }
+  }
+  if constexpr (TOP > 0) {
+    if (fwd_primes) {
+      __syncthreads();
+      const uint64_t* staged = rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>();
+      for (uint32_t item = threadIdx.x; item < s.out_len * G; item += 128) {
+        const uint32_t o = item / G, g2 = item % G;
+        uint64_t x[1 << TOP];
+#pragma unroll
+        for (int u = 0; u < (1 << TOP); u++) x[u] = staged[(o * (1 << TOP) + u) * G + g2];
+        fwd_top_stages<TOP>(x, fwd_primes[o]);
+        uint64_t* row = out.at(poly, o) + b0 + g2;
+#pragma unroll
+        for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
+      }
     }
   }
 }
 
 template <int MAXF, int MAXT, bool EXACT = false, int TOP = 0>
 void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
-                      uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop* top = nullptr) {
+                      uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop* top = nullptr,
+                      const ForwardTop* fwd = nullptr) {
   const RnsScalerHost& h = sc.host;
   const size_t F = h.from_len;
   for (uint32_t first = 0; first < out_len; first += MAXT) {
@@ -610,18 +648,20 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     o.base += (uint64_t)first << logn;
     const unsigned threads = 128;
     k_rns_scale<MAXF, MAXT, EXACT, TOP><<<blocks_for(total, threads), threads, 0, st>>>(
-        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u);
+        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u,
+        fwd ? fwd->primes + first : nullptr);
     after_launch("k_rns_scale");
   }
 }
 
 template <int MAXF, int MAXT>
 static void launch_rns_scale_top(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
-                                 uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop& top) {
+                                 uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop& top,
+                                 const ForwardTop* fwd) {
   switch (top.s1) {
-    case 1: launch_rns_scale<MAXF, MAXT, true, 1>(s, logn, in, out, start, out_len, total, st, &top); break;
-    case 2: launch_rns_scale<MAXF, MAXT, true, 2>(s, logn, in, out, start, out_len, total, st, &top); break;
-    case 3: launch_rns_scale<MAXF, MAXT, true, 3>(s, logn, in, out, start, out_len, total, st, &top); break;
+    case 1: launch_rns_scale<MAXF, MAXT, true, 1>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
+    case 2: launch_rns_scale<MAXF, MAXT, true, 2>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
+    case 3: launch_rns_scale<MAXF, MAXT, true, 3>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
     default: throw Error(FHEG_ERR_INTERNAL, "unsupported strided stage count");
   }
 }
@@ -633,19 +673,21 @@ bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, u
 }
 
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
-               uint64_t polys, cudaStream_t st, const InverseTop* top) {
+               uint64_t polys, cudaStream_t st, const InverseTop* top, const ForwardTop* fwd) {
   const uint64_t total = polys << logn;
   if (total == 0 || out_len == 0) return;
   const size_t F = s.host.from_len;
+  if (fwd && (!top || fwd->s1 != top->s1))
+    throw Error(FHEG_ERR_INTERNAL, "forward strided stages need the same count of inverse ones");
   if (top) {
     if (!rns_scale_takes_top(s, logn, out_len, top->s1))
       throw Error(FHEG_ERR_INTERNAL, "RNS scaling cannot apply these strided stages");
-    if (F == 6) launch_rns_scale_top<6, 8>(s, logn, in, out, start, out_len, total, st, *top);
-    else if (F == 13) launch_rns_scale_top<13, 8>(s, logn, in, out, start, out_len, total, st, *top);
-    else if (F == 3) launch_rns_scale_top<3, 8>(s, logn, in, out, start, out_len, total, st, *top);
-    else if (F == 7) launch_rns_scale_top<7, 8>(s, logn, in, out, start, out_len, total, st, *top);
-    else if (F == 12) launch_rns_scale_top<12, 16>(s, logn, in, out, start, out_len, total, st, *top);
-    else launch_rns_scale_top<25, 16>(s, logn, in, out, start, out_len, total, st, *top);
+    if (F == 6) launch_rns_scale_top<6, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
+    else if (F == 13) launch_rns_scale_top<13, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
+    else if (F == 3) launch_rns_scale_top<3, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
+    else if (F == 7) launch_rns_scale_top<7, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
+    else if (F == 12) launch_rns_scale_top<12, 16>(s, logn, in, out, start, out_len, total, st, *top, fwd);
+    else launch_rns_scale_top<25, 16>(s, logn, in, out, start, out_len, total, st, *top, fwd);
     return;
   }
   // Exact source counts of the default multiplications at L = 3, 6, 12
