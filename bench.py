@@ -49,15 +49,16 @@ STAGE_LIMBS = {
 }
 STAGE_KERNELS = {
     "A": "k_ntt_inv<12, SrcPair> (inverse NTT of the operands, block pass; its strided last stages run in B)",
-    "B": "k_rns_scale<6, 8> (strided last stages of A, then basis extension 6 -> 7 new moduli)",
-    "C": "k_ntt_fwd_top<2> + k_ntt_fwd<12> (forward NTT of the extension limbs)",
+    "B": "k_rns_scale<6, 8> (A's strided last stages, extension 6 -> 7 new moduli, C's strided first stages)",
+    "C": "k_ntt_fwd<12> (forward NTT of the extension limbs, block pass)",
     "D": "k_ntt_inv<12, SrcTensor> (tensor product + inverse NTT, block pass; its strided last stages run in E)",
-    "E": "k_rns_scale<13, 8> (strided last stages of D, then t/Q scale-down 13 -> 6 moduli)",
-    "F": "k_ntt_fwd_top<2> + k_ntt_fwd<12>, twice (digit NTTs in every key modulus, then c0/c1 NTTs)",
+    "E": "k_rns_scale<13, 8> (D's strided last stages, t/Q scale-down 13 -> 6, F's strided first stages and "
+         "digit expansion)",
+    "F": "k_ntt_fwd<12>, twice (digit NTTs in every key modulus, then c0/c1 NTTs; block passes)",
     "G": "k_key_mac (key inner product)",
 }
 # Kernel launches of each stage under the same plan.
-STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 2, "D": 1, "E": 1, "F": 4, "G": 1}
+STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # DRAM bytes (read + write) of each stage's kernels for one 64-pair
 # multiplication with the plan A,C,D,F = 12 (2^12-residue blocks; the forward
 # transforms after a strided pass over two stages, the inverse ones with those

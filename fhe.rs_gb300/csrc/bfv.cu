@@ -817,7 +817,23 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   // strided last stages of D's inverse NTT (Montgomery products) on the way.
   PolyRef dnref = plain_ref(dn, L, logn);
   const InverseTop top_d_args{top_d, 1u, mc.primes_dev()};
-  rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st, top_d ? &top_d_args : nullptr);
+  // F's strided first stages run in E's epilogue when F's plan has as many as
+  // D's: c0 and c1 get them over their own limbs (left in dn for F's block
+  // pass), and c2 is expanded there into the digit rows of every key modulus
+  // (written to D), so F runs only its block passes.
+  const uint32_t bf = plan_f ? plan_f : ntt_block_logn(logn);
+  const bool fuse_f = rk && top_d && bf < logn && logn - bf == top_d;
+  ForwardTop fwd_e{top_d, bc.primes_dev()};
+  if (fuse_f) {
+    fwd_e.period = 3;
+    fwd_e.take = 2;
+    fwd_e.digit_primes = rk->ctx_ksk->primes_dev();
+    fwd_e.digit_limbs = (uint32_t)Lk;
+    fwd_e.digit_raw = digits_fit(bc.moduli, rk->ctx_ksk->moduli);
+    fwd_e.digits = plain_ref(D, Lk, logn);
+  }
+  rns_scale(*down->rns, logn, prodref, dnref, 0, (uint32_t)L, 3 * count, st, top_d ? &top_d_args : nullptr,
+            fuse_f ? &fwd_e : nullptr);
   mark(5);
   NttGeom gb{bc.primes_dev(), (uint32_t)L, 0};
   if (rk) {
@@ -827,8 +843,10 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     PolyRef c01 = sub_ref(dn, L, logn, 3, 0, 2);
     PolyRef oref = plain_ref(dest, L, logn);
     NttGeom gk{kc.primes_dev(), (uint32_t)Lk, 0};
-    const uint32_t bf = plan_f ? plan_f : ntt_block_logn(logn);
-    if (bf >= logn && !f_split) {
+    if (fuse_f) {
+      ntt_forward_after_top<true>(logn, gk, count * L, DstPoly{dref}, st, bf);
+      ntt_forward_after_top<true>(logn, gb, 2 * count, DstPoly{c01}, DstPoly{oref}, st, bf);
+    } else if (bf >= logn && !f_split) {
       // F: digit NTTs and the c0 / c1 NTTs in one launch (Lk == L).
       const uint32_t ndp = (uint32_t)(count * L);
       ntt_fwd_single<true>(logn, gk, count * L + 2 * count, SrcKsF{c2, c01, (uint32_t)L, ndp},

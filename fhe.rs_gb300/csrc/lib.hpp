@@ -119,11 +119,20 @@ struct InverseTop {
   uint32_t mont;
   const DevPrime* primes;
 };
-// The strided first stages of a two-pass forward NTT applied by its
-// producer: `s1` stages, `primes` one DevPrime per output limb.
+// The strided first stages of two-pass forward NTTs applied by their
+// producer, the RNS scaler: `s1` stages. Polynomials with poly % period <
+// take (period 0: all) get them over their own output limbs (`primes`, one
+// per output limb). With `digit_primes` set, the other polynomials are the c2
+// of products: their output limb d is lifted into every key modulus j
+// (reduced first unless `digit_raw`), given the stages there and written to
+// digits.at((poly / period) * out_len + d, j).
 struct ForwardTop {
   uint32_t s1;
   const DevPrime* primes;
+  uint32_t period = 0, take = 1;
+  const DevPrime* digit_primes = nullptr;
+  uint32_t digit_limbs = 0, digit_raw = 0;
+  PolyRef digits{};
 };
 // top != nullptr: `in` is the block pass of such a transform, and the scaler
 // applies its last stages while loading (only where rns_scale_takes_top).

@@ -721,17 +721,25 @@ void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst,
 // The block pass of a two-pass forward NTT of `dst` in place, for data whose
 // strided first logn - bl stages a producer already applied
 // (fwd_top_stages). Requires a two-pass plan.
-template <bool REDUCE, class Dst>
-void ntt_forward_after_top(uint32_t logn, NttGeom g, uint64_t polys, Dst dst, cudaStream_t st, uint32_t bl = 0) {
+// `from` (a destination functor) names where the producer left that data
+// when it is not `dst` itself.
+template <bool REDUCE, class From, class Dst>
+void ntt_forward_after_top(uint32_t logn, NttGeom g, uint64_t polys, From from, Dst dst, cudaStream_t st,
+                           uint32_t bl = 0) {
   if (bl == 0) bl = ntt_block_logn(logn);
   if (bl >= logn || logn < 13) throw Error(12, "the forward NTT plan has no strided stages");
   g.s1 = logn - bl;
   switch (bl) {
-    case 12: launch_fwd_block<12, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
-    case 13: launch_fwd_block<13, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
-    case 14: launch_fwd_block<14, REDUCE>(g, polys, SrcReload<Dst>{dst}, dst, st); break;
+    case 12: launch_fwd_block<12, REDUCE>(g, polys, SrcReload<From>{from}, dst, st); break;
+    case 13: launch_fwd_block<13, REDUCE>(g, polys, SrcReload<From>{from}, dst, st); break;
+    case 14: launch_fwd_block<14, REDUCE>(g, polys, SrcReload<From>{from}, dst, st); break;
     default: throw Error(12, "unsupported NTT plan");
   }
+}
+
+template <bool REDUCE, class Dst>
+void ntt_forward_after_top(uint32_t logn, NttGeom g, uint64_t polys, Dst dst, cudaStream_t st, uint32_t bl = 0) {
+  ntt_forward_after_top<REDUCE>(logn, g, polys, dst, dst, st, bl);
 }
 
 // Full inverse NTT, any 3 <= logn <= 16: single pass, or the block pass into

@@ -450,14 +450,25 @@ __device__ __forceinline__ uint64_t* rns_stage_buffer() {
   return buf;
 }
 
+// Forward stages of the kernel's epilogue (ForwardTop for one launch; primes
+// null: none).
+struct FwdEpilogue {
+  const DevPrime* primes;
+  uint32_t period, take;
+  const DevPrime* digit_primes;
+  uint32_t digit_limbs, digit_raw;
+  PolyRef digits;
+};
+
 template <int MAXF, int MAXT, bool EXACT, int TOP>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
                                                    PolyRef in, PolyRef out, uint64_t total,
                                                    const DevPrime* src_primes, uint32_t src_mont,
-                                                   const DevPrime* fwd_primes) {
+                                                   const FwdEpilogue fe) {
   const uint32_t F = EXACT ? (uint32_t)MAXF : s.from_len;
   constexpr int G = 128 >> TOP;  // groups per CTA (TOP > 0)
   uint32_t i, poly, b0 = 0, logb = 0, t = 0, gi = 0;
+  bool fwd_here = false, dig_here = false;  // uniform across the CTA (one polynomial)
   uint64_t r[MAXF];
   if constexpr (TOP == 0) {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -490,7 +501,12 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     i = b0 + gi + (t << logb);
 #pragma unroll
     for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? staged[(k * (1 << TOP) + t) * G + gi] : 0;
-    if (fwd_primes) __syncthreads();  // the buffer takes the outputs next
+    if (fe.primes) {
+      const uint32_t part = fe.period ? poly % fe.period : 0;
+      fwd_here = part < fe.take;
+      dig_here = !fwd_here && fe.digit_primes != nullptr;
+    }
+    if (fwd_here || dig_here) __syncthreads();  // the buffer takes the outputs next
   }
 
   // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2).
@@ -586,7 +602,8 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       }
       const uint64_t y = reduce128(hi, lo, pr);
       if constexpr (TOP > 0) {
-        if (fwd_primes) rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>()[(o * (1 << TOP) + t) * G + gi] = y;
+        if (fwd_here || dig_here)
+          rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>()[(o * (1 << TOP) + t) * G + gi] = y;
         else dst[(uint64_t)o << logn] = y;
       } else {
         dst[(uint64_t)o << logn] = y;
@@ -594,18 +611,40 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     }
   }
   if constexpr (TOP > 0) {
-    if (fwd_primes) {
+    if (fwd_here || dig_here) {
       __syncthreads();
       const uint64_t* staged = rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>();
-      for (uint32_t item = threadIdx.x; item < s.out_len * G; item += 128) {
-        const uint32_t o = item / G, g2 = item % G;
-        uint64_t x[1 << TOP];
+      if (fwd_here) {
+        for (uint32_t item = threadIdx.x; item < s.out_len * G; item += 128) {
+          const uint32_t o = item / G, g2 = item % G;
+          uint64_t x[1 << TOP];
 #pragma unroll
-        for (int u = 0; u < (1 << TOP); u++) x[u] = staged[(o * (1 << TOP) + u) * G + g2];
-        fwd_top_stages<TOP>(x, fwd_primes[o]);
-        uint64_t* row = out.at(poly, o) + b0 + g2;
+          for (int u = 0; u < (1 << TOP); u++) x[u] = staged[(o * (1 << TOP) + u) * G + g2];
+          fwd_top_stages<TOP>(x, fe.primes[o]);
+          uint64_t* row = out.at(poly, o) + b0 + g2;
 #pragma unroll
-        for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
+          for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
+        }
+      } else {
+        // Digit d (output limb d) in key limb j: key_switching_key.rs:227-235
+        // with rq/mod.rs:518-540, the first forward stages of its transform.
+        const uint32_t per_digit = fe.digit_limbs * G;
+        const uint32_t pbase = (poly / fe.period) * s.out_len;
+        for (uint32_t item = threadIdx.x; item < s.out_len * per_digit; item += 128) {
+          const uint32_t d = item / per_digit, rem = item - d * per_digit;
+          const uint32_t j = rem / G, g2 = rem % G;
+          const DevPrime kp = fe.digit_primes[j];
+          uint64_t x[1 << TOP];
+#pragma unroll
+          for (int u = 0; u < (1 << TOP); u++) {
+            const uint64_t v = staged[(d * (1 << TOP) + u) * G + g2];
+            x[u] = fe.digit_raw ? v : reduce64_lazy(v, kp);
+          }
+          fwd_top_stages<TOP>(x, kp);
+          uint64_t* row = fe.digits.at(pbase + d, j) + b0 + g2;
+#pragma unroll
+          for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
+        }
       }
     }
   }
@@ -646,10 +685,15 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     }
     PolyRef o = out;
     o.base += (uint64_t)first << logn;
+    FwdEpilogue fe{};
+    if (fwd) {
+      if (fwd->digit_primes && first > 0) throw Error(FHEG_ERR_INTERNAL, "digit expansion needs one launch");
+      fe = FwdEpilogue{fwd->primes + first, fwd->period, fwd->take, fwd->digit_primes, fwd->digit_limbs,
+                       fwd->digit_raw, fwd->digits};
+    }
     const unsigned threads = 128;
     k_rns_scale<MAXF, MAXT, EXACT, TOP><<<blocks_for(total, threads), threads, 0, st>>>(
-        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u,
-        fwd ? fwd->primes + first : nullptr);
+        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u, fe);
     after_launch("k_rns_scale");
   }
 }
