@@ -43,8 +43,8 @@ STAGE_LIMBS = {
     "B": 4 * L + 4 * (2 * L + 1 - L),  # read 4L, write 4(M - L)
     "C": 8 * (2 * L + 1 - L),        # read + write the extension limbs
     "D": 4 * (2 * L + 1) + 3 * (2 * L + 1),  # read 4M operand limbs, write 3M
-    "E": 3 * (2 * L + 1) + 3 * L,    # read 3M, write 3L
-    "F": 3 * L + L * L + 2 * L,      # read c0, c1, c2; write the digit NTTs and c0, c1
+    "E": 3 * (2 * L + 1) + 2 * L + L * L,  # read 3M; write c0, c1 and the L * Lk digit rows
+    "F": 2 * (L * L + 2 * L),        # read + write the digit rows and c0, c1 (block passes)
     "G": L * L + 4 * L,              # read the digit NTTs, read + write c0, c1 (keys added per batch)
 }
 STAGE_KERNELS = {
@@ -60,12 +60,11 @@ STAGE_KERNELS = {
 # Kernel launches of each stage under the same plan.
 STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # DRAM bytes (read + write) of each stage's kernels for one 64-pair
-# multiplication with the plan A,C,D,F = 12 (2^12-residue blocks; the forward
-# transforms after a strided pass over two stages, the inverse ones with those
-# stages applied by the RNS scaler that reads them), from the ncu capture
-# summarised in profiles/stages_mul_relin_n16384_b64.md.
-STAGE_TRAFFIC_BYTES = {"A": 354.5e6, "B": 384.6e6, "C": 822.3e6, "D": 730.4e6, "E": 446.8e6, "F": 1137.9e6,
-                       "G": 493.3e6}
+# multiplication with the plan A,C,D,F = 12 (2^12-residue blocks; every
+# strided NTT stage applied inside the RNS scalers B and E), from the ncu
+# capture summarised in profiles/stages_mul_relin_n16384_b64.md.
+STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "E": 671.7e6, "F": 707.3e6,
+                       "G": 493.2e6}
 
 
 def _peaks():
