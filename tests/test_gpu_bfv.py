@@ -39,7 +39,7 @@ class Setup:
 
 
 @pytest.mark.parametrize("n,L,t,B", [(16, 3, 1153, 3), (4096, 2, 65537, 2), (16384, 6, 65537, 2),
-                                     (32768, 3, 65537, 1)])
+                                     (32768, 3, 65537, 1), (32768, 12, 65537, 2), (8192, 3, 65537, 2)])
 def test_multiply_default(fg, ora, cuda, n, L, t, B):
     s = Setup(fg, ora, n, L, t, seed=n + L)
     rk_o, rk = s.rk()
