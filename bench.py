@@ -65,6 +65,13 @@ STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # capture summarised in profiles/stages_mul_relin_n16384_b64.md.
 STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "E": 671.7e6, "F": 707.3e6,
                        "G": 493.2e6}
+# Share of the elapsed cycles in which the integer multipliers (the FMA-heavy
+# pipe, which executes every IMAD) were busy, per stage, from the ncu capture
+# of one 32-pair multiplication under the same plan summarised in
+# profiles/pipes_mul_relin_n16384_b32.md (F: time-weighted over its two
+# launches). The whole multiplication: 73.3%, time-weighted.
+STAGE_FMAHEAVY_PCT = {"A": 67.1, "B": 84.4, "C": 70.1, "D": 65.1, "E": 85.5, "F": 68.6, "G": 58.0}
+MULTIPLY_FMAHEAVY_PCT = 73.3
 
 
 def _peaks():
@@ -410,7 +417,12 @@ def run_ours(args, rank: int, world: int):
                          "traffic": STAGE_TRAFFIC_BYTES.get(dom) if traffic_plan_matches else None,
                          "traffic_plan": "A,C,D,F = 2^12 blocks", "kernel": STAGE_KERNELS[dom],
                          "algorithmic_bytes": stage_bytes[dom], "launch_ms": stage_ms[dom], "peak_kind": peak_kind,
-                         "note": "integer-issue bound: all arithmetic is exact 64-bit residue arithmetic on CUDA cores"},
+                         "note": "integer-multiplier bound, not HBM: all arithmetic is exact 64-bit residue "
+                                 "arithmetic on the CUDA cores' 32-bit multipliers",
+                         "int_pipe": {"kernel_fmaheavy_pct": STAGE_FMAHEAVY_PCT[dom] if traffic_plan_matches else None,
+                                      "multiply_fmaheavy_pct": MULTIPLY_FMAHEAVY_PCT if traffic_plan_matches else None,
+                                      "metric": "sm__pipe_fmaheavy_cycles_active.avg.pct_of_peak_sustained_elapsed",
+                                      "source": "ncu, profiles/pipes_mul_relin_n16384_b32.md"}},
             "stages": {k: {"ms": stage_ms[k], "gbs": stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9,
                            "kernel": STAGE_KERNELS[k]} for k in stage_ms},
             "ntt": {"kernel": "forward / inverse NTT alone, 256 polys x 6 limbs", "fwd_gbs": fwd_gbs,
