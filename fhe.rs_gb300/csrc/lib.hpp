@@ -83,6 +83,11 @@ struct RnsScalerD {
   std::vector<uint64_t> gamma_neg;     // (q_j - gamma_j) mod q_j
   std::vector<uint64_t> gamma_neg_hi;  // gamma_neg * 2^62 mod q_j
   std::vector<uint64_t> to_moduli, to_bhi, to_blo;
+  // Montgomery forms (times 2^64 mod q_j) of omega (row j: to_len x from_len),
+  // gamma_neg and gamma_neg_hi, and -q_j^-1 mod 2^64; set when every target
+  // modulus is odd (mont).
+  bool mont = false;
+  std::vector<uint64_t> omega_mont, gamma_neg_mont, gamma_neg_hi_mont, to_pinv;
   RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den);
 };
 

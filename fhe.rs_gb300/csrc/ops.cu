@@ -414,10 +414,18 @@ __device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t 
 // bank (fully unrolled loops give compile-time offsets). Outputs are limbs
 // start .. start + out_len of the target; the rows of omega, gamma and the
 // primes are pre-sliced on the host so output o uses row o.
+//
+// mont: every target modulus is odd, and omega, gamma_neg and gamma_neg_hi
+// are in Montgomery form (times 2^64 mod q_j), so the exact sum S is 2^64
+// times the output's sum and one Montgomery step divides it back out
+// (mont_fold), which takes about a third of the multiplies of a 128-bit
+// Barrett reduction. Otherwise the constants are plain and S is reduced by
+// Barrett.
 template <int MAXF, int MAXT>
 struct RnsLaunch {
   uint32_t from_len, out_len, is_one, shift;
   uint32_t tg_sign, to_sign;  // to_sign: bit k = sign of theta_omega_k
+  uint32_t mont;
   uint64_t tg_lo, tg_hi;
   uint64_t tgar_lo[MAXF], tgar_hi[MAXF];
   uint64_t to_lo[MAXF], to_hi[MAXF];
@@ -425,7 +433,17 @@ struct RnsLaunch {
   uint64_t gamma_neg[MAXT];     // (q_j - gamma_j) mod q_j
   uint64_t gamma_neg_hi[MAXT];  // gamma_neg * 2^62 mod q_j
   uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
+  uint64_t pinv[MAXT];  // -q_j^-1 mod 2^64 (mont)
 };
+
+// (hi * 2^64 + lo) * 2^-64 mod p, canonical, for hi < 4p: hi reduced by two
+// conditional subtractions, lo by one Montgomery step (lo * 2^-64 mod p in
+// [0, p], as in mont_reduce).
+__device__ __forceinline__ uint64_t mont_fold(uint64_t hi, uint64_t lo, uint64_t p, uint64_t pinv) {
+  const uint64_t h = csub(csub(hi, 2 * p), p);
+  const uint64_t m = lo * pinv;
+  return csub(h + __umul64hi(m, p) + (lo != 0), p);
+}
 
 // EXACT: the source count is MAXF itself (a compile-time constant), so the
 // unrolled loops carry no predicated-off terms; used for the counts the
@@ -583,24 +601,48 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       pr.p2 = 2 * s.p[o];
       pr.bhi = s.bhi[o];
       pr.blo = s.blo[o];
-      uint64_t lo = 0, hi = 0;
-      if (!s.is_one) {
-        const uint64_t wj = reduce128_lazy(whi, wlo, pr);
-        lo = w_sign ? pr.p2 - wj : wj;
-      }
-      mac128(hi, lo, v_low, s.gamma_neg[o]);
-      mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
+      uint64_t y;
+      if (s.mont) {
+        // Every term below 2^62 q_j (r_k, v_low < 2^62; v_top < 32), so 14
+        // products and the two gamma terms keep hi below 4 q_j.
+        uint64_t lo = 0, hi = 0, acc = 0;
+        mac128(hi, lo, v_low, s.gamma_neg[o]);
+        mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
 #pragma unroll
-      for (int k = 0; k < MAXF; k++) {
-        if (k < (int)F) {
-          mac128(hi, lo, r[k], s.omega[o][k]);
-          if ((k % 14) == 13) {  // keep the exact sum below 2^128
-            lo = reduce128(hi, lo, pr);
-            hi = 0;
+        for (int k = 0; k < MAXF; k++) {
+          if (k < (int)F) {
+            mac128(hi, lo, r[k], s.omega[o][k]);
+            if ((k % 14) == 13) {
+              acc = csub(acc + mont_fold(hi, lo, pr.p, s.pinv[o]), pr.p);
+              hi = lo = 0;
+            }
           }
         }
+        y = csub(acc + mont_fold(hi, lo, pr.p, s.pinv[o]), pr.p);
+        if (!s.is_one) {
+          const uint64_t wj = reduce128_lazy(whi, wlo, pr);
+          y = csub(csub(y + (w_sign ? pr.p2 - wj : wj), pr.p2), pr.p);
+        }
+      } else {
+        uint64_t lo = 0, hi = 0;
+        if (!s.is_one) {
+          const uint64_t wj = reduce128_lazy(whi, wlo, pr);
+          lo = w_sign ? pr.p2 - wj : wj;
+        }
+        mac128(hi, lo, v_low, s.gamma_neg[o]);
+        mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
+#pragma unroll
+        for (int k = 0; k < MAXF; k++) {
+          if (k < (int)F) {
+            mac128(hi, lo, r[k], s.omega[o][k]);
+            if ((k % 14) == 13) {  // keep the exact sum below 2^128
+              lo = reduce128(hi, lo, pr);
+              hi = 0;
+            }
+          }
+        }
+        y = reduce128(hi, lo, pr);
       }
-      const uint64_t y = reduce128(hi, lo, pr);
       if constexpr (TOP > 0) {
         if (fwd_here || dig_here)
           rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>()[(o * (1 << TOP) + t) * G + gi] = y;
@@ -674,11 +716,19 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
       s.to_hi[k] = h.theta_omega_hi[k];
       if (h.theta_omega_sign[k]) s.to_sign |= 1u << k;
     }
+    s.mont = sc.mont ? 1 : 0;
     for (uint32_t o = 0; o < n; o++) {
       const size_t j = start + first + o;
-      for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
-      s.gamma_neg[o] = sc.gamma_neg[j];
-      s.gamma_neg_hi[o] = sc.gamma_neg_hi[j];
+      if (sc.mont) {
+        for (size_t k = 0; k < F; k++) s.omega[o][k] = sc.omega_mont[j * F + k];
+        s.gamma_neg[o] = sc.gamma_neg_mont[j];
+        s.gamma_neg_hi[o] = sc.gamma_neg_hi_mont[j];
+        s.pinv[o] = sc.to_pinv[j];
+      } else {
+        for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
+        s.gamma_neg[o] = sc.gamma_neg[j];
+        s.gamma_neg_hi[o] = sc.gamma_neg_hi[j];
+      }
       s.p[o] = sc.to_moduli[j];
       s.bhi[o] = sc.to_bhi[j];
       s.blo[o] = sc.to_blo[j];
@@ -761,6 +811,25 @@ RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& nu
     gamma_neg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
     gamma_neg_hi[j] = mulmod(gamma_neg[j], (1ull << 62) % to.moduli[j], to.moduli[j]);
     barrett128(to.moduli[j], &to_bhi[j], &to_blo[j]);
+  }
+  mont = true;
+  for (size_t j = 0; j < T; j++) mont = mont && (to.moduli[j] & 1);
+  if (mont) {
+    const size_t F = host.from_len;
+    omega_mont.resize(T * F);
+    gamma_neg_mont.resize(T);
+    gamma_neg_hi_mont.resize(T);
+    to_pinv.resize(T);
+    for (size_t j = 0; j < T; j++) {
+      const uint64_t q = to.moduli[j];
+      const uint64_t r = (uint64_t)(((unsigned __int128)1 << 64) % q);
+      for (size_t k = 0; k < F; k++) omega_mont[j * F + k] = mulmod(host.omega[j * F + k], r, q);
+      gamma_neg_mont[j] = mulmod(gamma_neg[j], r, q);
+      gamma_neg_hi_mont[j] = mulmod(gamma_neg_hi[j], r, q);
+      uint64_t inv = q;  // q^-1 mod 2^64 by Newton's iteration
+      for (int it = 0; it < 6; it++) inv *= 2 - q * inv;
+      to_pinv[j] = 0 - inv;
+    }
   }
 }
 
