@@ -434,6 +434,10 @@ struct RnsLaunch {
   uint64_t gamma_neg_hi[MAXT];  // gamma_neg * 2^62 mod q_j
   uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
   uint64_t pinv[MAXT];  // -q_j^-1 mod 2^64 (mont)
+  // w mod q_j as whi * (2^64 mod q_j) + wlo (mont): the Shoup companions of
+  // 2^64 mod q_j and of 1, and wbig = every q_j above 2^61 (wlo < 8 q_j).
+  uint32_t wbig;
+  uint64_t r64[MAXT], r64_shoup[MAXT], one_shoup[MAXT];
 };
 
 // (hi * 2^64 + lo) * 2^-64 mod p, canonical, for hi < 4p: hi reduced by two
@@ -620,7 +624,13 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
         }
         y = csub(acc + mont_fold(hi, lo, pr.p, s.pinv[o]), pr.p);
         if (!s.is_one) {
-          const uint64_t wj = reduce128_lazy(whi, wlo, pr);
+          // whi < 2^63: w mod q_j = whi * 2^64 + wlo in [0, 2q_j) from one
+          // Shoup product and a reduction of wlo (conditional subtractions
+          // when wlo < 8 q_j), where a 128-bit Barrett takes three times the
+          // multiplies.
+          const uint64_t lo_red = s.wbig ? csub(csub(csub(wlo, 2 * pr.p2), pr.p2), pr.p)
+                                         : csub(mul_shoup_lazy(wlo, 1, s.one_shoup[o], pr.p), pr.p);
+          const uint64_t wj = csub(mul_shoup_lazy(whi, s.r64[o], s.r64_shoup[o], pr.p), pr.p) + lo_red;
           y = csub(csub(y + (w_sign ? pr.p2 - wj : wj), pr.p2), pr.p);
         }
       } else {
@@ -717,6 +727,7 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
       if (h.theta_omega_sign[k]) s.to_sign |= 1u << k;
     }
     s.mont = sc.mont ? 1 : 0;
+    s.wbig = 1;
     for (uint32_t o = 0; o < n; o++) {
       const size_t j = start + first + o;
       if (sc.mont) {
@@ -724,6 +735,11 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
         s.gamma_neg[o] = sc.gamma_neg_mont[j];
         s.gamma_neg_hi[o] = sc.gamma_neg_hi_mont[j];
         s.pinv[o] = sc.to_pinv[j];
+        const uint64_t q = sc.to_moduli[j];
+        s.r64[o] = (uint64_t)(((unsigned __int128)1 << 64) % q);
+        s.r64_shoup[o] = shoup(s.r64[o], q);
+        s.one_shoup[o] = shoup(1, q);
+        if (q <= (1ull << 61)) s.wbig = 0;
       } else {
         for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
         s.gamma_neg[o] = sc.gamma_neg[j];
