@@ -227,6 +227,15 @@ __device__ __forceinline__ uint64_t csub(uint64_t x, uint64_t m) {
 
 __device__ __forceinline__ uint64_t reduce_once(uint64_t x, uint64_t p) { return csub(x, p); }
 
+// (hi * 2^64 + lo) * 2^-64 mod p, canonical, for hi < 4p: hi reduced by two
+// conditional subtractions, lo by one Montgomery step (lo * 2^-64 mod p in
+// [0, p], as in mont_reduce).
+__device__ __forceinline__ uint64_t mont_fold(uint64_t hi, uint64_t lo, uint64_t p, uint64_t pinv) {
+  const uint64_t h = csub(csub(hi, 2 * p), p);
+  const uint64_t m = lo * pinv;
+  return csub(h + __umul64hi(m, p) + (lo != 0), p);
+}
+
 __device__ __forceinline__ uint64_t mul_shoup(uint64_t a, uint64_t b, uint64_t b_shoup, uint64_t p) {
   return reduce_once(mul_shoup_lazy(a, b, b_shoup, p), p);
 }

@@ -415,17 +415,16 @@ __device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t 
 // start .. start + out_len of the target; the rows of omega, gamma and the
 // primes are pre-sliced on the host so output o uses row o.
 //
-// mont: every target modulus is odd, and omega, gamma_neg and gamma_neg_hi
-// are in Montgomery form (times 2^64 mod q_j), so the exact sum S is 2^64
-// times the output's sum and one Montgomery step divides it back out
-// (mont_fold), which takes about a third of the multiplies of a 128-bit
-// Barrett reduction. Otherwise the constants are plain and S is reduced by
-// Barrett.
+// Kernels with an exact source count (EXACT) take odd target moduli, with
+// omega, gamma_neg and gamma_neg_hi in Montgomery form (times 2^64 mod q_j):
+// the exact sum S is then 2^64 times the output's sum, and one Montgomery
+// step divides it back out (mont_fold), with about a third of the multiplies
+// of a 128-bit Barrett reduction. The generic kernels take plain constants
+// and reduce S by Barrett (any moduli).
 template <int MAXF, int MAXT>
 struct RnsLaunch {
   uint32_t from_len, out_len, is_one, shift;
   uint32_t tg_sign, to_sign;  // to_sign: bit k = sign of theta_omega_k
-  uint32_t mont;
   uint64_t tg_lo, tg_hi;
   uint64_t tgar_lo[MAXF], tgar_hi[MAXF];
   uint64_t to_lo[MAXF], to_hi[MAXF];
@@ -433,21 +432,13 @@ struct RnsLaunch {
   uint64_t gamma_neg[MAXT];     // (q_j - gamma_j) mod q_j
   uint64_t gamma_neg_hi[MAXT];  // gamma_neg * 2^62 mod q_j
   uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
-  uint64_t pinv[MAXT];  // -q_j^-1 mod 2^64 (mont)
-  // w mod q_j as whi * (2^64 mod q_j) + wlo (mont): the Shoup companions of
+  uint64_t pinv[MAXT];  // -q_j^-1 mod 2^64 (EXACT)
+  // w mod q_j as whi * (2^64 mod q_j) + wlo (EXACT): the Shoup companions of
   // 2^64 mod q_j and of 1, and wbig = every q_j above 2^61 (wlo < 8 q_j).
   uint32_t wbig;
   uint64_t r64[MAXT], r64_shoup[MAXT], one_shoup[MAXT];
 };
 
-// (hi * 2^64 + lo) * 2^-64 mod p, canonical, for hi < 4p: hi reduced by two
-// conditional subtractions, lo by one Montgomery step (lo * 2^-64 mod p in
-// [0, p], as in mont_reduce).
-__device__ __forceinline__ uint64_t mont_fold(uint64_t hi, uint64_t lo, uint64_t p, uint64_t pinv) {
-  const uint64_t h = csub(csub(hi, 2 * p), p);
-  const uint64_t m = lo * pinv;
-  return csub(h + __umul64hi(m, p) + (lo != 0), p);
-}
 
 // EXACT: the source count is MAXF itself (a compile-time constant), so the
 // unrolled loops carry no predicated-off terms; used for the counts the
@@ -606,7 +597,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       pr.bhi = s.bhi[o];
       pr.blo = s.blo[o];
       uint64_t y;
-      if (s.mont) {
+      if constexpr (EXACT) {
         // Every term below 2^62 q_j (r_k, v_low < 2^62; v_top < 32), so 14
         // products and the two gamma terms keep hi below 4 q_j.
         uint64_t lo = 0, hi = 0, acc = 0;
@@ -726,11 +717,11 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
       s.to_hi[k] = h.theta_omega_hi[k];
       if (h.theta_omega_sign[k]) s.to_sign |= 1u << k;
     }
-    s.mont = sc.mont ? 1 : 0;
+    if (EXACT && !sc.mont) throw Error(FHEG_ERR_INTERNAL, "Montgomery scaling needs odd target moduli");
     s.wbig = 1;
     for (uint32_t o = 0; o < n; o++) {
       const size_t j = start + first + o;
-      if (sc.mont) {
+      if (EXACT) {
         for (size_t k = 0; k < F; k++) s.omega[o][k] = sc.omega_mont[j * F + k];
         s.gamma_neg[o] = sc.gamma_neg_mont[j];
         s.gamma_neg_hi[o] = sc.gamma_neg_hi_mont[j];
@@ -779,7 +770,7 @@ static void launch_rns_scale_top(const RnsScalerD& s, uint32_t logn, PolyRef in,
 bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1) {
   const size_t F = s.host.from_len;
   const bool exact = (F == 6 || F == 13 || F == 3 || F == 7) ? out_len <= 8 : (F == 12 || F == 25) && out_len <= 16;
-  return exact && s1 >= 1 && s1 <= 3 && logn >= 7;
+  return exact && s.mont && s1 >= 1 && s1 <= 3 && logn >= 7;
 }
 
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
@@ -801,7 +792,15 @@ void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint
     return;
   }
   // Exact source counts of the default multiplications at L = 3, 6, 12
-  // (extension from L, scale-down from 2L + 1).
+  // (extension from L, scale-down from 2L + 1), odd target moduli.
+  if (!s.mont) {
+    if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
+    else if (F <= 16 && out_len <= 8) launch_rns_scale<16, 8>(s, logn, in, out, start, out_len, total, st);
+    else if (F <= 16) launch_rns_scale<16, 16>(s, logn, in, out, start, out_len, total, st);
+    else if (F <= 32) launch_rns_scale<32, 16>(s, logn, in, out, start, out_len, total, st);
+    else throw Error(FHEG_ERR_UNSUPPORTED, "RNS scaling from more than 32 moduli is not supported");
+    return;
+  }
   if (F == 6 && out_len <= 8) launch_rns_scale<6, 8, true>(s, logn, in, out, start, out_len, total, st);
   else if (F == 13 && out_len <= 8) launch_rns_scale<13, 8, true>(s, logn, in, out, start, out_len, total, st);
   else if (F == 3 && out_len <= 8) launch_rns_scale<3, 8, true>(s, logn, in, out, start, out_len, total, st);
