@@ -69,9 +69,9 @@ STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "
 # pipe, which executes every IMAD) were busy, per stage, from the ncu capture
 # of one 32-pair multiplication under the same plan summarised in
 # profiles/pipes_mul_relin_n16384_b32.md (F: time-weighted over its two
-# launches). The whole multiplication: 73.3%, time-weighted.
-STAGE_FMAHEAVY_PCT = {"A": 67.1, "B": 84.4, "C": 70.1, "D": 65.1, "E": 85.5, "F": 68.6, "G": 58.0}
-MULTIPLY_FMAHEAVY_PCT = 73.3
+# launches). The whole multiplication: 72.0%, time-weighted.
+STAGE_FMAHEAVY_PCT = {"A": 67.0, "B": 85.5, "C": 70.3, "D": 65.3, "E": 79.8, "F": 68.6, "G": 58.5}
+MULTIPLY_FMAHEAVY_PCT = 72.0
 
 
 def _peaks():
