@@ -109,6 +109,7 @@ def _declare(L):
         "fheg_ksk_destroy": (None, [c_vp]),
         "fheg_ksk_create_seeded": (i, [c_vp, c_size, c_size, P_u64, ctypes.c_char_p, c_size, ctypes.POINTER(c_vp)]),
         "fheg_poly_random_from_seed": (i, [c_vp, c_vp, c_vp, c_size, c_size, c_vp]),
+        "fheg_sample_cbd_from_seed": (i, [c_vp, c_size, c_size, c_size, c_vp, c_vp]),
         "fheg_ksk_from_bytes": (i, [c_vp, ctypes.c_char_p, c_size, i, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
                                     ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
         "fheg_ciphertext_serialized_size": (i, [c_vp, c_size, c_size, i, i, ctypes.POINTER(c_size)]),
@@ -449,6 +450,20 @@ def random_from_seed(ctx: Context, seeds, out=None, poly_stride: int = 0):
         assert out.is_cuda and out.dtype == torch.int64
         ptr = out.data_ptr()
     check(lib().fheg_poly_random_from_seed(ctx._h, seeds.data_ptr(), ptr, poly_stride, count, _stream()))
+    return out
+
+
+def sample_cbd_from_seed(seeds, variance: int, n: int):
+    """sample_vec_cbd (fhe-util/src/lib.rs:22-55) of n samples per seed, from
+    ChaCha8Rng::from_seed of each row of a uint8 device tensor [count][32]: a
+    new int64 device tensor [count][n]."""
+    torch = _torch()
+    if seeds.dtype != torch.uint8 or seeds.dim() != 2 or seeds.shape[1] != 32 or not seeds.is_cuda:
+        raise FhegError(ERR_INVALID_ARGUMENT, "seeds must be a uint8 device tensor [count][32]")
+    seeds = seeds.contiguous()
+    out = torch.empty((seeds.shape[0], n), dtype=torch.int64, device=seeds.device)
+    check(lib().fheg_sample_cbd_from_seed(seeds.data_ptr(), variance, n, seeds.shape[0], out.data_ptr(),
+                                          _stream()))
     return out
 
 

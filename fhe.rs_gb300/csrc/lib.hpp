@@ -276,6 +276,10 @@ void poly_random_from_seed(const Context& c, const uint8_t* seeds, uint64_t* out
                            Workspace& ws, cudaStream_t st);
 // The seeds of c1[0 .. count) of a key-switching key with seed `seed` (32
 // bytes): 32 * count bytes (key_switching_key.rs:108-123).
+// sample_vec_cbd (fhe-util/src/lib.rs:22-55) of `count` vectors of n
+// samples, vector b drawn from ChaCha8Rng::from_seed(seeds[b]) (seeded.cu).
+void sample_cbd_from_seed(const uint8_t* seeds, size_t variance, size_t n, size_t count, int64_t* out,
+                          cudaStream_t st);
 std::vector<uint8_t> ksk_c1_seeds(const uint8_t* seed, size_t count);
 
 // External product with an RGSW ciphertext held as one key of 2L digits per

@@ -282,6 +282,66 @@ void poly_random_from_seed(const Context& c, const uint8_t* seeds, uint64_t* out
   after_launch("k_seeded_exact");
 }
 
+// fhe-util/src/lib.rs:22-55 `sample_vec_cbd` over the next_u64 stream of
+// ChaCha8Rng::from_seed(seed) (the 32 seed bytes are the key, little-endian
+// words; draw k joins keystream words 2k and 2k+1). The reference's bit pool
+// takes each 64-bit draw above the bits it holds and cuts 4v bits per sample
+// (v the variance): sample i is bits [4vi, 4vi + 4v) of the draws' little-endian
+// bit stream, the popcount of its low 2v bits minus that of its high 2v. So
+// 16 samples take exactly v draws: thread t makes samples 16t .. 16t + 15
+// from draws vt .. vt + v - 1, which it computes (up to three ChaCha blocks)
+// and stages in shared memory.
+constexpr int kCbdThreads = 128;
+
+__global__ void __launch_bounds__(kCbdThreads) k_sample_cbd(const uint8_t* seeds, uint32_t variance, uint32_t n,
+                                                            uint64_t chunks_per_vec, uint64_t total, int64_t* out) {
+  __shared__ uint64_t draws[kCbdThreads * 16];
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint64_t vec = gid / chunks_per_vec, chunk = gid - vec * chunks_per_vec;
+  uint32_t key[8];
+  const uint8_t* sd = seeds + 32 * vec;
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+    key[i] = (uint32_t)sd[4 * i] | ((uint32_t)sd[4 * i + 1] << 8) | ((uint32_t)sd[4 * i + 2] << 16) |
+             ((uint32_t)sd[4 * i + 3] << 24);
+  uint64_t* w = draws + threadIdx.x * 16;
+  const uint64_t first = chunk * variance;  // first draw of the chunk
+  uint32_t blk[16];
+  uint64_t have = ~0ull;
+  for (uint32_t k = 0; k < variance; k++) {
+    const uint64_t d = first + k;
+    if ((d >> 3) != have) {
+      have = d >> 3;
+      chacha8_block(key, have, blk);
+    }
+    const uint32_t o = 2 * (uint32_t)(d & 7);
+    w[k] = (uint64_t)blk[o] | ((uint64_t)blk[o + 1] << 32);
+  }
+  const uint32_t nb = 4 * variance, half = 2 * variance;
+  const uint64_t base = chunk * 16;
+  const uint32_t m = n - base < 16 ? (uint32_t)(n - base) : 16u;
+  for (uint32_t s = 0; s < m; s++) {
+    const uint32_t off = s * nb, k = off >> 6, sh = off & 63;
+    uint64_t v = w[k] >> sh;
+    if (sh && sh + nb > 64) v |= w[k + 1] << (64 - sh);
+    if (nb < 64) v &= (1ull << nb) - 1;
+    out[vec * n + base + s] =
+        (int64_t)__popcll(v & ((1ull << half) - 1)) - (int64_t)__popcll(v >> half);
+  }
+}
+
+void sample_cbd_from_seed(const uint8_t* seeds, size_t variance, size_t n, size_t count, int64_t* out,
+                          cudaStream_t st) {
+  if (variance < 1 || variance > 16) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The variance should be between 1 and 16");
+  if (n == 0 || count == 0) return;
+  if (n > (1u << 30)) throw Error(FHEG_ERR_INVALID_ARGUMENT, "vector size above 2^30");
+  const uint64_t chunks = (n + 15) / 16, total = chunks * count;
+  k_sample_cbd<<<grid_for(total, kCbdThreads), kCbdThreads, 0, st>>>(seeds, (uint32_t)variance, (uint32_t)n, chunks,
+                                                                     total, out);
+  after_launch("k_sample_cbd");
+}
+
 std::vector<uint8_t> ksk_c1_seeds(const uint8_t* seed, size_t count) {
   // rand_chacha from_seed: key words little-endian; generate_c1 takes 32
   // bytes (8 words) per c1[i] with Rng::fill.
@@ -302,6 +362,14 @@ std::vector<uint8_t> ksk_c1_seeds(const uint8_t* seed, size_t count) {
 }  // namespace fheg
 
 using namespace fheg;
+
+FHEG_API int fheg_sample_cbd_from_seed(const uint8_t* d_seeds, size_t variance, size_t n, size_t count,
+                                       int64_t* d_out, void* stream) {
+  return abi_call([&] {
+    abi_need((d_seeds && d_out) || !count || !n, "null input");
+    sample_cbd_from_seed(d_seeds, variance, n, count, d_out, static_cast<cudaStream_t>(stream));
+  });
+}
 
 FHEG_API int fheg_poly_random_from_seed(const fheg_context* ctx, const uint8_t* d_seeds, uint64_t* d_out,
                                         size_t poly_stride, size_t count, void* stream) {

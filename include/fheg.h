@@ -210,6 +210,16 @@ FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const u
 FHEG_API int fheg_poly_random_from_seed(const fheg_context* ctx, const uint8_t* d_seeds, uint64_t* d_out,
                                         size_t poly_stride, size_t count, void* stream);
 
+/* sample_vec_cbd (fhe-util/src/lib.rs:22-55): d_out [count][n] signed
+ * samples of the centered binomial distribution of `variance` (1..16), vector
+ * b drawn from the next_u64 stream of ChaCha8Rng::from_seed(d_seeds[b])
+ * (d_seeds [count][32] bytes on the device). With the seed of the caller's
+ * ChaCha8Rng these are the errors of Poly::small (rq/mod.rs:262-284), the e
+ * that SecretKey::try_encrypt (secret_key.rs:102-138) draws and that
+ * fheg_encrypt takes. */
+FHEG_API int fheg_sample_cbd_from_seed(const uint8_t* d_seeds, size_t variance, size_t n, size_t count,
+                                       int64_t* d_out, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* BFV (crate fhe).                                                           */
 

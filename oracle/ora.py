@@ -1035,9 +1035,26 @@ def sample_vec_cbd(size: int, variance: int, rng: np.random.Generator) -> np.nda
     nb = 4 * variance
     ndraws = (size * nb + 63) // 64 + 2
     draws = rng.integers(0, 1 << 64, size=ndraws, dtype=np.uint64, endpoint=False)
-    bits = np.unpackbits(draws.view(np.uint8), bitorder="little")[: size * nb].reshape(size, nb)
+    return _cbd_from_draws(draws, size, variance)
+
+
+def _cbd_from_draws(draws: np.ndarray, size: int, variance: int) -> np.ndarray:
+    nb = 4 * variance
+    bits = np.unpackbits(np.ascontiguousarray(draws, dtype=np.uint64).view(np.uint8),
+                         bitorder="little")[: size * nb].reshape(size, nb)
     half = 2 * variance
     return bits[:, :half].sum(axis=1).astype(np.int64) - bits[:, half:].sum(axis=1).astype(np.int64)
+
+
+def sample_vec_cbd_from_seed(size: int, variance: int, seed: bytes) -> np.ndarray:
+    """`sample_vec_cbd` (fhe-util/src/lib.rs:22-55) driven by the next_u64
+    stream of ChaCha8Rng::from_seed(seed) (rand_chacha 0.9.0): it takes
+    ceil(4 * variance * size / 64) draws."""
+    if not (1 <= variance <= 16):
+        raise ValueError("The variance should be between 1 and 16")
+    key = [int.from_bytes(seed[4 * i:4 * i + 4], "little") for i in range(8)]
+    ndraws = (size * 4 * variance + 63) // 64
+    return _cbd_from_draws(chacha_u64_draws(key, 0, ndraws), size, variance)
 
 
 # ---------------------------------------------------------------------------

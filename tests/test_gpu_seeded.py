@@ -48,6 +48,49 @@ def test_random_from_seed_rejections(fg, ora, cuda):
         assert np.array_equal(got[b], ora.random_from_seed(ctx_o, sd)), b
 
 
+@pytest.mark.parametrize("n,variance", [(16, 10), (4096, 10), (16384, 16), (8, 1), (1000, 7), (4096, 3)])
+def test_sample_cbd_from_seed_matches_oracle(fg, ora, cuda, n, variance):
+    """sample_vec_cbd (fhe-util/src/lib.rs:22-55) over ChaCha8Rng::from_seed
+    streams: each vector equals the oracle's (n = 1000 leaves a partial last
+    chunk of 16 samples; variance 16 takes whole 64-bit draws per sample)."""
+    seeds = _seeds(np.random.default_rng(n * variance), 3) + [bytes(32)]
+    got = fg.to_host(fg.sample_cbd_from_seed(_dev_seeds(fg, seeds), variance, n)).view(np.int64)
+    assert got.shape == (4, n)
+    for b, sd in enumerate(seeds):
+        assert np.array_equal(got[b], ora.sample_vec_cbd_from_seed(n, variance, sd)), b
+
+
+def test_sample_cbd_errors(fg, cuda):
+    seeds = _dev_seeds(fg, [bytes(32)])
+    for v in (0, 17):
+        with pytest.raises(fg.FhegError) as e:
+            fg.sample_cbd_from_seed(seeds, v, 16)
+        assert e.value.code == fg.ERR_INVALID_ARGUMENT
+
+
+def test_encrypt_from_seeds(fg, ora, cuda):
+    """SecretKey::try_encrypt (secret_key.rs:102-138) entirely on the device:
+    a from its seed (Poly::random_from_seed), e from the caller's
+    ChaCha8Rng::from_seed (Poly::small), b = e - a s + m; equal to the
+    oracle's ciphertext for the same seeds, and it decrypts."""
+    s = Setup(fg, ora, 4096, 3, 65537, seed=31)
+    sk = fg.SecretKey(s.par, s.sk.coeffs)
+    ctx_o = s.par_o.context_at_level(0)
+    ctx = fg.Context(ctx_o.moduli, 4096)
+    a_seeds, e_seeds = _seeds(s.rng, 3), _seeds(s.rng, 3)
+    vals = s.rng.integers(0, 65537, (3, 4096), dtype=np.uint64)
+    a = fg.random_from_seed(ctx, _dev_seeds(fg, a_seeds))
+    e = fg.sample_cbd_from_seed(_dev_seeds(fg, e_seeds), s.par_o.variance, 4096)
+    got = fg.to_host(sk.encrypt(fg.to_device(vals), a, e, 0, simd=True))
+    for b in range(3):
+        pt = ora.Plaintext.encode(vals[b], "simd", s.par_o, 0)
+        want = s.sk.encrypt_with(pt, ora.random_from_seed(ctx_o, a_seeds[b]),
+                                 ora.sample_vec_cbd_from_seed(4096, s.par_o.variance, e_seeds[b]))
+        assert np.array_equal(got[b], want.to_array()), b
+    dec = fg.to_host(sk.decrypt(fg.to_device(got), 0, simd=True))
+    assert np.array_equal(dec, vals)
+
+
 def test_seeded_ciphertexts(fg, ora, cuda):
     """A fresh ciphertext sent as (c0, seed): c1 expanded on the device into a
     [count][2][L][N] batch in place, equal to the oracle's, and the batch

@@ -317,6 +317,46 @@ def test_chacha_block_function(ora):
         assert got.astype("<u4").tobytes() == ks
 
 
+def _cbd_pool(size, variance, next_u64):
+    """fhe-util/src/lib.rs:22-55 step by step: a bit pool refilled with a
+    64-bit draw above the bits it holds whenever fewer than 4v remain."""
+    nb = 4 * variance
+    mask_add = ((2**64 - 1) >> (64 - nb)) >> (2 * variance)
+    mask_sub = mask_add << (2 * variance)
+    pool, nbits, out = 0, 0, []
+    for _ in range(size):
+        if nbits < nb:
+            pool |= next_u64() << nbits
+            nbits += 64
+        out.append(bin(pool & mask_add).count("1") - bin(pool & mask_sub).count("1"))
+        pool >>= nb
+        nbits -= nb
+    return out, nbits
+
+
+@pytest.mark.parametrize("size,variance", [(1, 1), (7, 3), (100, 10), (64, 16), (33, 5), (16, 16), (50, 2)])
+def test_cbd_from_seed_is_the_pool_algorithm(ora, size, variance):
+    """The oracle's CBD over a ChaCha8Rng::from_seed stream (cutting the
+    draws' bit stream into 4v-bit samples) equals the reference's pool
+    algorithm run on ChaChaRng.from_seed draws, and both take
+    ceil(4 v size / 64) draws."""
+    seed = bytes((7 * i + size) & 0xFF for i in range(32))
+    rng = ora.ChaChaRng.from_seed(seed)
+    draws = []
+
+    def next_u64():
+        draws.append(rng.next_u64())
+        return draws[-1]
+
+    want, _ = _cbd_pool(size, variance, next_u64)
+    assert len(draws) == (4 * variance * size + 63) // 64
+    got = ora.sample_vec_cbd_from_seed(size, variance, seed)
+    assert [int(x) for x in got] == want
+    assert all(abs(x) <= 2 * variance for x in want)
+    with pytest.raises(ValueError):
+        ora.sample_vec_cbd_from_seed(size, 17, seed)
+
+
 def test_random_from_seed(ora):
     """rq/mod.rs:239-257 and key_switching_key.rs:108-123: deterministic in
     the seed, uniform residues, seeds of c1 drawn 32 bytes at a time, and the
