@@ -404,7 +404,8 @@ def run_ours(args, rank: int, world: int):
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions by the CPU oracle)",
             "config": {"workload": "bfv_mul_relin_batched", "degree": N, "moduli": L, "moduli_bits": 62,
                        "extension_moduli": 7, "plaintext": T, "batch_pairs": B, "keys": "device resident",
-                       "ntt_block_logn": ntt_block, "step": f"one CUDA graph of {graph.kernels} kernels",
+                       "ntt_block_logn": ntt_block, "step": f"one CUDA graph of {graph.kernels} kernels"
+                       + (f" (two concurrent branches of {B // 2} and {B - B // 2} pairs)" if B >= 32 else ""),
                        "l2": "no flush: each step streams > 1 GB (inputs 201 MB, outputs 100 MB, scratch) through "
                              "the 126 MB L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "single": {"value": single_rate, "unit": UNIT, "note": f"{B} one-ciphertext launches"},

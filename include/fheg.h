@@ -515,8 +515,11 @@ FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, s
  * [count][2][L][N], d_out: the multiplicator's output shape) into a CUDA
  * graph; each fheg_graph_launch replays the whole pipeline with one call.
  * The graph owns its scratch. It runs the multiplication once before
- * recording (so d_out is written). Destroy the graph before the
- * multiplicator and its key. No counterpart in the reference. */
+ * recording (so d_out is written). Batches of 32 pairs or more are recorded
+ * as two independent branches of half the batch each, which the GPU runs
+ * concurrently (the kernels of one branch fill the gaps of the other).
+ * Destroy the graph before the multiplicator and its key. No counterpart in
+ * the reference. */
 typedef struct fheg_graph fheg_graph;
 FHEG_API int fheg_multiplicator_capture(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                         uint64_t* d_out, size_t count, fheg_graph** out);

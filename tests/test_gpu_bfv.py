@@ -148,6 +148,34 @@ def test_graph_replay(fg, ora, cuda):
     assert np.array_equal(want2[1], mo.multiply(cts[5], cts[7]).to_array())
 
 
+@pytest.mark.parametrize("count", [32, 33])
+def test_graph_two_branches(fg, ora, cuda, count):
+    """Batches of 32 pairs or more are captured as two concurrent branches
+    (halves with their own scratch; 33 splits 16 + 17): the replay equals
+    multiply() on the whole batch, and two products equal the oracle's."""
+    s = Setup(fg, ora, 4096, 2, 65537, seed=41 + count)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    q = np.array(s.par_o.moduli, dtype=np.uint64)[None, None, :, None]
+    rng = np.random.default_rng(count)
+    lhs_h = (rng.integers(0, 1 << 62, (count, 2, 2, 4096), dtype=np.uint64) % q).astype(np.uint64)
+    rhs_h = (rng.integers(0, 1 << 62, (count, 2, 2, 4096), dtype=np.uint64) % q).astype(np.uint64)
+    lhs, rhs = fg.to_device(lhs_h), fg.to_device(rhs_h)
+    out = fg.empty((count, 2, 2, 4096))
+    g = m.capture(lhs, rhs, out)
+    assert g.kernels >= 14
+    want = fg.to_host(m.multiply(lhs, rhs))
+    out.zero_()
+    g.launch()
+    cuda.cuda.synchronize()
+    assert np.array_equal(fg.to_host(out), want)
+    mo = ora.Multiplicator.default(rk_o)
+    for b in (0, count - 1):
+        lo = ora.Ciphertext.from_array(s.par_o, lhs_h[b], 0)
+        ro = ora.Ciphertext.from_array(s.par_o, rhs_h[b], 0)
+        assert np.array_equal(want[b], mo.multiply(lo, ro).to_array()), b
+
+
 def test_batched_equals_single_and_host(fg, ora, cuda):
     """A batch of 6 equals 6 single launches and the host entry point."""
     s = Setup(fg, ora, 4096, 2, 65537, seed=21)
