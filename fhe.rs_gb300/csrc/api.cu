@@ -790,7 +790,28 @@ FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* 
                                          uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
     abi_need(m && ((d_lhs && d_rhs && d_out) || !count), "null input");
-    m->m->multiply(d_lhs, d_rhs, d_out, count, as_stream(stream));
+    cudaStream_t st = as_stream(stream);
+    Multiplicator& mm = *m->m;
+    if (count < 32) {
+      mm.multiply(d_lhs, d_rhs, d_out, count, st);
+      return;
+    }
+    // Two halves side by side, the second on the multiplicator's own stream
+    // between a fork and a join on the caller's stream (so the call stays
+    // ordered on `stream`, and can be recorded into a graph): the branches
+    // fill one another's barriers, tails and latency-bound phases.
+    if (!m->side) check_cuda(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!m->fork) check_cuda(cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming), "cudaEventCreate");
+    if (!m->join) check_cuda(cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming), "cudaEventCreate");
+    const size_t N = mm.base->N(), L = mm.base->L();
+    const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * (mm.mod_switch ? L - 1 : L) * N;
+    const size_t c0 = count / 2;
+    check_cuda(cudaEventRecord(m->fork, st), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(m->side, m->fork, 0), "cudaStreamWaitEvent");
+    mm.multiply(d_lhs, d_rhs, d_out, c0, st);
+    mm.multiply(d_lhs + c0 * in_pair, d_rhs + c0 * in_pair, d_out + c0 * out_pair, count - c0, m->side, &m->side_ws);
+    check_cuda(cudaEventRecord(m->join, m->side), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(st, m->join, 0), "cudaStreamWaitEvent");
   });
 }
 

@@ -35,10 +35,18 @@ struct fheg_multiplicator {
   std::vector<cudaEvent_t> copied;  // end of each chunk's input copies
   size_t host_chunk = 0;            // pairs per chunk (0 = automatic)
   int host_streams = 4;
+  // Second branch of a large direct multiplication (api.cu): its stream,
+  // fork / join events and scratch.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  fheg::Workspace side_ws;
   ~fheg_multiplicator() {
     for (auto& s : pipe)
       if (s) cudaStreamDestroy(s);
     for (auto& e : copied) cudaEventDestroy(e);
+    if (side) cudaStreamDestroy(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
   }
 };
 struct fheg_secret_key {

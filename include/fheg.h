@@ -313,7 +313,9 @@ FHEG_API int fheg_multiplicator_enable_mod_switching(fheg_multiplicator* m);
 /* Shape of the product: parts (2 with relinearization, else 3) and level. */
 FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t* parts, size_t* level);
 /* Multiplicator::multiply (fhe/src/bfv/ops/mul.rs:158-227), batched:
- * d_lhs, d_rhs [count][2][L][N] (Ntt) -> d_out [count][parts][L'][N]. */
+ * d_lhs, d_rhs [count][2][L][N] (Ntt) -> d_out [count][parts][L'][N].
+ * From 32 pairs the two halves of the batch run concurrently, the second on
+ * a stream of the multiplicator's that forks from and joins `stream`. */
 FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                          uint64_t* d_out, size_t count, void* stream);
 /* Runs one multiplication with events at the stage boundaries and returns
