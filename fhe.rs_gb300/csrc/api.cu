@@ -664,7 +664,25 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
       abi_need(keys[b] && d_cts[b] && d_outs[b] && d_cts[b] != d_outs[b], "null or aliased batch entry");
       req[b] = RotRequest{&keys[b]->k, exponents[b], d_cts[b], d_outs[b]};
     }
-    galois_relinearize_batch(*par->p, req.data(), count, const_cast<fheg_params*>(par)->ws, as_stream(stream));
+    fheg_params* ph = const_cast<fheg_params*>(par);
+    cudaStream_t st = as_stream(stream);
+    if (count < 16) {
+      galois_relinearize_batch(*par->p, req.data(), count, ph->ws, st);
+      return;
+    }
+    // Two halves side by side, the second on the parameters' own stream
+    // between a fork and a join on the caller's stream (as the batched
+    // multiplication does).
+    if (!ph->side) check_cuda(cudaStreamCreateWithFlags(&ph->side, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!ph->fork) check_cuda(cudaEventCreateWithFlags(&ph->fork, cudaEventDisableTiming), "cudaEventCreate");
+    if (!ph->join) check_cuda(cudaEventCreateWithFlags(&ph->join, cudaEventDisableTiming), "cudaEventCreate");
+    const size_t c0 = count / 2;
+    check_cuda(cudaEventRecord(ph->fork, st), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(ph->side, ph->fork, 0), "cudaStreamWaitEvent");
+    galois_relinearize_batch(*par->p, req.data(), c0, ph->ws, st);
+    galois_relinearize_batch(*par->p, req.data() + c0, count - c0, ph->side_ws, ph->side);
+    check_cuda(cudaEventRecord(ph->join, ph->side), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(st, ph->join, 0), "cudaStreamWaitEvent");
   });
 }
 

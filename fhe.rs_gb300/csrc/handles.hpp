@@ -20,6 +20,19 @@ struct fheg_params {
   std::unique_ptr<fheg::Params> p;
   std::vector<fheg_context> level_handles;
   fheg::Workspace ws;  // scratch of the ragged batch entry points
+  // Second half of a large ragged rotation batch (api.cu): its stream, fork /
+  // join events and scratch.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  fheg::Workspace side_ws;
+  fheg_params() = default;
+  fheg_params(const fheg_params&) = delete;
+  fheg_params& operator=(const fheg_params&) = delete;
+  ~fheg_params() {
+    if (side) cudaStreamDestroy(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+  }
 };
 struct fheg_ksk {
   fheg::Ksk k;

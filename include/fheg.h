@@ -267,8 +267,10 @@ FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const 
  * exactly as GaloisKey::relinearize_into (galois_key.rs:90-124) would one at a
  * time (EvaluationKey::rotates_columns_by / rotates_rows,
  * evaluation_key.rs:92-131). Ciphertexts may sit at different levels; all keys
- * must come from `par`. One launch per stage covers the whole batch. Calls on
- * the same parameters must not run concurrently (shared scratch). */
+ * must come from `par`. One launch per stage covers the whole batch; from 16
+ * requests the two halves run concurrently, the second on a stream of the
+ * parameters' that forks from and joins `stream`. Calls on the same
+ * parameters must not run concurrently (shared scratch). */
 FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
                                            const size_t* exponents, const uint64_t* const* d_cts,
                                            uint64_t* const* d_outs, size_t count, void* stream);

@@ -268,10 +268,11 @@ def test_errors(fg, ora, cuda):
     assert e.value.code == fg.ERR_INVALID_LEVEL
 
 
-@pytest.mark.parametrize("n,L,count", [(4096, 4, 6), (32768, 5, 4)])
+@pytest.mark.parametrize("n,L,count", [(4096, 4, 6), (32768, 5, 4), (4096, 4, 17)])
 def test_rotate_ragged_batch(fg, ora, cuda, n, L, count):
     """Ciphertexts at different levels, each rotated with its own key in one
-    batched call, equal the oracle's one-at-a-time GaloisKey::relinearize."""
+    batched call, equal the oracle's one-at-a-time GaloisKey::relinearize
+    (17 requests run as two concurrent halves of 8 and 9)."""
     s = Setup(fg, ora, n, L, 65537, seed=1000 + n + L)
     rng = np.random.default_rng(77)
     levels = [int(x) for x in rng.integers(0, L - 1, count)]  # keep >= 2 moduli
