@@ -65,6 +65,10 @@ STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # capture summarised in profiles/stages_mul_relin_n16384_b64.md.
 STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "E": 671.7e6, "F": 707.3e6,
                        "G": 493.2e6}
+# The ncu figures above and below hold for the library sources they were
+# captured on: library_source_hash() of that tree. A run on other sources
+# reports null for them instead of stale numbers.
+PROFILED_SOURCE_HASH = "unprofiled"
 # Share of the elapsed cycles in which the integer multipliers (the FMA-heavy
 # pipe, which executes every IMAD) were busy, per stage, from the ncu capture
 # of one 32-pair multiplication under the same plan summarised in
@@ -72,6 +76,38 @@ STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "
 # launches). The whole multiplication: 72.0%, time-weighted.
 STAGE_FMAHEAVY_PCT = {"A": 67.0, "B": 85.5, "C": 70.3, "D": 65.3, "E": 79.8, "F": 68.6, "G": 58.5}
 MULTIPLY_FMAHEAVY_PCT = 72.0
+
+
+def library_source_hash() -> str:
+    """SHA-256 (first 16 hex digits) of the library's sources: every file of
+    fhe.rs_gb300/csrc and include/, in name order."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for d in (os.path.join(ROOT, "fhe.rs_gb300", "csrc"), os.path.join(ROOT, "include")):
+        for name in sorted(os.listdir(d)):
+            with open(os.path.join(d, name), "rb") as f:
+                h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (or architecture when none is listed)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.machine()
 
 
 def _peaks():
@@ -182,23 +218,37 @@ def replica_throughput(batch: int, ms: float, world: int) -> float:
     return world * batch / (ms / 1000.0)
 
 
-def cpu_multiply_rate(ora, rk, cts, threads: int, per_thread: int):
-    """Oracle products per second with `threads` host threads (independent
-    ciphertexts, the reference has no internal parallelism)."""
-    mult = ora.Multiplicator.default(rk)
-
-    def work(tid):
-        for k in range(per_thread):
-            mult.multiply(cts[(tid + k) % len(cts)], cts[(tid * 3 + k + 1) % len(cts)])
-
+def cpu_multiply_rate(driver, cts, threads: int, per_thread: int):
+    """Products per second of the CPU restatement of Multiplicator::multiply
+    (oracle.cpp's whole-product loop, no Python inside) on `threads` host
+    threads, `per_thread` independent pairs each (the reference has no
+    internal parallelism; callers parallelise over ciphertexts)."""
+    count = threads * per_thread
+    arrs = [c.to_array() for c in cts]
+    lhs = np.stack([arrs[k % len(arrs)] for k in range(count)])
+    rhs = np.stack([arrs[(3 * k + 1) % len(arrs)] for k in range(count)])
     t0 = time.perf_counter()
-    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
-    for th in ths:
-        th.start()
-    for th in ths:
-        th.join()
+    driver.multiply(lhs, rhs, threads)
     dt = time.perf_counter() - t0
-    return threads * per_thread / dt, dt
+    return count / dt, dt
+
+
+def cpu_baseline_sample(ora, rk, cts, seconds: float):
+    """Single-thread and all-core rates of the CPU restatement, the all-core
+    sample sized to about `seconds` of wall time."""
+    driver = ora.MultiplyDriver(ora.Multiplicator.default(rk))
+    cores = os.cpu_count() or 1
+    cpu_multiply_rate(driver, cts, 1, 1)  # warm the caches
+    single, _ = cpu_multiply_rate(driver, cts, 1, 3)
+    rate0, _ = cpu_multiply_rate(driver, cts, cores, 1)
+    per_thread = max(1, int(seconds * rate0 / cores))
+    rate, dt = cpu_multiply_rate(driver, cts, cores, per_thread)
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "single_thread": single,
+            "cpu": cpu_model(),
+            "sample": f"{cores * per_thread} products on {cores} host threads ({dt:.1f} s), single-thread "
+                      f"{single:.2f} ct/s; C++ restatement of fhe.rs Multiplicator::multiply "
+                      "(oracle.cpp, -O3 -mcpu/-march=native, std::thread over independent pairs); the Rust "
+                      "reference cannot be built here"}
 
 
 def run_reference(args, rank: int):
@@ -209,16 +259,16 @@ def run_reference(args, rank: int):
         return
     oracle_build.build()
     par, sk, rk, cts, _, _ = make_inputs(ora, 8, distinct=8)
+    driver = ora.MultiplyDriver(ora.Multiplicator.default(rk))
     cores = os.cpu_count() or 1
     # One step = the GPU arm's batch of products, spread over every host core.
     per_thread = -(-args.batch // cores)
-    cpu_multiply_rate(ora, rk, cts, 1, 1)  # warm the caches of the oracle
+    cpu_multiply_rate(driver, cts, 1, 1)  # warm the caches of the oracle
     for _ in range(max(args.warmup, 0)):
-        cpu_multiply_rate(ora, rk, cts, cores, per_thread)
-    t0 = time.perf_counter()
+        cpu_multiply_rate(driver, cts, cores, per_thread)
+    total = 0.0
     for _ in range(args.steps):
-        cpu_multiply_rate(ora, rk, cts, cores, per_thread)
-    total = time.perf_counter() - t0
+        total += cpu_multiply_rate(driver, cts, cores, per_thread)[1]
     value = args.steps * cores * per_thread / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -226,10 +276,10 @@ def run_reference(args, rank: int):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": "bfv_mul_relin", "degree": N, "moduli": L, "moduli_bits": 62, "plaintext": T,
                    "batch_pairs_per_step": cores * per_thread, "parallelism": "host threads"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                          "sample": f"{cores * per_thread} products per step ({per_thread} per host thread) of the "
-                                   "CPU restatement of "
-                                   "fhe.rs Multiplicator::default().multiply; the Rust reference cannot be built "
+                                   "C++ restatement of fhe.rs Multiplicator::default().multiply (oracle.cpp, "
+                                   "std::thread over independent pairs); the Rust reference cannot be built "
                                    "(no Rust toolchain)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -378,25 +428,23 @@ def run_ours(args, rank: int, world: int):
     dom = max(stage_ms, key=lambda k: stage_ms[k] / STAGE_LAUNCHES[k])
     dom_gbs = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
 
+    # The NTT's butterflies per second against the measured butterfly
+    # ceiling of this GPU (fheg_intpeak, register-resident Harvey
+    # butterflies), and what 60% of the HBM bandwidth would need.
+    probes, _ = measure_intpeak(fg, torch, kinds=(4, 5), steps=3)
+    bfly = polys * L * butterflies_per_transform(logn)
+    need_60 = 0.6 * peak * 1e9 / (data_bytes + tw_bytes) * bfly
+
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cores = os.cpu_count() or 1
-        cpu_multiply_rate(ora, rk_o, cts, 1, 1)
-        single_thread, _ = cpu_multiply_rate(ora, rk_o, cts, 1, 2)
-        # Calibrate on one product per core, then size the sample to about
-        # --cpu-seconds of wall time on all cores.
-        rate0, _ = cpu_multiply_rate(ora, rk_o, cts, cores, 1)
-        per_thread = max(1, int(args.cpu_seconds * rate0 / cores))
-        rate, dt = cpu_multiply_rate(ora, rk_o, cts, cores, per_thread)
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{cores * per_thread} products on {cores} host threads ({dt:.1f} s); single-thread "
-                         f"{single_thread:.2f} ct/s; CPU restatement of fhe.rs Multiplicator::multiply "
-                         "(the Rust reference cannot be built here)"}
+        cpu = cpu_baseline_sample(ora, rk_o, cts, args.cpu_seconds)
 
-    # The ncu traffic figures were captured under the 2^12-block plan; a run
-    # whose plan differs reports no traffic rather than a mismatched one.
+    # The ncu figures hold for one plan (A, C, D, F in 2^12 blocks) and one
+    # source tree; any other run reports null for them.
     # (A plan entry of 0 means the process-wide plan of the degree.)
-    traffic_plan_matches = all((ntt_block[k] or fg.ntt_plan_get(logn)) == 12 for k in ("A", "C", "D", "F"))
+    src_hash = library_source_hash()
+    traffic_plan_matches = all((ntt_block[k] or fg.ntt_plan_get(logn)) == 12 for k in ("A", "C", "D", "F")) \
+        and src_hash == PROFILED_SOURCE_HASH
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -417,6 +465,7 @@ def run_ours(args, rank: int, world: int):
             "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
                          "traffic": STAGE_TRAFFIC_BYTES.get(dom) if traffic_plan_matches else None,
                          "traffic_plan": "A,C,D,F = 2^12 blocks", "kernel": STAGE_KERNELS[dom],
+                         "source_hash": src_hash, "profiled_source_hash": PROFILED_SOURCE_HASH,
                          "algorithmic_bytes": stage_bytes[dom], "launch_ms": stage_ms[dom], "peak_kind": peak_kind,
                          "note": "integer-multiplier bound, not HBM: all arithmetic is exact 64-bit residue "
                                  "arithmetic on the CUDA cores' 32-bit multipliers",
@@ -428,7 +477,15 @@ def run_ours(args, rank: int, world: int):
                            "kernel": STAGE_KERNELS[k]} for k in stage_ms},
             "ntt": {"kernel": "forward / inverse NTT alone, 256 polys x 6 limbs", "fwd_gbs": fwd_gbs,
                     "inv_gbs": inv_gbs, "fwd_frac": fwd_gbs / peak, "inv_frac": inv_gbs / peak, "fwd_ms": fwd_ms,
-                    "inv_ms": inv_ms},
+                    "inv_ms": inv_ms, "cluster": fg.ntt_cluster_get(logn),
+                    "fwd_butterflies_per_s": bfly / (fwd_ms / 1000.0), "inv_butterflies_per_s": bfly / (inv_ms / 1000.0),
+                    "fwd_butterfly_ceiling_per_s": probes[4]["ops_per_s"],
+                    "inv_butterfly_ceiling_per_s": probes[5]["ops_per_s"],
+                    "fwd_frac_of_ceiling": bfly / (fwd_ms / 1000.0) / probes[4]["ops_per_s"],
+                    "inv_frac_of_ceiling": bfly / (inv_ms / 1000.0) / probes[5]["ops_per_s"],
+                    "butterflies_per_s_for_60pct_hbm": need_60,
+                    "note": "the butterfly ceiling is fheg_intpeak's register-resident Harvey butterfly: an NTT "
+                            "at 60% of HBM needs more butterflies per second than the integer pipes issue"},
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
@@ -729,19 +786,23 @@ def run_ntt(args):
     expect = one.copy()
     for i, m in enumerate(moduli):
         ora.ntt_operator(m, n).forward(expect[i])
-    plans = [bl for bl in (12, 13, 14) if bl <= logn and logn - bl <= 4 and (bl < logn or logn <= 14)] or [logn]
-    default = fg.ntt_plan_get(logn)
+    blocks = [bl for bl in (12, 13, 14) if bl <= logn and logn - bl <= 4 and (bl < logn or logn <= 14)] or [logn]
+    # (block size, cluster mode): the 2^12-block plans also run as one pass on
+    # clusters of the limb's blocks.
+    plans = [(bl, False) for bl in blocks] + [(12, True) for bl in blocks if bl == 12 and logn > 12]
+    default, default_cluster = fg.ntt_plan_get(logn), fg.ntt_cluster_get(logn)
     stream = torch.cuda.current_stream()
     start, mid, end = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     nbytes = 2 * 8 * polys * L * n + 2 * 8 * L * n
     results = {}
     launches = 0
-    for bl in plans:
+    for bl, cluster in plans:
         fg.ntt_plan_set(logn, bl)
+        fg.ntt_cluster_set(logn, cluster)
         fg.ntt_forward(ctx, buf)
         torch.cuda.synchronize()
         if not np.array_equal(fg.to_host(buf[:1])[0], expect):
-            raise SystemExit(f"bench: NTT (blocks of 2^{bl}) is not bit-exact with the oracle")
+            raise SystemExit(f"bench: NTT (blocks of 2^{bl}, cluster {cluster}) is not bit-exact with the oracle")
         fg.ntt_backward(ctx, buf)
         for _ in range(args.warmup):
             fg.ntt_forward(ctx, buf)
@@ -760,9 +821,10 @@ def run_ntt(args):
                 inv += mid.elapsed_time(end)
         fwd /= args.steps
         inv /= args.steps
-        results[bl] = {"fwd_ms": fwd, "inv_ms": inv, "gbs": 2 * nbytes / ((fwd + inv) / 1000.0) / 1e9,
-                       "clocks": clocks.summary(), "launches": fg.kernel_launch_count() - launches0}
+        results[(bl, cluster)] = {"fwd_ms": fwd, "inv_ms": inv, "gbs": 2 * nbytes / ((fwd + inv) / 1000.0) / 1e9,
+                                  "clocks": clocks.summary(), "launches": fg.kernel_launch_count() - launches0}
     fg.ntt_plan_set(logn, default)
+    fg.ntt_cluster_set(logn, default_cluster)
     best = max(results, key=lambda k: results[k]["gbs"])
     r = results[best]
     fwd, inv, gbs = r["fwd_ms"], r["inv_ms"], r["gbs"]
@@ -770,14 +832,107 @@ def run_ntt(args):
     line = {"metric": f"NTT fwd+inv GB/s N=2^{logn} L=6", "value": gbs, "unit": "GB/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": fwd + inv, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": "ntt_batched", "degree": n, "moduli": L, "polys": polys, "block_logn": best,
+            "config": {"workload": "ntt_batched", "degree": n, "moduli": L, "polys": polys, "block_logn": best[0],
+                       "cluster": best[1],
                        "l2": f"buffer {polys * L * n * 8 / 1e6:.0f} MB > L2"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "traffic": None, "peak_kind": kind, "fwd_ms": fwd, "inv_ms": inv,
                          "fwd_gbs": nbytes / (fwd / 1000) / 1e9, "inv_gbs": nbytes / (inv / 1000) / 1e9},
-            "plans": {str(k): {"fwd_ms": v["fwd_ms"], "inv_ms": v["inv_ms"], "gbs": v["gbs"]}
-                      for k, v in results.items()},
+            "plans": {f"{k[0]}{'-cluster' if k[1] else ''}": {"fwd_ms": v["fwd_ms"], "inv_ms": v["inv_ms"],
+                                                               "gbs": v["gbs"]} for k, v in results.items()},
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
+def measure_intpeak(fg, torch, kinds=(0, 1, 2, 3, 4, 5), steps=5):
+    """Operations per second of each integer probe (fheg_intpeak): 8 CTAs of
+    256 threads per SM, four waves; CUDA events on the launching stream."""
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    blocks = props.multi_processor_count * 8 * 4
+    sink = fg.empty((blocks * 256,))
+    stream = torch.cuda.current_stream()
+    out = {}
+    for kind in kinds:
+        iters = 2048 if kind >= 4 else 16384
+        fg.intpeak_launch(kind, blocks, iters, sink)  # warm-up
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        start.record(stream)
+        ops = sum(fg.intpeak_launch(kind, blocks, iters, sink) for _ in range(steps))
+        end.record(stream)
+        torch.cuda.synchronize()
+        ms = start.elapsed_time(end)
+        out[kind] = {"op": fg.INTPEAK_KINDS[kind], "ops_per_s": ops / (ms / 1000.0), "ms": ms / steps}
+    return out, props.multi_processor_count
+
+
+def butterflies_per_transform(logn: int) -> int:
+    """Butterflies of one negacyclic NTT of 2^logn residues: N/2 per stage."""
+    return (1 << logn) // 2 * logn
+
+
+def run_intpeak(args):
+    """Integer-throughput ceilings of this GPU: the 32-bit multiply forms the
+    residue products are built from, 32-bit additions, and the NTT's 64-bit
+    butterflies on register-resident values. Reported per second, per SM
+    and clock (with the sampled SM clock), and set against what the NTT
+    needs for 60% of the measured HBM bandwidth and what it reaches (forward
+    NTT of 256 polynomials x 6 limbs at N = 2^logn, the default plan)."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    with ClockSampler(0) as clocks:
+        probes, sms = measure_intpeak(fg, torch, steps=max(args.steps // 4, 3))
+    clk = clocks.summary()
+    mhz = clk["sm_mhz"] or 2070.0
+    for v in probes.values():
+        v["per_sm_per_clock"] = v["ops_per_s"] / (sms * mhz * 1e6)
+    # The forward NTT as the ntt workload times it.
+    logn = args.logn
+    n = 1 << logn
+    moduli, ub = [], 1 << 62
+    while len(moduli) < L:
+        ub = ora.generate_prime(62, 2 * n, ub)
+        moduli.append(ub)
+    ctx = fg.Context(moduli, n)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1)
+    q = torch.tensor([int(m) for m in moduli], dtype=torch.int64, device="cuda").view(1, L, 1)
+    buf = torch.randint(0, 1 << 62, (args.polys, L, n), dtype=torch.int64, device="cuda", generator=gen) % q
+    for _ in range(3):
+        fg.ntt_forward(ctx, buf)
+        fg.ntt_backward(ctx, buf)
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(args.steps):
+        fg.ntt_forward(ctx, buf)
+    end.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = start.elapsed_time(end) / args.steps
+    limbs = args.polys * L
+    bfly = limbs * butterflies_per_transform(logn)
+    nbytes = 16 * limbs * n
+    peak, kind = _peaks()
+    need = 0.6 * peak * 1e9 / nbytes * bfly  # butterflies/s for 60% of HBM
+    fwd_bps = bfly / (fwd_ms / 1000.0)
+    ceiling = probes[4]["ops_per_s"]
+    line = {"metric": "integer throughput ceilings (ops/s)", "value": ceiling, "unit": "butterflies/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": 1, "higher_is_better": True, "dtype": "u64",
+            "data": "synthetic", "config": {"workload": "intpeak", "sms": sms, "threads_per_sm": 2048},
+            "probes": {str(k): v for k, v in probes.items()},
+            "ntt": {"degree": n, "limbs": limbs, "fwd_ms": fwd_ms, "fwd_gbs": nbytes / (fwd_ms / 1000.0) / 1e9,
+                    "fwd_butterflies_per_s": fwd_bps, "frac_of_butterfly_ceiling": fwd_bps / ceiling,
+                    "hbm_frac": nbytes / (fwd_ms / 1000.0) / 1e9 / peak,
+                    "butterflies_per_s_for_60pct_hbm": need, "ceiling_over_need": ceiling / need,
+                    "peak_kind": kind},
+            "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -1046,14 +1201,15 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 400 for the batched multiplication, about 1 s; 20 otherwise)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="mul_relin", choices=["mul_relin", "ntt", "rotate", "serve", "stages", "codec", "compose",
-                                                             "serialize"])
+                                                             "serialize", "intpeak"])
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
@@ -1066,6 +1222,8 @@ def main():
     ap.add_argument("--serve-streams", type=int, default=4)
     ap.add_argument("--serve-batch", type=int, default=32)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 400 if args.workload == "mul_relin" and args.impl == "ours" else 20
     if args.workload == "serve":
         # A server loads every kernel when CUDA starts: with lazy loading the
         # first launch of each kernel instantiation (parameter set, level,
@@ -1093,6 +1251,8 @@ def main():
         run_compose(args)
     elif args.workload == "serialize":
         run_serialize(args)
+    elif args.workload == "intpeak":
+        run_intpeak(args)
     elif args.impl == "reference":
         run_reference(args, rank)
     else:

@@ -83,6 +83,22 @@ def _declare(L):
         "fheg_status_string": (ctypes.c_char_p, [i]),
         "fheg_last_error": (ctypes.c_char_p, []),
         "fheg_kernel_launch_count": (c_u64, []),
+        "fheg_multiply_groups": (i, [ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
+                                     ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_vp]),
+        "fheg_galois_relinearize_batch_capture": (i, [c_vp, ctypes.POINTER(c_vp), ctypes.POINTER(c_size),
+                                                      ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_size,
+                                                      ctypes.POINTER(c_vp)]),
+        "fheg_ksk_to_bytes": (i, [c_vp, i, c_size, ctypes.c_char_p, c_size, ctypes.POINTER(c_size)]),
+        "fheg_evaluation_key_to_bytes": (i, [ctypes.POINTER(c_vp), ctypes.POINTER(c_size), c_size, c_size, c_size,
+                                             ctypes.c_char_p, c_size, ctypes.POINTER(c_size)]),
+        "fheg_evaluation_key_from_bytes": (i, [c_vp, ctypes.c_char_p, c_size, ctypes.POINTER(c_vp),
+                                               ctypes.POINTER(c_size), c_size, ctypes.POINTER(c_size),
+                                               ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
+        "fheg_poly_compute_shoup": (i, [c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_poly_mul_shoup": (i, [c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
+        "fheg_ntt_cluster_set": (i, [ctypes.c_uint32, i]),
+        "fheg_ntt_cluster_get": (i, [ctypes.c_uint32, ctypes.POINTER(i)]),
+        "fheg_intpeak": (i, [i, c_size, ctypes.c_uint32, c_vp, c_vp, ctypes.POINTER(ctypes.c_double)]),
         "fheg_generate_prime": (i, [ctypes.c_uint32, c_u64, c_u64, P_u64]),
         "fheg_supports_ntt": (i, [c_u64, c_size]),
         "fheg_ntt_default_root": (i, [c_u64, c_size, P_u64]),
@@ -213,6 +229,19 @@ def _words(x: int) -> np.ndarray:
 
 def kernel_launch_count() -> int:
     return int(lib().fheg_kernel_launch_count())
+
+
+INTPEAK_KINDS = {0: "mad.lo.u32", 1: "mad.wide.u32", 2: "mad.hi.u32", 3: "add.u32",
+                 4: "NTT forward butterfly (64-bit Harvey, Shoup twiddle)",
+                 5: "NTT inverse butterfly (64-bit Gentleman-Sande, Shoup twiddle)"}
+
+
+def intpeak_launch(kind: int, blocks: int, iters: int, sink) -> float:
+    """Launches one integer-throughput probe on the current stream (see
+    fheg_intpeak) and returns the number of operations it performs."""
+    ops = ctypes.c_double(0.0)
+    check(lib().fheg_intpeak(kind, blocks, iters, _dp(sink), _stream(), ctypes.byref(ops)))
+    return ops.value
 
 
 # ---------------------------------------------------------------------------
@@ -378,6 +407,17 @@ def ntt_prefetch_set(on: bool):
     check(lib().fheg_ntt_prefetch_set(int(on)))
 
 
+def ntt_cluster_set(logn: int, on: bool):
+    """Single-pass cluster mode of the 2^12-block plan for 2^logn (see fheg.h)."""
+    check(lib().fheg_ntt_cluster_set(logn, int(on)))
+
+
+def ntt_cluster_get(logn: int) -> bool:
+    out = ctypes.c_int(0)
+    check(lib().fheg_ntt_cluster_get(logn, ctypes.byref(out)))
+    return bool(out.value)
+
+
 def ntt_plan_get(logn: int) -> int:
     out = ctypes.c_uint32(0)
     check(lib().fheg_ntt_plan_get(logn, ctypes.byref(out)))
@@ -389,6 +429,23 @@ def ntt_autotune(ctx: Context, count: int = 64) -> int:
     out = ctypes.c_uint32(0)
     check(lib().fheg_ntt_autotune(ctx._h, count, _stream(), ctypes.byref(out)))
     return out.value
+
+
+def compute_shoup(ctx: Context, t):
+    """Poly::compute_coefficients_shoup: the Shoup plane of Ntt values (the
+    second half of an NttShoup polynomial)."""
+    out = empty(t.shape, t.device)
+    count = t.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_poly_compute_shoup(ctx._h, _dp(t), _dp(out), count, _stream()))
+    return out
+
+
+def mul_shoup(ctx: Context, a, b, b_shoup):
+    """MulAssign<&Poly<NttShoup>> for Poly<Ntt>: a * b through b's Shoup plane."""
+    out = empty(a.shape, a.device)
+    count = a.numel() // (ctx.L * ctx.degree)
+    check(lib().fheg_poly_mul_shoup(ctx._h, _dp(a), _dp(b), _dp(b_shoup), _dp(out), count, _stream()))
+    return out
 
 
 def poly_op(ctx: Context, op: str, a, b=None):
@@ -631,6 +688,16 @@ class KeySwitchingKey:
             k.exponent = e.value
         return k
 
+    def to_bytes(self) -> bytes:
+        """KeySwitchingKey / RelinearizationKey / GaloisKey::to_bytes
+        (key_switching_key.rs:332-352)."""
+        n = c_size(0)
+        e = getattr(self, "exponent", 0)
+        check(lib().fheg_ksk_to_bytes(self._h, self.KIND, e, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        check(lib().fheg_ksk_to_bytes(self._h, self.KIND, e, buf, n.value, ctypes.byref(n)))
+        return buf.raw[:n.value]
+
     @classmethod
     def from_seed(cls, par: BfvParameters, c0: np.ndarray, seed: bytes, ciphertext_level: int = 0,
                   ksk_level: int = 0, **kw):
@@ -732,6 +799,40 @@ class RGSWCiphertext:
     __mul__ = external_product  # Mul<&Ciphertext> for &RGSWCiphertext (rgsw_ciphertext.rs:155-160)
 
 
+def evaluation_key_to_bytes(keys: Sequence["GaloisKey"], ciphertext_level: int, evaluation_key_level: int) -> bytes:
+    """EvaluationKey::to_bytes (evaluation_key.rs:210-213, 382-392) of Galois keys."""
+    k = len(keys)
+    kh = (c_vp * k)(*[g._h for g in keys])
+    ex = (c_size * k)(*[g.exponent for g in keys])
+    n = c_size(0)
+    check(lib().fheg_evaluation_key_to_bytes(kh, ex, k, ciphertext_level, evaluation_key_level, None, 0,
+                                             ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value)
+    check(lib().fheg_evaluation_key_to_bytes(kh, ex, k, ciphertext_level, evaluation_key_level, buf, n.value,
+                                             ctypes.byref(n)))
+    return buf.raw[:n.value]
+
+
+def evaluation_key_from_bytes(par: BfvParameters, msg: bytes):
+    """EvaluationKey::from_bytes (evaluation_key.rs:216-228, 394-432): its
+    Galois keys, ciphertext level and evaluation key level."""
+    msg = bytes(msg)
+    count, cl, el = c_size(0), c_size(0), c_size(0)
+    check(lib().fheg_evaluation_key_from_bytes(par._h, msg, len(msg), None, None, 0, ctypes.byref(count),
+                                               ctypes.byref(cl), ctypes.byref(el)))
+    hs = (c_vp * count.value)()
+    ex = (c_size * count.value)()
+    check(lib().fheg_evaluation_key_from_bytes(par._h, msg, len(msg), hs, ex, count.value, ctypes.byref(count),
+                                               ctypes.byref(cl), ctypes.byref(el)))
+    keys = []
+    for h, e in zip(hs, ex):
+        k = GaloisKey.__new__(GaloisKey)
+        k.par, k._h, k.exponent = par, c_vp(h), int(e)
+        k.ciphertext_level, k.ksk_level = cl.value, el.value
+        keys.append(k)
+    return keys, cl.value, el.value
+
+
 class EvaluationKey:
     """EvaluationKey (fhe/src/bfv/keys/evaluation_key.rs:23-131): rotations."""
 
@@ -759,6 +860,19 @@ def rotate_batch(par: BfvParameters, keys: Sequence["GaloisKey"], cts: Sequence,
     co = (c_vp * n)(*[_dp(o) for o in outs])
     check(lib().fheg_galois_relinearize_batch(par._h, kh, ex, ci, co, n, _stream()))
     return outs
+
+
+def capture_rotate_batch(par: BfvParameters, keys: Sequence["GaloisKey"], cts: Sequence, outs: Sequence):
+    """The ragged batch of rotate_batch recorded once as a CUDA graph over
+    fixed buffers; launch() replays it."""
+    n = len(keys)
+    kh = (c_vp * n)(*[k._h for k in keys])
+    ex = (c_size * n)(*[k.exponent for k in keys])
+    ci = (c_vp * n)(*[_dp(c) for c in cts])
+    co = (c_vp * n)(*[_dp(o) for o in outs])
+    h = c_vp()
+    check(lib().fheg_galois_relinearize_batch_capture(par._h, kh, ex, ci, co, n, ctypes.byref(h)))
+    return MultiplyGraph(h, (par, list(keys), list(cts), list(outs)))
 
 
 def ciphertext_switch_down(par: BfvParameters, level: int, ct):
@@ -995,6 +1109,25 @@ class Multiplicator:
         lhs, rhs = np.ascontiguousarray(lhs, dtype=np.uint64), np.ascontiguousarray(rhs, dtype=np.uint64)
         check(lib().fheg_multiplicator_multiply_host(self._h, _ptr(lhs), _ptr(rhs), _ptr(out), count))
         return out
+
+
+def multiply_groups(mults: Sequence["Multiplicator"], lhs: Sequence, rhs: Sequence, outs: Sequence = None):
+    """Several batched multiplications, one per multiplicator (typically one
+    per level), issued together so that they overlap (fheg_multiply_groups)."""
+    g = len(mults)
+    if outs is None:
+        outs = []
+        for m, a in zip(mults, lhs):
+            parts, level = m.output_shape()
+            ctx = m.par.context_at_level(level)
+            outs.append(empty((a.shape[0], parts, ctx.L, ctx.degree), a.device))
+    mh = (c_vp * g)(*[m._h for m in mults])
+    la = (c_vp * g)(*[_dp(a) for a in lhs])
+    ra = (c_vp * g)(*[_dp(b) for b in rhs])
+    oa = (c_vp * g)(*[_dp(o) for o in outs])
+    cn = (c_size * g)(*[a.shape[0] for a in lhs])
+    check(lib().fheg_multiply_groups(mh, la, ra, oa, cn, g, _stream()))
+    return outs
 
 
 class MultiplyGraph:

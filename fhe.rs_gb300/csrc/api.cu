@@ -162,6 +162,17 @@ FHEG_API int fheg_ntt_prefetch_set(int on) {
   return abi_call([&] { set_ntt_prefetch(on != 0); });
 }
 
+FHEG_API int fheg_ntt_cluster_set(uint32_t logn, int on) {
+  return abi_call([&] { set_ntt_cluster(logn, on != 0); });
+}
+
+FHEG_API int fheg_ntt_cluster_get(uint32_t logn, int* on) {
+  return abi_call([&] {
+    abi_need(on && logn <= 16, "bad size or null output");
+    *on = ntt_cluster_enabled(logn) ? 1 : 0;
+  });
+}
+
 FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
   return abi_call([&] {
     abi_need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");
@@ -173,19 +184,25 @@ FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
 // a timed pass) and installs the fastest.
 template <class F>
 uint32_t autotune_plans(uint32_t logn, cudaStream_t st, F run) {
-  std::vector<uint32_t> plans;
+  // (block size, cluster mode) candidates.
+  std::vector<std::pair<uint32_t, bool>> plans;
   for (uint32_t bl = 12; bl <= 14; bl++)
-    if (bl <= logn && logn - bl <= 4 && (bl < logn || logn <= 14)) plans.push_back(bl);
+    if (bl <= logn && logn - bl <= 4 && (bl < logn || logn <= 14)) {
+      plans.push_back({bl, false});
+      if (bl == 12 && bl < logn) plans.push_back({bl, true});
+    }
   const uint32_t before = ntt_block_logn(logn);
+  const bool before_cluster = ntt_cluster_enabled(logn);
   if (plans.empty()) return before;
   cudaEvent_t e0, e1;
   check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
   check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
   float best_ms = 0;
-  uint32_t best = before;
+  std::pair<uint32_t, bool> best{before, before_cluster};
   try {
-    for (uint32_t bl : plans) {
-      set_ntt_block_logn(logn, bl);
+    for (const auto& plan : plans) {
+      set_ntt_block_logn(logn, plan.first);
+      set_ntt_cluster(logn, plan.second);
       for (int rep = 0; rep < 2; rep++) {
         check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
         run();
@@ -196,19 +213,21 @@ uint32_t autotune_plans(uint32_t logn, cudaStream_t st, F run) {
       check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
       if (best_ms == 0 || ms < best_ms) {
         best_ms = ms;
-        best = bl;
+        best = plan;
       }
     }
   } catch (...) {
     set_ntt_block_logn(logn, before);
+    set_ntt_cluster(logn, before_cluster);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     throw;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  set_ntt_block_logn(logn, best);
-  return best;
+  set_ntt_block_logn(logn, best.first);
+  set_ntt_cluster(logn, best.second);
+  return best.first;
 }
 
 FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn) {
@@ -441,6 +460,28 @@ FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, 
   });
 }
 
+FHEG_API int fheg_poly_compute_shoup(const fheg_context* ctx, const uint64_t* d_polys, uint64_t* d_shoup,
+                                     size_t count, void* stream) {
+  return abi_call([&] {
+    abi_need(ctx && ((d_polys && d_shoup) || !count), "null input");
+    const Context& c = *ctx->c;
+    poly_compute_shoup(c, plain_ref(const_cast<uint64_t*>(d_polys), c.L(), c.logn), plain_ref(d_shoup, c.L(), c.logn),
+                       count, as_stream(stream));
+  });
+}
+
+FHEG_API int fheg_poly_mul_shoup(const fheg_context* ctx, const uint64_t* d_a, const uint64_t* d_b,
+                                 const uint64_t* d_b_shoup, uint64_t* d_out, size_t count, void* stream) {
+  return abi_call([&] {
+    abi_need(ctx && ((d_a && d_b && d_b_shoup && d_out) || !count), "null input");
+    const Context& c = *ctx->c;
+    poly_mul_shoup(c, plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn),
+                   plain_ref(const_cast<uint64_t*>(d_b), c.L(), c.logn),
+                   plain_ref(const_cast<uint64_t*>(d_b_shoup), c.L(), c.logn), plain_ref(d_out, c.L(), c.logn), count,
+                   as_stream(stream));
+  });
+}
+
 FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation, const uint64_t* d_in,
                                   uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
@@ -532,7 +573,7 @@ FHEG_API size_t fheg_params_max_level(const fheg_params* par) { return par ? par
 // A key-switching key with room for c0 and c1, c0 uploaded from h_c0 unless
 // it is null (shared by the plain, seeded and message constructors).
 fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
-                         size_t count) {
+                         size_t count, int64_t log_base) {
   const Params& p = *par->p;
   if (ciphertext_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
   if (ksk_level > ciphertext_level) throw Error(FHEG_ERR_INVALID_LEVEL, "Unexpected levels");
@@ -544,9 +585,22 @@ fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t
     k.ksk_level = ksk_level;
     k.ctx_ct = p.ctx(ciphertext_level);
     k.ctx_ksk = p.ctx(ksk_level);
-    if (k.ctx_ksk->L() < 2) throw Error(FHEG_ERR_UNSUPPORTED, "These parameters do not support key switching");
-    if (count != k.ctx_ct->L()) throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
+    if (log_base < 0) log_base = k.ctx_ksk->L() == 1 ? log_modulus_of(k.ctx_ksk->moduli[0]) / 2 : 0;
+    if (log_base > 0) {
+      // key_switching_key.rs:63-89, 360-372: the base-2^log_base digits of a
+      // single-modulus ciphertext, against a key at the last level.
+      if (ksk_level != p.max_level() || ciphertext_level != p.max_level())
+        throw Error(FHEG_ERR_INVALID_LEVEL, "A decomposition size is specified but the levels are not maximal");
+      if (log_base > 62) throw Error(FHEG_ERR_INVALID_ARGUMENT, "decomposition base above 2^62");
+      const uint32_t lm = log_modulus_of(k.ctx_ksk->moduli[0]);
+      if (count != (lm + log_base - 1) / log_base)
+        throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the decomposition's digits");
+      k.log_base = (uint32_t)log_base;
+    } else if (count != k.ctx_ct->L()) {
+      throw Error(FHEG_ERR_KEY_MISMATCH, "count must equal the ciphertext moduli");
+    }
     k.count = count;
+    ksk_build_switch_chain(k);
     const size_t words = count * k.ctx_ksk->L() * k.ctx_ksk->N();
     k.keys.alloc(2 * words * 8);
     if (h_c0) upload(k.values(0), h_c0, words * 8);
@@ -579,7 +633,8 @@ FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_le
     abi_need(par && h_c0 && seed && out, "null input");
     fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
-      const Ksk& k = h->k;
+      Ksk& k = h->k;
+      k.seed.assign(seed, seed + 32);
       const std::vector<uint8_t> seeds = ksk_c1_seeds(seed, count);
       DevBuf d_seeds(seeds.size());
       upload(d_seeds.ptr, seeds.data(), seeds.size());
@@ -666,6 +721,9 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
     }
     fheg_params* ph = const_cast<fheg_params*>(par);
     cudaStream_t st = as_stream(stream);
+    // Every request is checked before the first launch, so an invalid one in
+    // the second half cannot leave the first half's outputs written.
+    validate_rot_requests(*par->p, req.data(), count);
     if (count < 16) {
       galois_relinearize_batch(*par->p, req.data(), count, ph->ws, st);
       return;
@@ -780,8 +838,6 @@ FHEG_API int fheg_multiplicator_enable_relinearization(fheg_multiplicator* m, co
     // mul.rs:133-142
     if (!rk->k.ctx_ct->same_as(*m->m->base) || rk->k.par != m->m->par)
       throw Error(FHEG_ERR_KEY_MISMATCH, "Invalid relinearization key context");
-    if (rk->k.ctx_ksk->L() != rk->k.ctx_ct->L())
-      throw Error(FHEG_ERR_UNSUPPORTED, "key switching keys at a lower level than the ciphertext are not supported");
     m->m->rk = &rk->k;
   });
 }
@@ -830,6 +886,39 @@ FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* 
     mm.multiply(d_lhs + c0 * in_pair, d_rhs + c0 * in_pair, d_out + c0 * out_pair, count - c0, m->side, &m->side_ws);
     check_cuda(cudaEventRecord(m->join, m->side), "cudaEventRecord");
     check_cuda(cudaStreamWaitEvent(st, m->join, 0), "cudaStreamWaitEvent");
+  });
+}
+
+FHEG_API int fheg_multiply_groups(fheg_multiplicator* const* mults, const uint64_t* const* d_lhs,
+                                  const uint64_t* const* d_rhs, uint64_t* const* d_out, const size_t* counts,
+                                  size_t groups, void* stream) {
+  return abi_call([&] {
+    abi_need((mults && d_lhs && d_rhs && d_out && counts) || !groups, "null input");
+    for (size_t g = 0; g < groups; g++) {
+      abi_need(mults[g] && ((d_lhs[g] && d_rhs[g] && d_out[g]) || !counts[g]), "null group entry");
+      for (size_t h = 0; h < g; h++)
+        abi_need(mults[h] != mults[g], "a multiplicator appears in two groups (merge them into one batch)");
+    }
+    cudaStream_t st = as_stream(stream);
+    // Every group on its multiplicator's own stream, forked from and joined
+    // back into `st`: the groups' kernels overlap on the GPU and the call
+    // stays ordered on `st`.
+    cudaEvent_t fork = nullptr;
+    check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    struct EventGuard {
+      cudaEvent_t e;
+      ~EventGuard() { cudaEventDestroy(e); }
+    } guard{fork};
+    check_cuda(cudaEventRecord(fork, st), "cudaEventRecord");
+    for (size_t g = 0; g < groups; g++) {
+      fheg_multiplicator* m = mults[g];
+      if (!m->side) check_cuda(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking), "cudaStreamCreate");
+      if (!m->join) check_cuda(cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming), "cudaEventCreate");
+      check_cuda(cudaStreamWaitEvent(m->side, fork, 0), "cudaStreamWaitEvent");
+      m->m->multiply(d_lhs[g], d_rhs[g], d_out[g], counts[g], m->side);
+      check_cuda(cudaEventRecord(m->join, m->side), "cudaEventRecord");
+    }
+    for (size_t g = 0; g < groups; g++) check_cuda(cudaStreamWaitEvent(st, mults[g]->join, 0), "cudaStreamWaitEvent");
   });
 }
 

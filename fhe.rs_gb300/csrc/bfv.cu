@@ -17,6 +17,7 @@
 // forward NTT of c2 followed by `into_power_basis` is the identity.
 
 #include <algorithm>
+#include <functional>
 
 #include "lib.hpp"
 #include "ntt.cuh"
@@ -185,6 +186,22 @@ struct SrcDigit {
   }
 };
 
+// Digit d of the base-2^log_base decomposition of a single-limb power-basis
+// row (key_switching_key.rs:300-314), lazily reduced into the key modulus
+// (rq/mod.rs:525-528): polynomial b * nd + d reads row b.
+struct SrcDecompDigit {
+  PolyRef rows;  // poly b, limb 0
+  uint32_t nd, log_base;
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
+    const uint32_t b = j.poly / nd, d = j.poly % nd;
+    const uint64_t x = (rows.at(b, 0)[i] >> (d * log_base)) & ((1ull << log_base) - 1);
+    return reduce64_lazy(x, pr);
+  }
+  __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
+    prefetch_l2(rows.at(j.poly / nd, 0) + i);
+  }
+};
+
 // Ntt input gathered through the substitution x -> x^e (rq/mod.rs:324-334).
 __device__ __forceinline__ uint32_t brev_n(uint32_t x, uint32_t logn) { return __brev(x) >> (32 - logn); }
 __device__ __forceinline__ uint32_t gather_index(uint32_t i, uint64_t e, uint32_t logn) {
@@ -349,37 +366,224 @@ static uint32_t digits_fit(const std::vector<uint64_t>& digit_moduli, const std:
 }
 
 // ---------------------------------------------------------------------------
+// Keys below the ciphertext level: the key switch's output lives in the key
+// context (Lk > L moduli) and is brought down to the ciphertext context by
+// switch_down_to (rq/mod.rs:455-462), i.e. Lk - L successive switch_down
+// steps (rq/mod.rs:390-448), each dropping the last modulus with rounding.
+// The steps work column by column, so all of them run in one kernel with the
+// residues of a coefficient in registers, in the reference's order.
+
+static size_t round32(size_t words) { return (words + 31) & ~(size_t)31; }
+
+void ksk_build_switch_chain(Ksk& k) {
+  const size_t Lk = k.ctx_ksk->L(), L = k.ctx_ct->L();
+  k.chain.release();
+  if (Lk <= L) return;
+  const std::vector<uint64_t>& q = k.ctx_ksk->moduli;
+  std::vector<uint64_t> t;
+  for (size_t m = Lk - 1; m >= L; m--) {
+    // The constants of the context with m + 1 moduli (rq/context.rs:66-73,
+    // rq/mod.rs:427), for the step that drops q_m.
+    t.push_back(q[m]);
+    std::vector<uint64_t> inv(m);
+    for (size_t i = 0; i < m; i++) inv[i] = invmod(q[m] % q[i], q[i]);
+    for (size_t i = 0; i < m; i++) t.push_back(inv[i]);
+    for (size_t i = 0; i < m; i++) t.push_back(shoup(inv[i], q[i]));
+    for (size_t i = 0; i < m; i++) t.push_back(q[i] - (q[m] / 2) % q[i]);
+    if (m == L) break;
+  }
+  k.chain.alloc(t.size() * 8);
+  upload(k.chain.ptr, t.data(), t.size() * 8);
+}
+
+// One step (rq/mod.rs:417-438) for residue x (mod q_k) given the dropped
+// residue xm (mod q_m) and the step's constants c (see Ksk::chain).
+__device__ __forceinline__ uint64_t chain_step(uint64_t x, uint64_t last, const DevPrime& pr, const uint64_t* c,
+                                               uint32_t m, uint32_t k) {
+  const uint64_t tmp = reduce64_lazy(last, pr) + __ldg(c + 1 + 2 * m + k);
+  return mul_shoup(x + 3 * pr.p - tmp, __ldg(c + 1 + k), __ldg(c + 1 + m + k), pr.p);
+}
+
+// The steps m = lk-1 .. l on the residues x[0..lk) of one coefficient, held
+// in registers (every index static after unrolling).
+template <int MAXK>
+__device__ __forceinline__ void chain_coeff(uint64_t* x, const DevPrime* primes, const uint64_t* c, uint32_t lk,
+                                            uint32_t l) {
+#pragma unroll
+  for (int m = MAXK - 1; m >= 1; m--) {
+    if ((uint32_t)m < lk && (uint32_t)m >= l) {
+      const uint64_t qm = __ldg(c);
+      const uint64_t last = reduce_once(x[m] + (qm >> 1), qm);
+#pragma unroll
+      for (int k = 0; k < m; k++) x[k] = chain_step(x[k], last, primes[k], c, (uint32_t)m, (uint32_t)k);
+      c += 1 + 3 * m;
+    }
+  }
+}
+
+// `polys` polynomials: in [poly][lk][N] power basis -> out [poly][l][N].
+template <int MAXK>
+__global__ void k_switch_chain(const DevPrime* primes, const uint64_t* chain, uint32_t lk, uint32_t l, uint32_t logn,
+                               PolyRef in, PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint32_t poly = row_of(gid, logn);
+  uint64_t x[MAXK];
+#pragma unroll
+  for (int k = 0; k < MAXK; k++)
+    if ((uint32_t)k < lk) x[k] = in.at(poly, k)[i];
+  chain_coeff<MAXK>(x, primes, chain, lk, l);
+#pragma unroll
+  for (int k = 0; k < MAXK; k++)
+    if ((uint32_t)k < l) out.at(poly, k)[i] = x[k];
+}
+
+// Key contexts of more than 32 moduli: the same steps with the residues
+// updated in place in `in`.
+__global__ void k_switch_chain_mem(const DevPrime* primes, const uint64_t* chain, uint32_t lk, uint32_t l,
+                                   uint32_t logn, PolyRef in, PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint32_t poly = row_of(gid, logn);
+  const uint64_t* c = chain;
+  for (uint32_t m = lk - 1; m >= l; m--) {
+    const uint64_t qm = __ldg(c);
+    const uint64_t last = reduce_once(in.at(poly, m)[i] + (qm >> 1), qm);
+    for (uint32_t k = 0; k < m; k++) {
+      uint64_t* xp = in.at(poly, k) + i;
+      *xp = chain_step(*xp, last, primes[k], c, m, k);
+    }
+    c += 1 + 3 * (uint64_t)m;
+    if (m == l) break;
+  }
+  for (uint32_t k = 0; k < l; k++) out.at(poly, k)[i] = in.at(poly, k)[i];
+}
+
+void switch_down_chain(const Ksk& k, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st) {
+  const Context& kc = *k.ctx_ksk;
+  const uint32_t lk = (uint32_t)kc.L(), l = (uint32_t)k.ctx_ct->L();
+  const uint64_t total = polys << kc.logn;
+  if (total == 0 || lk <= l) return;
+  const uint64_t* c = k.chain.u64();
+  const unsigned blocks = nblocks(total, 256);
+  if (lk <= 8) k_switch_chain<8><<<blocks, 256, 0, st>>>(kc.primes_dev(), c, lk, l, kc.logn, in, out, total);
+  else if (lk <= 16) k_switch_chain<16><<<blocks, 256, 0, st>>>(kc.primes_dev(), c, lk, l, kc.logn, in, out, total);
+  else if (lk <= 32) k_switch_chain<32><<<blocks, 256, 0, st>>>(kc.primes_dev(), c, lk, l, kc.logn, in, out, total);
+  else k_switch_chain_mem<<<blocks, 256, 0, st>>>(kc.primes_dev(), c, lk, l, kc.logn, in, out, total);
+  after_launch("k_switch_chain");
+}
+
+// Destination of the last forward NTT of a switched-down key switch: part
+// `poly & 1` of ciphertext `poly >> 1`, plus the ciphertext part it is added
+// to (add0 optionally read through the substitution of exponent add0_e).
+struct DstAddParts {
+  uint64_t* out;
+  uint64_t out_stride;
+  const uint64_t* add0;
+  uint64_t add0_stride, add0_e;
+  const uint64_t* add1;
+  uint64_t add1_stride;
+  uint32_t L, logn;
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime& pr, uint32_t i, uint64_t v) const {
+    const uint64_t b = j.poly >> 1;
+    const uint32_t part = j.poly & 1;
+    uint64_t a = 0;
+    if (part == 0) {
+      if (add0) a = add0[b * add0_stride + ((uint64_t)j.limb << logn) + (add0_e ? gather_index(i, add0_e, logn) : i)];
+    } else if (add1) {
+      a = add1[b * add1_stride + ((uint64_t)j.limb << logn) + i];
+    }
+    out[b * out_stride + ((uint64_t)(part * L + j.limb) << logn) + i] = add_mod(v, a, pr.p);
+  }
+};
+
+// Forward NTT of `inplace` (reduced) whose final values go to `dst`; a
+// two-pass plan runs its strided pass in place first.
+template <class Dst>
+void ntt_forward_into(uint32_t logn, NttGeom g, uint64_t polys, PolyRef inplace, Dst dst, cudaStream_t st) {
+  const uint32_t bl = ntt_block_logn(logn);
+  if (bl >= logn || logn < 13) {
+    g.s1 = 0;
+    ntt_fwd_single<true>(logn, g, polys, SrcPoly{inplace}, dst, st);
+    return;
+  }
+  if (bl == 12 && ntt_cluster_enabled(logn) &&
+      launch_fwd_cluster<12, true>(g, logn - bl, polys, SrcPoly{inplace}, dst, st))
+    return;
+  launch_fwd_top(logn - bl, g, bl, polys, SrcPoly{inplace}, DstPoly{inplace}, st);
+  ntt_forward_after_top<true>(logn, g, polys, DstPoly{inplace}, dst, st, bl);
+}
+
+// The key context's (c0, c1) of `batch` key switches in `ks` ([batch][2][Lk][N],
+// Ntt; overwritten) into the power basis, down to the ciphertext context
+// (`sd`, [batch][2][L][N]), back to Ntt, plus add0 / add1, into out.
+static void finish_switch_down(const Ksk& k, uint64_t* ks, uint64_t* sd, uint64_t batch, const uint64_t* add0,
+                               uint64_t add0_poly_stride, uint64_t add0_exponent, const uint64_t* add1,
+                               uint64_t add1_poly_stride, uint64_t* out, uint64_t out_poly_stride, cudaStream_t st) {
+  const Context& kc = *k.ctx_ksk;
+  const Context& cc = *k.ctx_ct;
+  const uint32_t logn = kc.logn;
+  PolyRef ksref = plain_ref(ks, kc.L(), logn);
+  PolyRef sdref = plain_ref(sd, cc.L(), logn);
+  ntt_backward(kc, ksref, ksref, 2 * batch, st);
+  switch_down_chain(k, ksref, sdref, 2 * batch, st);
+  NttGeom g{cc.primes_dev(), (uint32_t)cc.L(), 0};
+  DstAddParts dst{out, out_poly_stride, add0, add0_poly_stride, add0_exponent, add1, add1_poly_stride,
+                  (uint32_t)cc.L(), logn};
+  ntt_forward_into(logn, g, 2 * batch, sdref, dst, st);
+}
+
+// ---------------------------------------------------------------------------
 // Key switching (key_switching_key.rs:214-289) on digits in the power basis.
+
+size_t key_switch_scratch_words(const Ksk& k, uint64_t batch) {
+  const size_t Lk = k.ctx_ksk->L(), L = k.ctx_ct->L(), N = k.ctx_ct->N();
+  size_t w = round32(batch * k.count * Lk * N);
+  if (k.switches_down()) w += round32(batch * 2 * Lk * N) + round32(batch * 2 * L * N);
+  return w;
+}
 
 void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* add0, uint64_t add0_poly_stride,
                 uint64_t add0_exponent, const uint64_t* add1, uint64_t add1_poly_stride, uint64_t* out,
                 uint64_t out_poly_stride, uint64_t* D, cudaStream_t st) {
   const Context& kc = *k.ctx_ksk;
-  const size_t Lk = kc.L(), nd = k.count;
+  const size_t Lk = kc.L(), nd = k.count, N = kc.N();
   const uint32_t logn = kc.logn;
   PolyRef dref = plain_ref(D, Lk, logn);
   NttGeom g{kc.primes_dev(), (uint32_t)Lk, 0};
   // Every digit in every key modulus (rq/mod.rs:518-540), reduced output.
-  ntt_forward_any<true>(logn, g, batch * nd,
-                        SrcDigit{digits, (uint32_t)nd, digits_fit(k.ctx_ct->moduli, kc.moduli)}, DstPoly{dref}, st);
-  launch_key_mac(kc.primes_dev(), dref, k.values(0), k.values(1), add0, add0_poly_stride, add0_exponent, add1,
-                 add1_poly_stride, out, out_poly_stride, (uint32_t)nd, (uint32_t)Lk, logn, batch, st);
-}
-
-static void require_same_level_key(const Ksk& k) {
-  if (k.ctx_ksk->L() != k.ctx_ct->L())
-    throw Error(FHEG_ERR_UNSUPPORTED, "key switching keys at a lower level than the ciphertext are not supported");
+  if (k.log_base)
+    ntt_forward_any<true>(logn, g, batch * nd, SrcDecompDigit{digits, (uint32_t)nd, k.log_base}, DstPoly{dref}, st);
+  else
+    ntt_forward_any<true>(logn, g, batch * nd,
+                          SrcDigit{digits, (uint32_t)nd, digits_fit(k.ctx_ct->moduli, kc.moduli)}, DstPoly{dref},
+                          st);
+  if (!k.switches_down()) {
+    launch_key_mac(kc.primes_dev(), dref, k.values(0), k.values(1), add0, add0_poly_stride, add0_exponent, add1,
+                   add1_poly_stride, out, out_poly_stride, (uint32_t)nd, (uint32_t)Lk, logn, batch, st);
+    return;
+  }
+  // relinearization_key.rs:84-92, galois_key.rs:113-120: the sums in the key
+  // context, switched down, then added.
+  uint64_t* ks = D + round32(batch * nd * Lk * N);
+  uint64_t* sd = ks + round32(batch * 2 * Lk * N);
+  launch_key_mac(kc.primes_dev(), dref, k.values(0), k.values(1), nullptr, 0, 0, nullptr, 0, ks, 2 * Lk * N,
+                 (uint32_t)nd, (uint32_t)Lk, logn, batch, st);
+  finish_switch_down(k, ks, sd, batch, add0, add0_poly_stride, add0_exponent, add1, add1_poly_stride, out,
+                     out_poly_stride, st);
 }
 
 void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, Workspace& ws, cudaStream_t st) {
-  require_same_level_key(rk);
   const Context& c = *rk.ctx_ct;
-  const size_t L = c.L(), N = c.N(), Lk = rk.ctx_ksk->L();
+  const size_t L = c.L(), N = c.N();
   if (count == 0) return;
-  ws.reserve((count * L * N + count * L * Lk * N + 64) * 8);
+  const size_t d_words = key_switch_scratch_words(rk, count);
+  ws.reserve((round32(count * L * N) + d_words) * 8);
   size_t off = 0;
   uint64_t* digits = ws.take(count * L * N, &off);
-  uint64_t* D = ws.take(count * L * Lk * N, &off);
+  uint64_t* D = ws.take(d_words, &off);
   // relinearization_key.rs:81: c2 into the power basis.
   PolyRef src = sub_ref(const_cast<uint64_t*>(ct3), L, c.logn, 3, 2, 1);
   PolyRef dst = plain_ref(digits, L, c.logn);
@@ -389,10 +593,10 @@ void relinearize(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t cou
 }
 
 // Relinearization with caller-provided scratch: `digits` holds count*L*N
-// words and `D` count*L*Lk*N words. Same computation as relinearize().
+// words and `D` key_switch_scratch_words(rk, count) words. Same computation
+// as relinearize().
 void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint64_t count, uint64_t* digits,
                          uint64_t* D, cudaStream_t st) {
-  require_same_level_key(rk);
   const Context& c = *rk.ctx_ct;
   const size_t L = c.L(), N = c.N();
   if (count == 0) return;
@@ -404,16 +608,16 @@ void relinearize_scratch(const Ksk& rk, const uint64_t* ct3, uint64_t* out, uint
 
 void galois_relinearize(const Ksk& gk, uint64_t exponent, const uint64_t* ct, uint64_t* out, uint64_t count,
                         Workspace& ws, cudaStream_t st) {
-  require_same_level_key(gk);
   const Context& c = *gk.ctx_ct;
-  const size_t L = c.L(), N = c.N(), Lk = gk.ctx_ksk->L();
+  const size_t L = c.L(), N = c.N();
   const uint64_t e = exponent % (2 * N);
   if ((e & 1) == 0) throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
   if (count == 0) return;
-  ws.reserve((count * L * N + count * L * Lk * N + 64) * 8);
+  const size_t d_words = key_switch_scratch_words(gk, count);
+  ws.reserve((round32(count * L * N) + d_words) * 8);
   size_t off = 0;
   uint64_t* digits = ws.take(count * L * N, &off);
-  uint64_t* D = ws.take(count * L * Lk * N, &off);
+  uint64_t* D = ws.take(d_words, &off);
   // galois_key.rs:110: c2 = substitute(ct[1]) in the power basis; the
   // substitution is a gather fused into the inverse NTT.
   PolyRef src = sub_ref(const_cast<uint64_t*>(ct), L, c.logn, 2, 1, 1);
@@ -452,16 +656,26 @@ void external_product(const Ksk& rgsw, const uint64_t* ct, uint64_t* out, uint64
 // in one launch per stage. Levels are prefixes of one moduli chain, so limb
 // j of every ciphertext uses modulus j.
 
-struct RotDesc {
-  const uint64_t* ct;  // [2][L][N] Ntt
-  uint64_t* out;       // [2][L][N] Ntt
-  uint64_t* digits;    // [L][N] scratch: substituted c1 in the power basis
-  uint64_t* D;         // [L digits][L limbs][N] scratch: digit NTTs
-  const uint64_t* k0;  // [L][L][N] key values, part 0
-  const uint64_t* k1;  // part 1
-  uint64_t e;          // substitution exponent mod 2N
-  uint32_t L, pad;
+// 16-byte size: the uint4 job table follows `count` descriptors in memory.
+struct alignas(16) RotDesc {
+  const uint64_t* ct;     // [2][L][N] Ntt
+  uint64_t* out;          // [2][L][N] Ntt
+  uint64_t* digits;       // [L][N] scratch: substituted c1 in the power basis
+  uint64_t* D;            // [L digits][Lk limbs][N] scratch: digit NTTs
+  const uint64_t* k0;     // [L][Lk][N] key values, part 0
+  const uint64_t* k1;     // part 1
+  // Keys below the ciphertext level (Lk > L): the key-context sums [2][Lk][N]
+  // (then their power basis), their switch-down [2][L][N] (then its Ntt)
+  // and the switch-down constants; null otherwise.
+  uint64_t* ks;
+  uint64_t* sd;
+  const uint64_t* chain;
+  uint64_t e;             // substitution exponent mod 2N
+  uint32_t L, Lk;
+  uint32_t nd;            // digits: L, or those of a base-2^log_base decomposition
+  uint32_t log_base;      // 0 for RNS digits
 };
+static_assert(sizeof(RotDesc) % 16 == 0, "the job table after the descriptors needs 16-byte alignment");
 
 // R1: substituted c1, gathered into the inverse NTT (jobs: poly = b, limb = i).
 struct SrcRotSubst {
@@ -500,7 +714,10 @@ struct SrcRotDigit {
   const RotDesc* d;
   uint32_t logn;
   __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime& pr, uint32_t i) const {
-    return reduce64_lazy(d[j.poly].digits[((uint64_t)j.aux << logn) + i], pr);
+    const RotDesc& r = d[j.poly];
+    if (r.log_base)
+      return reduce64_lazy((r.digits[i] >> (j.aux * r.log_base)) & ((1ull << r.log_base) - 1), pr);
+    return reduce64_lazy(r.digits[((uint64_t)j.aux << logn) + i], pr);
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
     prefetch_l2(d[j.poly].digits + ((uint64_t)j.aux << logn) + i);
@@ -512,7 +729,7 @@ struct DstRotD {
   uint32_t logn;
   __device__ __forceinline__ uint64_t* at(const NttJob& j, uint32_t i) const {
     const RotDesc& r = d[j.poly];
-    return r.D + ((uint64_t)(j.aux * r.L + j.limb) << logn) + i;
+    return r.D + ((uint64_t)(j.aux * r.Lk + j.limb) << logn) + i;
   }
   __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
     *at(j, i) = v;
@@ -521,7 +738,8 @@ struct DstRotD {
 };
 
 // G: out0 = substitute(ct0) + sum_d D[d] * k0[d], out1 = sum_d D[d] * k1[d]
-// for row (poly, limb) = rows[blockIdx.y]; exact sums reduced once.
+// for row (poly, limb) = rows[blockIdx.y]; exact sums reduced once. Requests
+// whose key switches down write the bare sums (key context) to ks instead.
 __global__ void k_rot_mac(const DevPrime* primes, const RotDesc* d, const uint2* rows, uint32_t logn) {
   const uint2 row = rows[blockIdx.y];
   const RotDesc& r = d[row.x];
@@ -529,10 +747,11 @@ __global__ void k_rot_mac(const DevPrime* primes, const RotDesc* d, const uint2*
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (1u << logn)) return;
   const DevPrime pr = primes[j];
-  const uint64_t plane = (uint64_t)r.L << logn;
-  uint64_t lo0 = r.ct[((uint64_t)j << logn) + gather_index(i, r.e, logn)], hi0 = 0, lo1 = 0, hi1 = 0;
-  for (uint32_t dd = 0; dd < r.L; dd++) {
-    const uint64_t off = ((uint64_t)(dd * r.L + j) << logn) + i;
+  const uint64_t plane = (uint64_t)r.Lk << logn;
+  uint64_t* const o = r.ks ? r.ks : r.out;
+  uint64_t lo0 = r.ks ? 0 : r.ct[((uint64_t)j << logn) + gather_index(i, r.e, logn)], hi0 = 0, lo1 = 0, hi1 = 0;
+  for (uint32_t dd = 0; dd < r.nd; dd++) {
+    const uint64_t off = ((uint64_t)(dd * r.Lk + j) << logn) + i;
     const uint64_t x = r.D[off];
     mac128(hi0, lo0, x, __ldg(r.k0 + off));
     mac128(hi1, lo1, x, __ldg(r.k1 + off));
@@ -543,57 +762,170 @@ __global__ void k_rot_mac(const DevPrime* primes, const RotDesc* d, const uint2*
       hi1 = 0;
     }
   }
-  r.out[((uint64_t)j << logn) + i] = reduce128(hi0, lo0, pr);
-  r.out[plane + ((uint64_t)j << logn) + i] = reduce128(hi1, lo1, pr);
+  o[((uint64_t)j << logn) + i] = reduce128(hi0, lo0, pr);
+  o[plane + ((uint64_t)j << logn) + i] = reduce128(hi1, lo1, pr);
 }
+
+// Switch-down of the requests whose key lies below their level
+// (galois_key.rs:113-120): part `aux` of request `poly`, limb `limb`, of the
+// key-context sums (inverse NTT in place) and of the switched-down result
+// (forward NTT in place).
+struct RotKs {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t* at(const NttJob& j, uint32_t i) const {
+    const RotDesc& r = d[j.poly];
+    return r.ks + ((uint64_t)(j.aux * r.Lk + j.limb) << logn) + i;
+  }
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    return *at(j, i);
+  }
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    *at(j, i) = v;
+  }
+  __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const { return *at(j, i); }
+};
+
+struct RotSd {
+  const RotDesc* d;
+  uint32_t logn;
+  __device__ __forceinline__ uint64_t* at(const NttJob& j, uint32_t i) const {
+    const RotDesc& r = d[j.poly];
+    return r.sd + ((uint64_t)(j.aux * r.L + j.limb) << logn) + i;
+  }
+  __device__ __forceinline__ uint64_t operator()(const NttJob& j, const DevPrime&, uint32_t i) const {
+    return *at(j, i);
+  }
+  __device__ __forceinline__ void operator()(const NttJob& j, const DevPrime&, uint32_t i, uint64_t v) const {
+    *at(j, i) = v;
+  }
+  __device__ __forceinline__ uint64_t reload(const NttJob& j, uint32_t i) const { return *at(j, i); }
+};
+
+// The switch-down chain of part jobs[blockIdx.y] = (request, part): its Lk
+// power-basis residues of each coefficient down to L (moduli are a prefix of
+// one chain, so limb k of every request uses primes[k]).
+template <int MAXK>
+__global__ void k_rot_chain(const DevPrime* primes, const RotDesc* d, const uint2* jobs, uint32_t logn) {
+  const uint2 job = jobs[blockIdx.y];
+  const RotDesc& r = d[job.x];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (1u << logn)) return;
+  const uint64_t* in = r.ks + ((uint64_t)(job.y * r.Lk) << logn) + i;
+  uint64_t* out = r.sd + ((uint64_t)(job.y * r.L) << logn) + i;
+  uint64_t x[MAXK];
+#pragma unroll
+  for (int k = 0; k < MAXK; k++)
+    if ((uint32_t)k < r.Lk) x[k] = in[(uint64_t)k << logn];
+  chain_coeff<MAXK>(x, primes, r.chain, r.Lk, r.L);
+#pragma unroll
+  for (int k = 0; k < MAXK; k++)
+    if ((uint32_t)k < r.L) out[(uint64_t)k << logn] = x[k];
+}
+
+// Last step of those requests: out0 = sd0 + substitute(ct0), out1 = sd1, for
+// row rows[blockIdx.y] = (request, part * L + limb).
+__global__ void k_rot_add(const DevPrime* primes, const RotDesc* d, const uint2* rows, uint32_t logn) {
+  const uint2 row = rows[blockIdx.y];
+  const RotDesc& r = d[row.x];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (1u << logn)) return;
+  const uint32_t part = row.y >= r.L ? 1 : 0, j = row.y - part * r.L;
+  const uint64_t at = ((uint64_t)row.y << logn) + i;
+  uint64_t v = r.sd[at];
+  if (part == 0) v = add_mod(v, r.ct[((uint64_t)j << logn) + gather_index(i, r.e, logn)], primes[j].p);
+  r.out[at] = v;
+}
+
+namespace {
+// Scratch words and table entries of a ragged batch.
+struct RotCounts {
+  size_t digit_words = 0, d_words = 0, ks_words = 0, sd_words = 0;
+  size_t n_r1 = 0, n_f = 0, n_inv = 0, n_fwd = 0, n_rows = 0, n_chain = 0, n_add = 0;
+  uint32_t max_lk = 0;
+  size_t table_words(size_t count) const {
+    return (count * sizeof(RotDesc) + (n_r1 + n_f + n_inv + n_fwd) * sizeof(uint4) +
+            (n_rows + n_chain + n_add) * sizeof(uint2)) / 8 + 8;
+  }
+};
+
+RotCounts rot_counts(const RotRequest* req, size_t count) {
+  RotCounts c;
+  for (size_t b = 0; b < count; b++) {
+    const Ksk& k = *req[b].key;
+    const size_t L = k.ctx_ct->L(), Lk = k.ctx_ksk->L(), N = k.ctx_ct->N(), nd = k.count;
+    c.digit_words += L * N;
+    c.d_words += nd * Lk * N;
+    c.n_r1 += L;
+    c.n_f += nd * Lk;
+    c.n_rows += Lk;
+    if (k.switches_down()) {
+      c.ks_words += 2 * Lk * N;
+      c.sd_words += 2 * L * N;
+      c.n_inv += 2 * Lk;
+      c.n_fwd += 2 * L;
+      c.n_chain += 2;
+      c.n_add += 2 * L;
+      c.max_lk = std::max(c.max_lk, (uint32_t)Lk);
+    }
+  }
+  return c;
+}
+}  // namespace
 
 size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count) {
-  size_t words = 0, n_r1 = 0, n_f = 0;
-  for (size_t b = 0; b < count; b++) {
-    const size_t L = req[b].key->ctx_ct->L(), N = req[b].key->ctx_ct->N();
-    words += L * N + L * L * N;
-    n_r1 += L;
-    n_f += L * L;
-  }
-  const size_t table_words = (count * sizeof(RotDesc) + (n_r1 + n_f) * sizeof(uint4) + n_r1 * sizeof(uint2)) / 8 + 8;
-  return (words + table_words + 128 + 3 * 32) * 8;
+  const RotCounts c = rot_counts(req, count);
+  return (c.digit_words + c.d_words + c.ks_words + c.sd_words + c.table_words(count) + 128 + 6 * 32) * 8;
 }
 
-void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
-                              cudaStream_t st) {
-  if (count == 0) return;
-  const Context& top = *par.ctx(0);
-  const size_t N = top.N();
-  const uint32_t logn = top.logn;
-  // Scratch and tables.
-  size_t digit_words = 0, d_words = 0, n_r1 = 0, n_f = 0;
+void validate_rot_requests(const Params& par, const RotRequest* req, size_t count) {
+  const size_t N = par.degree;
   for (size_t b = 0; b < count; b++) {
     const Ksk& k = *req[b].key;
     if (k.par != &par) throw Error(FHEG_ERR_KEY_MISMATCH, "all keys of a batch must share the parameters");
-    require_same_level_key(k);
     if ((req[b].exponent % (2 * N)) % 2 == 0)
       throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
-    const size_t L = k.ctx_ct->L();
-    digit_words += L * N;
-    d_words += L * L * N;
-    n_r1 += L;
-    n_f += L * L;
+    if (k.switches_down() && k.ctx_ksk->L() > 32)
+      throw Error(FHEG_ERR_UNSUPPORTED, "batched rotations switch down from key contexts of at most 32 moduli");
   }
+}
+
+// The device tables and scratch of one ragged batch, ready to launch.
+struct RotBatchPlan {
+  const Params* par = nullptr;
+  RotCounts cnt;
+  const RotDesc* d_desc = nullptr;
+  const uint4* d_jobs = nullptr;
+  const uint2* d_rows = nullptr;
+};
+
+static void launch_rot_batch(const RotBatchPlan& pl, cudaStream_t st);
+
+// Builds the batch's tables in `ws` (scratch included) and uploads them on
+// `st`; the copies from host memory complete before this returns.
+static RotBatchPlan prepare_rot_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
+                                     cudaStream_t st) {
+  validate_rot_requests(par, req, count);
+  const size_t N = par.ctx(0)->N();
+  // Scratch and tables.
+  const RotCounts cnt = rot_counts(req, count);
+  const size_t table_words = cnt.table_words(count);
+  ws.reserve((cnt.digit_words + cnt.d_words + cnt.ks_words + cnt.sd_words + table_words + 128 + 6 * 32) * 8);
+  size_t off = 0;
+  uint64_t* digits = ws.take(cnt.digit_words, &off);
+  uint64_t* D = ws.take(cnt.d_words, &off);
+  uint64_t* KS = ws.take(cnt.ks_words, &off);
+  uint64_t* SD = ws.take(cnt.sd_words, &off);
+  uint64_t* tables = ws.take(table_words, &off);
   std::vector<RotDesc> desc(count);
   std::vector<uint4> jobs;
-  jobs.reserve(n_r1 + n_f);
+  jobs.reserve(cnt.n_r1 + cnt.n_f + cnt.n_inv + cnt.n_fwd);
   std::vector<uint2> rows;
-  rows.reserve(n_r1);
-  const size_t table_words = (count * sizeof(RotDesc) + (n_r1 + n_f) * sizeof(uint4) + n_r1 * sizeof(uint2)) / 8 + 8;
-  ws.reserve((digit_words + d_words + table_words + 128) * 8);
-  size_t off = 0;
-  uint64_t* digits = ws.take(digit_words, &off);
-  uint64_t* D = ws.take(d_words, &off);
-  uint64_t* tables = ws.take(table_words, &off);
-  size_t dpos = 0, Dpos = 0;
+  rows.reserve(cnt.n_rows + cnt.n_chain + cnt.n_add);
+  size_t dpos = 0, Dpos = 0, kpos = 0, spos = 0;
   for (size_t b = 0; b < count; b++) {
     const Ksk& k = *req[b].key;
-    const uint32_t L = (uint32_t)k.ctx_ct->L();
+    const uint32_t L = (uint32_t)k.ctx_ct->L(), Lk = (uint32_t)k.ctx_ksk->L();
     RotDesc& r = desc[b];
     r.ct = req[b].ct;
     r.out = req[b].out;
@@ -601,36 +933,108 @@ void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t c
     r.D = D + Dpos;
     r.k0 = k.values(0);
     r.k1 = k.values(1);
+    r.ks = r.sd = nullptr;
+    r.chain = nullptr;
+    if (k.switches_down()) {
+      r.ks = KS + kpos;
+      r.sd = SD + spos;
+      r.chain = k.chain.u64();
+      kpos += (size_t)2 * Lk * N;
+      spos += (size_t)2 * L * N;
+    }
     r.e = req[b].exponent % (2 * N);
     r.L = L;
-    r.pad = 0;
+    r.Lk = Lk;
+    r.nd = (uint32_t)k.count;
+    r.log_base = k.log_base;
     dpos += (size_t)L * N;
-    Dpos += (size_t)L * L * N;
+    Dpos += (size_t)r.nd * Lk * N;
     for (uint32_t i = 0; i < L; i++) jobs.push_back(make_uint4((uint32_t)b, i, 0, 0));
   }
   for (size_t b = 0; b < count; b++)
-    for (uint32_t dd = 0; dd < desc[b].L; dd++)
-      for (uint32_t j = 0; j < desc[b].L; j++) jobs.push_back(make_uint4((uint32_t)b, j, dd, 0));
+    for (uint32_t dd = 0; dd < desc[b].nd; dd++)
+      for (uint32_t j = 0; j < desc[b].Lk; j++) jobs.push_back(make_uint4((uint32_t)b, j, dd, 0));
   for (size_t b = 0; b < count; b++)
-    for (uint32_t j = 0; j < desc[b].L; j++) rows.push_back(make_uint2((uint32_t)b, j));
+    if (desc[b].ks)
+      for (uint32_t part = 0; part < 2; part++)
+        for (uint32_t j = 0; j < desc[b].Lk; j++) jobs.push_back(make_uint4((uint32_t)b, j, part, 0));
+  for (size_t b = 0; b < count; b++)
+    if (desc[b].ks)
+      for (uint32_t part = 0; part < 2; part++)
+        for (uint32_t j = 0; j < desc[b].L; j++) jobs.push_back(make_uint4((uint32_t)b, j, part, 0));
+  for (size_t b = 0; b < count; b++)
+    for (uint32_t j = 0; j < desc[b].Lk; j++) rows.push_back(make_uint2((uint32_t)b, j));
+  for (size_t b = 0; b < count; b++)
+    if (desc[b].ks)
+      for (uint32_t part = 0; part < 2; part++) rows.push_back(make_uint2((uint32_t)b, part));
+  for (size_t b = 0; b < count; b++)
+    if (desc[b].ks)
+      for (uint32_t j = 0; j < 2 * desc[b].L; j++) rows.push_back(make_uint2((uint32_t)b, j));
   // Upload the tables (pageable source: the copy completes before return).
-  uint8_t* tb = reinterpret_cast<uint8_t*>(tables);
+  uint8_t* tb = reinterpret_cast<uint8_t*>(tables);  // 256-byte aligned (Workspace::take)
   RotDesc* d_desc = reinterpret_cast<RotDesc*>(tb);
   uint4* d_jobs = reinterpret_cast<uint4*>(tb + count * sizeof(RotDesc));
   uint2* d_rows = reinterpret_cast<uint2*>(tb + count * sizeof(RotDesc) + jobs.size() * sizeof(uint4));
   check_cuda(cudaMemcpyAsync(d_desc, desc.data(), count * sizeof(RotDesc), cudaMemcpyHostToDevice, st), "H2D");
   check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(uint4), cudaMemcpyHostToDevice, st), "H2D");
   check_cuda(cudaMemcpyAsync(d_rows, rows.data(), rows.size() * sizeof(uint2), cudaMemcpyHostToDevice, st), "H2D");
+  RotBatchPlan pl;
+  pl.par = &par;
+  pl.cnt = cnt;
+  pl.d_desc = d_desc;
+  pl.d_jobs = d_jobs;
+  pl.d_rows = d_rows;
+  return pl;
+}
+
+// The launches of a prepared batch (capturable: no host memory is read).
+static void launch_rot_batch(const RotBatchPlan& pl, cudaStream_t st) {
+  const Context& top = *pl.par->ctx(0);
+  const size_t N = top.N();
+  const uint32_t logn = top.logn;
+  const RotCounts& cnt = pl.cnt;
+  const RotDesc* d_desc = pl.d_desc;
+  const uint4* d_jobs = pl.d_jobs;
+  const uint2* d_rows = pl.d_rows;
   // R1: substituted c1 into the power basis.
   NttGeom g1{top.primes_dev(), 1, 0, d_jobs};
-  ntt_inverse_any(logn, g1, n_r1, SrcRotSubst{d_desc, logn}, DstRotDigits{d_desc, logn}, st);
+  ntt_inverse_any(logn, g1, cnt.n_r1, SrcRotSubst{d_desc, logn}, DstRotDigits{d_desc, logn}, st);
   // F: every digit in every key limb.
-  NttGeom g2{top.primes_dev(), 1, 0, d_jobs + n_r1};
-  ntt_forward_any<true>(logn, g2, n_f, SrcRotDigit{d_desc, logn}, DstRotD{d_desc, logn}, st);
+  NttGeom g2{top.primes_dev(), 1, 0, d_jobs + cnt.n_r1};
+  ntt_forward_any<true>(logn, g2, cnt.n_f, SrcRotDigit{d_desc, logn}, DstRotD{d_desc, logn}, st);
   // G: inner products and the substituted c0.
-  dim3 grid((unsigned)((N + 255) / 256), (unsigned)rows.size());
-  k_rot_mac<<<grid, 256, 0, st>>>(top.primes_dev(), d_desc, d_rows, logn);
+  const unsigned gx = (unsigned)((N + 255) / 256);
+  k_rot_mac<<<dim3(gx, (unsigned)cnt.n_rows), 256, 0, st>>>(top.primes_dev(), d_desc, d_rows, logn);
   after_launch("k_rot_mac");
+  if (cnt.n_chain == 0) return;
+  // Requests with keys below their level: the sums into the power basis, down
+  // to the ciphertext context, back to Ntt, plus the substituted c0.
+  NttGeom g3{top.primes_dev(), 1, 0, d_jobs + cnt.n_r1 + cnt.n_f};
+  ntt_inverse_any(logn, g3, cnt.n_inv, RotKs{d_desc, logn}, RotKs{d_desc, logn}, st);
+  const uint2* d_chain = d_rows + cnt.n_rows;
+  const dim3 gc(gx, (unsigned)cnt.n_chain);
+  if (cnt.max_lk <= 8) k_rot_chain<8><<<gc, 256, 0, st>>>(top.primes_dev(), d_desc, d_chain, logn);
+  else if (cnt.max_lk <= 16) k_rot_chain<16><<<gc, 256, 0, st>>>(top.primes_dev(), d_desc, d_chain, logn);
+  else k_rot_chain<32><<<gc, 256, 0, st>>>(top.primes_dev(), d_desc, d_chain, logn);
+  after_launch("k_rot_chain");
+  NttGeom g4{top.primes_dev(), 1, 0, d_jobs + cnt.n_r1 + cnt.n_f + cnt.n_inv};
+  ntt_forward_any<true>(logn, g4, cnt.n_fwd, RotSd{d_desc, logn}, RotSd{d_desc, logn}, st);
+  k_rot_add<<<dim3(gx, (unsigned)cnt.n_add), 256, 0, st>>>(top.primes_dev(), d_desc, d_chain + cnt.n_chain, logn);
+  after_launch("k_rot_add");
+}
+
+void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
+                              cudaStream_t st) {
+  if (count == 0) return;
+  launch_rot_batch(prepare_rot_batch(par, req, count, ws, st), st);
+}
+
+std::function<void(cudaStream_t)> prepare_galois_batch(const Params& par, const RotRequest* req, size_t count,
+                                                       Workspace& ws, cudaStream_t st) {
+  if (count == 0) return [](cudaStream_t) {};
+  const RotBatchPlan pl = prepare_rot_batch(par, req, count, ws, st);
+  check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return [pl](cudaStream_t s) { launch_rot_batch(pl, s); };
 }
 
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
@@ -683,7 +1087,6 @@ std::unique_ptr<Multiplicator> make_default_multiplicator(const Ksk& rk) {
   }
   BigUint one(1), t(par.plaintext);
   auto m = make_multiplicator(par, rk.ciphertext_level, one, one, one, one, ext, t, ctx.rns->product);
-  require_same_level_key(rk);
   m->rk = &rk;
   return m;
 }
@@ -691,8 +1094,11 @@ std::unique_ptr<Multiplicator> make_default_multiplicator(const Ksk& rk) {
 size_t Multiplicator::scratch_bytes(uint64_t count) const {
   const size_t L = base->L(), M = mul->L(), N = base->N();
   const size_t Lk = rk ? rk->ctx_ksk->L() : 0;
-  const size_t words = count * 4 * L * N + count * 4 * M * N + count * 3 * M * N + count * 3 * L * N +
-                       (rk ? count * L * Lk * N : 0) + (mod_switch ? count * out_parts() * L * N : 0) + 6 * 32;
+  const bool down = rk && rk->switches_down();
+  const size_t d_words = !rk ? 0 : rk->log_base ? key_switch_scratch_words(*rk, count) : count * L * Lk * N;
+  const size_t words = count * 4 * L * N + count * 4 * M * N + count * 3 * M * N + count * 3 * L * N + d_words +
+                       (mod_switch ? count * out_parts() * L * N : 0) +
+                       (down ? count * 2 * Lk * N + count * 2 * L * N : 0) + 8 * 32;
   return words * 8;
 }
 
@@ -711,9 +1117,15 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   const size_t parts = out_parts();
   const size_t Lk = rk ? rk->ctx_ksk->L() : 0;
   // Workspace layout (words).
+  const bool ks_down = rk && rk->switches_down();
+  // Decomposition keys (single-modulus contexts) take the generic key switch
+  // on c2 in the power basis.
+  const bool ks_decomp = rk && rk->log_base;
   const size_t w_pb = count * 4 * L * N, w_ext = count * 4 * M * N, w_prod = count * 3 * M * N,
-               w_down = count * 3 * L * N, w_d = rk ? count * L * Lk * N : 0,
-               w_tmp = mod_switch ? count * parts * L * N : 0;
+               w_down = count * 3 * L * N,
+               w_d = !rk ? 0 : ks_decomp ? key_switch_scratch_words(*rk, count) : count * L * Lk * N,
+               w_tmp = mod_switch ? count * parts * L * N : 0, w_ks = ks_down ? count * 2 * Lk * N : 0,
+               w_sd = ks_down ? count * 2 * L * N : 0;
   ws.reserve(scratch_bytes(count));
   size_t off = 0;
   uint64_t* pb = ws.take(w_pb, &off);
@@ -722,6 +1134,8 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   uint64_t* dn = ws.take(w_down, &off);
   uint64_t* D = ws.take(w_d, &off);
   uint64_t* tmp = ws.take(w_tmp, &off);
+  uint64_t* ks = ws.take(w_ks, &off);
+  uint64_t* sd = ws.take(w_sd, &off);
   uint64_t* dest = mod_switch ? tmp : out;
 
   // Stage plans: the small-batch plan when it applies.
@@ -822,7 +1236,7 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
   // pass), and c2 is expanded there into the digit rows of every key modulus
   // (written to D), so F runs only its block passes.
   const uint32_t bf = plan_f ? plan_f : ntt_block_logn(logn);
-  const bool fuse_f = rk && top_d && bf < logn && logn - bf == top_d;
+  const bool fuse_f = rk && !ks_decomp && top_d && bf < logn && logn - bf == top_d;
   ForwardTop fwd_e{top_d, bc.primes_dev()};
   if (fuse_f) {
     fwd_e.period = 3;
@@ -843,10 +1257,14 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
     PolyRef c01 = sub_ref(dn, L, logn, 3, 0, 2);
     PolyRef oref = plain_ref(dest, L, logn);
     NttGeom gk{kc.primes_dev(), (uint32_t)Lk, 0};
-    if (fuse_f) {
+    if (ks_decomp) {
+      // mul.rs:196-210 with key_switching_key.rs:292-329: c0, c1 into Ntt;
+      // G below adds the decomposed key switch of c2.
+      ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st, bf);
+    } else if (fuse_f) {
       ntt_forward_after_top<true>(logn, gk, count * L, DstPoly{dref}, st, bf);
       ntt_forward_after_top<true>(logn, gb, 2 * count, DstPoly{c01}, DstPoly{oref}, st, bf);
-    } else if (bf >= logn && !f_split) {
+    } else if (bf >= logn && !f_split && !ks_down) {
       // F: digit NTTs and the c0 / c1 NTTs in one launch (Lk == L).
       const uint32_t ndp = (uint32_t)(count * L);
       ntt_fwd_single<true>(logn, gk, count * L + 2 * count, SrcKsF{c2, c01, (uint32_t)L, ndp},
@@ -857,9 +1275,21 @@ void Multiplicator::multiply(const uint64_t* lhs, const uint64_t* rhs, uint64_t*
       ntt_forward_any<true>(logn, gb, 2 * count, SrcPoly{c01}, DstPoly{oref}, st, bf);
     }
     mark(6);
-    // G: key inner product added to c0, c1 in place.
-    launch_key_mac(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest, 2 * L * N, 0, dest + L * N,
-                   2 * L * N, dest, 2 * L * N, (uint32_t)L, (uint32_t)Lk, logn, count, st);
+    if (ks_decomp) {
+      // G: digit NTTs and the key inner product, added to c0, c1 in place.
+      key_switch(*rk, c2, count, dest, 2 * L * N, 0, dest + L * N, 2 * L * N, dest, 2 * L * N, D, st);
+    } else if (!ks_down) {
+      // G: key inner product added to c0, c1 in place.
+      launch_key_mac(bc.primes_dev(), dref, rk->values(0), rk->values(1), dest, 2 * L * N, 0, dest + L * N,
+                     2 * L * N, dest, 2 * L * N, (uint32_t)L, (uint32_t)Lk, logn, count, st);
+    } else {
+      // G with a key below the multiplication level (mul.rs:199-206): the
+      // inner product in the key context, switched down to the ciphertext
+      // context and added to c0, c1.
+      launch_key_mac(kc.primes_dev(), dref, rk->values(0), rk->values(1), nullptr, 0, 0, nullptr, 0, ks, 2 * Lk * N,
+                     (uint32_t)L, (uint32_t)Lk, logn, count, st);
+      finish_switch_down(*rk, ks, sd, count, dest, 2 * L * N, 0, dest + L * N, 2 * L * N, dest, 2 * L * N, st);
+    }
   } else {
     PolyRef o = plain_ref(dest, L, logn);
     ntt_forward_any<true>(logn, gb, 3 * count, SrcPoly{dnref}, DstPoly{o}, st);

@@ -54,6 +54,11 @@ bool ntt_prefetch_enabled();
 void set_ntt_prefetch(bool on);
 // The valid block sizes for 2^logn, ascending.
 std::vector<uint32_t> ntt_plans(uint32_t logn);
+// Whether two-pass plans with 2^12-residue blocks run instead as one pass on
+// clusters of 2^(logn - 12) CTAs exchanging through distributed shared
+// memory (fheg_ntt_cluster_set).
+bool ntt_cluster_enabled(uint32_t logn);
+void set_ntt_cluster(uint32_t logn, bool on);
 
 inline void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw Error(10 /*FHEG_ERR_CUDA*/, std::string(what) + ": " + cudaGetErrorString(e));

@@ -1,4 +1,5 @@
-// CUDA graphs of the batched multiplication: the whole pipeline of
+// CUDA graphs of the batched multiplication and of the ragged rotation batch.
+// The multiplication: the whole pipeline of
 // Multiplicator::multiply for fixed device buffers recorded once and replayed
 // with one launch call. A batch of 32 pairs or more is recorded as two
 // branches of half the batch, each with its own scratch: running them side by
@@ -29,6 +30,21 @@ namespace {
 int fail(const fheg::Error& e) {
   fheg::set_last_error(e.what());
   return e.code;
+}
+
+// Kernel nodes of a graph (counted into the launch counter per replay).
+uint64_t kernel_nodes(cudaGraph_t graph) {
+  size_t n = 0;
+  fheg::check_cuda(cudaGraphGetNodes(graph, nullptr, &n), "cudaGraphGetNodes");
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n) fheg::check_cuda(cudaGraphGetNodes(graph, nodes.data(), &n), "cudaGraphGetNodes");
+  uint64_t k = 0;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType t;
+    fheg::check_cuda(cudaGraphNodeGetType(node, &t), "cudaGraphNodeGetType");
+    if (t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
 }
 
 }  // namespace
@@ -88,15 +104,76 @@ FHEG_API int fheg_multiplicator_capture(fheg_multiplicator* m, const uint64_t* d
     }
     fheg::check_cuda(cudaStreamEndCapture(st, &g->graph), "cudaStreamEndCapture");
     fheg::check_cuda(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
-    size_t n = 0;
-    fheg::check_cuda(cudaGraphGetNodes(g->graph, nullptr, &n), "cudaGraphGetNodes");
-    std::vector<cudaGraphNode_t> nodes(n);
-    if (n) fheg::check_cuda(cudaGraphGetNodes(g->graph, nodes.data(), &n), "cudaGraphGetNodes");
-    for (cudaGraphNode_t node : nodes) {
-      cudaGraphNodeType t;
-      fheg::check_cuda(cudaGraphNodeGetType(node, &t), "cudaGraphNodeGetType");
-      if (t == cudaGraphNodeTypeKernel) g->kernels++;
+    g->kernels = kernel_nodes(g->graph);
+    release();
+    *out = g;
+    return FHEG_OK;
+  } catch (const fheg::Error& e) {
+    release();
+    delete g;
+    return fail(e);
+  } catch (const std::exception& e) {
+    release();
+    delete g;
+    return fail(fheg::Error(FHEG_ERR_INTERNAL, e.what()));
+  }
+}
+
+FHEG_API int fheg_galois_relinearize_batch_capture(const fheg_params* par, const fheg_ksk* const* keys,
+                                                   const size_t* exponents, const uint64_t* const* d_cts,
+                                                   uint64_t* const* d_outs, size_t count, fheg_graph** out) {
+  fheg::set_last_error("");
+  if (!par || !out || !count || !keys || !exponents || !d_cts || !d_outs)
+    return fail(fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "null input"));
+  cudaStream_t st = nullptr, st2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  auto release = [&] {
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (st2) cudaStreamDestroy(st2);
+    if (st) cudaStreamDestroy(st);
+  };
+  auto g = new fheg_graph();
+  try {
+    std::vector<fheg::RotRequest> req(count);
+    for (size_t b = 0; b < count; b++) {
+      if (!keys[b] || !d_cts[b] || !d_outs[b] || d_cts[b] == d_outs[b])
+        throw fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "null or aliased batch entry");
+      req[b] = fheg::RotRequest{&keys[b]->k, exponents[b], d_cts[b], d_outs[b]};
     }
+    const fheg::Params& p = *par->p;
+    fheg::validate_rot_requests(p, req.data(), count);
+    fheg::check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    fheg::check_cuda(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
+    fheg::check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    fheg::check_cuda(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
+    // As the direct call: from 16 requests two halves side by side, each
+    // with its tables and scratch in the graph's own workspaces.
+    const size_t c0 = count >= 16 ? count / 2 : count;
+    auto run0 = fheg::prepare_galois_batch(p, req.data(), c0, g->ws, st);
+    auto run1 = fheg::prepare_galois_batch(p, req.data() + c0, count - c0, g->ws2, st);
+    // One ordinary run sets every kernel attribute before the capture.
+    run0(st);
+    run1(st2);
+    fheg::check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    fheg::check_cuda(cudaStreamSynchronize(st2), "cudaStreamSynchronize");
+    fheg::check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    try {
+      fheg::check_cuda(cudaEventRecord(fork, st), "cudaEventRecord");
+      fheg::check_cuda(cudaStreamWaitEvent(st2, fork, 0), "cudaStreamWaitEvent");
+      run0(st);
+      run1(st2);
+      fheg::check_cuda(cudaEventRecord(join, st2), "cudaEventRecord");
+      fheg::check_cuda(cudaStreamWaitEvent(st, join, 0), "cudaStreamWaitEvent");
+    } catch (...) {
+      cudaGraph_t partial = nullptr;
+      cudaStreamEndCapture(st, &partial);
+      if (partial) cudaGraphDestroy(partial);
+      throw;
+    }
+    fheg::check_cuda(cudaStreamEndCapture(st, &g->graph), "cudaStreamEndCapture");
+    fheg::check_cuda(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+    g->kernels = kernel_nodes(g->graph);
     release();
     *out = g;
     return FHEG_OK;

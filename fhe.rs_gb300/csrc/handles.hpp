@@ -68,6 +68,9 @@ struct fheg_secret_key {
 };
 
 // A key-switching key at the given levels with device room for `count`
-// digits; c0 is uploaded from h_c0 unless it is null (api.cu).
+// digits; c0 is uploaded from h_c0 unless it is null (api.cu). log_base < 0:
+// as KeySwitchingKey::new, a single-modulus key context decomposes in base
+// 2^(log2 q / 2) (key_switching_key.rs:70-76); otherwise the base a key
+// message names (0 for RNS digits).
 fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
-                         size_t count);
+                         size_t count, int64_t log_base = -1);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -105,6 +106,11 @@ struct Scaler {
 void ntt_forward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, bool lazy, cudaStream_t st);
 void ntt_backward(const Context& ctx, PolyRef src, PolyRef dst, uint64_t polys, cudaStream_t st);
 void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint64_t polys, cudaStream_t st);
+// Representation::NttShoup (rq/mod.rs:37-47, 209-223): the Shoup plane of
+// Ntt values, and the product of MulAssign<&Poly<NttShoup>> (rq/ops.rs:208-245).
+void poly_compute_shoup(const Context& ctx, PolyRef a, PolyRef out, uint64_t polys, cudaStream_t st);
+void poly_mul_shoup(const Context& ctx, PolyRef a, PolyRef b, PolyRef bs, PolyRef out, uint64_t polys,
+                    cudaStream_t st);
 constexpr size_t kMaxScalarLimbs = 64;
 void poly_scalar_mul(const Context& ctx, const BigUint& scalar, PolyRef in, PolyRef out, uint64_t polys,
                      cudaStream_t st);
@@ -211,17 +217,49 @@ struct Ksk {
   const Params* par = nullptr;
   size_t ciphertext_level = 0, ksk_level = 0;
   std::shared_ptr<Context> ctx_ct, ctx_ksk;
-  size_t count = 0;  // digits = moduli of the ciphertext context
+  size_t count = 0;  // digits: the moduli of the ciphertext context, or the decomposition's digits
+  // Keys of a single-modulus key context decompose the input in base
+  // 2^log_base instead of by residues (key_switching_key.rs:63-89, 292-329);
+  // 0 for RNS-digit keys.
+  uint32_t log_base = 0;
+  // The 32-byte seed c1 was expanded from, when the key was made from one
+  // (key_switching_key.rs:27-28); its message then carries the seed again.
+  std::vector<uint8_t> seed;
   // [2 parts][count][Lk][N] values (canonical, Ntt representation).
   DevBuf keys;
   mutable Workspace ws;  // scratch of relinearize / galois_relinearize
+  // When the key context has more moduli than the ciphertext context (a key
+  // at a lower level), the constants of the switch-downs that bring a key
+  // switch's output from one to the other (rq/mod.rs:455-462 switch_down_to,
+  // one rq/mod.rs:390-448 switch_down per dropped modulus q_m, m = Lk-1 down
+  // to L): per step [q_m, inv[0..m), inv_shoup[0..m), half[0..m)] with
+  // inv[i] = q_m^-1 mod q_i and half[i] = q_i - (floor(q_m / 2) mod q_i).
+  DevBuf chain;
   uint64_t* values(int part) const { return keys.u64() + (size_t)part * count * ctx_ksk->L() * ctx_ksk->N(); }
+  // Whether the key switch ends in the key context and needs the switch-down.
+  bool switches_down() const { return ctx_ksk->L() > ctx_ct->L(); }
 };
+
+// ilog2(next_power_of_two(q)) (key_switching_key.rs:71, 302-308).
+inline uint32_t log_modulus_of(uint64_t q) { return 64 - (uint32_t)__builtin_clzll(q - 1); }
+// Fills k.chain (nothing when the key and ciphertext contexts are equal).
+void ksk_build_switch_chain(Ksk& k);
+// Words of the D scratch key_switch() needs for `batch` polynomials: the
+// digit NTTs and, for keys that switch down, the key context's outputs and
+// their switched-down power basis.
+size_t key_switch_scratch_words(const Ksk& k, uint64_t batch);
+// switch_down_to (rq/mod.rs:455-462) of `polys` power-basis polynomials from
+// the key context of `k` (Lk limbs, `in`) to its ciphertext context (L limbs,
+// `out`), all steps fused per coefficient.
+void switch_down_chain(const Ksk& k, PolyRef in, PolyRef out, uint64_t polys, cudaStream_t st);
 
 
 // Key switch of digits already in the power basis: (out0, out1) =
 // (add0 + sum_i NTT(d_i) * k0_i, add1 + sum_i NTT(d_i) * k1_i) where add0/add1
 // are optional Ntt polynomials (with an optional substitution gather on add0).
+// D holds key_switch_scratch_words(k, batch) words. With a key below the
+// ciphertext level the sums are switched down to the ciphertext context
+// before the additions (out then has the ciphertext context's L limbs).
 void key_switch(const Ksk& k, PolyRef digits, uint64_t batch, const uint64_t* add0, uint64_t add0_poly_stride,
                 uint64_t add0_exponent, const uint64_t* add1, uint64_t add1_poly_stride, uint64_t* out,
                 uint64_t out_poly_stride, uint64_t* D, cudaStream_t st);
@@ -294,9 +332,17 @@ struct RotRequest {
   const uint64_t* ct;
   uint64_t* out;
 };
+// Checks every request of a batch (shared parameters, key levels, odd
+// exponents) and throws before any device work if one is invalid.
+void validate_rot_requests(const Params& par, const RotRequest* req, size_t count);
 void galois_relinearize_batch(const Params& par, const RotRequest* req, size_t count, Workspace& ws,
                               cudaStream_t st);
 size_t galois_batch_scratch_bytes(const RotRequest* req, size_t count);
+// The batch's tables built in `ws` and uploaded (complete on return); the
+// returned call launches the batch on a stream, reading no host memory, so
+// it can be recorded into a CUDA graph. Buffers and keys must outlive it.
+std::function<void(cudaStream_t)> prepare_galois_batch(const Params& par, const RotRequest* req, size_t count,
+                                                       Workspace& ws, cudaStream_t st);
 void ciphertext_switch_down(const Params& par, size_t level, size_t parts, uint64_t* ct, uint64_t* out,
                             uint64_t count, cudaStream_t st);
 

@@ -56,9 +56,21 @@ FHEG_API int fheg_relinearize_noalloc(const fheg_ksk* rk, const uint64_t* d_ct3,
     if (!rk || (count && (!d_ct3 || !d_out))) throw fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "null input");
     const fheg::Ksk& k = rk->k;
     const size_t L = k.ctx_ct->L(), Lk = k.ctx_ksk->L(), N = k.ctx_ct->N();
-    // Two regions, each rounded to 256 bytes: the digits of c2 and their NTTs.
+    // Reject by division first, so that a huge count cannot wrap the size
+    // computation below around to a small value. A key below the ciphertext
+    // level also needs the key context's two output parts and their
+    // switched-down copies.
+    const size_t per_ct =
+        sizeof(uint64_t) * N * (L * (1 + Lk) + (k.switches_down() ? 2 * Lk + 2 * L : 0));
+    if (count > kNoAllocScratchBytes / per_ct)
+      throw fheg::Error(FHEG_ERR_INVALID_ARGUMENT,
+                        "fheg_relinearize_noalloc: " + std::to_string(count) + " ciphertexts need " +
+                            std::to_string(per_ct) + " bytes of scratch each; the fixed scratch holds " +
+                            std::to_string(kNoAllocScratchBytes) + " bytes");
+    // Two regions, each rounded to 256 bytes: the digits of c2, and the key
+    // switch's own scratch (their NTTs, plus the switch-down buffers).
     const size_t digit_words = (count * L * N + 31) & ~(size_t)31;
-    const size_t d_words = (count * L * Lk * N + 31) & ~(size_t)31;
+    const size_t d_words = fheg::key_switch_scratch_words(k, count);
     const size_t need = (digit_words + d_words) * sizeof(uint64_t);
     if (need > kNoAllocScratchBytes)
       throw fheg::Error(FHEG_ERR_INVALID_ARGUMENT,

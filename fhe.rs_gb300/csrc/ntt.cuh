@@ -147,7 +147,18 @@ __device__ __forceinline__ NttJob decode_job(const NttGeom& g) {
 // bits 4-7 and 5-8. Every access pattern of the rounds below (and of the
 // coalesced staging) then maps the 16 threads of a half warp to 16 distinct
 // 8-byte bank pairs, for every supported size.
-__device__ __forceinline__ uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 15) ^ ((i >> 5) & 15); }
+__host__ __device__ __forceinline__ constexpr uint32_t swz(uint32_t i) { return i ^ ((i >> 4) & 15) ^ ((i >> 5) & 15); }
+
+// The swizzle is linear over GF(2): swz(a ^ b) = swz(a) ^ swz(b). Every
+// shared-memory index of the kernels below is the bitwise OR of a part that
+// depends on the thread and a compile-time part with disjoint bits, so an
+// access costs one XOR of the thread's swizzled byte offset with a constant
+// (instead of shifts, masks and XORs per access).
+__device__ __forceinline__ uint64_t& sm_at(uint64_t* sm, uint32_t off8) {
+  return *reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sm) + off8);
+}
+// Byte offset of the swizzled word index i.
+__host__ __device__ __forceinline__ constexpr uint32_t swz8(uint32_t i) { return swz(i) << 3; }
 
 // Residues per thread: 16 (radix-16 rounds) in blocks of 2^12 to 2^14, 32
 // (radix-32 rounds) in smaller blocks. With 32 residues the 2^12-2^14 kernels
@@ -200,9 +211,11 @@ __device__ __forceinline__ void fwd_round(uint64_t* x, uint32_t tid, const DevPr
   }
 }
 
-// Index of element (q, t) of a forward round.
+// Index of element (q, t) of a forward round. Since tid < T (a power of
+// two), g = tid | q*T and the result is fwd_index(tid, 0, 0) | fwd_index(0,
+// q, t) with disjoint bits.
 template <int LOGN, int S0, int K>
-__device__ __forceinline__ uint32_t fwd_index(uint32_t tid, int q, int t) {
+__host__ __device__ __forceinline__ constexpr uint32_t fwd_index(uint32_t tid, int q, int t) {
   constexpr int T = NttShape<LOGN>::T;
   constexpr int LMIN_LOG = LOGN - S0 - K;
   const uint32_t g = tid + q * T;
@@ -214,15 +227,17 @@ __device__ __forceinline__ uint32_t fwd_index(uint32_t tid, int q, int t) {
 template <int LOGN, int S0, int K>
 __device__ __forceinline__ void fwd_to_smem(const uint64_t* x, uint64_t* sm, uint32_t tid) {
   constexpr int E = NttShape<LOGN>::E;
+  const uint32_t base = swz8(fwd_index<LOGN, S0, K>(tid, 0, 0));
 #pragma unroll
-  for (int e = 0; e < E; e++) sm[swz(fwd_index<LOGN, S0, K>(tid, e >> K, e & ((1 << K) - 1)))] = x[e];
+  for (int e = 0; e < E; e++) sm_at(sm, base ^ swz8(fwd_index<LOGN, S0, K>(0, e >> K, e & ((1 << K) - 1)))) = x[e];
 }
 
 template <int LOGN, int S0, int K>
-__device__ __forceinline__ void fwd_from_smem(uint64_t* x, const uint64_t* sm, uint32_t tid) {
+__device__ __forceinline__ void fwd_from_smem(uint64_t* x, uint64_t* sm, uint32_t tid) {
   constexpr int E = NttShape<LOGN>::E;
+  const uint32_t base = swz8(fwd_index<LOGN, S0, K>(tid, 0, 0));
 #pragma unroll
-  for (int e = 0; e < E; e++) x[e] = sm[swz(fwd_index<LOGN, S0, K>(tid, e >> K, e & ((1 << K) - 1)))];
+  for (int e = 0; e < E; e++) x[e] = sm_at(sm, base ^ swz8(fwd_index<LOGN, S0, K>(0, e >> K, e & ((1 << K) - 1))));
 }
 
 // Applies forward rounds S0, S0+LOGE, ... up to LOGN, exchanging through smem.
@@ -265,10 +280,11 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
 #pragma unroll
   for (int e = 0; e < E; e++) x[e] = src(jb, pr, base + tid + e * T);
   fwd_rounds<LOGN, 0>(x, sm, tid, pr, (1u << g.s1) + jb.beta);
+  const uint32_t sb = swz8(tid);
 #pragma unroll
   for (int e = 0; e < E; e++) {
     const uint32_t i = tid + e * T;
-    uint64_t v = sm[swz(i)];
+    uint64_t v = sm_at(sm, sb ^ swz8(e * T));
     if (REDUCE) v = reduce4(v, pr.p, pr.p2);
     dst(jb, pr, base + i, v);
   }
@@ -278,7 +294,7 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
 // Inverse rounds: global GS stages with half-size l = 2^(U0+r), r < K.
 // Group g = c * 2^U0 + b holds elements c * 2^(U0+K) + b + t * 2^U0.
 template <int LOGN, int U0, int K>
-__device__ __forceinline__ uint32_t inv_index(uint32_t tid, int q, int t) {
+__host__ __device__ __forceinline__ constexpr uint32_t inv_index(uint32_t tid, int q, int t) {
   constexpr int T = NttShape<LOGN>::T;
   const uint32_t g = tid + q * T;
   const uint32_t c = g >> U0;
@@ -313,18 +329,21 @@ __device__ __forceinline__ void inv_round(uint64_t* x, uint32_t tid, const DevPr
   }
 }
 
+// As fwd_index: inv_index(tid, q, t) = inv_index(tid, 0, 0) | inv_index(0, q, t).
 template <int LOGN, int U0, int K>
 __device__ __forceinline__ void inv_to_smem(const uint64_t* x, uint64_t* sm, uint32_t tid) {
   constexpr int E = NttShape<LOGN>::E;
+  const uint32_t base = swz8(inv_index<LOGN, U0, K>(tid, 0, 0));
 #pragma unroll
-  for (int e = 0; e < E; e++) sm[swz(inv_index<LOGN, U0, K>(tid, e >> K, e & ((1 << K) - 1)))] = x[e];
+  for (int e = 0; e < E; e++) sm_at(sm, base ^ swz8(inv_index<LOGN, U0, K>(0, e >> K, e & ((1 << K) - 1)))) = x[e];
 }
 
 template <int LOGN, int U0, int K>
-__device__ __forceinline__ void inv_from_smem(uint64_t* x, const uint64_t* sm, uint32_t tid) {
+__device__ __forceinline__ void inv_from_smem(uint64_t* x, uint64_t* sm, uint32_t tid) {
   constexpr int E = NttShape<LOGN>::E;
+  const uint32_t base = swz8(inv_index<LOGN, U0, K>(tid, 0, 0));
 #pragma unroll
-  for (int e = 0; e < E; e++) x[e] = sm[swz(inv_index<LOGN, U0, K>(tid, e >> K, e & ((1 << K) - 1)))];
+  for (int e = 0; e < E; e++) x[e] = sm_at(sm, base ^ swz8(inv_index<LOGN, U0, K>(0, e >> K, e & ((1 << K) - 1))));
 }
 
 // Size of the first inverse round: the remainder, so that later rounds are
@@ -368,15 +387,16 @@ __global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
   // Coalesced loads, then regroup through shared memory for the first round.
   // (Staging a single row the same way measured slower: the extra shared-
   // memory round trip costs more than the load latency it hides.)
+  const uint32_t sb = swz8(tid);
   if constexpr (src_is_staged<Src>(0)) {
     src.template stage<LOGN, T, E>(jb, pr, base, sm, tid, x);
 #pragma unroll
-    for (int e = 0; e < E; e++) sm[swz(tid + e * T)] = x[e];
+    for (int e = 0; e < E; e++) sm_at(sm, sb ^ swz8(e * T)) = x[e];
   } else {
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const uint32_t i = tid + e * T;
-      sm[swz(i)] = src(jb, pr, base + i);
+      sm_at(sm, sb ^ swz8(e * T)) = src(jb, pr, base + i);
     }
   }
   __syncthreads();
@@ -535,6 +555,164 @@ __global__ void __launch_bounds__(256) k_ntt_inv_top(NttGeom g, uint32_t logb, u
 }
 
 // ---------------------------------------------------------------------------
+// Single-pass transforms of 2^(12 + s1) residues (s1 = 1..4) on a cluster of
+// 2^s1 CTAs: CTA r of the cluster holds block r (2^12 residues) in its shared
+// memory, and the strided stages (the first s1 forward / last s1 inverse)
+// exchange through distributed shared memory instead of a second pass over
+// HBM. Every thread of every CTA reaches both cluster barriers, which are
+// hardware barriers among co-scheduled CTAs.
+
+// Shared::cluster address of word offset `off8` (bytes) of CTA `rank`'s
+// dynamic shared memory.
+__device__ __forceinline__ uint32_t cluster_addr(uint64_t* sm, uint32_t rank, uint32_t off8) {
+  uint32_t out;
+  const uint32_t local = (uint32_t)__cvta_generic_to_shared(sm) + off8;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(local), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ void st_cluster(uint32_t addr, uint64_t v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_cluster(uint32_t addr) {
+  uint64_t v;
+  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
+  return v;
+}
+// All threads of all CTAs of the cluster; orders the shared-memory writes
+// before it with the reads after it, across the cluster.
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// The two halves of a barrier that only establishes that every CTA of the
+// cluster has started (before the first write into a peer's shared memory).
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+
+// Forward phase 1: the first S1 stages on the groups b + t 2^LOGB (t < 2^S1)
+// with b in this CTA's share of [0, 2^LOGB); element b + t 2^LOGB lands at
+// local index b of CTA t.
+template <int LOGB, int S1, class Src>
+__device__ __forceinline__ void fwd_cluster_top(const Src& src, const NttJob& jb, const DevPrime& pr, uint64_t* sm,
+                                                uint32_t tid, uint32_t rank) {
+  constexpr int E = NttShape<LOGB>::E, T = NttShape<LOGB>::T, C = 1 << S1, GPT = E / C;
+  constexpr uint32_t NB = 1u << LOGB;
+  static_assert(GPT >= 1, "cluster larger than the residues per thread");
+  const uint32_t b0 = rank * (NB / C) + tid;  // bits of rank, tid and q * T are disjoint
+  uint64_t x[E];
+#pragma unroll
+  for (int q = 0; q < GPT; q++)
+#pragma unroll
+    for (int t = 0; t < C; t++) x[q * C + t] = src(jb, pr, b0 + q * T + t * NB);
+#pragma unroll
+  for (int q = 0; q < GPT; q++) fwd_top_stages<S1>(x + q * C, pr);
+  const uint32_t sb = swz8(b0);
+  cluster_wait();  // every peer has started (arrival at kernel entry)
+#pragma unroll
+  for (int t = 0; t < C; t++) {
+    const uint32_t peer = cluster_addr(sm, t, 0);
+#pragma unroll
+    for (int q = 0; q < GPT; q++) st_cluster(peer + (sb ^ swz8(q * T)), x[q * C + t]);
+  }
+}
+
+template <int LOGN, bool REDUCE, class Src, class Dst>
+__global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
+    k_ntt_fwd_cl(NttGeom g, Src src, Dst dst) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  extern __shared__ uint64_t sm[];
+  const uint32_t tid = threadIdx.x;
+  cluster_arrive_relaxed();
+  const NttJob jb = decode_job(g);  // beta = the CTA's rank in its cluster
+  const DevPrime pr = g.primes[jb.limb];
+  switch (g.s1) {
+    case 1: fwd_cluster_top<LOGN, 1>(src, jb, pr, sm, tid, jb.beta); break;
+    case 2: fwd_cluster_top<LOGN, 2>(src, jb, pr, sm, tid, jb.beta); break;
+    case 3: fwd_cluster_top<LOGN, 3>(src, jb, pr, sm, tid, jb.beta); break;
+    default: fwd_cluster_top<LOGN, 4>(src, jb, pr, sm, tid, jb.beta); break;
+  }
+  cluster_sync();
+  uint64_t x[E];
+  const uint32_t sb = swz8(tid);
+#pragma unroll
+  for (int e = 0; e < E; e++) x[e] = sm_at(sm, sb ^ swz8(e * T));
+  fwd_rounds<LOGN, 0>(x, sm, tid, pr, (1u << g.s1) + jb.beta);
+  const uint32_t base = jb.beta << LOGN;
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    uint64_t v = sm_at(sm, sb ^ swz8(e * T));
+    if (REDUCE) v = reduce4(v, pr.p, pr.p2);
+    dst(jb, pr, base + tid + e * T, v);
+  }
+}
+
+// Inverse phase 2: the last S1 stages (and the final scale) on the groups of
+// this CTA's share, read from the cluster's blocks.
+template <int LOGB, int S1, class Dst>
+__device__ __forceinline__ void inv_cluster_top(const NttGeom& g, const Dst& dst, const NttJob& jb,
+                                                const DevPrime& pr, uint64_t* sm, uint32_t tid, uint32_t rank) {
+  constexpr int E = NttShape<LOGB>::E, T = NttShape<LOGB>::T, C = 1 << S1, GPT = E / C;
+  constexpr uint32_t NB = 1u << LOGB;
+  const uint32_t b0 = rank * (NB / C) + tid;
+  const uint32_t sb = swz8(b0);
+  uint64_t x[E];
+#pragma unroll
+  for (int t = 0; t < C; t++) {
+    const uint32_t peer = cluster_addr(sm, t, 0);
+#pragma unroll
+    for (int q = 0; q < GPT; q++) x[q * C + t] = ld_cluster(peer + (sb ^ swz8(q * T)));
+  }
+#pragma unroll
+  for (int q = 0; q < GPT; q++) inv_top_stages<S1>(x + q * C, pr, NB << S1, g.mont != 0);
+#pragma unroll
+  for (int q = 0; q < GPT; q++)
+#pragma unroll
+    for (int t = 0; t < C; t++) dst(jb, pr, b0 + q * T + t * NB, x[q * C + t]);
+}
+
+template <int LOGN, class Src, class Dst>
+__global__ void __launch_bounds__(NttShape<LOGN>::T, NttShape<LOGN>::MIN_BLOCKS)
+    k_ntt_inv_cl(NttGeom g, Src src, Dst dst) {
+  constexpr int E = NttShape<LOGN>::E;
+  constexpr int T = NttShape<LOGN>::T;
+  constexpr int K0 = InvFirst<LOGN>::K;
+  extern __shared__ uint64_t sm[];
+  const uint32_t tid = threadIdx.x;
+  const NttJob jb = decode_job(g);
+  const DevPrime pr = g.primes[jb.limb];
+  const uint32_t base = jb.beta << LOGN;
+  uint64_t x[E];
+  const uint32_t sb = swz8(tid);
+  if constexpr (src_is_staged<Src>(0)) {
+    src.template stage<LOGN, T, E>(jb, pr, base, sm, tid, x);
+#pragma unroll
+    for (int e = 0; e < E; e++) sm_at(sm, sb ^ swz8(e * T)) = x[e];
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; e++) sm_at(sm, sb ^ swz8(e * T)) = src(jb, pr, base + tid + e * T);
+  }
+  __syncthreads();
+  inv_from_smem<LOGN, 0, K0>(x, sm, tid);
+  inv_rounds<LOGN, 0, K0>(x, sm, tid, pr, 1u << (LOGN + g.s1), g.s1, jb.beta);
+  // Every thread has read its last exchange: the block's results go to
+  // shared memory for the cluster.
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) sm_at(sm, sb ^ swz8(e * T)) = x[e];
+  cluster_sync();
+  switch (g.s1) {
+    case 1: inv_cluster_top<LOGN, 1>(g, dst, jb, pr, sm, tid, jb.beta); break;
+    case 2: inv_cluster_top<LOGN, 2>(g, dst, jb, pr, sm, tid, jb.beta); break;
+    case 3: inv_cluster_top<LOGN, 3>(g, dst, jb, pr, sm, tid, jb.beta); break;
+    default: inv_cluster_top<LOGN, 4>(g, dst, jb, pr, sm, tid, jb.beta); break;
+  }
+  // No CTA leaves while another may still read its shared memory.
+  cluster_sync();
+}
+
+// ---------------------------------------------------------------------------
 // Basic source / destination functors.
 
 struct SrcPoly {
@@ -624,6 +802,87 @@ void launch_inv_block(NttGeom g, uint64_t polys, Src src, Dst dst, cudaStream_t 
   after_launch("k_ntt_inv");
 }
 
+// Launch of a kernel on clusters of `csize` CTAs along x.
+template <class K, class... Args>
+void launch_cluster(K kern, uint64_t blocks, unsigned threads, size_t smem, unsigned csize, cudaStream_t st,
+                    Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  check_cuda(cudaLaunchKernelEx(&cfg, kern, args...), "cudaLaunchKernelEx");
+}
+
+// Whether clusters of 2^s1 CTAs of `kern` fit on the GPU (state per s1:
+// 0 unknown, 1 yes, -1 no; computed once). 16-CTA clusters need the
+// non-portable size opt-in.
+template <class K>
+bool cluster_fits(K kern, uint32_t s1, unsigned threads, size_t smem, int* state) {
+  if (s1 < 1 || s1 > 4) return false;
+  if (state[s1] == 0) {
+    int n = 0;
+    bool ok = true;
+    if (s1 == 4) ok = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    if (ok) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(1u << s1, 1, 1);
+      cfg.blockDim = dim3(threads, 1, 1);
+      cfg.dynamicSmemBytes = smem;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 1u << s1;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      ok = cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n > 0;
+    }
+    if (!ok) (void)cudaGetLastError();
+    state[s1] = ok ? 1 : -1;
+  }
+  return state[s1] > 0;
+}
+
+// Single-pass cluster transforms of 2^(LOGN + s1) residues; false (nothing
+// launched) when the GPU cannot run the cluster size.
+template <int LOGN, bool REDUCE, class Src, class Dst>
+bool launch_fwd_cluster(NttGeom g, uint32_t s1, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  auto kern = k_ntt_fwd_cl<LOGN, REDUCE, Src, Dst>;
+  const size_t smem = ntt_smem_bytes<LOGN>();
+  static bool done = false;
+  set_smem(kern, smem, &done);
+  static int fits[5] = {0, 0, 0, 0, 0};
+  if (!cluster_fits(kern, s1, NttShape<LOGN>::T, smem, fits)) return false;
+  g.s1 = s1;
+  g.pf_stride = 0;
+  launch_cluster(kern, polys * g.limbs << s1, NttShape<LOGN>::T, smem, 1u << s1, st, g, src, dst);
+  after_launch("k_ntt_fwd_cl");
+  return true;
+}
+
+template <int LOGN, class Src, class Dst>
+bool launch_inv_cluster(NttGeom g, uint32_t s1, uint64_t polys, Src src, Dst dst, cudaStream_t st) {
+  auto kern = k_ntt_inv_cl<LOGN, Src, Dst>;
+  const size_t smem = ntt_smem_bytes<LOGN>();
+  static bool done = false;
+  set_smem(kern, smem, &done);
+  static int fits[5] = {0, 0, 0, 0, 0};
+  if (!cluster_fits(kern, s1, NttShape<LOGN>::T, smem, fits)) return false;
+  g.s1 = s1;
+  g.pf_stride = 0;
+  launch_cluster(kern, polys * g.limbs << s1, NttShape<LOGN>::T, smem, 1u << s1, st, g, src, dst);
+  after_launch("k_ntt_inv_cl");
+  return true;
+}
+
 // Dispatch over log2(N) for a single-pass transform (3 <= logn <= 14).
 constexpr uint32_t kMinUnrolledLogN = 12;
 
@@ -708,6 +967,7 @@ void ntt_forward_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst,
     return;
   }
   const uint32_t s1 = logn - bl;
+  if (bl == 12 && ntt_cluster_enabled(logn) && launch_fwd_cluster<12, REDUCE>(g, s1, polys, src, dst, st)) return;
   launch_fwd_top(s1, g, bl, polys, src, dst, st);
   g.s1 = s1;
   switch (bl) {
@@ -755,6 +1015,7 @@ void ntt_inverse_any(uint32_t logn, NttGeom g, uint64_t polys, Src src, Dst dst,
     return;
   }
   const uint32_t s1 = logn - bl;
+  if (bl == 12 && ntt_cluster_enabled(logn) && launch_inv_cluster<12>(g, s1, polys, src, dst, st)) return;
   g.s1 = s1;
   switch (bl) {
     case 12: launch_inv_block<12, false>(g, polys, src, dst, st); break;

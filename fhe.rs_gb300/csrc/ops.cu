@@ -14,11 +14,15 @@ namespace fheg {
 
 std::atomic<uint64_t> g_launches{0};
 
-// Default NTT plan: single pass up to 2^13 (the whole limb in shared memory);
-// 2^14 to 2^16 as strided stages in front of 2^12-residue blocks, which run
-// three CTAs per SM (forward + inverse on GB300 at 256 x 6 limbs: 1,209 GB/s
-// at 2^14 against 1,056 single-pass, 1,215 at 2^15, 1,121 at 2^16).
-static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 12, 12, 12};
+// Default NTT plan: single pass up to 2^12 (the whole limb in shared memory);
+// 2^13 to 2^16 in 2^12-residue blocks, which run three CTAs per SM. At 2^13
+// and 2^14 the blocks of a limb form one cluster that exchanges the strided
+// stages through distributed shared memory (GB300, 256 x 6 limbs, forward /
+// inverse GB/s: 2^13 1,435 / 1,400 against 1,223 / 1,211 in two passes and
+// about 1,141 single-pass; 2^14 1,370 / 1,343 against 1,318 / 1,286); at 2^15
+// (equal) and 2^16 (1,050 / 958 against 1,166 / 1,135) they run as a strided
+// pass plus blocks.
+static std::atomic<uint32_t> g_ntt_block[17] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 12, 12, 12, 12};
 
 uint32_t ntt_block_logn(uint32_t logn) { return logn <= 16 ? g_ntt_block[logn].load(std::memory_order_relaxed) : 14; }
 
@@ -41,6 +45,14 @@ std::vector<uint32_t> ntt_plans(uint32_t logn) {
     if (ntt_plan_valid(logn, bl)) out.push_back(bl);
   if (out.empty() && ntt_plan_valid(logn, logn)) out.push_back(logn);
   return out;
+}
+
+static std::atomic<bool> g_ntt_cluster[17] = {false, false, false, false, false, false, false, false, false,
+                                               false, false, false, false, true,  true,  false, false};
+bool ntt_cluster_enabled(uint32_t logn) { return logn <= 16 && g_ntt_cluster[logn].load(std::memory_order_relaxed); }
+void set_ntt_cluster(uint32_t logn, bool on) {
+  if (logn > 16) throw Error(FHEG_ERR_INVALID_ARGUMENT, "unsupported NTT size");
+  g_ntt_cluster[logn].store(on, std::memory_order_relaxed);
 }
 
 void set_ntt_block_logn(uint32_t logn, uint32_t block_logn) {
@@ -191,6 +203,59 @@ __global__ void k_poly_op(const DevPrime* primes, uint32_t limbs, uint32_t logn,
 }
 
 static unsigned blocks_for(uint64_t total, unsigned threads) { return (unsigned)((total + threads - 1) / threads); }
+
+// zq/mod.rs:195-199 `shoup`: floor(x * 2^64 / q) for x < q. With b =
+// floor(2^128 / q), t = floor(x * b / 2^64) is that quotient or one less
+// (x * (2^128 / q - b) / 2^64 < 1); the remainder x * 2^64 - t q, below 2q,
+// tells which.
+__device__ __forceinline__ uint64_t shoup_of(uint64_t x, const DevPrime& pr) {
+  uint64_t t = x * pr.bhi + __umul64hi(x, pr.blo);
+  const uint64_t rem = 0 - t * pr.p;  // x * 2^64 - t q, taken modulo 2^64
+  if (rem >= pr.p) t++;
+  return t;
+}
+
+// Poly::compute_coefficients_shoup (rq/mod.rs:209-223): the Shoup plane of
+// NttShoup polynomials.
+__global__ void k_poly_shoup(const DevPrime* primes, uint32_t limbs, uint32_t logn, PolyRef a, PolyRef out,
+                             uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint32_t job = row_of(gid, logn);
+  const uint32_t limb = job % limbs, poly = job / limbs;
+  const DevPrime pr = primes[limb];
+  out.at(poly, limb)[i] = shoup_of(a.at(poly, limb)[i], pr);
+}
+
+// MulAssign<&Poly<NttShoup>> for Poly<Ntt> (rq/ops.rs:208-245): Shoup
+// products with b's companions, reduced (zq/mod.rs:407-416 `mul_shoup_vec`).
+__global__ void k_poly_mul_shoup(const DevPrime* primes, uint32_t limbs, uint32_t logn, PolyRef a, PolyRef b,
+                                 PolyRef bs, PolyRef out, uint64_t total) {
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total) return;
+  const uint32_t i = gid & ((1u << logn) - 1);
+  const uint32_t job = row_of(gid, logn);
+  const uint32_t limb = job % limbs, poly = job / limbs;
+  const uint64_t p = primes[limb].p;
+  out.at(poly, limb)[i] = mul_shoup(a.at(poly, limb)[i], b.at(poly, limb)[i], bs.at(poly, limb)[i], p);
+}
+
+void poly_compute_shoup(const Context& ctx, PolyRef a, PolyRef out, uint64_t polys, cudaStream_t st) {
+  const uint64_t total = polys * ctx.L() << ctx.logn;
+  if (total == 0) return;
+  k_poly_shoup<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), (uint32_t)ctx.L(), ctx.logn, a, out, total);
+  after_launch("k_poly_shoup");
+}
+
+void poly_mul_shoup(const Context& ctx, PolyRef a, PolyRef b, PolyRef bs, PolyRef out, uint64_t polys,
+                    cudaStream_t st) {
+  const uint64_t total = polys * ctx.L() << ctx.logn;
+  if (total == 0) return;
+  k_poly_mul_shoup<<<blocks_for(total, 256), 256, 0, st>>>(ctx.primes_dev(), (uint32_t)ctx.L(), ctx.logn, a, b, bs,
+                                                           out, total);
+  after_launch("k_poly_mul_shoup");
+}
 
 void poly_op(const Context& ctx, int op, PolyRef a, PolyRef b, PolyRef out, uint64_t polys, cudaStream_t st) {
   uint64_t total = polys * ctx.L() << ctx.logn;
@@ -395,6 +460,116 @@ __device__ __forceinline__ void sub256w(uint32_t* a, const uint32_t* b) {
       : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
 }
 
+// High parts of the scaler's sums. The sums only matter at bit 96 and above
+// (v needs G >> (shift - 1) with shift >= 123, w needs S >> 126), so the
+// fast path adds only the partial products x_i b_j (32-bit words) that
+// reach word 3: those with i + j >= 3, and the high halves of those with
+// i + j = 2. The rest of a term x * b (x < 2^64, b < 2^128) is below
+// 2^64 + 4 * 2^96 < 5 * 2^96, so a sum of F such terms is its kept part (a
+// multiple of 2^96) plus less than 5F * 2^96; a result whose kept part is
+// that close to a rounding boundary is recomputed exactly.
+//
+// h[0..NH) are words 3 .. 2 + NH of the sum: NH = 3 for a sum below 2^192,
+// NH = 5 for a sum taken modulo 2^256.
+template <int NH>
+__device__ __forceinline__ void mac_hi(uint32_t* h, uint64_t x, uint64_t blo, uint64_t bhi) {
+  static_assert(NH == 3 || NH == 5, "three or five high words");
+  if constexpr (NH == 3) {
+    asm("{\n\t"
+        ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
+        "mov.b64 {x0, x1}, %3;\n\t"
+        "mov.b64 {b0, b1}, %4;\n\t"
+        "mov.b64 {b2, b3}, %5;\n\t"
+        "mad.hi.cc.u32 %0, x0, b2, %0;\n\t"
+        "madc.hi.cc.u32 %1, x0, b3, %1;\n\t"
+        "madc.hi.u32 %2, x1, b3, %2;\n\t"
+        "mad.lo.cc.u32 %0, x0, b3, %0;\n\t"
+        "madc.lo.cc.u32 %1, x1, b3, %1;\n\t"
+        "addc.u32 %2, %2, 0;\n\t"
+        "mad.hi.cc.u32 %0, x1, b1, %0;\n\t"
+        "madc.hi.cc.u32 %1, x1, b2, %1;\n\t"
+        "addc.u32 %2, %2, 0;\n\t"
+        "mad.lo.cc.u32 %0, x1, b2, %0;\n\t"
+        "addc.cc.u32 %1, %1, 0;\n\t"
+        "addc.u32 %2, %2, 0;\n\t"
+        "}"
+        : "+r"(h[0]), "+r"(h[1]), "+r"(h[2])
+        : "l"(x), "l"(blo), "l"(bhi));
+  } else {
+    asm("{\n\t"
+        ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
+        "mov.b64 {x0, x1}, %5;\n\t"
+        "mov.b64 {b0, b1}, %6;\n\t"
+        "mov.b64 {b2, b3}, %7;\n\t"
+        "mad.hi.cc.u32 %0, x0, b2, %0;\n\t"
+        "madc.hi.cc.u32 %1, x0, b3, %1;\n\t"
+        "madc.hi.cc.u32 %2, x1, b3, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %0, x0, b3, %0;\n\t"
+        "madc.lo.cc.u32 %1, x1, b3, %1;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.hi.cc.u32 %0, x1, b1, %0;\n\t"
+        "madc.hi.cc.u32 %1, x1, b2, %1;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %0, x1, b2, %0;\n\t"
+        "addc.cc.u32 %1, %1, 0;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "}"
+        : "+r"(h[0]), "+r"(h[1]), "+r"(h[2]), "+r"(h[3]), "+r"(h[4])
+        : "l"(x), "l"(blo), "l"(bhi));
+  }
+}
+
+// Words 3..7 of v * theta_gamma for v < 2^96 (vlo, vhi, vhi < 2^32), kept
+// as in mac_hi: the low 64 bits of v through mac_hi (dropping less than
+// 5 * 2^96), the third word's partial products at word 2 and above (dropping
+// the low half of its lowest one, less than 2^96).
+__device__ __forceinline__ void mul_v_hi(uint32_t* h, uint64_t vlo, uint64_t vhi, uint64_t blo, uint64_t bhi) {
+#pragma unroll
+  for (int k = 0; k < 5; k++) h[k] = 0;
+  mac_hi<5>(h, vlo, blo, bhi);
+  asm("{\n\t"
+      ".reg .u32 v2, b0, b1, b2, b3;\n\t"
+      "cvt.u32.u64 v2, %5;\n\t"
+      "mov.b64 {b0, b1}, %6;\n\t"
+      "mov.b64 {b2, b3}, %7;\n\t"
+      "mad.hi.cc.u32 %0, v2, b0, %0;\n\t"
+      "madc.hi.cc.u32 %1, v2, b1, %1;\n\t"
+      "madc.hi.cc.u32 %2, v2, b2, %2;\n\t"
+      "madc.hi.cc.u32 %3, v2, b3, %3;\n\t"
+      "addc.u32 %4, %4, 0;\n\t"
+      "mad.lo.cc.u32 %0, v2, b1, %0;\n\t"
+      "madc.lo.cc.u32 %1, v2, b2, %1;\n\t"
+      "madc.lo.cc.u32 %2, v2, b3, %2;\n\t"
+      "addc.cc.u32 %3, %3, 0;\n\t"
+      "addc.u32 %4, %4, 0;\n\t"
+      "}"
+      : "+r"(h[0]), "+r"(h[1]), "+r"(h[2]), "+r"(h[3]), "+r"(h[4])
+      : "l"(vhi), "l"(blo), "l"(bhi));
+}
+
+// 160-bit a += b, a -= b (32-bit words).
+__device__ __forceinline__ void add160w(uint32_t* a, const uint32_t* b) {
+  asm("add.cc.u32 %0, %0, %5;\n\taddc.cc.u32 %1, %1, %6;\n\taddc.cc.u32 %2, %2, %7;\n\taddc.cc.u32 %3, %3, %8;\n\t"
+      "addc.u32 %4, %4, %9;"
+      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4])
+      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]));
+}
+
+__device__ __forceinline__ void sub160w(uint32_t* a, const uint32_t* b) {
+  asm("sub.cc.u32 %0, %0, %5;\n\tsubc.cc.u32 %1, %1, %6;\n\tsubc.cc.u32 %2, %2, %7;\n\tsubc.cc.u32 %3, %3, %8;\n\t"
+      "subc.u32 %4, %4, %9;"
+      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4])
+      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]));
+}
+
 // Full 128 x 128 -> 256-bit product (32-bit words).
 __device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
 #pragma unroll
@@ -473,6 +648,36 @@ struct FwdEpilogue {
   PolyRef digits;
 };
 
+// The exact sums of the rare coefficients whose fast high-word sums sit next
+// to a rounding boundary, kept out of line so that the hot kernel body stays
+// small in the instruction cache: G (six words) and S (eight words, mod
+// 2^256) as the reference accumulates them.
+template <int MAXF, int MAXT>
+__device__ __noinline__ void rns_exact_g(const RnsLaunch<MAXF, MAXT>* s, const uint64_t* r, uint32_t F, uint32_t* g) {
+#pragma unroll 1
+  for (int k = 0; k < 6; k++) g[k] = 0;
+#pragma unroll 1
+  for (uint32_t k = 0; k < F; k++) mac192(g, r[k], s->tgar_lo[k], s->tgar_hi[k]);
+}
+
+template <int MAXF, int MAXT>
+__device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const uint64_t* r, uint32_t F, uint64_t vlo,
+                                        uint64_t vhi, uint32_t* pos) {
+  uint32_t neg[8];
+#pragma unroll 1
+  for (int k = 0; k < 8; k++) pos[k] = neg[k] = 0;
+#pragma unroll 1
+  for (uint32_t k = 0; k < F; k++) {
+    if ((s->to_sign >> k) & 1) mac256(neg, r[k], s->to_lo[k], s->to_hi[k]);
+    else mac256(pos, r[k], s->to_lo[k], s->to_hi[k]);
+  }
+  sub256w(pos, neg);
+  uint32_t vt[8];
+  mul128x128w(vt, vlo, vhi, s->tg_lo, s->tg_hi);
+  if (s->tg_sign) add256w(pos, vt);
+  else sub256w(pos, vt);
+}
+
 template <int MAXF, int MAXT, bool EXACT, int TOP>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
                                                    PolyRef in, PolyRef out, uint64_t total,
@@ -522,11 +727,18 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     if (fwd_here || dig_here) __syncthreads();  // the buffer takes the outputs next
   }
 
-  // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2).
+  // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2). Fast path: the
+  // kept high words of G; exact when G >> (shift - 1) cannot change under
+  // the dropped part (below 5F * 2^96): (H mod 2^e) + 5F < 2^e, e = shift - 97.
   uint32_t g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
   for (int k = 0; k < MAXF; k++)
-    if (k < (int)F) mac192(g, r[k], s.tgar_lo[k], s.tgar_hi[k]);
+    if (k < (int)F) mac_hi<3>(g + 3, r[k], s.tgar_lo[k], s.tgar_hi[k]);
+  // shift >= 122 for any source count up to 128 moduli below 2^62; smaller
+  // shifts (never produced) take the exact path.
+  const uint32_t e_bits = s.shift >= 104 ? s.shift - 97 : 7;
+  bool exact = s.shift < 104 || (g[3] & ((1u << e_bits) - 1)) >= (1u << e_bits) - 5 * F;
+  if (exact) rns_exact_g<MAXF, MAXT>(&s, r, F, g);
   uint64_t vlo, vhi;
   shr_words(g, 6, s.shift - 1, &vlo, &vhi);
   {
@@ -537,23 +749,31 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     vhi += (vlo < odd);
   }
 
-  // scaler.rs:276-314.
+  // scaler.rs:276-314. Fast path: the kept high words of the signed sum S
+  // (the dropped part lies in (-(5F + 6), 5F + 6) * 2^96: 5 * 2^96 per term
+  // and 6 * 2^96 for v * theta_gamma); exact when S >> 126 cannot change,
+  // i.e. H mod 2^30 is at least 5F + 6 away from a multiple of 2^30.
   bool w_sign = false;
   uint64_t wlo = 0, whi = 0;
   if (!s.is_one) {
     uint32_t pos[8] = {0, 0, 0, 0, 0, 0, 0, 0}, neg[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (!exact) {
 #pragma unroll
-    for (int k = 0; k < MAXF; k++) {
-      if (k < (int)F) {
-        if ((s.to_sign >> k) & 1) mac256(neg, r[k], s.to_lo[k], s.to_hi[k]);
-        else mac256(pos, r[k], s.to_lo[k], s.to_hi[k]);
+      for (int k = 0; k < MAXF; k++) {
+        if (k < (int)F) {
+          if ((s.to_sign >> k) & 1) mac_hi<5>(neg + 3, r[k], s.to_lo[k], s.to_hi[k]);
+          else mac_hi<5>(pos + 3, r[k], s.to_lo[k], s.to_hi[k]);
+        }
       }
+      sub160w(pos + 3, neg + 3);
+      uint32_t vt[5];
+      mul_v_hi(vt, vlo, vhi, s.tg_lo, s.tg_hi);
+      if (s.tg_sign) add160w(pos + 3, vt);
+      else sub160w(pos + 3, vt);
+      const uint32_t m = pos[3] & ((1u << 30) - 1), margin = 5 * F + 6;
+      exact = m < margin || m > (1u << 30) - 1 - margin;
     }
-    sub256w(pos, neg);
-    uint32_t vt[8];
-    mul128x128w(vt, vlo, vhi, s.tg_lo, s.tg_hi);
-    if (s.tg_sign) add256w(pos, vt);
-    else sub256w(pos, vt);
+    if (exact) rns_exact_s<MAXF, MAXT>(&s, r, F, vlo, vhi, pos);
     w_sign = (pos[7] >> 31) != 0;
     if (w_sign) {
       uint32_t nw[8];

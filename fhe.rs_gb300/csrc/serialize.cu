@@ -128,7 +128,7 @@ void pack_polys(const Context& c, int representation, PolyRef in, uint8_t* bytes
   if (count == 0) return;
   const PackLayout lay = make_layout(c);
   PolyRef src = in;
-  if (representation == 1) {
+  if (representation >= 1) {  // Ntt and NttShoup values go through the power basis
     src = plain_ref(tmp, c.L(), c.logn);
     ntt_backward(c, in, src, count, st);
   }
@@ -145,15 +145,15 @@ void unpack_polys(const Context& c, int representation, const uint8_t* bytes, Po
   const uint64_t total = count * c.L() << c.logn;
   k_unpack<<<nblk(total, 256), 256, 0, st>>>(lay, bytes, out, total);
   after_launch("k_unpack");
-  if (representation == 1) ntt_forward(c, out, out, count, false, st);
+  if (representation >= 1) ntt_forward(c, out, out, count, false, st);
 }
 
 void poly_serialize(const Context& c, int representation, const uint64_t* polys, uint8_t* bytes, uint64_t count,
                     DevBuf& scratch, cudaStream_t st) {
   if (count == 0) return;
-  if (representation == 1) scratch.reserve(count * c.L() * c.N() * 8);
+  if (representation >= 1) scratch.reserve(count * c.L() * c.N() * 8);
   pack_polys(c, representation, plain_ref(const_cast<uint64_t*>(polys), c.L(), c.logn), bytes, count,
-             representation == 1 ? scratch.u64() : nullptr, st);
+             representation >= 1 ? scratch.u64() : nullptr, st);
 }
 
 void poly_deserialize(const Context& c, int representation, const uint8_t* bytes, uint64_t* polys, uint64_t count,
@@ -170,7 +170,7 @@ void poly_deserialize(const Context& c, int representation, const uint8_t* bytes
 
 namespace {
 
-constexpr uint64_t kReprCode[2] = {1, 2};  // fheg representation -> rq.proto Representation
+constexpr uint64_t kReprCode[3] = {1, 2, 3};  // fheg representation -> rq.proto Representation
 
 size_t varint_len(uint64_t v) {
   size_t n = 1;
@@ -459,9 +459,13 @@ fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t le
     }
   }
   if (ct_level > p.max_level() || ksk_level > p.max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
-  if (log_base != 0)
-    throw Error(FHEG_ERR_UNSUPPORTED, "keys with a decomposition base (single-modulus key contexts) are not supported");
-  const size_t count = p.ctx(ct_level)->L();
+  // key_switching_key.rs:360-372: a decomposition base names the digit count
+  // and needs both levels maximal.
+  if (log_base != 0 && (ksk_level != p.max_level() || ct_level != p.max_level()))
+    throw Error(FHEG_ERR_INVALID_ARGUMENT, "A decomposition size is specified but the levels are not maximal");
+  if (log_base > 62) throw Error(FHEG_ERR_INVALID_ARGUMENT, "decomposition base above 2^62");
+  const uint32_t log_modulus = log_modulus_of(p.moduli[0]);
+  const size_t count = log_base ? (log_modulus + log_base - 1) / log_base : p.ctx(ct_level)->L();
   if (c0.size() != count) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incorrect number of values in c0");
   if (seed.n == 0 && c1.size() != count) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incorrect number of values in c1");
   if (seed.n != 0 && seed.n != 32) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid seed");
@@ -470,7 +474,7 @@ fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t le
     if (exp % 2 == 0 || exp >= two_n)
       throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid exponent");  // SubstitutionExponent::new
   }
-  fheg_ksk* h = new_ksk_handle(par, ct_level, ksk_level, nullptr, count);
+  fheg_ksk* h = new_ksk_handle(par, ct_level, ksk_level, nullptr, count, (int64_t)log_base);
   try {
     const Ksk& k = h->k;
     const Context& kc = *k.ctx_ksk;
@@ -487,6 +491,7 @@ fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t le
     const uint8_t* db = static_cast<const uint8_t*>(d.ptr);
     unpack_polys(kc, 1, db, plain_ref(k.values(0), kc.L(), kc.logn), count, nullptr);
     if (seeded) {
+      h->k.seed.assign(seed.p, seed.p + 32);
       const std::vector<uint8_t> seeds = ksk_c1_seeds(seed.p, count);
       DevBuf ds(seeds.size());
       upload(ds.ptr, seeds.data(), seeds.size());
@@ -506,6 +511,82 @@ fheg_ksk* ksk_from_message(const fheg_params* par, const uint8_t* msg, size_t le
   return h;
 }
 
+// Length-delimited field (wire type 2) header.
+uint8_t* put_len_field(uint8_t* o, uint32_t field, size_t len) {
+  o = put_varint(o, ((uint64_t)field << 3) | 2);
+  return put_varint(o, len);
+}
+uint8_t* put_varint_field(uint8_t* o, uint32_t field, uint64_t v) {
+  if (v == 0) return o;  // proto3 default left out
+  o = put_varint(o, (uint64_t)field << 3);
+  return put_varint(o, v);
+}
+size_t varint_field_len(uint32_t field, uint64_t v) {
+  return v ? varint_len((uint64_t)field << 3) + varint_len(v) : 0;
+}
+
+// The KeySwitchingKey message of a device key (key_switching_key.rs:332-352):
+// c0[i], then c1[i] or the seed, as NttShoup Rq messages whose payloads are
+// the power basis of the key values (rq/convert.rs:17-42), with
+// allow_variable_time set as on the reference's keys; then the levels and
+// the decomposition base.
+std::vector<uint8_t> ksk_message_bytes(const Ksk& k) {
+  const Context& kc = *k.ctx_ksk;
+  const size_t n = k.count, payload = poly_serialized_bytes(kc);
+  const bool seeded = !k.seed.empty();
+  const size_t polys = seeded ? n : 2 * n;  // c1 follows c0 in the key's buffer
+  DevBuf tmp(polys * kc.L() * kc.N() * 8), packed(polys * payload);
+  pack_polys(kc, 2, plain_ref(k.values(0), kc.L(), kc.logn), static_cast<uint8_t*>(packed.ptr), polys, tmp.u64(),
+             nullptr);
+  std::vector<uint8_t> hp(polys * payload);
+  check_cuda(cudaMemcpy(hp.data(), packed.ptr, hp.size(), cudaMemcpyDeviceToHost), "D2H");
+  const size_t rq = rq_message_len(kc, true);
+  const size_t rq_field = 1 + varint_len(rq) + rq;
+  const size_t len = polys * rq_field + (seeded ? 34 : 0) + varint_field_len(4, k.ciphertext_level) +
+                     varint_field_len(5, k.ksk_level) + varint_field_len(6, k.log_base);
+  std::vector<uint8_t> out(len);
+  uint8_t* o = out.data();
+  for (size_t i = 0; i < n; i++) {
+    o = put_len_field(o, 1, rq);
+    o = put_rq(o, kc, 2, hp.data() + i * payload, true);
+  }
+  if (seeded) {
+    o = put_len_field(o, 3, 32);
+    std::memcpy(o, k.seed.data(), 32);
+    o += 32;
+  } else {
+    for (size_t i = 0; i < n; i++) {
+      o = put_len_field(o, 2, rq);
+      o = put_rq(o, kc, 2, hp.data() + (n + i) * payload, true);
+    }
+  }
+  o = put_varint_field(o, 4, k.ciphertext_level);
+  o = put_varint_field(o, 5, k.ksk_level);
+  o = put_varint_field(o, 6, k.log_base);
+  if ((size_t)(o - out.data()) != len) throw Error(FHEG_ERR_INTERNAL, "key message length");
+  return out;
+}
+
+// RelinearizationKey { ksk = 1 } (relinearization_key.rs:109-115) or
+// GaloisKey { ksk = 1, exponent = 2 } (galois_key.rs:127-134) around it.
+std::vector<uint8_t> wrap_ksk(const std::vector<uint8_t>& ksk, int kind, uint64_t exponent) {
+  if (kind == 0) return ksk;
+  const size_t len = 1 + varint_len(ksk.size()) + ksk.size() + (kind == 2 ? varint_field_len(2, exponent) : 0);
+  std::vector<uint8_t> out(len);
+  uint8_t* o = put_len_field(out.data(), 1, ksk.size());
+  std::memcpy(o, ksk.data(), ksk.size());
+  o += ksk.size();
+  if (kind == 2) o = put_varint_field(o, 2, exponent);
+  return out;
+}
+
+void copy_out(const std::vector<uint8_t>& msg, uint8_t* h_out, size_t cap, size_t* len) {
+  *len = msg.size();
+  if (!h_out) return;
+  if (cap < msg.size()) throw Error(FHEG_ERR_INVALID_ARGUMENT, "output buffer too small for the message");
+  std::memcpy(h_out, msg.data(), msg.size());
+}
+
 }  // namespace fheg
 
 using namespace fheg;
@@ -520,7 +601,7 @@ FHEG_API int fheg_poly_serialized_size(const fheg_context* ctx, size_t* bytes) {
 FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, const uint64_t* d_polys,
                                  uint8_t* d_bytes, size_t count, void* stream) {
   return abi_call([&] {
-    abi_need(ctx && (representation == 0 || representation == 1), "bad context or representation");
+    abi_need(ctx && representation >= 0 && representation <= 2, "bad context or representation");
     abi_need((d_polys && d_bytes) || !count, "null input");
     DevBuf scratch;
     poly_serialize(*ctx->c, representation, d_polys, d_bytes, count, scratch, static_cast<cudaStream_t>(stream));
@@ -531,7 +612,7 @@ FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, co
 FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, const uint8_t* d_bytes,
                                    uint64_t* d_polys, size_t count, void* stream) {
   return abi_call([&] {
-    abi_need(ctx && (representation == 0 || representation == 1), "bad context or representation");
+    abi_need(ctx && representation >= 0 && representation <= 2, "bad context or representation");
     abi_need((d_polys && d_bytes) || !count, "null input");
     poly_deserialize(*ctx->c, representation, d_bytes, d_polys, count, static_cast<cudaStream_t>(stream));
   });
@@ -578,6 +659,91 @@ FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* c
     fheg_params* p = const_cast<fheg_params*>(par);
     ciphertext_from_bytes(*p->p, h_msgs, lens, count, level, parts, d_out, p->ws, *p->level_handles[level].ws,
                           static_cast<cudaStream_t>(stream));
+  });
+}
+
+FHEG_API int fheg_ksk_to_bytes(const fheg_ksk* key, int kind, size_t exponent, uint8_t* h_out, size_t cap,
+                               size_t* len) {
+  return abi_call([&] {
+    abi_need(key && len && kind >= 0 && kind <= 2, "null input or bad kind");
+    if (kind == 2 && (exponent % 2 == 0 || exponent >= 2 * key->k.ctx_ct->N()))
+      throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid exponent");
+    copy_out(wrap_ksk(ksk_message_bytes(key->k), kind, exponent), h_out, cap, len);
+  });
+}
+
+FHEG_API int fheg_evaluation_key_to_bytes(const fheg_ksk* const* keys, const size_t* exponents, size_t count,
+                                          size_t ciphertext_level, size_t evaluation_key_level, uint8_t* h_out,
+                                          size_t cap, size_t* len) {
+  return abi_call([&] {
+    abi_need(len && ((keys && exponents) || !count), "null input");
+    // evaluation_key.rs:382-392: { repeated GaloisKey gk = 2; ciphertext_level = 3;
+    // evaluation_key_level = 4 }, keys in the order given.
+    std::vector<std::vector<uint8_t>> gks;
+    size_t total = varint_field_len(3, ciphertext_level) + varint_field_len(4, evaluation_key_level);
+    for (size_t i = 0; i < count; i++) {
+      abi_need(keys[i] != nullptr, "null key");
+      const Ksk& k = keys[i]->k;
+      if (k.ciphertext_level != ciphertext_level || k.ksk_level != evaluation_key_level)
+        throw Error(FHEG_ERR_KEY_MISMATCH, "Galois key at other levels than the evaluation key");
+      if (exponents[i] % 2 == 0 || exponents[i] >= 2 * k.ctx_ct->N())
+        throw Error(FHEG_ERR_INVALID_ARGUMENT, "Invalid exponent");
+      gks.push_back(wrap_ksk(ksk_message_bytes(k), 2, exponents[i]));
+      total += 1 + varint_len(gks.back().size()) + gks.back().size();
+    }
+    std::vector<uint8_t> out(total);
+    uint8_t* o = out.data();
+    for (const auto& g : gks) {
+      o = put_len_field(o, 2, g.size());
+      std::memcpy(o, g.data(), g.size());
+      o += g.size();
+    }
+    o = put_varint_field(o, 3, ciphertext_level);
+    o = put_varint_field(o, 4, evaluation_key_level);
+    copy_out(out, h_out, cap, len);
+  });
+}
+
+FHEG_API int fheg_evaluation_key_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len,
+                                            fheg_ksk** keys, size_t* exponents, size_t cap, size_t* count,
+                                            size_t* ciphertext_level, size_t* evaluation_key_level) {
+  return abi_call([&] {
+    abi_need(par && h_msg && count, "null input");
+    // evaluation_key.rs:394-432.
+    std::vector<Span> gks;
+    uint64_t ct_level = 0, ek_level = 0;
+    {
+      Reader r{h_msg, h_msg + len, "EvaluationKey"};
+      Field f;
+      while (r.next(f)) {
+        if (f.num == 2) r.expect(f, 2), gks.push_back(f.bytes);
+        else if (f.num == 3) r.expect(f, 0), ct_level = f.value & 0xffffffffu;
+        else if (f.num == 4) r.expect(f, 0), ek_level = f.value & 0xffffffffu;
+      }
+    }
+    *count = gks.size();
+    if (ciphertext_level) *ciphertext_level = (size_t)ct_level;
+    if (evaluation_key_level) *evaluation_key_level = (size_t)ek_level;
+    if (!keys) return;
+    abi_need(exponents != nullptr, "null exponents");
+    if (cap < gks.size()) throw Error(FHEG_ERR_INVALID_ARGUMENT, "too few key slots for the evaluation key");
+    std::vector<fheg_ksk*> made;
+    try {
+      for (const Span& g : gks) {
+        uint64_t e = 0;
+        fheg_ksk* h = ksk_from_message(par, g.p, g.n, 2, &e);
+        made.push_back(h);
+        if (h->k.ciphertext_level != ct_level)
+          throw Error(FHEG_ERR_INVALID_ARGUMENT, "Galois key has incorrect ciphertext level");
+        if (h->k.ksk_level != ek_level)
+          throw Error(FHEG_ERR_INVALID_ARGUMENT, "Galois key has incorrect evaluation key level");
+        exponents[made.size() - 1] = (size_t)e;
+      }
+    } catch (...) {
+      for (fheg_ksk* h : made) delete h;
+      throw;
+    }
+    for (size_t i = 0; i < made.size(); i++) keys[i] = made[i];
   });
 }
 

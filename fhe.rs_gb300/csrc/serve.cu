@@ -184,7 +184,9 @@ void describe(Req& q) {
       q.L = m.base->L();
       q.out_parts = m.out_parts();
       q.out_L = par.ctx(m.out_level())->L();
-      q.group = (uint64_t)(uintptr_t)r.mult * 8 + 0;
+      // One group per parameter set: a batch may mix levels (multiplicators)
+      // and runs as one sub-batch per multiplicator.
+      q.group = (uint64_t)(uintptr_t)m.par * 8 + 0;
       break;
     }
     case FHEG_OP_ROTATE: {
@@ -192,8 +194,6 @@ void describe(Req& q) {
       if (r.key->k.par != &par) throw Error(FHEG_ERR_KEY_MISMATCH, "key of other parameters");
       if ((r.exponent % (2 * q.N)) % 2 == 0)
         throw Error(FHEG_ERR_INVALID_ARGUMENT, "The exponent should be odd modulo 2 * degree");
-      if (r.key->k.ctx_ksk->L() != r.key->k.ctx_ct->L())
-        throw Error(FHEG_ERR_UNSUPPORTED, "key switching keys at a lower level than the ciphertext are not supported");
       q.L = q.out_L = r.key->k.ctx_ct->L();
       q.out_parts = 2;
       q.group = (uint64_t)(uintptr_t)r.par * 8 + 1;
@@ -224,14 +224,32 @@ void describe(Req& q) {
 size_t batch_io_bytes(const std::vector<Req*>& b) {
   size_t words = 0;
   for (Req* q : b) words += (q->r.op == FHEG_OP_MUL_RELIN || q->r.op == FHEG_OP_ADD ? 2 : 1) * q->in_words + q->out_words;
-  return words * 8 + (2 * b.size() + 4) * 256;  // each carved region is rounded up to 256 bytes
+  // Each carved region is rounded up to 256 bytes: at most four per request
+  // (mul+relin sub-batches: inputs, output, scratch), plus a few.
+  return words * 8 + (4 * b.size() + 4) * 256;
+}
+
+// The mul+relin requests of a batch split by multiplicator, in order of
+// first appearance (each sub-batch keeps arrival order).
+std::vector<std::vector<Req*>> by_multiplicator(const std::vector<Req*>& b) {
+  std::vector<std::vector<Req*>> groups;
+  for (Req* q : b) {
+    size_t g = 0;
+    while (g < groups.size() && groups[g][0]->r.mult != q->r.mult) g++;
+    if (g == groups.size()) groups.emplace_back();
+    groups[g].push_back(q);
+  }
+  return groups;
 }
 
 size_t batch_scratch_bytes(const std::vector<Req*>& b) {
   const Req& q = *b[0];
   switch (q.r.op) {
-    case FHEG_OP_MUL_RELIN:
-      return q.r.mult->m->scratch_bytes(b.size());
+    case FHEG_OP_MUL_RELIN: {
+      size_t bytes = 0;
+      for (const auto& g : by_multiplicator(b)) bytes += g[0]->r.mult->m->scratch_bytes(g.size()) + 256;
+      return bytes;
+    }
     case FHEG_OP_ROTATE: {
       std::vector<fheg::RotRequest> rr;
       for (Req* x : b) rr.push_back(fheg::RotRequest{&x->r.key->k, x->r.exponent, nullptr, nullptr});
@@ -285,7 +303,30 @@ void fheg_server::launch(Slot& s, const std::vector<Req*>& batch, size_t scratch
     fheg::check_cuda(cudaMemcpyAsync(h, d, words * 8, cudaMemcpyDeviceToHost, st), "D2H");
   };
   fheg::Workspace ws;
-  if (q0.r.op == FHEG_OP_MUL_RELIN || q0.r.op == FHEG_OP_ADD) {
+  if (q0.r.op == FHEG_OP_MUL_RELIN) {
+    // One sub-batch per multiplicator (level), one after the other on the
+    // slot's stream, each with its own inputs, outputs and scratch.
+    for (const auto& g : by_multiplicator(batch)) {
+      const Req& g0 = *g[0];
+      const size_t G = g.size();
+      uint64_t* a = carve(G * g0.in_words);
+      uint64_t* b = carve(G * g0.in_words);
+      uint64_t* o = carve(G * g0.out_words);
+      for (size_t k = 0; k < G; k++) {
+        const size_t i = (size_t)(std::find(batch.begin(), batch.end(), g[k]) - batch.begin());
+        h2d(a + k * g0.in_words, g[k]->r.in0, g0.in_words, pin_in0[i]);
+        h2d(b + k * g0.in_words, g[k]->r.in1, g0.in_words, pin_in1[i]);
+      }
+      const size_t sb = g0.r.mult->m->scratch_bytes(G);
+      fheg::Workspace gws;
+      gws.attach(carve(sb / 8), sb);
+      g0.r.mult->m->multiply(a, b, o, G, st, &gws);
+      for (size_t k = 0; k < G; k++) {
+        const size_t i = (size_t)(std::find(batch.begin(), batch.end(), g[k]) - batch.begin());
+        d2h(g[k]->r.out, o + k * g0.out_words, g0.out_words, pin_out[i]);
+      }
+    }
+  } else if (q0.r.op == FHEG_OP_ADD) {
     uint64_t* a = carve(B * q0.in_words);
     uint64_t* b = carve(B * q0.in_words);
     uint64_t* o = carve(B * q0.out_words);
@@ -293,15 +334,10 @@ void fheg_server::launch(Slot& s, const std::vector<Req*>& batch, size_t scratch
       h2d(a + k * q0.in_words, batch[k]->r.in0, q0.in_words, pin_in0[k]);
       h2d(b + k * q0.in_words, batch[k]->r.in1, q0.in_words, pin_in1[k]);
     }
-    if (q0.r.op == FHEG_OP_MUL_RELIN) {
-      ws.attach(carve(scratch_bytes / 8), scratch_bytes);
-      q0.r.mult->m->multiply(a, b, o, B, st, &ws);
-    } else {
-      const fheg::Context& c = *q0.r.par->p->ctx(q0.r.level);
-      fheg::PolyRef ra = fheg::plain_ref(a, c.L(), c.logn), rb = fheg::plain_ref(b, c.L(), c.logn),
-                    ro = fheg::plain_ref(o, c.L(), c.logn);
-      fheg::poly_op(c, 0, ra, rb, ro, 2 * B, st);
-    }
+    const fheg::Context& c = *q0.r.par->p->ctx(q0.r.level);
+    fheg::PolyRef ra = fheg::plain_ref(a, c.L(), c.logn), rb = fheg::plain_ref(b, c.L(), c.logn),
+                  ro = fheg::plain_ref(o, c.L(), c.logn);
+    fheg::poly_op(c, 0, ra, rb, ro, 2 * B, st);
     for (size_t k = 0; k < B; k++) d2h(batch[k]->r.out, o + k * q0.out_words, q0.out_words, pin_out[k]);
   } else if (q0.r.op == FHEG_OP_SWITCH_DOWN) {
     uint64_t* a = carve(B * q0.in_words);

@@ -18,7 +18,10 @@
  *    device); `h_` pointers are host pointers. `stream` is a `cudaStream_t`
  *    (NULL = the legacy default stream).
  *  - Representations follow `rq::Representation`
- *    (fhe-math/src/rq/mod.rs:37-47): 0 = PowerBasis, 1 = Ntt.
+ *    (fhe-math/src/rq/mod.rs:37-47): 0 = PowerBasis, 1 = Ntt, 2 = NttShoup.
+ *    An NttShoup polynomial is its Ntt values plus, where an operation reads
+ *    it, a second array of the same shape holding the Shoup plane
+ *    (`coefficients_shoup`, rq/mod.rs:209-223; fheg_poly_compute_shoup).
  *  - Handles are opaque and thread-compatible: a handle may be used from
  *    several threads as long as calls on the same multiplicator or server are
  *    not concurrent.
@@ -61,6 +64,7 @@ typedef struct fheg_scaler fheg_scaler;
 typedef struct fheg_params fheg_params;
 typedef struct fheg_ksk fheg_ksk;
 typedef struct fheg_multiplicator fheg_multiplicator;
+typedef struct fheg_graph fheg_graph;
 
 /* ------------------------------------------------------------------------ */
 /* Library                                                                    */
@@ -72,6 +76,16 @@ FHEG_API const char* fheg_last_error(void);
 /* Number of kernels this library has launched in this process (all devices).
  * Used by benchmarks to report how many of the library's kernels ran. */
 FHEG_API uint64_t fheg_kernel_launch_count(void);
+/* No counterpart in the reference: integer-throughput probes giving the
+ * ceilings the NTT and RNS kernels are compared with. One launch of `blocks`
+ * CTAs of 256 threads, each running `iters` iterations of 8 independent
+ * register-resident chains of: kind 0 a 32-bit multiply-add (low half),
+ * 1 a 32 x 32 -> 64-bit multiply-add, 2 a 32-bit multiply-add (high half),
+ * 3 a 32-bit addition, 4 the NTT's Harvey forward butterfly (62-bit prime,
+ * Shoup twiddle), 5 its Gentleman-Sande inverse butterfly. One word per
+ * thread is written to d_sink (blocks * 256 words); *ops receives the
+ * thread-level operations of the launch (time it on `stream`). */
+FHEG_API int fheg_intpeak(int kind, size_t blocks, uint32_t iters, uint64_t* d_sink, void* stream, double* ops);
 
 /* Device memory for callers without their own CUDA bindings (a Rust -sys
  * crate): plain cudaMalloc / cudaFree and stream-ordered copies. The copy to
@@ -144,8 +158,16 @@ FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn);
 /* Whether NTT kernels hint the next CTA's input rows into L2 while they
  * work (off by default; schedules only). */
 FHEG_API int fheg_ntt_prefetch_set(int on);
+/* Cluster mode of a two-pass plan with 2^12-residue blocks (logn 13..16): the
+ * transform runs as one pass on clusters of 2^(logn - 12) CTAs that exchange
+ * the strided stages through distributed shared memory instead of a second
+ * pass over device memory (GPUs that cannot run the cluster size fall back
+ * to two passes). Schedules only; process-wide per logn. */
+FHEG_API int fheg_ntt_cluster_set(uint32_t logn, int on);
+FHEG_API int fheg_ntt_cluster_get(uint32_t logn, int* on);
 /* Times every valid plan for the context's degree on `count` scratch
- * polynomials (forward + inverse), installs the fastest and returns it. */
+ * polynomials (forward + inverse), cluster mode included, installs the
+ * fastest and returns its block size (fheg_ntt_cluster_get tells the mode). */
 FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn);
 
 /* Coefficient-wise ring operations (fhe-math/src/rq/ops.rs:10-418):
@@ -158,7 +180,8 @@ FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, 
  * (fhe-math/src/rq/convert.rs:17-93): the power-basis coefficients of every
  * limb bit-packed little-endian with bitlen(q_j - 1) bits each
  * (zq/mod.rs:783-793, fhe-util/src/lib.rs:57-135), limbs concatenated.
- * representation 1 (Ntt) goes through the power basis as the reference does.
+ * representations 1 (Ntt) and 2 (NttShoup, values only) go through the power
+ * basis as the reference does.
  * d_bytes holds count * fheg_poly_serialized_size bytes. Unpacked values are
  * reduced modulo their limb's modulus. The protobuf framing (representation,
  * degree, the bytes field) stays with the caller. */
@@ -168,6 +191,17 @@ FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, co
 FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, const uint8_t* d_bytes,
                                    uint64_t* d_polys, size_t count, void* stream);
 
+/* Poly::compute_coefficients_shoup (fhe-math/src/rq/mod.rs:209-223, the
+ * conversion to NttShoup): d_shoup = floor(d_polys * 2^64 / q_j) for every
+ * canonical residue. */
+FHEG_API int fheg_poly_compute_shoup(const fheg_context* ctx, const uint64_t* d_polys, uint64_t* d_shoup,
+                                     size_t count, void* stream);
+/* MulAssign<&Poly<NttShoup>> for Poly<Ntt> (fhe-math/src/rq/ops.rs:208-245):
+ * d_out = d_a * d_b coefficient-wise through d_b's Shoup plane, reduced.
+ * d_out may alias d_a. */
+FHEG_API int fheg_poly_mul_shoup(const fheg_context* ctx, const uint64_t* d_a, const uint64_t* d_b,
+                                 const uint64_t* d_b_shoup, uint64_t* d_out, size_t count, void* stream);
+
 /* MulAssign<&BigUint> for Poly (fhe-math/src/rq/ops.rs:297-352): every limb
  * times scalar mod q_j (scalar: little-endian u64 words), in either
  * representation. d_out may alias d_in. */
@@ -175,7 +209,9 @@ FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scala
                                   const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream);
 
 /* Poly::substitute (fhe-math/src/rq/mod.rs:319-369) for an odd exponent,
- * in Ntt (representation 1) or PowerBasis (0). d_out must not alias d_in. */
+ * in Ntt (representation 1) or PowerBasis (0); NttShoup (2) permutes the
+ * values as Ntt does (recompute the Shoup plane of the result with
+ * fheg_poly_compute_shoup, rq/mod.rs:336-339). d_out must not alias d_in. */
 FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation,
                                   const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream);
 
@@ -251,7 +287,12 @@ FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_le
 FHEG_API void fheg_ksk_destroy(fheg_ksk* k);
 
 /* RelinearizationKey::relinearizes (fhe/src/bfv/keys/relinearization_key.rs:71-98):
- * d_ct3 [count][3][L][N] (Ntt) -> d_out [count][2][L][N] (Ntt). */
+ * d_ct3 [count][3][L][N] (Ntt) -> d_out [count][2][L][N] (Ntt). A key whose
+ * level is below the ciphertext level (more moduli) key-switches in its own
+ * context and switches the result down to the ciphertext context before the
+ * additions (relinearization_key.rs:84-92); the same holds for Galois keys
+ * (galois_key.rs:113-120) and for the relinearization of the Multiplicator
+ * (fhe/src/bfv/ops/mul.rs:199-206). */
 FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count,
                               void* stream);
 
@@ -274,6 +315,14 @@ FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const 
 FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ksk* const* keys,
                                            const size_t* exponents, const uint64_t* const* d_cts,
                                            uint64_t* const* d_outs, size_t count, void* stream);
+/* No counterpart in the reference: the same ragged batch recorded once as a
+ * CUDA graph (fheg_graph_launch replays it on whatever the ciphertext buffers
+ * hold then; fheg_graph_destroy frees it). Its tables and scratch belong to
+ * the graph; the keys and buffers must outlive it. Runs the batch once while
+ * recording (the outputs are written). */
+FHEG_API int fheg_galois_relinearize_batch_capture(const fheg_params* par, const fheg_ksk* const* keys,
+                                                   const size_t* exponents, const uint64_t* const* d_cts,
+                                                   uint64_t* const* d_outs, size_t count, fheg_graph** out);
 
 /* Ciphertext::switch_down (fhe/src/bfv/ciphertext.rs:86-97) for ciphertexts
  * at `level` with `parts` polynomials: d_ct [count][parts][L][N] ->
@@ -320,6 +369,17 @@ FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t
  * a stream of the multiplicator's that forks from and joins `stream`. */
 FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                          uint64_t* d_out, size_t count, void* stream);
+/* No counterpart in the reference: several batched multiplications issued
+ * together, typically one per level of one parameter set (a batch of
+ * ciphertexts at mixed levels, grouped by level): group g multiplies
+ * counts[g] pairs d_lhs[g] x d_rhs[g] -> d_out[g] with mults[g] (layouts as
+ * fheg_multiplicator_multiply at that multiplicator's level). Each group runs
+ * on its multiplicator's own stream, forked from and joined back into
+ * `stream`, so the groups' kernels overlap on the GPU. A multiplicator may
+ * appear in one group only (merge its pairs into one batch). */
+FHEG_API int fheg_multiply_groups(fheg_multiplicator* const* mults, const uint64_t* const* d_lhs,
+                                  const uint64_t* const* d_rhs, uint64_t* const* d_out, const size_t* counts,
+                                  size_t groups, void* stream);
 /* Runs one multiplication with events at the stage boundaries and returns
  * the duration of each stage in ms[7]: A inverse NTT of the operands,
  * B basis extension, C forward NTT of the extension limbs, D tensor product
@@ -369,8 +429,9 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
  * [count][2][L][N] Ntt) and calls no cudaMalloc / cudaFree: its scratch is a
  * fixed 16 MiB device array inside the library, which every GPU that loads the
  * library holds until the process exits. A call needs
- * 8 * count * L * N * (1 + L_ksk) bytes (each of its two regions rounded up to
- * 256 bytes); larger batches are rejected with FHEG_ERR_INVALID_ARGUMENT
+ * 8 * count * L * N * (1 + L_ksk) bytes, plus 8 * count * N * 2 * (L_ksk + L)
+ * for a key below the ciphertext level (each region rounded up to 256 bytes);
+ * larger batches are rejected with FHEG_ERR_INVALID_ARGUMENT
  * (split them). The first call on a device looks the array's address up, so
  * make it before any stream capture. All calls share the array and it keeps
  * the last call's contents: calls whose work overlaps on the GPU (different
@@ -505,12 +566,43 @@ FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* c
  * odd and below 2N). c0[i] and c1[i] are NttShoup Rq messages over the key
  * context; a key that carries its seed has its c1 expanded on the device
  * (generate_c1). Errors as the reference: wrong number of c0 / c1 values or
- * a seed of another length -> FHEG_ERR_INVALID_ARGUMENT, levels above the
- * maximum -> FHEG_ERR_INVALID_LEVEL; keys with a decomposition base
- * (log_base != 0) -> FHEG_ERR_UNSUPPORTED. The key's levels are returned in
- * *ciphertext_level and *ksk_level (each output nullable). */
+ * a seed of another length, a decomposition base (log_base != 0) with levels
+ * that are not maximal -> FHEG_ERR_INVALID_ARGUMENT, levels above the
+ * maximum -> FHEG_ERR_INVALID_LEVEL. A decomposition base names a
+ * single-modulus key of ceil(log2 q / log_base) digits (key_switching_key.rs:
+ * 360-372). The key's levels are returned in *ciphertext_level and
+ * *ksk_level (each output nullable). */
 FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len, int kind,
                                  fheg_ksk** out, size_t* exponent, size_t* ciphertext_level, size_t* ksk_level);
+
+/* KeySwitchingKey (kind 0), RelinearizationKey (1) and GaloisKey (2, with its
+ * `exponent`) to_bytes (key_switching_key.rs:332-352,
+ * relinearization_key.rs:109-115, 129-131, galois_key.rs:127-134) of a
+ * device key: c0[i], then c1[i] or, for a key made from its seed, the seed,
+ * as NttShoup Rq messages (payloads of the power basis of the values, with
+ * allow_variable_time set, as the reference's keys carry it), then the
+ * levels and the decomposition base; fields in prost's order. The message
+ * goes to h_out (capacity `cap`); *len receives its length. h_out = NULL
+ * asks for the length only. */
+FHEG_API int fheg_ksk_to_bytes(const fheg_ksk* key, int kind, size_t exponent, uint8_t* h_out, size_t cap,
+                               size_t* len);
+/* EvaluationKey::to_bytes (fhe/src/bfv/keys/evaluation_key.rs:210-213,
+ * 382-392): { repeated GaloisKey gk = 2; ciphertext_level = 3;
+ * evaluation_key_level = 4 } with the `count` keys in the order given (the
+ * reference iterates a hash map, so its order is unspecified). Every key must
+ * be at the two levels (FHEG_ERR_KEY_MISMATCH). Output as fheg_ksk_to_bytes. */
+FHEG_API int fheg_evaluation_key_to_bytes(const fheg_ksk* const* keys, const size_t* exponents, size_t count,
+                                          size_t ciphertext_level, size_t evaluation_key_level, uint8_t* h_out,
+                                          size_t cap, size_t* len);
+/* EvaluationKey::from_bytes (evaluation_key.rs:216-228, 394-432): decodes
+ * every Galois key of the message into keys[i] with its exponent in
+ * exponents[i] (the caller destroys them); *count receives the number of keys
+ * and the levels go to the nullable outputs. keys = NULL asks for the count
+ * only; fewer than *count slots -> FHEG_ERR_INVALID_ARGUMENT. A key at other
+ * levels than the message names fails as in the reference. */
+FHEG_API int fheg_evaluation_key_from_bytes(const fheg_params* par, const uint8_t* h_msg, size_t len,
+                                            fheg_ksk** keys, size_t* exponents, size_t cap, size_t* count,
+                                            size_t* ciphertext_level, size_t* evaluation_key_level);
 
 /* ------------------------------------------------------------------------ */
 /* CUDA graphs                                                                */
@@ -524,7 +616,6 @@ FHEG_API int fheg_ksk_from_bytes(const fheg_params* par, const uint8_t* h_msg, s
  * concurrently (the kernels of one branch fill the gaps of the other).
  * Destroy the graph before the multiplicator and its key. No counterpart in
  * the reference. */
-typedef struct fheg_graph fheg_graph;
 FHEG_API int fheg_multiplicator_capture(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                         uint64_t* d_out, size_t count, fheg_graph** out);
 FHEG_API int fheg_graph_launch(const fheg_graph* g, void* stream);

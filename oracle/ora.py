@@ -82,6 +82,20 @@ class OraKskLimb(ctypes.Structure):
     _fields_ = [("mod", ctypes.c_uint64 * 5), ("omegas", U64P), ("omegas_shoup", U64P)]
 
 
+class OraCtx(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_uint64), ("n", ctypes.c_uint64), ("moduli", U64P),
+                ("omegas", ctypes.POINTER(U64P)), ("omegas_shoup", ctypes.POINTER(U64P)),
+                ("zetas_inv", ctypes.POINTER(U64P)), ("zetas_inv_shoup", ctypes.POINTER(U64P)),
+                ("size_inv", U64P), ("size_inv_shoup", U64P)]
+
+
+class OraMult(ctypes.Structure):
+    _fields_ = [("base", OraCtx), ("mul", OraCtx), ("ext_lhs", ctypes.POINTER(OraScaler)), ("ncm_lhs", ctypes.c_uint64),
+                ("ext_rhs", ctypes.POINTER(OraScaler)), ("ncm_rhs", ctypes.c_uint64),
+                ("down", ctypes.POINTER(OraScaler)), ("c0", U64P), ("c0_shoup", U64P), ("c1", U64P),
+                ("c1_shoup", U64P)]
+
+
 def _declare(L):
     sz = ctypes.c_size_t
     L.ora_ntt_tables.argtypes = [U64P, sz, ctypes.c_uint64, ctypes.c_uint64, U64P, U64P, U64P, U64P]
@@ -98,6 +112,7 @@ def _declare(L):
     L.ora_switch_down.argtypes = [U64P, sz, sz, U64P, U64P, U64P, U64P]
     L.ora_key_switch.argtypes = [ctypes.POINTER(OraKskLimb), sz, sz, U64P, sz, U64P, U64P, U64P, U64P,
                                  U64P, U64P]
+    L.ora_multiply.argtypes = [ctypes.POINTER(OraMult), U64P, U64P, U64P, sz, sz]
 
 
 def _p(a: np.ndarray):
@@ -1353,9 +1368,30 @@ class SecretKey:
         return max(min(x.bit_length(), (q - x).bit_length()) for x in c.to_biguints())
 
 
+def decomposition_log_base(ctx: Context) -> int:
+    """key_switching_key.rs:70-73: half the bit length of the (single) key
+    modulus rounded up to a power of two."""
+    log_modulus = _next_pow2(ctx.moduli[0]).bit_length() - 1
+    return log_modulus // 2
+
+
+def decomposition_digits(p: Poly, log_base: int) -> np.ndarray:
+    """key_switching_key.rs:300-314: the base-2^log_base digits of the
+    coefficients (every limb's row in turn), one row per digit."""
+    log_modulus = _next_pow2(p.ctx.moduli[0]).bit_length() - 1
+    coeffs = p.coefficients.reshape(-1).copy()
+    mask = np.uint64((1 << log_base) - 1)
+    out = []
+    for _ in range(-(-log_modulus // log_base)):
+        out.append(coeffs & mask)
+        coeffs >>= np.uint64(log_base)
+    return np.stack(out)
+
+
 class KeySwitchingKey:
-    """keys/key_switching_key.rs:21-329 (RNS-digit variant; the ksk context has
-    at least two moduli)."""
+    """keys/key_switching_key.rs:21-329: RNS digits (one per ciphertext
+    modulus), or for a single-modulus key context the bit decomposition with
+    base 2^log_base (generate_c0_decomposition, key_switch_decomposition)."""
 
     def __init__(self, sk: SecretKey, frm: Poly, ciphertext_level: int, ksk_level: int,
                  rng: np.random.Generator, seed: Optional[bytes] = None):
@@ -1366,9 +1402,13 @@ class KeySwitchingKey:
         self.ciphertext_level, self.ksk_level = ciphertext_level, ksk_level
         if frm.ctx != self.ctx_ksk:
             raise ValueError("Incorrect context for polynomial from")
-        if len(self.ctx_ksk.moduli) == 1:
-            raise NotImplementedError("bit decomposition keys (single-modulus key context)")
+        self.log_base = 0
         size = len(self.ctx_ciphertext.moduli)
+        if len(self.ctx_ksk.moduli) == 1:
+            # key_switching_key.rs:70-76
+            self.log_base = decomposition_log_base(self.ctx_ksk)
+            log_modulus = _next_pow2(self.ctx_ksk.moduli[0]).bit_length() - 1
+            size = -(-log_modulus // self.log_base)
         # generate_c1 (108-123): uniform NttShoup polys, from the key's seed
         # when one is given (as the reference always does), else drawn from
         # the numpy generator.
@@ -1377,9 +1417,11 @@ class KeySwitchingKey:
             self.c1 = [Poly.random(self.ctx_ksk, NTT_SHOUP, rng) for _ in range(size)]
         else:
             self.c1 = [Poly.random_from_seed(self.ctx_ksk, s, NTT_SHOUP) for s in ksk_c1_seeds(seed, size)]
-        # generate_c0 (126-169)
+        # generate_c0 (126-169) / generate_c0_decomposition (172-211): the
+        # i-th c0 carries `from` times the i-th Garner coefficient, or times
+        # 2^(i * log_base).
         s = sk.s_ntt(self.ctx_ksk)
-        rns = RnsContext(par.moduli[:size])
+        rns = None if self.log_base else RnsContext(par.moduli[:size])
         self.c0 = []
         for i, c1i in enumerate(self.c1):
             a_s = Poly(self.ctx_ksk, c1i.coefficients.copy(), NTT)
@@ -1387,17 +1429,18 @@ class KeySwitchingKey:
             a_s.into_power_basis()
             b = Poly.small(self.ctx_ksk, POWER_BASIS, par.variance, rng)
             b -= a_s
-            b += frm * rns.get_garner(i)
+            b += frm * (1 << (i * self.log_base) if self.log_base else rns.get_garner(i))
             self.c0.append(b.into_ntt_shoup())
 
     @staticmethod
     def from_arrays(par: BfvParameters, c0: np.ndarray, c1: np.ndarray, ciphertext_level: int,
-                    ksk_level: int) -> "KeySwitchingKey":
+                    ksk_level: int, log_base: int = 0) -> "KeySwitchingKey":
         k = KeySwitchingKey.__new__(KeySwitchingKey)
         k.par = par
         k.ctx_ksk = par.context_at_level(ksk_level)
         k.ctx_ciphertext = par.context_at_level(ciphertext_level)
         k.ciphertext_level, k.ksk_level = ciphertext_level, ksk_level
+        k.log_base = log_base
         k.c0 = [Poly(k.ctx_ksk, c0[i], NTT_SHOUP) for i in range(c0.shape[0])]
         k.c1 = [Poly(k.ctx_ksk, c1[i], NTT_SHOUP) for i in range(c1.shape[0])]
         return k
@@ -1409,9 +1452,13 @@ class KeySwitchingKey:
         return np.stack([p.coefficients for p in self.c1])
 
     def key_switch(self, p: Poly):
-        """key_switching_key.rs:214-241 (loop in oracle.cpp)."""
+        """key_switching_key.rs:214-241 (loop in oracle.cpp); for
+        decomposition keys key_switching_key.rs:292-329, the same loop over
+        the base-2^log_base digits of the coefficients."""
         if p.ctx != self.ctx_ciphertext:
             raise ValueError("The input polynomial does not have the correct context.")
+        rows = decomposition_digits(p, self.log_base) if self.log_base else p.coefficients
+        rows = np.ascontiguousarray(rows, dtype=np.uint64)
         ctx = self.ctx_ksk
         n, Lk = ctx.degree, len(ctx.moduli)
         limbs = (OraKskLimb * Lk)()
@@ -1426,7 +1473,7 @@ class KeySwitchingKey:
         c1s = np.ascontiguousarray(np.stack([k.coefficients_shoup for k in self.c1]))
         out0 = np.zeros((Lk, n), dtype=np.uint64)
         out1 = np.zeros((Lk, n), dtype=np.uint64)
-        lib().ora_key_switch(limbs, Lk, n, _p(p.coefficients), p.coefficients.shape[0], _p(c0), _p(c0s), _p(c1),
+        lib().ora_key_switch(limbs, Lk, n, _p(rows), rows.shape[0], _p(c0), _p(c0s), _p(c1),
                              _p(c1s), _p(out0), _p(out1))
         return Poly(ctx, out0, NTT), Poly(ctx, out1, NTT)
 
@@ -1691,6 +1738,52 @@ class Multiplicator:
         return out
 
 
+def _ctx_desc(ctx: Context, keep: list) -> OraCtx:
+    """The tables of a context for oracle.cpp's whole-product loop."""
+    n = ctx.degree
+    mods = _u64(np.concatenate([q.fields for q in ctx.q]))
+    ptrs = []
+    for name in ("omegas", "omegas_shoup", "zetas_inv", "zetas_inv_shoup"):
+        arr = (U64P * len(ctx.ops))(*[_p(getattr(op, name)) for op in ctx.ops])
+        ptrs.append(arr)
+    sinv = _u64([op.size_inv for op in ctx.ops])
+    sinv_s = _u64([op.size_inv_shoup for op in ctx.ops])
+    keep += [mods, sinv, sinv_s] + ptrs
+    return OraCtx(len(ctx.moduli), n, _p(mods), ptrs[0], ptrs[1], ptrs[2], ptrs[3], _p(sinv), _p(sinv_s))
+
+
+class MultiplyDriver:
+    """ops/mul.rs:158-227 `Multiplicator::multiply` run whole in oracle.cpp
+    over independent pairs on host threads: the timed CPU baseline. Covers the
+    default multiplicator (relinearization key at the multiplication level, no
+    modulus switching); outputs equal `Multiplicator.multiply`."""
+
+    def __init__(self, m: "Multiplicator"):
+        if m.rk is None or m.mod_switch or m.rk.ksk.ctx_ksk != m.base_ctx:
+            raise ValueError("the driver runs the default multiplicator only")
+        self.m = m
+        self._keep = []
+        k = m.rk.ksk
+        self.c0 = np.ascontiguousarray(np.stack([p.coefficients for p in k.c0]))
+        self.c0s = np.ascontiguousarray(np.stack([p.coefficients_shoup for p in k.c0]))
+        self.c1 = np.ascontiguousarray(np.stack([p.coefficients for p in k.c1]))
+        self.c1s = np.ascontiguousarray(np.stack([p.coefficients_shoup for p in k.c1]))
+        self.desc = OraMult(
+            _ctx_desc(m.base_ctx, self._keep), _ctx_desc(m.mul_ctx, self._keep),
+            ctypes.pointer(m.extender_lhs.scaler._desc), m.extender_lhs.number_common_moduli,
+            ctypes.pointer(m.extender_rhs.scaler._desc), m.extender_rhs.number_common_moduli,
+            ctypes.pointer(m.down_scaler.scaler._desc), _p(self.c0), _p(self.c0s), _p(self.c1), _p(self.c1s))
+
+    def multiply(self, lhs: np.ndarray, rhs: np.ndarray, threads: int = 1) -> np.ndarray:
+        """lhs, rhs [count][2][L][N] (Ntt) -> [count][2][L][N]."""
+        lhs = np.ascontiguousarray(lhs, dtype=np.uint64)
+        rhs = np.ascontiguousarray(rhs, dtype=np.uint64)
+        assert lhs.shape == rhs.shape and lhs.shape[1:] == (2, len(self.m.base_ctx.moduli), self.m.base_ctx.degree)
+        out = np.zeros_like(lhs)
+        lib().ora_multiply(ctypes.byref(self.desc), _p(lhs), _p(rhs), _p(out), lhs.shape[0], threads)
+        return out
+
+
 def dot_product_scalar(cts: Sequence[Ciphertext], pts: Sequence[Poly]) -> Ciphertext:
     """ops/dot_product.rs:56-140: sum_i ct_i * pt_i (pt_i the plaintexts' Ntt
     polynomials), accumulated exactly and reduced once per coefficient."""
@@ -1912,7 +2005,8 @@ def ksk_message(ksk: "KeySwitchingKey", allow_variable_time: bool = True) -> byt
         out += b"".join(_pb_bytes(2, rq_message(p, allow_variable_time), repeated=True) for p in ksk.c1)
     else:
         out += _pb_bytes(3, seed)
-    return out + _pb_varint(4, ksk.ciphertext_level) + _pb_varint(5, ksk.ksk_level)
+    return (out + _pb_varint(4, ksk.ciphertext_level) + _pb_varint(5, ksk.ksk_level)
+            + _pb_varint(6, getattr(ksk, "log_base", 0)))
 
 
 def relinearization_key_message(rk: "RelinearizationKey") -> bytes:
@@ -1923,3 +2017,10 @@ def relinearization_key_message(rk: "RelinearizationKey") -> bytes:
 def galois_key_message(gk: "GaloisKey") -> bytes:
     """galois_key.rs:127-134: { ksk = 1, exponent = 2 }."""
     return _pb_bytes(1, ksk_message(gk.ksk), repeated=True) + _pb_varint(2, gk.element.exponent)
+
+
+def evaluation_key_message(gks: Sequence["GaloisKey"], ciphertext_level: int, evaluation_key_level: int) -> bytes:
+    """evaluation_key.rs:382-392: { repeated GaloisKey gk = 2; ciphertext_level
+    = 3; evaluation_key_level = 4 }, the keys in the order given."""
+    return (b"".join(_pb_bytes(2, galois_key_message(g), repeated=True) for g in gks)
+            + _pb_varint(3, ciphertext_level) + _pb_varint(4, evaluation_key_level))

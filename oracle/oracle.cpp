@@ -15,6 +15,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 typedef unsigned __int128 u128;
@@ -512,6 +513,130 @@ void ora_key_switch(const ora_ksk_limb* limbs, size_t Lk, size_t n, const uint64
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Whole products, for the timed CPU baseline: fhe/src/bfv/ops/mul.rs:158-227
+// `Multiplicator::multiply` with relinearization (key at the multiplication
+// level, relinearization_key.rs:71-98 without the switch-down branch), over
+// independent ciphertext pairs on `threads` host threads (the reference has no
+// internal parallelism; callers parallelise over ciphertexts).
+
+// A context: moduli and NTT tables per limb (ntt/native.rs:15-73).
+struct ora_ctx {
+  uint64_t L, n;
+  const uint64_t* moduli;  // [L][5]
+  const uint64_t* const* omegas;
+  const uint64_t* const* omegas_shoup;
+  const uint64_t* const* zetas_inv;
+  const uint64_t* const* zetas_inv_shoup;
+  const uint64_t* size_inv;        // [L]
+  const uint64_t* size_inv_shoup;  // [L]
+};
+
+struct ora_mult {
+  ora_ctx base, mul;
+  const ora_scaler* ext_lhs;
+  uint64_t ncm_lhs;
+  const ora_scaler* ext_rhs;
+  uint64_t ncm_rhs;
+  const ora_scaler* down;
+  // Relinearization key (ksk context = base context): [L][L][n] values and
+  // Shoup companions.
+  const uint64_t* c0;
+  const uint64_t* c0_shoup;
+  const uint64_t* c1;
+  const uint64_t* c1_shoup;
+};
+
+static NttOp ctx_op(const ora_ctx& c, size_t j) {
+  return make_op(c.moduli + 5 * j, c.n, c.omegas[j], c.omegas_shoup[j], c.zetas_inv[j], c.zetas_inv_shoup[j],
+                 c.size_inv[j], c.size_inv_shoup[j]);
+}
+
+// rq/scaler.rs:63-115 `Scaler::scale` of an Ntt polynomial [from.L][n] into
+// [to.L][n] (Ntt): the common prefix copied, the other limbs through the
+// power basis and `RnsScaler::scale`.
+static void scaler_scale_ntt(const ora_scaler* s, size_t ncm, const ora_ctx& from, const ora_ctx& to,
+                             const uint64_t* in, uint64_t* out, std::vector<uint64_t>& tmp) {
+  const size_t n = from.n;
+  std::memcpy(out, in, sizeof(uint64_t) * ncm * n);
+  if (ncm >= to.L) return;
+  tmp.assign(in, in + from.L * n);
+  for (size_t j = 0; j < from.L; j++) ntt_backward(ctx_op(from, j), tmp.data() + j * n);
+  ora_rns_scale(s, tmp.data(), out + ncm * n, n, ncm, to.L - ncm);
+  for (size_t k = ncm; k < to.L; k++) ntt_forward(ctx_op(to, k), out + k * n);
+}
+
+static void multiply_one(const ora_mult* m, const uint64_t* lhs, const uint64_t* rhs, uint64_t* out,
+                         std::vector<uint64_t>* buf) {
+  const size_t L = m->base.L, M = m->mul.L, n = m->base.n;
+  std::vector<uint64_t>& e = buf[0];    // [4][M][n]: c00, c01, c10, c11
+  std::vector<uint64_t>& c = buf[1];    // [3][M][n]: the tensor
+  std::vector<uint64_t>& d = buf[2];    // [3][L][n]: scaled down
+  std::vector<uint64_t>& tmp = buf[3];
+  std::vector<uint64_t>& ks = buf[4];   // [2][L][n]
+  e.resize(4 * M * n);
+  c.resize(3 * M * n);
+  d.resize(3 * L * n);
+  ks.resize(2 * L * n);
+  // mul.rs:176-179: extend.
+  for (int w = 0; w < 4; w++) {
+    const bool left = w < 2;
+    const uint64_t* src = (left ? lhs : rhs) + (size_t)(w & 1) * L * n;
+    scaler_scale_ntt(left ? m->ext_lhs : m->ext_rhs, left ? m->ncm_lhs : m->ncm_rhs, m->base, m->mul, src,
+                     e.data() + (size_t)w * M * n, tmp);
+  }
+  // mul.rs:182-185: c0 = c00 c10, c1 = c00 c11 + c01 c10, c2 = c01 c11.
+  for (size_t j = 0; j < M; j++) {
+    const Modulus q = load_modulus(m->mul.moduli + 5 * j);
+    const uint64_t* c00 = e.data() + (0 * M + j) * n;
+    const uint64_t* c01 = e.data() + (1 * M + j) * n;
+    const uint64_t* c10 = e.data() + (2 * M + j) * n;
+    const uint64_t* c11 = e.data() + (3 * M + j) * n;
+    for (size_t i = 0; i < n; i++) {
+      c[(0 * M + j) * n + i] = mul(q, c00[i], c10[i]);
+      c[(1 * M + j) * n + i] = reduce1(mul(q, c00[i], c11[i]) + mul(q, c01[i], c10[i]), q.p);
+      c[(2 * M + j) * n + i] = mul(q, c01[i], c11[i]);
+    }
+  }
+  // mul.rs:188-190: scale down.
+  for (int k = 0; k < 3; k++)
+    scaler_scale_ntt(m->down, 0, m->mul, m->base, c.data() + (size_t)k * M * n, d.data() + (size_t)k * L * n, tmp);
+  // mul.rs:196-210: relinearize c2.
+  tmp.assign(d.data() + 2 * L * n, d.data() + 3 * L * n);
+  for (size_t j = 0; j < L; j++) ntt_backward(ctx_op(m->base, j), tmp.data() + j * n);
+  std::vector<ora_ksk_limb> limbs(L);
+  for (size_t j = 0; j < L; j++) {
+    for (int f = 0; f < 5; f++) limbs[j].mod[f] = m->base.moduli[5 * j + f];
+    limbs[j].omegas = m->base.omegas[j];
+    limbs[j].omegas_shoup = m->base.omegas_shoup[j];
+  }
+  ora_key_switch(limbs.data(), L, n, tmp.data(), L, m->c0, m->c0_shoup, m->c1, m->c1_shoup, ks.data(),
+                 ks.data() + L * n);
+  for (size_t part = 0; part < 2; part++)
+    for (size_t j = 0; j < L; j++) {
+      const uint64_t p = m->base.moduli[5 * j];
+      for (size_t i = 0; i < n; i++) {
+        const size_t at = (part * L + j) * n + i;
+        out[at] = reduce1(d[at] + ks[at], p);
+      }
+    }
+}
+
+// `count` products: lhs, rhs [count][2][L][n] (Ntt) -> out [count][2][L][n].
+// Pair k runs on thread k % threads.
+void ora_multiply(const ora_mult* m, const uint64_t* lhs, const uint64_t* rhs, uint64_t* out, size_t count,
+                  size_t threads) {
+  const size_t ct = 2 * m->base.L * m->base.n;
+  if (threads < 1) threads = 1;
+  std::vector<std::thread> pool;
+  for (size_t t = 0; t < threads; t++)
+    pool.emplace_back([=] {
+      std::vector<uint64_t> buf[5];
+      for (size_t k = t; k < count; k += threads) multiply_one(m, lhs + k * ct, rhs + k * ct, out + k * ct, buf);
+    });
+  for (auto& th : pool) th.join();
 }
 
 }  // extern "C"

@@ -94,11 +94,12 @@ def test_mul_scaler_constants_match_oracle(fg, ora):
 
 
 def test_ntt_plan_validation(fg):
-    """Plan entries are checked on the host: defaults single pass up to 2^13
-    and 2^12 blocks above; blocks of 2^12..2^14 with at most four strided
-    stages."""
+    """Plan entries are checked on the host: defaults single pass up to 2^12
+    and 2^12 blocks above, in clusters at 2^13 and 2^14; blocks of 2^12..2^14
+    with at most four strided stages."""
     for logn in range(3, 17):
-        assert fg.ntt_plan_get(logn) == (logn if logn <= 13 else 12)
+        assert fg.ntt_plan_get(logn) == (logn if logn <= 12 else 12)
+        assert fg.ntt_cluster_get(logn) == (logn in (13, 14))
     for logn, bl in [(12, 11), (14, 15), (15, 15), (16, 11), (17, 14), (11, 12)]:
         with pytest.raises(fg.FhegError):
             fg.ntt_plan_set(logn, bl)

@@ -150,9 +150,10 @@ def test_graph_replay(fg, ora, cuda):
 
 @pytest.mark.parametrize("count", [32, 33])
 def test_graph_two_branches(fg, ora, cuda, count):
-    """Batches of 32 pairs or more are captured as two concurrent branches
-    (halves with their own scratch; 33 splits 16 + 17): the replay equals
-    multiply() on the whole batch, and two products equal the oracle's."""
+    """Batches of 32 pairs or more run as two concurrent halves, each with its
+    own scratch (33 splits 16 + 17), both as direct calls and as captured
+    graphs. Every product of both forms equals the single-pass path (chunks of
+    fewer than 32 pairs), and two products equal the oracle's."""
     s = Setup(fg, ora, 4096, 2, 65537, seed=41 + count)
     rk_o, rk = s.rk()
     m = fg.Multiplicator.default(rk)
@@ -161,14 +162,18 @@ def test_graph_two_branches(fg, ora, cuda, count):
     lhs_h = (rng.integers(0, 1 << 62, (count, 2, 2, 4096), dtype=np.uint64) % q).astype(np.uint64)
     rhs_h = (rng.integers(0, 1 << 62, (count, 2, 2, 4096), dtype=np.uint64) % q).astype(np.uint64)
     lhs, rhs = fg.to_device(lhs_h), fg.to_device(rhs_h)
+    single_pass = np.concatenate([
+        fg.to_host(m.multiply(fg.to_device(lhs_h[k:k + 12]), fg.to_device(rhs_h[k:k + 12])))
+        for k in range(0, count, 12)])
     out = fg.empty((count, 2, 2, 4096))
     g = m.capture(lhs, rhs, out)
     assert g.kernels >= 14
     want = fg.to_host(m.multiply(lhs, rhs))
+    assert np.array_equal(want, single_pass)
     out.zero_()
     g.launch()
     cuda.cuda.synchronize()
-    assert np.array_equal(fg.to_host(out), want)
+    assert np.array_equal(fg.to_host(out), single_pass)
     mo = ora.Multiplicator.default(rk_o)
     for b in (0, count - 1):
         lo = ora.Ciphertext.from_array(s.par_o, lhs_h[b], 0)
@@ -260,9 +265,9 @@ def test_errors(fg, ora, cuda):
         fg.RelinearizationKey(s.par, c, c)
     assert e.value.code == fg.ERR_KEY_MISMATCH
     one = np.zeros((1, 1, 16), dtype=np.uint64)
-    with pytest.raises(fg.FhegError) as e:  # single-modulus key context
+    with pytest.raises(fg.FhegError) as e:  # single-modulus key context: two base-2^31 digits, not one
         fg.RelinearizationKey(s.par, one, one, 2, 2)
-    assert e.value.code == fg.ERR_UNSUPPORTED
+    assert e.value.code == fg.ERR_KEY_MISMATCH
     with pytest.raises(fg.FhegError) as e:
         s.par.context_at_level(3)
     assert e.value.code == fg.ERR_INVALID_LEVEL
@@ -292,6 +297,70 @@ def test_rotate_ragged_batch(fg, ora, cuda, n, L, count):
         assert np.array_equal(fg.to_host(outs[b]), want[b]), f"entry {b} (level {levels[b]})"
 
 
+def test_multiply_groups_mixed_levels(fg, ora, cuda):
+    """A batch of pairs at four levels, grouped by level (one multiplicator
+    per level, one of them with its key two levels below) and issued together:
+    every product equals the oracle's and the per-level direct call."""
+    n, L = 4096, 5
+    s = Setup(fg, ora, n, L, 65537, seed=1400)
+    mults, mults_o, lhs, rhs, pairs = [], [], [], [], []
+    for lvl, count, klvl in [(0, 5, 0), (1, 3, 1), (2, 4, 0), (3, 2, 3)]:
+        rk_o = ora.RelinearizationKey(s.sk, s.rng, lvl, klvl)
+        rk = fg.RelinearizationKey(s.par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array(), lvl, klvl)
+        mults.append(fg.Multiplicator.default(rk))
+        mults_o.append(ora.Multiplicator.default(rk_o))
+        _, cts = s.encrypt(2 * count, level=lvl)
+        pairs.append(cts)
+        lhs.append(fg.to_device(np.stack([c.to_array() for c in cts[:count]])))
+        rhs.append(fg.to_device(np.stack([c.to_array() for c in cts[count:]])))
+    outs = fg.multiply_groups(mults, lhs, rhs)
+    cuda.cuda.synchronize()
+    for g, (m, mo, cts) in enumerate(zip(mults, mults_o, pairs)):
+        count = lhs[g].shape[0]
+        got = fg.to_host(outs[g])
+        assert np.array_equal(got, fg.to_host(m.multiply(lhs[g], rhs[g]))), g
+        for b in range(count):
+            assert np.array_equal(got[b], mo.multiply(cts[b], cts[count + b]).to_array()), (g, b)
+    with pytest.raises(fg.FhegError):
+        fg.multiply_groups([mults[0], mults[0]], lhs[:1] * 2, rhs[:1] * 2)
+
+
+@pytest.mark.parametrize("count", [5, 17])
+def test_rotate_batch_graph(fg, ora, cuda, count):
+    """A ragged rotation batch (levels 0-2, some keys below the ciphertext
+    level; 17 requests as two concurrent halves) recorded as a CUDA graph:
+    each replay equals the direct batched call on what the buffers hold."""
+    n, L = 4096, 4
+    s = Setup(fg, ora, n, L, 65537, seed=1300 + count)
+    rng = np.random.default_rng(count)
+    keys, want_keys = [], []
+    levels = [int(x) for x in rng.integers(0, L - 1, count)]
+    for b in range(count):
+        lvl = levels[b]
+        klvl = lvl if b % 2 else int(rng.integers(0, lvl + 1))
+        e = ora.rotation_exponent(s.par_o, int(rng.integers(1, n // 2)))
+        gk_o = ora.GaloisKey(s.sk, e, lvl, klvl, s.rng)
+        want_keys.append(gk_o)
+        keys.append(fg.GaloisKey(s.par, e, gk_o.ksk.c0_array(), gk_o.ksk.c1_array(), lvl, klvl))
+    cts = [fg.to_device(s.encrypt(1, level=lv)[1][0].to_array()) for lv in levels]
+    outs = [fg.empty(c.shape) for c in cts]
+    g = fg.capture_rotate_batch(s.par, keys, cts, outs)
+    assert g.kernels >= 3
+    for rep in range(2):
+        fresh = [s.encrypt(1, level=lv)[1][0] for lv in levels]
+        for c, f in zip(cts, fresh):
+            c.copy_(fg.to_device(f.to_array()))
+        for o in outs:
+            o.zero_()
+        g.launch()
+        cuda.cuda.synchronize()
+        direct = fg.rotate_batch(s.par, keys, cts)
+        for b in range(count):
+            got = fg.to_host(outs[b])
+            assert np.array_equal(got, fg.to_host(direct[b])), (rep, b)
+            assert np.array_equal(got, want_keys[b].relinearize(fresh[b]).to_array()), (rep, b)
+
+
 @pytest.mark.parametrize("n,plans", [(16384, [12, 13]), (32768, [12, 13])])
 def test_pipelines_under_every_ntt_plan(fg, ora, cuda, n, plans):
     """mul+relin, a rotation and a switch-down give the same bytes under every
@@ -313,14 +382,17 @@ def test_pipelines_under_every_ntt_plan(fg, ora, cuda, n, plans):
     want = (ora.Multiplicator.default(rk_o).multiply(cts[0], cts[1]).to_array(),
             gk_o.relinearize(cts[0]).to_array(), cts[0].copy().switch_down().to_array())
     default = fg.ntt_plan_get(logn)
+    default_cluster = fg.ntt_cluster_get(logn)
     try:
-        for bl in plans + [default]:
+        for bl, cluster in [(b, False) for b in plans] + [(12, True), (default, default_cluster)]:
             fg.ntt_plan_set(logn, bl)
+            fg.ntt_cluster_set(logn, cluster)
             got = run()
             for g, w in zip(got, want):
-                assert np.array_equal(g[0], w), f"plan {bl}"
+                assert np.array_equal(g[0], w), f"plan {bl} cluster {cluster}"
     finally:
         fg.ntt_plan_set(logn, default)
+        fg.ntt_cluster_set(logn, default_cluster)
 
 
 def test_multiplicator_stage_plans_and_times(fg, ora, cuda):
@@ -373,8 +445,8 @@ def test_errors_of_the_wider_api(fg, ora, cuda):
     _, cts = s.encrypt(2)
     ct = fg.to_device(np.stack([c.to_array() for c in cts]))
     ctx = s.par.context_at_level(0)
-    with pytest.raises(fg.FhegError) as e:  # representation 2 (NttShoup) has no payload form here
-        fg.check(fg.lib().fheg_poly_serialize(ctx._h, 2, None, None, 0, None))
+    with pytest.raises(fg.FhegError) as e:  # no representation 3
+        fg.check(fg.lib().fheg_poly_serialize(ctx._h, 3, None, None, 0, None))
     assert e.value.code == fg.ERR_INVALID_ARGUMENT
     sk = fg.SecretKey(s.par, s.sk.coeffs)
     with pytest.raises(fg.FhegError) as e:

@@ -41,25 +41,29 @@ def test_ntt_forward_backward_bit_exact(fg, ora, cuda, logn, L, B):
     assert np.array_equal(fg.to_host(t), data)
 
 
-PLANS = [(13, 12), (14, 12), (14, 13), (15, 12), (15, 13), (16, 12), (16, 13)]
+PLANS = [(13, 12, 0), (14, 12, 0), (14, 13, 0), (15, 12, 0), (15, 13, 0), (16, 12, 0), (16, 13, 0),
+         (13, 12, 1), (14, 12, 1), (15, 12, 1), (16, 12, 1)]
 
 
-@pytest.mark.parametrize("logn,bl", PLANS)
-def test_ntt_plans_bit_exact(fg, ora, cuda, logn, bl):
-    """Every two-pass plan (strided pass + blocks of 2^bl) gives the oracle's
-    output, lazy and reduced, and inverts."""
+@pytest.mark.parametrize("logn,bl,cluster", PLANS)
+def test_ntt_plans_bit_exact(fg, ora, cuda, logn, bl, cluster):
+    """Every two-pass plan (strided pass + blocks of 2^bl), and the single-pass
+    cluster form of the 2^12-block plans (2 to 16 CTAs per cluster), gives
+    the oracle's output, lazy and reduced, and inverts."""
     n = 1 << logn
-    moduli = _moduli(ora, n, 2)
+    moduli = _moduli(ora, n, 3)
     rng = np.random.default_rng(logn * 7 + bl)
-    data = np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli]) for _ in range(2)])
+    data = np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli]) for _ in range(3)])
     expect = data.copy()
-    for b in range(2):
+    for b in range(3):
         for i, m in enumerate(moduli):
             ora.ntt_operator(m, n).forward(expect[b, i])
     ctx = fg.Context(moduli, n)
     default = fg.ntt_plan_get(logn)
+    default_cluster = fg.ntt_cluster_get(logn)
     try:
         fg.ntt_plan_set(logn, bl)
+        fg.ntt_cluster_set(logn, bool(cluster))
         t = fg.to_device(data)
         fg.ntt_forward(ctx, t)
         assert np.array_equal(fg.to_host(t), expect)
@@ -73,17 +77,21 @@ def test_ntt_plans_bit_exact(fg, ora, cuda, logn, bl):
         assert np.array_equal(fg.to_host(t), data)
     finally:
         fg.ntt_plan_set(logn, default)
+        fg.ntt_cluster_set(logn, default_cluster)
 
 
 def test_ntt_autotune_installs_a_valid_plan(fg, ora, cuda):
     n = 1 << 14
     ctx = fg.Context(_moduli(ora, n, 2), n)
     default = fg.ntt_plan_get(14)
+    default_cluster = fg.ntt_cluster_get(14)
     try:
         bl = fg.ntt_autotune(ctx, 8)
         assert bl in (12, 13, 14) and fg.ntt_plan_get(14) == bl
+        assert bl == 12 or not fg.ntt_cluster_get(14)
     finally:
         fg.ntt_plan_set(14, default)
+        fg.ntt_cluster_set(14, default_cluster)
 
 
 def test_ntt_lazy_inputs(fg, ora, cuda):

@@ -86,6 +86,56 @@ def test_scaler(fg, ora, cuda, num, den):
             assert np.array_equal(got[k], want.coefficients), rep
 
 
+def _boundary_values(q_from, num, den, n, rng):
+    """n coefficients in [0, Q) at the scaler's rounding boundaries
+    (rns/scaler.rs:249-352): near 0, Q/2 and Q, where the CRT overflow
+    estimate v rounds, and, for a factor num/den other than one, values
+    where x * num / den is within a few units of a half-integer, where w
+    rounds. Both sums then sit next to a rounding boundary, which is where a
+    kernel that keeps only their high words must fall back to the exact sums."""
+    vals = [0, 1, 2, 3, q_from - 1, q_from - 2, q_from - 3] + [q_from // 2 + d for d in range(-4, 5)]
+    if num != den:
+        top = num * q_from // den
+        for u in rng.integers(0, 1 << 62, 64, dtype=np.uint64):
+            m = (int(u) * top) >> 62  # spread over [0, top)
+            x = ((2 * m + 1) * den) // (2 * num)
+            vals += [x + d for d in range(-2, 3) if 0 <= x + d < q_from]
+    vals = [v % q_from for v in vals]
+    rng.shuffle(vals)
+    return (vals * (n // len(vals) + 1))[:n]
+
+
+@pytest.mark.parametrize("setup", ["ring_3001", "ring_t_over_q", "mul_up_6", "mul_down_13", "mul_down_25"])
+def test_scaler_rounding_boundaries(fg, ora, cuda, setup):
+    """Coefficients chosen at the rounding boundaries of RnsScaler::scale, in
+    both representations, for generic and exact-count scaler kernels: the
+    results equal the oracle's exact big-integer computation."""
+    rng = np.random.default_rng(["ring_3001", "ring_t_over_q", "mul_up_6", "mul_down_13", "mul_down_25"].index(setup))
+    n = 4096
+    if setup.startswith("ring"):
+        frm, to = Q, P
+        num, den = (3, 1001) if setup == "ring_3001" else (65537, ora.RnsContext(Q).modulus())
+    else:
+        L = {"mul_up_6": 6, "mul_down_13": 6, "mul_down_25": 12}[setup]
+        n = 16384 if L == 6 else 32768
+        par = ora.BfvParameters(n, 65537, moduli_sizes=[62] * L)
+        ext = ora.Multiplicator.default_extended_basis(par, 0)
+        if setup == "mul_up_6":
+            frm, to, num, den = list(par.moduli), ext, 1, 1
+        else:
+            frm, to, num, den = ext, list(par.moduli), 65537, par.context_at_level(0).modulus()
+    frm_o, to_o = ora.Context(frm, n), ora.Context(to, n)
+    sc_o = ora.Scaler(frm_o, to_o, ora.ScalingFactor(num, den) if num != den else ora.ScalingFactor.one())
+    sc = fg.Scaler(fg.Context(frm, n), fg.Context(to, n),
+                   fg.ScalingFactor(num, den) if num != den else fg.ScalingFactor.one())
+    pb = ora.Poly.from_biguints(frm_o, _boundary_values(frm_o.modulus(), num, den, n, rng))
+    got = fg.to_host(sc.scale(fg.to_device(pb.coefficients[None]), 0))[0]
+    assert np.array_equal(got, sc_o.scale(pb).coefficients)
+    nt = pb.copy().into_ntt()
+    got = fg.to_host(sc.scale(fg.to_device(nt.coefficients[None]), 1))[0]
+    assert np.array_equal(got, sc_o.scale(nt).coefficients)
+
+
 @pytest.mark.parametrize("n,L", [(4096, 2), (16384, 6)])
 def test_mul_scalers(fg, ora, cuda, n, L):
     """The Multiplicator's scalers: extension Q -> Q u P (factor one, common
@@ -107,6 +157,44 @@ def test_mul_scalers(fg, ora, cuda, n, L):
     got = fg.to_host(down.scale(fg.to_device(b), 1))
     for k in range(2):
         assert np.array_equal(got[k], down_o.scale(ora.Poly(mul_o, b[k], ora.NTT)).coefficients)
+
+
+@pytest.mark.parametrize("n", [16, 1 << 14])
+def test_ntt_shoup_representation(fg, ora, cuda, n):
+    """Representation::NttShoup (rq/mod.rs:37-47, 209-223): the Shoup plane
+    equals the oracle's, the NttShoup product (rq/ops.rs:208-245) equals the
+    oracle's, and representation 2 serializes through the power basis and
+    substitutes like Ntt (rq/mod.rs:319-369)."""
+    rng = np.random.default_rng(12)
+    moduli = [m for m in MODULI if ora.supports_ntt(m, n)] or [ora.generate_prime(62, 2 * n, 1 << 62)]
+    moduli = moduli + [ora.generate_prime(40, 2 * n, 1 << 40)]
+    ctx_o, ctx = ora.Context(moduli, n), fg.Context(moduli, n)
+    a, b = _rand(rng, moduli, n, 3), _rand(rng, moduli, n, 3)
+    for k in range(3):  # extreme residues
+        b[k, :, 0] = 0
+        for i, m in enumerate(moduli):
+            b[k, i, 1] = m - 1
+    db = fg.to_device(b)
+    bs = fg.compute_shoup(ctx, db)
+    got_s = fg.to_host(bs)
+    prod = fg.to_host(fg.mul_shoup(ctx, fg.to_device(a), db, bs))
+    for k in range(3):
+        po = ora.Poly(ctx_o, b[k].copy(), ora.NTT_SHOUP)
+        po.compute_coefficients_shoup()
+        assert np.array_equal(got_s[k], po.coefficients_shoup)
+        want = ora.Poly(ctx_o, a[k].copy(), ora.NTT)
+        want.mul_assign(po)
+        assert np.array_equal(prod[k], want.coefficients)
+    payload = fg.serialize(ctx, db, 2)
+    host = payload.cpu().numpy()
+    for k in range(3):
+        pb = ora.Poly(ctx_o, b[k].copy(), ora.NTT).into_power_basis()
+        assert bytes(host[k]) == ora.rq_payload(pb)
+    assert np.array_equal(fg.to_host(fg.deserialize(ctx, payload, 2)), b)
+    ex = ora.SubstitutionExponent(ctx_o, 3)
+    sub = fg.to_host(fg.substitute(ctx, db, 3, 2))
+    for k in range(3):
+        assert np.array_equal(sub[k], ora.Poly(ctx_o, b[k], ora.NTT_SHOUP).substitute(ex).coefficients)
 
 
 def test_scalar_mul(fg, ora, cuda):

@@ -127,7 +127,7 @@ def test_key_message_errors(fg, ora, cuda):
     assert code(c0 + ora._pb_bytes(3, bytes(31))) == fg.ERR_INVALID_ARGUMENT  # seed length
     assert code(c0) == fg.ERR_INVALID_ARGUMENT  # no c1 and no seed
     assert code(c0 + tail + ora._pb_varint(4, 9)) == fg.ERR_INVALID_LEVEL
-    assert code(c0 + tail + ora._pb_varint(6, 30)) == fg.ERR_UNSUPPORTED  # decomposition base
+    assert code(c0 + tail + ora._pb_varint(6, 30)) == fg.ERR_INVALID_ARGUMENT  # decomposition base, levels not maximal
     ntt = b"".join(ora._pb_bytes(1, ora.rq_message(ora.Poly(p.ctx, p.coefficients, ora.NTT)), repeated=True)
                    for p in k.c0)
     assert code(ntt + tail) == fg.ERR_INVALID_ARGUMENT  # Ntt instead of NttShoup
@@ -136,3 +136,43 @@ def test_key_message_errors(fg, ora, cuda):
     assert code(even, fg.GaloisKey) == fg.ERR_INVALID_ARGUMENT
     ok = fg.GaloisKey.from_bytes(s.par, ora.galois_key_message(gk_o))
     assert ok.exponent == 3
+
+
+@pytest.mark.parametrize("n,L", [(16, 3), (4096, 3)])
+def test_key_to_bytes_and_evaluation_key(fg, ora, cuda, n, L):
+    """KeySwitchingKey / RelinearizationKey / GaloisKey::to_bytes from device
+    keys (key_switching_key.rs:332-352) equal the reference's messages, seeded
+    or not and with a decomposition base; EvaluationKey messages
+    (evaluation_key.rs:382-432) decode into working keys and encode back."""
+    s = Setup(fg, ora, n, L, 65537 if n > 16 else 1153, seed=n + 9)
+    for seed in (None, bytes(range(9, 41))):
+        rk_o = ora.RelinearizationKey(s.sk, s.rng, seed=seed)
+        msg = ora.relinearization_key_message(rk_o)
+        if seed:
+            rk = fg.RelinearizationKey.from_seed(s.par, rk_o.ksk.c0_array(), seed)
+        else:
+            rk = fg.RelinearizationKey(s.par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
+        assert rk.to_bytes() == msg
+        assert fg.RelinearizationKey.from_bytes(s.par, msg).to_bytes() == msg
+        gk_o = ora.GaloisKey(s.sk, 2 * n - 1, 1, 0, s.rng, seed=seed)
+        gmsg = ora.galois_key_message(gk_o)
+        assert fg.GaloisKey.from_bytes(s.par, gmsg).to_bytes() == gmsg
+        assert fg.KeySwitchingKey.from_bytes(s.par, ora.ksk_message(gk_o.ksk)).to_bytes() == ora.ksk_message(gk_o.ksk)
+    last = L - 1
+    dk_o = ora.GaloisKey(s.sk, 3, last, last, s.rng)
+    dk = fg.GaloisKey(s.par, 3, dk_o.ksk.c0_array(), dk_o.ksk.c1_array(), last, last)
+    assert dk.to_bytes() == ora.galois_key_message(dk_o)
+    # EvaluationKey at (ciphertext level 1, key level 0).
+    gks_o = [ora.GaloisKey(s.sk, ora.rotation_exponent(s.par_o, i), 1, 0, s.rng, seed=bytes([i]) * 32)
+             for i in (1, 2)] + [ora.GaloisKey(s.sk, 2 * n - 1, 1, 0, s.rng)]
+    emsg = ora.evaluation_key_message(gks_o, 1, 0)
+    keys, cl, el = fg.evaluation_key_from_bytes(s.par, emsg)
+    assert (cl, el) == (1, 0) and [k.exponent for k in keys] == [g.element.exponent for g in gks_o]
+    _, cts = s.encrypt(1, level=1)
+    ct = fg.to_device(cts[0].to_array()[None])
+    for k, g in zip(keys, gks_o):
+        assert np.array_equal(fg.to_host(k.relinearize(ct))[0], g.relinearize(cts[0]).to_array())
+    assert fg.evaluation_key_to_bytes(keys, 1, 0) == emsg
+    with pytest.raises(fg.FhegError) as e:  # a key at other levels than the message names
+        fg.evaluation_key_from_bytes(s.par, ora.evaluation_key_message(gks_o, 1, 1))
+    assert e.value.code == fg.ERR_INVALID_ARGUMENT

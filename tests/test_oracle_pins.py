@@ -228,6 +228,47 @@ def test_multiplicator_decrypts(ora, L):
         assert list(sk.decrypt(ct3).decode("simd")) == list(expected)
 
 
+def test_key_switch_decomposition(ora):
+    """key_switching_key.rs:529-561 (default_arc(6, 16), level 5: a single
+    modulus, so the key switches by base-2^31 digits): c0 + c1 s - input * p
+    stays within half the modulus' bits plus 10 (the same bound)."""
+    rng = np.random.default_rng(530)
+    par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 6)
+    ctx = par.context_at_level(5)
+    for _ in range(20):
+        sk = ora.SecretKey.random(par, rng)
+        p = ora.Poly.small(ctx, ora.POWER_BASIS, 10, rng)
+        ksk = ora.KeySwitchingKey(sk, p, 5, 5, rng)
+        assert ksk.log_base == 31 and len(ksk.c0) == 2
+        s = sk.s_ntt(ctx)
+        inp = ora.Poly.random(ctx, ora.POWER_BASIS, rng)
+        c0, c1 = ksk.key_switch(inp)
+        c2 = (c0 + c1 * s).into_power_basis()
+        c3 = (inp.copy().into_ntt() * p.copy().into_ntt()).into_power_basis()
+        q = ctx.modulus()
+        for b in (c2 - c3).to_biguints():
+            assert min(b.bit_length(), (q - b).bit_length()) <= q.bit_length() // 2 + 10
+
+
+@pytest.mark.parametrize("n,L,threads", [(16, 3, 1), (4096, 2, 3), (8192, 3, 2)])
+def test_multiply_driver_equals_orchestrated_oracle(ora, n, L, threads):
+    """The whole-product C++ loop of the timed CPU baseline (ops/mul.rs:158-227
+    on host threads) equals the orchestrated oracle Multiplicator, product by
+    product."""
+    t = 1153 if n == 16 else 65537
+    rng = np.random.default_rng(n + L)
+    par = ora.BfvParameters(n, t, moduli_sizes=[62] * L)
+    sk = ora.SecretKey.random(par, rng)
+    m = ora.Multiplicator.default(ora.RelinearizationKey(sk, rng))
+    cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, t, n, dtype=np.uint64), "simd", par), rng)
+           for _ in range(6)]
+    lhs = np.stack([c.to_array() for c in cts[:3]])
+    rhs = np.stack([c.to_array() for c in cts[3:]])
+    got = ora.MultiplyDriver(m).multiply(lhs, rhs, threads)
+    for k in range(3):
+        assert np.array_equal(got[k], m.multiply(cts[k], cts[3 + k]).to_array()), k
+
+
 @pytest.mark.parametrize("L", [2, 8])
 def test_rgsw_external_product_decrypts(ora, L):
     """rgsw_ciphertext.rs:172-210 (default_arc(2, 16) and (8, 16)): ct1 x
@@ -427,18 +468,23 @@ def _proto_classes():
     gk = fd.message_type.add(name="GaloisKey")
     gk.field.add(name="ksk", number=1, type=F.TYPE_MESSAGE, type_name=".pin.KeySwitchingKey", label=F.LABEL_OPTIONAL)
     gk.field.add(name="exponent", number=2, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    ek = fd.message_type.add(name="EvaluationKey")
+    ek.field.add(name="gk", number=2, type=F.TYPE_MESSAGE, type_name=".pin.GaloisKey", label=F.LABEL_REPEATED)
+    ek.field.add(name="ciphertext_level", number=3, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
+    ek.field.add(name="evaluation_key_level", number=4, type=F.TYPE_UINT32, label=F.LABEL_OPTIONAL)
     pool = descriptor_pool.DescriptorPool()
     pool.Add(fd)
     get = message_factory.GetMessageClass
     return (get(pool.FindMessageTypeByName("pin.Rq")), get(pool.FindMessageTypeByName("pin.Ciphertext")),
-            get(pool.FindMessageTypeByName("pin.KeySwitchingKey")), get(pool.FindMessageTypeByName("pin.GaloisKey")))
+            get(pool.FindMessageTypeByName("pin.KeySwitchingKey")), get(pool.FindMessageTypeByName("pin.GaloisKey")),
+            get(pool.FindMessageTypeByName("pin.EvaluationKey")))
 
 
 def test_protobuf_framing_pinned(ora):
     """The oracle's Rq / Ciphertext encoding equals the protobuf package's for
     the same field values (seeded and unseeded, levels 0 and 1, the variable
     time flag), and its decoder inverts it."""
-    Rq, Ct, _, _ = _proto_classes()
+    Rq, Ct, _, _, _ = _proto_classes()
     rng = np.random.default_rng(41)
     par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3)
     sk = ora.SecretKey.random(par, rng)
@@ -466,7 +512,7 @@ def test_protobuf_framing_pinned(ora):
 def test_key_messages_pinned(ora):
     """KeySwitchingKey / GaloisKey encoding (key_switching_key.rs:332-352,
     galois_key.rs:127-134) equals the protobuf package's, seeded and not."""
-    Rq, _, Ksk, Gk = _proto_classes()
+    Rq, _, Ksk, Gk, Ek = _proto_classes()
     rng = np.random.default_rng(43)
     par = ora.BfvParameters(16, 1153, moduli_sizes=[62] * 3)
     sk = ora.SecretKey.random(par, rng)
@@ -482,3 +528,12 @@ def test_key_messages_pinned(ora):
                    ciphertext_level=1, ksk_level=0)
         assert ora.ksk_message(k) == want.SerializeToString()
         assert ora.galois_key_message(gk) == Gk(ksk=want, exponent=3).SerializeToString()
+    # A decomposition key (single-modulus context: log_base 31) and an
+    # EvaluationKey of two Galois keys (evaluation_key.rs:382-392).
+    dk = ora.GaloisKey(sk, 5, 2, 2, rng).ksk
+    assert ora.ksk_message(dk) == Ksk(c0=[rq(p).SerializeToString() for p in dk.c0],
+                                      c1=[rq(p).SerializeToString() for p in dk.c1], ciphertext_level=2,
+                                      ksk_level=2, log_base=31).SerializeToString()
+    gks = [ora.GaloisKey(sk, e, 1, 0, rng) for e in (3, 2 * 16 - 1)]
+    want = Ek(gk=[Gk.FromString(ora.galois_key_message(g)) for g in gks], ciphertext_level=1, evaluation_key_level=0)
+    assert ora.evaluation_key_message(gks, 1, 0) == want.SerializeToString()

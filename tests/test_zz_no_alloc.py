@@ -14,27 +14,30 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _ct3_batch(ora, par, sk, rng, count):
+def _ct3_batch(ora, par, sk, rng, count, level=0):
     cts = []
     for _ in range(count):
         vals = rng.integers(0, par.plaintext, par.degree, dtype=np.uint64)
-        a = sk.encrypt(ora.Plaintext.encode(vals, "simd", par), rng)
-        b = sk.encrypt(ora.Plaintext.encode(vals, "simd", par), rng)
+        a = sk.encrypt(ora.Plaintext.encode(vals, "simd", par, level), rng)
+        b = sk.encrypt(ora.Plaintext.encode(vals, "simd", par, level), rng)
         cts.append((a * b).to_array())
     return np.stack(cts)
 
 
-def test_relinearize_noalloc_matches_relinearize(fg, ora, cuda):
-    rng = np.random.default_rng(404)
+# (ciphertext level, key level): a key at the ciphertext's level, and a key one
+# level below it, whose key switch also switches down.
+@pytest.mark.parametrize("ct_level,key_level", [(0, 0), (1, 0)])
+def test_relinearize_noalloc_matches_relinearize(fg, ora, cuda, ct_level, key_level):
+    rng = np.random.default_rng(404 + ct_level)
     par_o = ora.BfvParameters(4096, 65537, moduli_sizes=[62, 62, 62])
     sk = ora.SecretKey.random(par_o, rng)
-    rk_o = ora.RelinearizationKey(sk, rng)
+    rk_o = ora.RelinearizationKey(sk, rng, ct_level, key_level)
     par = fg.BfvParameters(4096, par_o.moduli, 65537)
-    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
+    rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array(), ct_level, key_level)
     lib = fg.lib()
     stream = cuda.cuda.current_stream().cuda_stream
     for call in range(2):
-        ct3 = fg.to_device(_ct3_batch(ora, par_o, sk, rng, 3))
+        ct3 = fg.to_device(_ct3_batch(ora, par_o, sk, rng, 3, ct_level))
         expected = rk.relinearizes(ct3)
         out = fg.empty(expected.shape)
         fg.check(lib.fheg_relinearize_noalloc(rk._h, ct3.data_ptr(), out.data_ptr(), 3, stream))
