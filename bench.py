@@ -202,6 +202,46 @@ def make_inputs(ora, batch: int, seed: int = 2026, distinct: int = 16):
     return par, sk, rk, cts, lhs, rhs
 
 
+def measure_mixed_levels(fg, ora, torch, par_o, sk, per_level: int = 16, reps: int = 20):
+    """A 64-pair batch spread over levels 0-3 (16 pairs each, the level-2
+    group relinearized by a key at level 0, which switches down after the key
+    switch), issued as one multiply_groups call: one multiplicator per level,
+    the groups overlapping on side streams. The first product of every group
+    is checked against the oracle before timing."""
+    rng = np.random.default_rng(77)
+    par = fg.BfvParameters(N, par_o.moduli, T)
+    mults, lhs, rhs, first = [], [], [], []
+    for lvl, klvl in [(0, 0), (1, 1), (2, 0), (3, 3)]:
+        rk_o = ora.RelinearizationKey(sk, rng, lvl, klvl)
+        rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array(), lvl, klvl)
+        mults.append(fg.Multiplicator.default(rk))
+        cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, N, dtype=np.uint64), "simd", par_o, lvl), rng)
+               for _ in range(4)]
+        arrs = [c.to_array() for c in cts]
+        lhs.append(fg.to_device(np.stack([arrs[i % 4] for i in range(per_level)])))
+        rhs.append(fg.to_device(np.stack([arrs[(i + 1) % 4] for i in range(per_level)])))
+        first.append((ora.Multiplicator.default(rk_o), cts[0], cts[1]))
+    outs = fg.multiply_groups(mults, lhs, rhs)
+    torch.cuda.synchronize()
+    for g, (mo, a, b) in enumerate(first):
+        if not np.array_equal(fg.to_host(outs[g][:1])[0], mo.multiply(a, b).to_array()):
+            raise SystemExit(f"bench: mixed-level group {g} is not bit-exact with the oracle")
+    for _ in range(3):
+        fg.multiply_groups(mults, lhs, rhs, outs)
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(reps):
+        fg.multiply_groups(mults, lhs, rhs, outs)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / reps
+    return {"value": 4 * per_level / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
+            "note": f"{4 * per_level} pairs at levels 0-3 ({per_level} each; level 2 with its key at level 0) "
+                    "in one multiply_groups call"}
+
+
 def max_over_ranks(ms: float, dist) -> float:
     """The slowest rank's step time (replicas: every rank runs its own batch)."""
     import torch
@@ -307,6 +347,7 @@ def run_ours(args, rank: int, world: int):
     par = fg.BfvParameters(N, par_o.moduli, T)
     rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
     mult = fg.Multiplicator.default(rk)
+    fg.rns_tensor_set(args.rns_tensor == "on")
     lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
     out_d = fg.empty((B, 2, L, N))
     stream = torch.cuda.current_stream()
@@ -435,6 +476,8 @@ def run_ours(args, rank: int, world: int):
     bfly = polys * L * butterflies_per_transform(logn)
     need_60 = 0.6 * peak * 1e9 / (data_bytes + tw_bytes) * bfly
 
+    mixed = measure_mixed_levels(fg, ora, torch, par_o, sk)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(ora, rk_o, cts, args.cpu_seconds)
@@ -452,7 +495,9 @@ def run_ours(args, rank: int, world: int):
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded encryptions by the CPU oracle)",
             "config": {"workload": "bfv_mul_relin_batched", "degree": N, "moduli": L, "moduli_bits": 62,
                        "extension_moduli": 7, "plaintext": T, "batch_pairs": B, "keys": "device resident",
-                       "ntt_block_logn": ntt_block, "step": f"one CUDA graph of {graph.kernels} kernels"
+                       "ntt_block_logn": ntt_block, "rns_scaling": "tensor cores (tcgen05 byte-sliced products)"
+                       if args.rns_tensor == "on" else "CUDA cores",
+                       "step": f"one CUDA graph of {graph.kernels} kernels"
                        + (f" (two concurrent branches of {B // 2} and {B - B // 2} pairs)" if B >= 32 else ""),
                        "l2": "no flush: each step streams > 1 GB (inputs 201 MB, outputs 100 MB, scratch) through "
                              "the 126 MB L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
@@ -460,6 +505,7 @@ def run_ours(args, rank: int, world: int):
             "direct_calls": {"value": B / (direct_ms / 1000.0), "unit": UNIT, "ms_per_step": direct_ms,
                              "note": "the batch without the graph"},
             "batch_vs_single": value / world / single_rate,
+            "mixed_levels": mixed,
             "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
                     "d2h_bytes_per_step": int(h_o.nbytes)},
             "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
@@ -517,11 +563,14 @@ def run_stages(args):
         mult.plan = [int(x) for x in args.stage_plan.split(",")]
     lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
     out_d = fg.empty((B, 2, L, N))
+    fg.rns_tensor_set(args.rns_tensor == "on")
     for _ in range(args.warmup):
         mult.multiply(lhs_d, rhs_d, out_d)
-    ms = mult.stage_times(lhs_d, rhs_d, out_d)
+    runs = [mult.stage_times(lhs_d, rhs_d, out_d) for _ in range(max(1, args.stage_runs))]
+    ms = {k: statistics.median(r[k] for r in runs) for k in runs[0]}
     torch.cuda.synchronize()
-    print(json.dumps({"workload": "stages", "batch_pairs": B, "plan": mult.plan, "stage_ms": ms}), flush=True)
+    print(json.dumps({"workload": "stages", "batch_pairs": B, "plan": mult.plan, "rns_tensor": args.rns_tensor,
+                      "runs": len(runs), "stage_ms": ms}), flush=True)
 
 
 def run_codec(args):
@@ -1217,6 +1266,9 @@ def main():
                     help="L2 prefetch of the next CTA's NTT input")
     ap.add_argument("--stage-plan", default="", help="A,C,D,F,F-split,D-split plan of the multiply stages")
     ap.add_argument("--ntt-block", default="auto", help="NTT plan for the degree: auto (autotune) or a block log2")
+    ap.add_argument("--rns-tensor", default="on", choices=["on", "off"],
+                    help="RNS scalings of the multiplication on the tensor cores (on) or the CUDA cores (off)")
+    ap.add_argument("--stage-runs", type=int, default=1, help="stages workload: median over this many runs")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-budget-gb", type=float, default=24.0)
     ap.add_argument("--serve-streams", type=int, default=4)

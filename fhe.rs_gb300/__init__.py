@@ -98,6 +98,9 @@ def _declare(L):
         "fheg_poly_mul_shoup": (i, [c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
         "fheg_ntt_cluster_set": (i, [ctypes.c_uint32, i]),
         "fheg_ntt_cluster_get": (i, [ctypes.c_uint32, ctypes.POINTER(i)]),
+        "fheg_rns_tensor_set": (i, [i]),
+        "fheg_rns_tensor_get": (i, [ctypes.POINTER(i)]),
+        "fheg_rns_tensor_wait_failures": (i, [ctypes.POINTER(c_u64)]),
         "fheg_intpeak": (i, [i, c_size, ctypes.c_uint32, c_vp, c_vp, ctypes.POINTER(ctypes.c_double)]),
         "fheg_generate_prime": (i, [ctypes.c_uint32, c_u64, c_u64, P_u64]),
         "fheg_supports_ntt": (i, [c_u64, c_size]),
@@ -416,6 +419,24 @@ def ntt_cluster_get(logn: int) -> bool:
     out = ctypes.c_int(0)
     check(lib().fheg_ntt_cluster_get(logn, ctypes.byref(out)))
     return bool(out.value)
+
+
+def rns_tensor_set(on: bool):
+    """Tensor-core form of the exact RNS scalings (see fheg.h; on by default)."""
+    check(lib().fheg_rns_tensor_set(int(on)))
+
+
+def rns_tensor_get() -> bool:
+    out = ctypes.c_int(0)
+    check(lib().fheg_rns_tensor_get(ctypes.byref(out)))
+    return bool(out.value)
+
+
+def rns_tensor_wait_failures() -> int:
+    """Bounded waits of the tensor-core scaler that ran out (0 when healthy)."""
+    out = c_u64(0)
+    check(lib().fheg_rns_tensor_wait_failures(ctypes.byref(out)))
+    return out.value
 
 
 def ntt_plan_get(logn: int) -> int:

@@ -20,7 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = GENCODE + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                         "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
-SOURCES = ["host_math.cpp", "ops.cu", "bfv.cu", "api.cu", "noalloc.cu", "serve.cu", "graph.cu", "codec.cu", "compose.cu", "serialize.cu", "seeded.cu", "intpeak.cu"]
+SOURCES = ["host_math.cpp", "ops.cu", "scale.cu", "bfv.cu", "api.cu", "noalloc.cu", "serve.cu", "graph.cu", "codec.cu", "compose.cu", "serialize.cu", "seeded.cu", "intpeak.cu"]
 
 
 def _nvcc():

@@ -173,6 +173,24 @@ FHEG_API int fheg_ntt_cluster_get(uint32_t logn, int* on) {
   });
 }
 
+FHEG_API int fheg_rns_tensor_set(int on) {
+  return abi_call([&] { set_rns_tc(on != 0); });
+}
+
+FHEG_API int fheg_rns_tensor_get(int* on) {
+  return abi_call([&] {
+    abi_need(on, "null output");
+    *on = rns_tc_enabled() ? 1 : 0;
+  });
+}
+
+FHEG_API int fheg_rns_tensor_wait_failures(uint64_t* count) {
+  return abi_call([&] {
+    abi_need(count, "null output");
+    *count = rns_tc_wait_failures();
+  });
+}
+
 FHEG_API int fheg_ntt_plan_get(uint32_t logn, uint32_t* block_logn) {
   return abi_call([&] {
     abi_need(block_logn && logn >= 3 && logn <= 16, "bad size or null output");

@@ -89,7 +89,14 @@ struct RnsScalerD {
   // modulus is odd (mont).
   bool mont = false;
   std::vector<uint64_t> omega_mont, gamma_neg_mont, gamma_neg_hi_mont, to_pinv;
+  // Byte matrix of the tensor-core form (scale.cu), with its padded width;
+  // empty when that form does not apply.
+  DevBuf tc_mat;
+  uint32_t tc_kp = 0;
   RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den);
+
+ private:
+  void build_tc_matrix();
 };
 
 // rq::Scaler (fhe-math/src/rq/scaler.rs:17-23).
@@ -151,6 +158,11 @@ struct ForwardTop {
 // first stages of the forward NTT that consumes them.
 void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
                uint64_t polys, cudaStream_t st, const InverseTop* top = nullptr, const ForwardTop* fwd = nullptr);
+// Whether exact RNS scalings run on the tensor cores (default on), and the
+// count of that form's bounded waits that ran out since the process started.
+bool rns_tc_enabled();
+void set_rns_tc(bool on);
+uint64_t rns_tc_wait_failures();
 bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1);
 // Scaler::scale. `scratch` must hold polys * max(L_from, L_to) * N words.
 void scaler_scale(const Scaler& s, bool ntt, PolyRef in, PolyRef out, uint64_t polys, uint64_t* scratch,

@@ -1,5 +1,5 @@
-// Ring-level operations: contexts, NTTs, element-wise ops, substitution,
-// modulus switch-down and RNS scaling (fhe-math `rq`, `ntt`, `rns`).
+// Ring-level operations: contexts, NTTs, element-wise ops, substitution and
+// modulus switch-down (fhe-math `rq`, `ntt`); RNS scaling is in scale.cu.
 
 #include <algorithm>
 #include <cstring>
@@ -411,673 +411,6 @@ void poly_switch_down_ntt(const Context& ctx, PolyRef in, PolyRef out, uint64_t 
   ntt_backward(ctx, in, in, polys, st);
   NttGeom g{ctx.primes_dev(), c.lm1, 0};
   ntt_forward_any<true>(ctx.logn, g, polys, SrcSwitchDown{in, c}, DstPoly{out}, st);
-}
-
-// ---------------------------------------------------------------------------
-// RNS scaling (rns/scaler.rs:249-352), one thread per coefficient.
-//
-// The reference accumulates in wrapping 256-bit integers; the sums here are
-// the same integers accumulated exactly in 32-bit words:
-//   G = sum_k r_k * theta_garner_k           (< 2^192 by the choice of shift)
-//   O = sum_k (+/-) r_k * theta_omega_k - (+/-) v * theta_gamma   (mod 2^256)
-// and each output residue is one exact dot product reduced once:
-//   y_j = sum_k r_k * omega_jk + v_j * (q_j - gamma_j) + w_term  (mod q_j),
-// which equals the reference's lazily reduced sum modulo q_j.
-
-__device__ __forceinline__ uint64_t join(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
-
-// Low 128 bits of (w >> s) for an nw-word little-endian value (32-bit words).
-__device__ __forceinline__ void shr_words(const uint32_t* w, int nw, uint32_t s, uint64_t* lo, uint64_t* hi) {
-  uint32_t o[4];
-  const uint32_t ws = s >> 5, bs = s & 31;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const uint32_t idx = ws + k;
-    uint32_t a = 0, b = 0;
-#pragma unroll
-    for (int m = 0; m < 8; m++) {
-      if (m < nw && (uint32_t)m == idx) a = w[m];
-      if (m < nw && (uint32_t)m == idx + 1) b = w[m];
-    }
-    o[k] = bs ? ((a >> bs) | (b << (32 - bs))) : a;
-  }
-  *lo = join(o[0], o[1]);
-  *hi = join(o[2], o[3]);
-}
-
-// 256-bit a += b, a -= b (32-bit words).
-__device__ __forceinline__ void add256w(uint32_t* a, const uint32_t* b) {
-  asm("add.cc.u32 %0, %0, %8;\n\taddc.cc.u32 %1, %1, %9;\n\taddc.cc.u32 %2, %2, %10;\n\taddc.cc.u32 %3, %3, %11;\n\t"
-      "addc.cc.u32 %4, %4, %12;\n\taddc.cc.u32 %5, %5, %13;\n\taddc.cc.u32 %6, %6, %14;\n\taddc.u32 %7, %7, %15;"
-      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
-}
-
-__device__ __forceinline__ void sub256w(uint32_t* a, const uint32_t* b) {
-  asm("sub.cc.u32 %0, %0, %8;\n\tsubc.cc.u32 %1, %1, %9;\n\tsubc.cc.u32 %2, %2, %10;\n\tsubc.cc.u32 %3, %3, %11;\n\t"
-      "subc.cc.u32 %4, %4, %12;\n\tsubc.cc.u32 %5, %5, %13;\n\tsubc.cc.u32 %6, %6, %14;\n\tsubc.u32 %7, %7, %15;"
-      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
-}
-
-// High parts of the scaler's sums. The sums only matter at bit 96 and above
-// (v needs G >> (shift - 1) with shift >= 123, w needs S >> 126), so the
-// fast path adds only the partial products x_i b_j (32-bit words) that
-// reach word 3: those with i + j >= 3, and the high halves of those with
-// i + j = 2. The rest of a term x * b (x < 2^64, b < 2^128) is below
-// 2^64 + 4 * 2^96 < 5 * 2^96, so a sum of F such terms is its kept part (a
-// multiple of 2^96) plus less than 5F * 2^96; a result whose kept part is
-// that close to a rounding boundary is recomputed exactly.
-//
-// h[0..NH) are words 3 .. 2 + NH of the sum: NH = 3 for a sum below 2^192,
-// NH = 5 for a sum taken modulo 2^256.
-template <int NH>
-__device__ __forceinline__ void mac_hi(uint32_t* h, uint64_t x, uint64_t blo, uint64_t bhi) {
-  static_assert(NH == 3 || NH == 5, "three or five high words");
-  if constexpr (NH == 3) {
-    asm("{\n\t"
-        ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
-        "mov.b64 {x0, x1}, %3;\n\t"
-        "mov.b64 {b0, b1}, %4;\n\t"
-        "mov.b64 {b2, b3}, %5;\n\t"
-        "mad.hi.cc.u32 %0, x0, b2, %0;\n\t"
-        "madc.hi.cc.u32 %1, x0, b3, %1;\n\t"
-        "madc.hi.u32 %2, x1, b3, %2;\n\t"
-        "mad.lo.cc.u32 %0, x0, b3, %0;\n\t"
-        "madc.lo.cc.u32 %1, x1, b3, %1;\n\t"
-        "addc.u32 %2, %2, 0;\n\t"
-        "mad.hi.cc.u32 %0, x1, b1, %0;\n\t"
-        "madc.hi.cc.u32 %1, x1, b2, %1;\n\t"
-        "addc.u32 %2, %2, 0;\n\t"
-        "mad.lo.cc.u32 %0, x1, b2, %0;\n\t"
-        "addc.cc.u32 %1, %1, 0;\n\t"
-        "addc.u32 %2, %2, 0;\n\t"
-        "}"
-        : "+r"(h[0]), "+r"(h[1]), "+r"(h[2])
-        : "l"(x), "l"(blo), "l"(bhi));
-  } else {
-    asm("{\n\t"
-        ".reg .u32 x0, x1, b0, b1, b2, b3;\n\t"
-        "mov.b64 {x0, x1}, %5;\n\t"
-        "mov.b64 {b0, b1}, %6;\n\t"
-        "mov.b64 {b2, b3}, %7;\n\t"
-        "mad.hi.cc.u32 %0, x0, b2, %0;\n\t"
-        "madc.hi.cc.u32 %1, x0, b3, %1;\n\t"
-        "madc.hi.cc.u32 %2, x1, b3, %2;\n\t"
-        "addc.cc.u32 %3, %3, 0;\n\t"
-        "addc.u32 %4, %4, 0;\n\t"
-        "mad.lo.cc.u32 %0, x0, b3, %0;\n\t"
-        "madc.lo.cc.u32 %1, x1, b3, %1;\n\t"
-        "addc.cc.u32 %2, %2, 0;\n\t"
-        "addc.cc.u32 %3, %3, 0;\n\t"
-        "addc.u32 %4, %4, 0;\n\t"
-        "mad.hi.cc.u32 %0, x1, b1, %0;\n\t"
-        "madc.hi.cc.u32 %1, x1, b2, %1;\n\t"
-        "addc.cc.u32 %2, %2, 0;\n\t"
-        "addc.cc.u32 %3, %3, 0;\n\t"
-        "addc.u32 %4, %4, 0;\n\t"
-        "mad.lo.cc.u32 %0, x1, b2, %0;\n\t"
-        "addc.cc.u32 %1, %1, 0;\n\t"
-        "addc.cc.u32 %2, %2, 0;\n\t"
-        "addc.cc.u32 %3, %3, 0;\n\t"
-        "addc.u32 %4, %4, 0;\n\t"
-        "}"
-        : "+r"(h[0]), "+r"(h[1]), "+r"(h[2]), "+r"(h[3]), "+r"(h[4])
-        : "l"(x), "l"(blo), "l"(bhi));
-  }
-}
-
-// Words 3..7 of v * theta_gamma for v < 2^96 (vlo, vhi, vhi < 2^32), kept
-// as in mac_hi: the low 64 bits of v through mac_hi (dropping less than
-// 5 * 2^96), the third word's partial products at word 2 and above (dropping
-// the low half of its lowest one, less than 2^96).
-__device__ __forceinline__ void mul_v_hi(uint32_t* h, uint64_t vlo, uint64_t vhi, uint64_t blo, uint64_t bhi) {
-#pragma unroll
-  for (int k = 0; k < 5; k++) h[k] = 0;
-  mac_hi<5>(h, vlo, blo, bhi);
-  asm("{\n\t"
-      ".reg .u32 v2, b0, b1, b2, b3;\n\t"
-      "cvt.u32.u64 v2, %5;\n\t"
-      "mov.b64 {b0, b1}, %6;\n\t"
-      "mov.b64 {b2, b3}, %7;\n\t"
-      "mad.hi.cc.u32 %0, v2, b0, %0;\n\t"
-      "madc.hi.cc.u32 %1, v2, b1, %1;\n\t"
-      "madc.hi.cc.u32 %2, v2, b2, %2;\n\t"
-      "madc.hi.cc.u32 %3, v2, b3, %3;\n\t"
-      "addc.u32 %4, %4, 0;\n\t"
-      "mad.lo.cc.u32 %0, v2, b1, %0;\n\t"
-      "madc.lo.cc.u32 %1, v2, b2, %1;\n\t"
-      "madc.lo.cc.u32 %2, v2, b3, %2;\n\t"
-      "addc.cc.u32 %3, %3, 0;\n\t"
-      "addc.u32 %4, %4, 0;\n\t"
-      "}"
-      : "+r"(h[0]), "+r"(h[1]), "+r"(h[2]), "+r"(h[3]), "+r"(h[4])
-      : "l"(vhi), "l"(blo), "l"(bhi));
-}
-
-// 160-bit a += b, a -= b (32-bit words).
-__device__ __forceinline__ void add160w(uint32_t* a, const uint32_t* b) {
-  asm("add.cc.u32 %0, %0, %5;\n\taddc.cc.u32 %1, %1, %6;\n\taddc.cc.u32 %2, %2, %7;\n\taddc.cc.u32 %3, %3, %8;\n\t"
-      "addc.u32 %4, %4, %9;"
-      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4])
-      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]));
-}
-
-__device__ __forceinline__ void sub160w(uint32_t* a, const uint32_t* b) {
-  asm("sub.cc.u32 %0, %0, %5;\n\tsubc.cc.u32 %1, %1, %6;\n\tsubc.cc.u32 %2, %2, %7;\n\tsubc.cc.u32 %3, %3, %8;\n\t"
-      "subc.u32 %4, %4, %9;"
-      : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4])
-      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]));
-}
-
-// Full 128 x 128 -> 256-bit product (32-bit words).
-__device__ __forceinline__ void mul128x128w(uint32_t* r, uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
-#pragma unroll
-  for (int k = 0; k < 8; k++) r[k] = 0;
-  uint32_t t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  mac256(t, alo, blo, bhi);  // alo * b at word 0
-  uint32_t hi6[6] = {0, 0, 0, 0, 0, 0};
-  mac192(hi6, ahi, blo, bhi);  // ahi * b at word 2 (< 2^192)
-  uint32_t u[8] = {0, 0, hi6[0], hi6[1], hi6[2], hi6[3], hi6[4], hi6[5]};
-  add256w(t, u);
-#pragma unroll
-  for (int k = 0; k < 8; k++) r[k] = t[k];
-}
-
-// All constants of one launch travel in the kernel's parameter space, so
-// every multiply-add reads its constant operand straight from the constant
-// bank (fully unrolled loops give compile-time offsets). Outputs are limbs
-// start .. start + out_len of the target; the rows of omega, gamma and the
-// primes are pre-sliced on the host so output o uses row o.
-//
-// Kernels with an exact source count (EXACT) take odd target moduli, with
-// omega, gamma_neg and gamma_neg_hi in Montgomery form (times 2^64 mod q_j):
-// the exact sum S is then 2^64 times the output's sum, and one Montgomery
-// step divides it back out (mont_fold), with about a third of the multiplies
-// of a 128-bit Barrett reduction. The generic kernels take plain constants
-// and reduce S by Barrett (any moduli).
-template <int MAXF, int MAXT>
-struct RnsLaunch {
-  uint32_t from_len, out_len, is_one, shift;
-  uint32_t tg_sign, to_sign;  // to_sign: bit k = sign of theta_omega_k
-  uint64_t tg_lo, tg_hi;
-  uint64_t tgar_lo[MAXF], tgar_hi[MAXF];
-  uint64_t to_lo[MAXF], to_hi[MAXF];
-  uint64_t omega[MAXT][MAXF];
-  uint64_t gamma_neg[MAXT];     // (q_j - gamma_j) mod q_j
-  uint64_t gamma_neg_hi[MAXT];  // gamma_neg * 2^62 mod q_j
-  uint64_t p[MAXT], bhi[MAXT], blo[MAXT];
-  uint64_t pinv[MAXT];  // -q_j^-1 mod 2^64 (EXACT)
-  // w mod q_j as whi * (2^64 mod q_j) + wlo (EXACT): the Shoup companions of
-  // 2^64 mod q_j and of 1, and wbig = every q_j above 2^61 (wlo < 8 q_j).
-  uint32_t wbig;
-  uint64_t r64[MAXT], r64_shoup[MAXT], one_shoup[MAXT];
-};
-
-
-// EXACT: the source count is MAXF itself (a compile-time constant), so the
-// unrolled loops carry no predicated-off terms; used for the counts the
-// default multiplications produce (L and 2L + 1 source moduli).
-//
-// TOP > 0: `in` holds the block pass of a two-pass inverse NTT whose last TOP
-// strided stages and final scale have not run. Each CTA of 128 threads then
-// owns the 128 coefficients b + t * 2^(logn - TOP) of 128 >> TOP groups b
-// (t < 2^TOP); it applies those stages to every source limb of its groups
-// (inv_top_stages, the strided inverse pass's arithmetic) into shared memory,
-// and each thread scales one coefficient from there. The strided pass and
-// its round trip through HBM disappear; the results are the same.
-//
-// With TOP > 0 and fwd_primes set, the outputs are themselves the input of a
-// two-pass forward NTT whose strided first TOP stages this kernel applies
-// (fwd_top_stages, output limb o in fwd_primes[o]): they go through shared
-// memory so that each group's 2^TOP coefficients meet, and leave lazy in
-// [0, 4p) for the block pass.
-template <int WORDS>
-__device__ __forceinline__ uint64_t* rns_stage_buffer() {
-  __shared__ uint64_t buf[WORDS];
-  return buf;
-}
-
-// Forward stages of the kernel's epilogue (ForwardTop for one launch; primes
-// null: none).
-struct FwdEpilogue {
-  const DevPrime* primes;
-  uint32_t period, take;
-  const DevPrime* digit_primes;
-  uint32_t digit_limbs, digit_raw;
-  PolyRef digits;
-};
-
-// The exact sums of the rare coefficients whose fast high-word sums sit next
-// to a rounding boundary, kept out of line so that the hot kernel body stays
-// small in the instruction cache: G (six words) and S (eight words, mod
-// 2^256) as the reference accumulates them.
-template <int MAXF, int MAXT>
-__device__ __noinline__ void rns_exact_g(const RnsLaunch<MAXF, MAXT>* s, const uint64_t* r, uint32_t F, uint32_t* g) {
-#pragma unroll 1
-  for (int k = 0; k < 6; k++) g[k] = 0;
-#pragma unroll 1
-  for (uint32_t k = 0; k < F; k++) mac192(g, r[k], s->tgar_lo[k], s->tgar_hi[k]);
-}
-
-template <int MAXF, int MAXT>
-__device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const uint64_t* r, uint32_t F, uint64_t vlo,
-                                        uint64_t vhi, uint32_t* pos) {
-  uint32_t neg[8];
-#pragma unroll 1
-  for (int k = 0; k < 8; k++) pos[k] = neg[k] = 0;
-#pragma unroll 1
-  for (uint32_t k = 0; k < F; k++) {
-    if ((s->to_sign >> k) & 1) mac256(neg, r[k], s->to_lo[k], s->to_hi[k]);
-    else mac256(pos, r[k], s->to_lo[k], s->to_hi[k]);
-  }
-  sub256w(pos, neg);
-  uint32_t vt[8];
-  mul128x128w(vt, vlo, vhi, s->tg_lo, s->tg_hi);
-  if (s->tg_sign) add256w(pos, vt);
-  else sub256w(pos, vt);
-}
-
-template <int MAXF, int MAXT, bool EXACT, int TOP>
-__global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
-                                                   PolyRef in, PolyRef out, uint64_t total,
-                                                   const DevPrime* src_primes, uint32_t src_mont,
-                                                   const FwdEpilogue fe) {
-  const uint32_t F = EXACT ? (uint32_t)MAXF : s.from_len;
-  constexpr int G = 128 >> TOP;  // groups per CTA (TOP > 0)
-  uint32_t i, poly, b0 = 0, logb = 0, t = 0, gi = 0;
-  bool fwd_here = false, dig_here = false;  // uniform across the CTA (one polynomial)
-  uint64_t r[MAXF];
-  if constexpr (TOP == 0) {
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= total) return;
-    i = gid & ((1u << logn) - 1);
-    poly = (uint32_t)(gid >> logn);
-    const uint64_t* src = in.at(poly, 0) + i;
-#pragma unroll
-    for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? src[(uint64_t)k << logn] : 0;
-  } else {
-    // The grid covers whole polynomials (2^logn is a multiple of 128), so
-    // every thread reaches the barriers.
-    uint64_t* staged = rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>();
-    poly = blockIdx.x >> (logn - 7);
-    b0 = (blockIdx.x & ((1u << (logn - 7)) - 1)) * G;
-    logb = logn - TOP;
-    for (uint32_t item = threadIdx.x; item < F * G; item += 128) {
-      const uint32_t k = item / G, gi = item % G;
-      const uint64_t* row = in.at(poly, k) + b0 + gi;
-      uint64_t x[1 << TOP];
-#pragma unroll
-      for (int t = 0; t < (1 << TOP); t++) x[t] = row[(uint64_t)t << logb];
-      inv_top_stages<TOP>(x, src_primes[k], 1u << logn, src_mont != 0);
-#pragma unroll
-      for (int t = 0; t < (1 << TOP); t++) staged[(k * (1 << TOP) + t) * G + gi] = x[t];
-    }
-    __syncthreads();
-    t = threadIdx.x / G;
-    gi = threadIdx.x % G;
-    i = b0 + gi + (t << logb);
-#pragma unroll
-    for (int k = 0; k < MAXF; k++) r[k] = k < (int)F ? staged[(k * (1 << TOP) + t) * G + gi] : 0;
-    if (fe.primes) {
-      const uint32_t part = fe.period ? poly % fe.period : 0;
-      fwd_here = part < fe.take;
-      dig_here = !fwd_here && fe.digit_primes != nullptr;
-    }
-    if (fwd_here || dig_here) __syncthreads();  // the buffer takes the outputs next
-  }
-
-  // scaler.rs:260-272: v = ceil((G >> (shift - 1)) / 2). Fast path: the
-  // kept high words of G; exact when G >> (shift - 1) cannot change under
-  // the dropped part (below 5F * 2^96): (H mod 2^e) + 5F < 2^e, e = shift - 97.
-  uint32_t g[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-  for (int k = 0; k < MAXF; k++)
-    if (k < (int)F) mac_hi<3>(g + 3, r[k], s.tgar_lo[k], s.tgar_hi[k]);
-  // shift >= 122 for any source count up to 128 moduli below 2^62; smaller
-  // shifts (never produced) take the exact path.
-  const uint32_t e_bits = s.shift >= 104 ? s.shift - 97 : 7;
-  bool exact = s.shift < 104 || (g[3] & ((1u << e_bits) - 1)) >= (1u << e_bits) - 5 * F;
-  if (exact) rns_exact_g<MAXF, MAXT>(&s, r, F, g);
-  uint64_t vlo, vhi;
-  shr_words(g, 6, s.shift - 1, &vlo, &vhi);
-  {
-    const uint64_t odd = vlo & 1;
-    vlo = (vlo >> 1) | (vhi << 63);
-    vhi >>= 1;
-    vlo += odd;
-    vhi += (vlo < odd);
-  }
-
-  // scaler.rs:276-314. Fast path: the kept high words of the signed sum S
-  // (the dropped part lies in (-(5F + 6), 5F + 6) * 2^96: 5 * 2^96 per term
-  // and 6 * 2^96 for v * theta_gamma); exact when S >> 126 cannot change,
-  // i.e. H mod 2^30 is at least 5F + 6 away from a multiple of 2^30.
-  bool w_sign = false;
-  uint64_t wlo = 0, whi = 0;
-  if (!s.is_one) {
-    uint32_t pos[8] = {0, 0, 0, 0, 0, 0, 0, 0}, neg[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (!exact) {
-#pragma unroll
-      for (int k = 0; k < MAXF; k++) {
-        if (k < (int)F) {
-          if ((s.to_sign >> k) & 1) mac_hi<5>(neg + 3, r[k], s.to_lo[k], s.to_hi[k]);
-          else mac_hi<5>(pos + 3, r[k], s.to_lo[k], s.to_hi[k]);
-        }
-      }
-      sub160w(pos + 3, neg + 3);
-      uint32_t vt[5];
-      mul_v_hi(vt, vlo, vhi, s.tg_lo, s.tg_hi);
-      if (s.tg_sign) add160w(pos + 3, vt);
-      else sub160w(pos + 3, vt);
-      const uint32_t m = pos[3] & ((1u << 30) - 1), margin = 5 * F + 6;
-      exact = m < margin || m > (1u << 30) - 1 - margin;
-    }
-    if (exact) rns_exact_s<MAXF, MAXT>(&s, r, F, vlo, vhi, pos);
-    w_sign = (pos[7] >> 31) != 0;
-    if (w_sign) {
-      uint32_t nw[8];
-#pragma unroll
-      for (int k = 0; k < 8; k++) nw[k] = ~pos[k];
-      shr_words(nw, 8, 126, &wlo, &whi);
-      wlo += 1;
-      whi += (wlo == 0);
-      wlo = (wlo >> 1) | (whi << 63);
-      whi >>= 1;
-    } else {
-      shr_words(pos, 8, 126, &wlo, &whi);
-      const uint64_t odd = wlo & 1;
-      wlo = (wlo >> 1) | (whi << 63);
-      whi >>= 1;
-      wlo += odd;
-      whi += (wlo < odd);
-    }
-  }
-
-  // scaler.rs:316-351. Above 8 source moduli the output loop stays
-  // rolled: unrolling it as well made the kernel body overflow the
-  // instruction cache (ncu: a third of the stall cycles waiting for
-  // instructions); its constants are then read with an indexed constant-bank
-  // load per term. Smaller bodies run faster unrolled.
-  constexpr int kOutUnroll = MAXF > 8 ? 1 : MAXT;
-  // v <= 32 * 2^62 (at most 32 sources, each residue below 2^62), so
-  // v * gamma = (v mod 2^62) * gamma + (v >> 62) * (gamma * 2^62 mod q_j):
-  // two exact terms of the 128-bit sum below, and v needs no reduction
-  // modulo each q_j. The sum then holds at most 15 terms below 2^124 (and a
-  // few small ones) between reductions: below 2^128.
-  const uint64_t v_low = vlo & ((1ull << 62) - 1);
-  const uint64_t v_top = (vlo >> 62) | (vhi << 2);
-  uint64_t* dst = out.at(poly, 0) + i;
-#pragma unroll kOutUnroll
-  for (int o = 0; o < MAXT; o++) {
-    if (o < (int)s.out_len) {
-      DevPrime pr;
-      pr.p = s.p[o];
-      pr.p2 = 2 * s.p[o];
-      pr.bhi = s.bhi[o];
-      pr.blo = s.blo[o];
-      uint64_t y;
-      if constexpr (EXACT) {
-        // Every term below 2^62 q_j (r_k, v_low < 2^62; v_top < 32), so 14
-        // products and the two gamma terms keep hi below 4 q_j.
-        uint64_t lo = 0, hi = 0, acc = 0;
-        mac128(hi, lo, v_low, s.gamma_neg[o]);
-        mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
-#pragma unroll
-        for (int k = 0; k < MAXF; k++) {
-          if (k < (int)F) {
-            mac128(hi, lo, r[k], s.omega[o][k]);
-            if ((k % 14) == 13) {
-              acc = csub(acc + mont_fold(hi, lo, pr.p, s.pinv[o]), pr.p);
-              hi = lo = 0;
-            }
-          }
-        }
-        y = csub(acc + mont_fold(hi, lo, pr.p, s.pinv[o]), pr.p);
-        if (!s.is_one) {
-          // whi < 2^63: w mod q_j = whi * 2^64 + wlo in [0, 2q_j) from one
-          // Shoup product and a reduction of wlo (conditional subtractions
-          // when wlo < 8 q_j), where a 128-bit Barrett takes three times the
-          // multiplies.
-          const uint64_t lo_red = s.wbig ? csub(csub(csub(wlo, 2 * pr.p2), pr.p2), pr.p)
-                                         : csub(mul_shoup_lazy(wlo, 1, s.one_shoup[o], pr.p), pr.p);
-          const uint64_t wj = csub(mul_shoup_lazy(whi, s.r64[o], s.r64_shoup[o], pr.p), pr.p) + lo_red;
-          y = csub(csub(y + (w_sign ? pr.p2 - wj : wj), pr.p2), pr.p);
-        }
-      } else {
-        uint64_t lo = 0, hi = 0;
-        if (!s.is_one) {
-          const uint64_t wj = reduce128_lazy(whi, wlo, pr);
-          lo = w_sign ? pr.p2 - wj : wj;
-        }
-        mac128(hi, lo, v_low, s.gamma_neg[o]);
-        mac128(hi, lo, v_top, s.gamma_neg_hi[o]);
-#pragma unroll
-        for (int k = 0; k < MAXF; k++) {
-          if (k < (int)F) {
-            mac128(hi, lo, r[k], s.omega[o][k]);
-            if ((k % 14) == 13) {  // keep the exact sum below 2^128
-              lo = reduce128(hi, lo, pr);
-              hi = 0;
-            }
-          }
-        }
-        y = reduce128(hi, lo, pr);
-      }
-      if constexpr (TOP > 0) {
-        if (fwd_here || dig_here)
-          rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>()[(o * (1 << TOP) + t) * G + gi] = y;
-        else dst[(uint64_t)o << logn] = y;
-      } else {
-        dst[(uint64_t)o << logn] = y;
-      }
-    }
-  }
-  if constexpr (TOP > 0) {
-    if (fwd_here || dig_here) {
-      __syncthreads();
-      const uint64_t* staged = rns_stage_buffer<(MAXF > MAXT ? MAXF : MAXT) * 128>();
-      if (fwd_here) {
-        for (uint32_t item = threadIdx.x; item < s.out_len * G; item += 128) {
-          const uint32_t o = item / G, g2 = item % G;
-          uint64_t x[1 << TOP];
-#pragma unroll
-          for (int u = 0; u < (1 << TOP); u++) x[u] = staged[(o * (1 << TOP) + u) * G + g2];
-          fwd_top_stages<TOP>(x, fe.primes[o]);
-          uint64_t* row = out.at(poly, o) + b0 + g2;
-#pragma unroll
-          for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
-        }
-      } else {
-        // Digit d (output limb d) in key limb j: key_switching_key.rs:227-235
-        // with rq/mod.rs:518-540, the first forward stages of its transform.
-        const uint32_t per_digit = fe.digit_limbs * G;
-        const uint32_t pbase = (poly / fe.period) * s.out_len;
-        for (uint32_t item = threadIdx.x; item < s.out_len * per_digit; item += 128) {
-          const uint32_t d = item / per_digit, rem = item - d * per_digit;
-          const uint32_t j = rem / G, g2 = rem % G;
-          const DevPrime kp = fe.digit_primes[j];
-          uint64_t x[1 << TOP];
-#pragma unroll
-          for (int u = 0; u < (1 << TOP); u++) {
-            const uint64_t v = staged[(d * (1 << TOP) + u) * G + g2];
-            x[u] = fe.digit_raw ? v : reduce64_lazy(v, kp);
-          }
-          fwd_top_stages<TOP>(x, kp);
-          uint64_t* row = fe.digits.at(pbase + d, j) + b0 + g2;
-#pragma unroll
-          for (int u = 0; u < (1 << TOP); u++) row[(uint64_t)u << logb] = x[u];
-        }
-      }
-    }
-  }
-}
-
-template <int MAXF, int MAXT, bool EXACT = false, int TOP = 0>
-void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
-                      uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop* top = nullptr,
-                      const ForwardTop* fwd = nullptr) {
-  const RnsScalerHost& h = sc.host;
-  const size_t F = h.from_len;
-  for (uint32_t first = 0; first < out_len; first += MAXT) {
-    const uint32_t n = std::min<uint32_t>(MAXT, out_len - first);
-    RnsLaunch<MAXF, MAXT> s;
-    memset(&s, 0, sizeof(s));
-    s.from_len = (uint32_t)F;
-    s.out_len = n;
-    s.is_one = h.is_one ? 1 : 0;
-    s.shift = (uint32_t)h.theta_garner_shift;
-    s.tg_sign = h.theta_gamma_sign ? 1 : 0;
-    s.tg_lo = h.theta_gamma_lo;
-    s.tg_hi = h.theta_gamma_hi;
-    for (size_t k = 0; k < F; k++) {
-      s.tgar_lo[k] = h.theta_garner_lo[k];
-      s.tgar_hi[k] = h.theta_garner_hi[k];
-      s.to_lo[k] = h.theta_omega_lo[k];
-      s.to_hi[k] = h.theta_omega_hi[k];
-      if (h.theta_omega_sign[k]) s.to_sign |= 1u << k;
-    }
-    if (EXACT && !sc.mont) throw Error(FHEG_ERR_INTERNAL, "Montgomery scaling needs odd target moduli");
-    s.wbig = 1;
-    for (uint32_t o = 0; o < n; o++) {
-      const size_t j = start + first + o;
-      if (EXACT) {
-        for (size_t k = 0; k < F; k++) s.omega[o][k] = sc.omega_mont[j * F + k];
-        s.gamma_neg[o] = sc.gamma_neg_mont[j];
-        s.gamma_neg_hi[o] = sc.gamma_neg_hi_mont[j];
-        s.pinv[o] = sc.to_pinv[j];
-        const uint64_t q = sc.to_moduli[j];
-        s.r64[o] = (uint64_t)(((unsigned __int128)1 << 64) % q);
-        s.r64_shoup[o] = shoup(s.r64[o], q);
-        s.one_shoup[o] = shoup(1, q);
-        if (q <= (1ull << 61)) s.wbig = 0;
-      } else {
-        for (size_t k = 0; k < F; k++) s.omega[o][k] = h.omega[j * F + k];
-        s.gamma_neg[o] = sc.gamma_neg[j];
-        s.gamma_neg_hi[o] = sc.gamma_neg_hi[j];
-      }
-      s.p[o] = sc.to_moduli[j];
-      s.bhi[o] = sc.to_bhi[j];
-      s.blo[o] = sc.to_blo[j];
-    }
-    PolyRef o = out;
-    o.base += (uint64_t)first << logn;
-    FwdEpilogue fe{};
-    if (fwd) {
-      if (fwd->digit_primes && first > 0) throw Error(FHEG_ERR_INTERNAL, "digit expansion needs one launch");
-      fe = FwdEpilogue{fwd->primes + first, fwd->period, fwd->take, fwd->digit_primes, fwd->digit_limbs,
-                       fwd->digit_raw, fwd->digits};
-    }
-    const unsigned threads = 128;
-    k_rns_scale<MAXF, MAXT, EXACT, TOP><<<blocks_for(total, threads), threads, 0, st>>>(
-        s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u, fe);
-    after_launch("k_rns_scale");
-  }
-}
-
-template <int MAXF, int MAXT>
-static void launch_rns_scale_top(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start,
-                                 uint32_t out_len, uint64_t total, cudaStream_t st, const InverseTop& top,
-                                 const ForwardTop* fwd) {
-  switch (top.s1) {
-    case 1: launch_rns_scale<MAXF, MAXT, true, 1>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
-    case 2: launch_rns_scale<MAXF, MAXT, true, 2>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
-    case 3: launch_rns_scale<MAXF, MAXT, true, 3>(s, logn, in, out, start, out_len, total, st, &top, fwd); break;
-    default: throw Error(FHEG_ERR_INTERNAL, "unsupported strided stage count");
-  }
-}
-
-bool rns_scale_takes_top(const RnsScalerD& s, uint32_t logn, uint32_t out_len, uint32_t s1) {
-  const size_t F = s.host.from_len;
-  const bool exact = (F == 6 || F == 13 || F == 3 || F == 7) ? out_len <= 8 : (F == 12 || F == 25) && out_len <= 16;
-  return exact && s.mont && s1 >= 1 && s1 <= 3 && logn >= 7;
-}
-
-void rns_scale(const RnsScalerD& s, uint32_t logn, PolyRef in, PolyRef out, uint32_t start, uint32_t out_len,
-               uint64_t polys, cudaStream_t st, const InverseTop* top, const ForwardTop* fwd) {
-  const uint64_t total = polys << logn;
-  if (total == 0 || out_len == 0) return;
-  const size_t F = s.host.from_len;
-  if (fwd && (!top || fwd->s1 != top->s1))
-    throw Error(FHEG_ERR_INTERNAL, "forward strided stages need the same count of inverse ones");
-  if (top) {
-    if (!rns_scale_takes_top(s, logn, out_len, top->s1))
-      throw Error(FHEG_ERR_INTERNAL, "RNS scaling cannot apply these strided stages");
-    if (F == 6) launch_rns_scale_top<6, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    else if (F == 13) launch_rns_scale_top<13, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    else if (F == 3) launch_rns_scale_top<3, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    else if (F == 7) launch_rns_scale_top<7, 8>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    else if (F == 12) launch_rns_scale_top<12, 16>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    else launch_rns_scale_top<25, 16>(s, logn, in, out, start, out_len, total, st, *top, fwd);
-    return;
-  }
-  // Exact source counts of the default multiplications at L = 3, 6, 12
-  // (extension from L, scale-down from 2L + 1), odd target moduli.
-  if (!s.mont) {
-    if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
-    else if (F <= 16 && out_len <= 8) launch_rns_scale<16, 8>(s, logn, in, out, start, out_len, total, st);
-    else if (F <= 16) launch_rns_scale<16, 16>(s, logn, in, out, start, out_len, total, st);
-    else if (F <= 32) launch_rns_scale<32, 16>(s, logn, in, out, start, out_len, total, st);
-    else throw Error(FHEG_ERR_UNSUPPORTED, "RNS scaling from more than 32 moduli is not supported");
-    return;
-  }
-  if (F == 6 && out_len <= 8) launch_rns_scale<6, 8, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F == 13 && out_len <= 8) launch_rns_scale<13, 8, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F == 3 && out_len <= 8) launch_rns_scale<3, 8, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F == 7 && out_len <= 8) launch_rns_scale<7, 8, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F == 12 && out_len <= 16) launch_rns_scale<12, 16, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F == 25 && out_len <= 16) launch_rns_scale<25, 16, true>(s, logn, in, out, start, out_len, total, st);
-  else if (F <= 8) launch_rns_scale<8, 8>(s, logn, in, out, start, out_len, total, st);
-  else if (F <= 16 && out_len <= 8) launch_rns_scale<16, 8>(s, logn, in, out, start, out_len, total, st);
-  else if (F <= 16) launch_rns_scale<16, 16>(s, logn, in, out, start, out_len, total, st);
-  else if (F <= 32) launch_rns_scale<32, 16>(s, logn, in, out, start, out_len, total, st);
-  else throw Error(FHEG_ERR_UNSUPPORTED, "RNS scaling from more than 32 moduli is not supported");
-}
-
-RnsScalerD::RnsScalerD(const Context& from, const Context& to, const BigUint& num, const BigUint& den)
-    : host(make_rns_scaler(*from.rns, *to.rns, num, den)) {
-  const size_t T = host.to_len;
-  gamma_neg.resize(T);
-  gamma_neg_hi.resize(T);
-  to_moduli = to.moduli;
-  to_bhi.resize(T);
-  to_blo.resize(T);
-  for (size_t j = 0; j < T; j++) {
-    gamma_neg[j] = (to.moduli[j] - host.gamma[j]) % to.moduli[j];
-    gamma_neg_hi[j] = mulmod(gamma_neg[j], (1ull << 62) % to.moduli[j], to.moduli[j]);
-    barrett128(to.moduli[j], &to_bhi[j], &to_blo[j]);
-  }
-  mont = true;
-  for (size_t j = 0; j < T; j++) mont = mont && (to.moduli[j] & 1);
-  if (mont) {
-    const size_t F = host.from_len;
-    omega_mont.resize(T * F);
-    gamma_neg_mont.resize(T);
-    gamma_neg_hi_mont.resize(T);
-    to_pinv.resize(T);
-    for (size_t j = 0; j < T; j++) {
-      const uint64_t q = to.moduli[j];
-      const uint64_t r = (uint64_t)(((unsigned __int128)1 << 64) % q);
-      for (size_t k = 0; k < F; k++) omega_mont[j * F + k] = mulmod(host.omega[j * F + k], r, q);
-      gamma_neg_mont[j] = mulmod(gamma_neg[j], r, q);
-      gamma_neg_hi_mont[j] = mulmod(gamma_neg_hi[j], r, q);
-      uint64_t inv = q;  // q^-1 mod 2^64 by Newton's iteration
-      for (int it = 0; it < 6; it++) inv *= 2 - q * inv;
-      to_pinv[j] = 0 - inv;
-    }
-  }
-}
-
-Scaler::Scaler(std::shared_ptr<Context> f, std::shared_ptr<Context> t, const BigUint& n, const BigUint& d)
-    : from(std::move(f)), to(std::move(t)), num(n), den(d) {
-  if (from->degree != to->degree) throw Error(FHEG_ERR_INVALID_ARGUMENT, "Incompatible degrees");
-  rns.reset(new RnsScalerD(*from, *to, num, den));
-  number_common_moduli = 0;
-  if (rns->host.is_one) {  // rq/scaler.rs:32-40
-    while (number_common_moduli < from->L() && number_common_moduli < to->L() &&
-           from->moduli[number_common_moduli] == to->moduli[number_common_moduli])
-      number_common_moduli++;
-  }
 }
 
 __global__ void k_copy_limbs(PolyRef in, PolyRef out, uint32_t limbs, uint32_t logn, uint64_t total) {

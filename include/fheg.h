@@ -165,6 +165,19 @@ FHEG_API int fheg_ntt_prefetch_set(int on);
  * to two passes). Schedules only; process-wide per logn. */
 FHEG_API int fheg_ntt_cluster_set(uint32_t logn, int on);
 FHEG_API int fheg_ntt_cluster_get(uint32_t logn, int* on);
+/* Tensor-core form of the exact RNS scalings (rns/scaler.rs:249-352 through
+ * RnsScaler::scale; no separate counterpart in the reference): for 12 to 16
+ * source moduli and odd target moduli above 2^20, the products of the
+ * residues with the scaler's constants run as byte-sliced FP16 matrix
+ * products on tcgen05 (exact: every column sum stays below 2^23), and the
+ * carries, rounding and reductions on the CUDA cores. On by default;
+ * results are identical either way. Process-wide. */
+FHEG_API int fheg_rns_tensor_set(int on);
+FHEG_API int fheg_rns_tensor_get(int* on);
+/* Number of bounded waits of the tensor-core scaler (operand copy, MMA
+ * completion) that ran out since the library was loaded on the current
+ * device; non-zero means some outputs of those launches are not valid. */
+FHEG_API int fheg_rns_tensor_wait_failures(uint64_t* count);
 /* Times every valid plan for the context's degree on `count` scratch
  * polynomials (forward + inverse), cluster mode included, installs the
  * fastest and returns its block size (fheg_ntt_cluster_get tells the mode). */

@@ -56,6 +56,34 @@ def test_multiply_default(fg, ora, cuda, n, L, t, B):
         assert list(s.decrypt(out[b], 0)) == s.product(vals[b], vals[B + b])
 
 
+@pytest.mark.parametrize("n,L,B", [(8192, 3, 3), (16384, 6, 33), (32768, 12, 2)])
+def test_multiply_tensor_core_scalers(fg, ora, cuda, n, L, B):
+    """The multiplication with its scalers of 12 or more source moduli on the
+    tensor cores (the default: the L = 6 scale-down, the L = 12 extension)
+    equals the same multiplication on the CUDA cores, for every pair, and the
+    oracle's product for the first and last (33 pairs run as two concurrent
+    halves; L = 3 has no such scaler and checks the switch alone)."""
+    s = Setup(fg, ora, n, L, 65537, seed=n + 7 * L)
+    rk_o, rk = s.rk()
+    mult = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(4)
+    lhs = fg.to_device(np.stack([cts[b % 2].to_array() for b in range(B)]))
+    rhs = fg.to_device(np.stack([cts[2 + b % 2].to_array() for b in range(B)]))
+    default = fg.rns_tensor_get()
+    try:
+        fg.rns_tensor_set(True)
+        on = fg.to_host(mult.multiply(lhs, rhs))
+        fg.rns_tensor_set(False)
+        off = fg.to_host(mult.multiply(lhs, rhs))
+    finally:
+        fg.rns_tensor_set(default)
+    assert fg.rns_tensor_wait_failures() == 0
+    assert np.array_equal(on, off)
+    mult_o = ora.Multiplicator.default(rk_o)
+    for b in (0, B - 1):
+        assert np.array_equal(on[b], mult_o.multiply(cts[b % 2], cts[2 + b % 2]).to_array()), b
+
+
 def test_multiply_variants(fg, ora, cuda):
     """mul.rs:246-339: mod switching and no relinearization."""
     s = Setup(fg, ora, 4096, 3, 65537, seed=77)

@@ -105,22 +105,34 @@ def _boundary_values(q_from, num, den, n, rng):
     return (vals * (n // len(vals) + 1))[:n]
 
 
-@pytest.mark.parametrize("setup", ["ring_3001", "ring_t_over_q", "mul_up_6", "mul_down_13", "mul_down_25"])
-def test_scaler_rounding_boundaries(fg, ora, cuda, setup):
+@pytest.mark.parametrize("tc", [True, False])
+@pytest.mark.parametrize("setup", ["ring_3001", "ring_t_over_q", "mul_up_6", "mul_up_12", "mul_down_13", "mul_down_25"])
+def test_scaler_rounding_boundaries(fg, ora, cuda, setup, tc):
     """Coefficients chosen at the rounding boundaries of RnsScaler::scale, in
-    both representations, for generic and exact-count scaler kernels: the
+    both representations, for generic and exact-count scaler kernels, with the
+    exact counts' products on the tensor cores (tc) and on the CUDA cores: the
     results equal the oracle's exact big-integer computation."""
-    rng = np.random.default_rng(["ring_3001", "ring_t_over_q", "mul_up_6", "mul_down_13", "mul_down_25"].index(setup))
+    default = fg.rns_tensor_get()
+    fg.rns_tensor_set(tc)
+    try:
+        _scaler_boundaries(fg, ora, setup)
+    finally:
+        fg.rns_tensor_set(default)
+    assert fg.rns_tensor_wait_failures() == 0
+
+
+def _scaler_boundaries(fg, ora, setup):
+    rng = np.random.default_rng(["ring_3001", "ring_t_over_q", "mul_up_6", "mul_up_12", "mul_down_13", "mul_down_25"].index(setup))
     n = 4096
     if setup.startswith("ring"):
         frm, to = Q, P
         num, den = (3, 1001) if setup == "ring_3001" else (65537, ora.RnsContext(Q).modulus())
     else:
-        L = {"mul_up_6": 6, "mul_down_13": 6, "mul_down_25": 12}[setup]
+        L = {"mul_up_6": 6, "mul_up_12": 12, "mul_down_13": 6, "mul_down_25": 12}[setup]
         n = 16384 if L == 6 else 32768
         par = ora.BfvParameters(n, 65537, moduli_sizes=[62] * L)
         ext = ora.Multiplicator.default_extended_basis(par, 0)
-        if setup == "mul_up_6":
+        if setup.startswith("mul_up"):
             frm, to, num, den = list(par.moduli), ext, 1, 1
         else:
             frm, to, num, den = ext, list(par.moduli), 65537, par.context_at_level(0).modulus()
@@ -136,10 +148,22 @@ def test_scaler_rounding_boundaries(fg, ora, cuda, setup):
     assert np.array_equal(got, sc_o.scale(nt).coefficients)
 
 
-@pytest.mark.parametrize("n,L", [(4096, 2), (16384, 6)])
-def test_mul_scalers(fg, ora, cuda, n, L):
+@pytest.mark.parametrize("tc", [True, False])
+@pytest.mark.parametrize("n,L", [(4096, 2), (8192, 3), (16384, 6)])
+def test_mul_scalers(fg, ora, cuda, n, L, tc):
     """The Multiplicator's scalers: extension Q -> Q u P (factor one, common
-    prefix) and t/Q scale-down Q u P -> Q, in Ntt representation."""
+    prefix) and t/Q scale-down Q u P -> Q, in Ntt representation, with the
+    products on the tensor cores (tc) and on the CUDA cores."""
+    default = fg.rns_tensor_get()
+    fg.rns_tensor_set(tc)
+    try:
+        _mul_scalers(fg, ora, n, L)
+    finally:
+        fg.rns_tensor_set(default)
+    assert fg.rns_tensor_wait_failures() == 0
+
+
+def _mul_scalers(fg, ora, n, L):
     rng = np.random.default_rng(5)
     par = ora.BfvParameters(n, 65537, moduli_sizes=[62] * L)
     ext = ora.Multiplicator.default_extended_basis(par, 0)
