@@ -297,16 +297,20 @@ __device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const u
 // multiply-adds of the unrolled sums per coefficient.
 //
 // Column groups of 8 (one group = 8 bytes of one sum): 0-2 G, 3-6 S, then one
-// per output modulus. The launch's operand B is the groups of its sums (G and
-// S unless the factor is one, and its output slice), copied from the scaler's
-// matrix by two bulk copies; N = 8 groups rounded up to a multiple of 16.
+// per output modulus. A launch runs two passes through the same tensor-memory
+// columns: pass 0 multiplies by the groups of G (and S unless the factor is
+// one), pass 1 by the groups of its output slice; each pass's operand B is
+// bulk-copied from the scaler's matrix into one shared buffer (pass 1's copy
+// once pass 0's MMAs are done with it). N of a pass is 8 groups rounded up to
+// a multiple of 16; the rows beyond its groups hold stale bytes whose columns
+// are never read.
 struct TcMat {
   const uint16_t* mat;   // FP16 bit patterns, 16 * kp bytes per group (tc.cuh layout)
   uint32_t kp;           // 8 F rounded up to a multiple of 16
   uint32_t head_groups;  // G (and S) groups: 3 or 7
   uint32_t out_group0;   // first output group of the launch (7 + start)
-  uint32_t groups;       // head_groups + out_len, rounded up to even
-  uint32_t cols;         // tensor-memory columns allocated (128)
+  uint32_t n0, n1;       // N of pass 0 and pass 1
+  uint32_t cols;         // tensor-memory columns allocated (64 or 128)
   uint32_t b_offset;     // byte offset of B in the dynamic shared memory
 };
 
@@ -315,6 +319,28 @@ struct TcMat {
 __device__ uint32_t g_tc_wait_failures;
 
 constexpr uint32_t kTcWaitTries = 1u << 20;
+
+// Thread 0: the MMAs of one pass (K / 16 of them, N = n) once its operand B
+// has landed (phase `phase` of bar_b), committed to bar_mma. A copy that does
+// not land in time is counted, the pass's MMAs are skipped (its outputs are
+// then not valid) and bar_mma is released by hand so that no thread waits
+// longer than its own bounded wait.
+template <uint32_t KP>
+__device__ __forceinline__ void tc_pass(uint32_t bar_b, uint32_t bar_mma, uint32_t phase, uint32_t tmem, uint32_t sa,
+                                        uint32_t sb, uint32_t n) {
+  if (mbar_wait(bar_b, phase, kTcWaitTries)) {
+    const uint32_t idesc = tc_idesc_f16_f32(128, n);
+#pragma unroll
+    for (uint32_t kk = 0; kk < KP / 16; kk++)
+      tc_mma_f16(tmem, tc_smem_desc(sa + kk * 256, 16 * KP), tc_smem_desc(sb + kk * 256, 16 * KP), idesc,
+                 kk > 0 ? 1u : 0u);
+    tc_commit(bar_mma);
+  } else {
+    atomicAdd(&g_tc_wait_failures, 1u);
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_mma) : "memory");
+    mbar_wait(bar_b, phase, kTcWaitTries);
+  }
+}
 
 // Two bytes of w (prmt selector sel) as the half2 (b0, b1): 0x64bb is the
 // FP16 value 1024 + b, less 1024.
@@ -395,17 +421,10 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
       mbar_init(bar_b, 1);
       mbar_init(bar_mma, 1);
       fence_proxy_async_smem();
-      const uint32_t head = tc.head_groups * group_bytes, outs = (s.out_len) * group_bytes;
-      mbar_expect_tx(bar_b, head + outs);
-      bulk_g2s(smem_u32(tc_b), tc.mat, head, bar_b);
-      bulk_g2s(smem_u32(tc_b) + head, reinterpret_cast<const uint8_t*>(tc.mat) + tc.out_group0 * group_bytes, outs,
-               bar_b);
+      mbar_expect_tx(bar_b, tc.head_groups * group_bytes);
+      bulk_g2s(smem_u32(tc_b), tc.mat, tc.head_groups * group_bytes, bar_b);
     }
     if ((threadIdx.x >> 5) == 1) tc_alloc(smem_u32(&tc_slot), tc.cols);
-    // The padding group (N a multiple of 16) reads as zeros.
-    const uint32_t used = (tc.head_groups + s.out_len) * group_bytes, all = tc.groups * group_bytes;
-    for (uint32_t off = used + 16 * threadIdx.x; off < all; off += 16 * 128)
-      *reinterpret_cast<uint4*>(tc_b + off) = make_uint4(0, 0, 0, 0);
   }
   if constexpr (TOP == 0) {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -422,8 +441,10 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     poly = blockIdx.x >> (logn - 7);
     b0 = (blockIdx.x & ((1u << (logn - 7)) - 1)) * G;
     logb = logn - TOP;
-    if constexpr (EXACT) {
-      // Every load of the thread's items issued before the first use.
+    if constexpr (TC) {
+      // Every load of the thread's items issued before the first use (the
+      // tensor-core form runs fewer warps per SM; the CUDA-core kernels,
+      // with more warps and fewer registers, measured faster without).
       constexpr int IT = (MAXF * G + 127) / 128;
       uint64_t x[IT][1 << TOP];
 #pragma unroll
@@ -491,25 +512,18 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     __syncthreads();
     tc_fence_after();
     tmem = tc_slot;
-    if (threadIdx.x == 0) {
-      if (mbar_wait(bar_b, 0, kTcWaitTries)) {
-        const uint32_t sa = smem_u32(tc_a), sb = sa + 128 * KP * 2;
-        const uint32_t idesc = tc_idesc_f16_f32(128, 8 * tc.groups);
-#pragma unroll
-        for (uint32_t kk = 0; kk < KP / 16; kk++)
-          tc_mma_f16(tmem, tc_smem_desc(sa + kk * 256, 16 * KP), tc_smem_desc(sb + kk * 256, 16 * KP), idesc,
-                     kk > 0 ? 1u : 0u);
-        tc_commit(bar_mma);
-      } else {
-        // The operand copy did not land: count it, let the CTA through (its
-        // outputs are not valid) and give the copy one more bounded wait.
-        atomicAdd(&g_tc_wait_failures, 1u);
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_mma) : "memory");
-        mbar_wait(bar_b, 0, kTcWaitTries);
-      }
-    }
+    const uint32_t sa = smem_u32(tc_a), sb = sa + tc.b_offset;
+    if (threadIdx.x == 0) tc_pass<KP>(bar_b, bar_mma, 0, tmem, sa, sb, tc.n0);
     if (!mbar_wait(bar_mma, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
     tc_fence_after();
+    // Pass 0's MMAs are done with B: pass 1's operand lands while its columns
+    // are read.
+    if (threadIdx.x == 0) {
+      const uint32_t group_bytes = 16 * KP;
+      mbar_expect_tx(bar_b, s.out_len * group_bytes);
+      bulk_g2s(sb, reinterpret_cast<const uint8_t*>(tc.mat) + tc.out_group0 * group_bytes, s.out_len * group_bytes,
+               bar_b);
+    }
     lane = tmem + (((threadIdx.x >> 5) * 32u) << 16);
   }
 
@@ -523,6 +537,15 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   if constexpr (TC) {
     if (s.is_one) tc_ld24(lane, gs);
     else tc_ld56(lane, gs);
+    // Every lane's pass-0 columns are read: pass 1 may overwrite them, and
+    // its MMAs run while the sums below are carried and rounded.
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0) {
+      const uint32_t sa = smem_u32(tc_a);
+      tc_pass<KP>(bar_b, bar_mma, 1, tmem, sa, sa + tc.b_offset, tc.n1);
+    }
     uint64_t acc = 0;
 #pragma unroll
     for (uint32_t q = 0; q < 3; q++) tc_words(gs + 8 * q, acc, g + 2 * q);
@@ -629,6 +652,10 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   // two exact terms of the 128-bit sum below, and v needs no reduction
   // modulo each q_j. The sum then holds at most 15 terms below 2^124 (and a
   // few small ones) between reductions: below 2^128.
+  if constexpr (TC) {
+    if (!mbar_wait(bar_mma, 1, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+    tc_fence_after();
+  }
   const uint64_t v_low = vlo & ((1ull << 62) - 1);
   const uint64_t v_top = (vlo >> 62) | (vhi << 2);
   uint64_t* dst = out.at(poly, 0) + i;
@@ -649,7 +676,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
           // The output's sum below 2^80 (8 bytes of sums below 2^23), so hi
           // stays below 4 q_j with the gamma terms for q_j above 2^20.
           uint32_t c[8], w2[2];
-          tc_ld8(lane + 8 * (tc.head_groups + o), c);
+          tc_ld8(lane + 8 * o, c);
           tc_words(c, acc, w2);
           lo = join(w2[0], w2[1]);
           hi = acc;
@@ -849,23 +876,26 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     // cost about what the multiplies they replace did, and its shared memory
     // halves the CTAs per SM (6 sources: 0.40 against 0.33 ms on GB300).
     if constexpr (EXACT && MAXF >= 12 && MAXF <= 16) {
-      const uint32_t head = h.is_one ? 3 : 7, groups = (head + n + 1) / 2 * 2;
-      if (sc.tc_mat.ptr && rns_tc_enabled() && groups <= 16 && (TOP > 0 || total % 128 == 0)) {
+      const uint32_t head = h.is_one ? 3 : 7;
+      const uint32_t n0 = (8 * head + 15) / 16 * 16, n1 = (8 * n + 15) / 16 * 16;
+      if (sc.tc_mat.ptr && rns_tc_enabled() && n1 <= 128 && (TOP > 0 || total % 128 == 0)) {
         constexpr uint32_t KP = (8 * MAXF + 15) / 16 * 16;
         if (sc.tc_kp != KP) throw Error(FHEG_ERR_INTERNAL, "tensor-core scaler matrix of another width");
         auto kern = k_rns_scale<MAXF, MAXT, EXACT, TOP, false, true>;
-        constexpr uint32_t kCols = 128;
-        // The stage buffer (TOP > 0) overlaid by A, then B.
+        const uint32_t cols = std::max(n0, n1) <= 64 ? 64 : 128;
+        // The stage buffer (TOP > 0) overlaid by A, then B (the larger pass).
         constexpr size_t kStage = TOP > 0 ? (size_t)(MAXF > MAXT ? MAXF : MAXT) * 128 * 8 : 0;
         constexpr size_t kBOff = ((128 * KP * 2 > kStage ? 128 * KP * 2 : kStage) + 127) / 128 * 128;
-        const TcMat tc{static_cast<const uint16_t*>(sc.tc_mat.ptr), KP, head, 7 + start + first, groups, kCols,
+        const TcMat tc{static_cast<const uint16_t*>(sc.tc_mat.ptr), KP, head, 7 + start + first, n0, n1, cols,
                        (uint32_t)kBOff};
-        // At least kCols * 456 bytes of shared memory per CTA (with the 1 KB
+        // At least cols * 456 bytes of shared memory per CTA (with the 1 KB
         // the SM reserves per CTA): the SM's 228 KB then never holds CTAs
         // asking for more than its 512 tensor-memory columns.
-        const size_t floor_dyn = kCols * kTcSmemPerColumn - 1024 - tc_static_smem(kern);
-        const size_t dyn = std::max<size_t>(kBOff + groups * 16 * KP, floor_dyn);
-        tc_prepare(reinterpret_cast<const void*>(kern), std::max<size_t>(kBOff + 16 * 16 * KP, floor_dyn));
+        const size_t stat = tc_static_smem(kern);
+        const size_t floor_dyn = cols * kTcSmemPerColumn - 1024 - stat;
+        const size_t dyn = std::max<size_t>(kBOff + std::max(n0, n1) * 2 * KP, floor_dyn);
+        tc_prepare(reinterpret_cast<const void*>(kern),
+                   std::max<size_t>(kBOff + 128 * 2 * KP, 128 * kTcSmemPerColumn - 1024 - stat));
         kern<<<blocks_for(total, threads), threads, dyn, st>>>(s, logn, in, o, total, top ? top->primes : nullptr,
                                                               top ? top->mont : 0u, fe, tc);
         after_launch("k_rns_scale");
