@@ -282,7 +282,9 @@ struct DstKsF {
 // D is a plain array [batch * ndig][lk][N] (digit d of ciphertext b at row
 // b * ndig + d, dstride words apart), addressed directly: a PolyRef lookup
 // per digit would cost a division per residue.
-template <int KB>
+// MAXD > 0 (KB = 1, ndig <= MAXD): every digit and key residue is loaded
+// before the first product, so all of a thread's loads are in flight at once.
+template <int KB, int MAXD = 0>
 __global__ void k_key_mac(const DevPrime* primes, const uint64_t* D, uint64_t dstride, const uint64_t* k0,
                           const uint64_t* k1,
                           const uint64_t* add0, uint64_t add0_stride, uint64_t add0_e, const uint64_t* add1,
@@ -309,7 +311,33 @@ __global__ void k_key_mac(const DevPrime* primes, const uint64_t* D, uint64_t ds
   const uint64_t kstride = (uint64_t)lk << logn;
   const uint64_t* kp0 = k0 + ((uint64_t)j << logn) + i;
   const uint64_t* kp1 = k1 + ((uint64_t)j << logn) + i;
-  for (uint32_t d = 0; d < ndig; d++) {
+  if constexpr (MAXD > 0) {
+    static_assert(KB == 1, "digits up front take one ciphertext per thread");
+    uint64_t x[MAXD], w0[MAXD], w1[MAXD];
+    const uint64_t* dp = D + b0 * ndig * dstride + ((uint64_t)j << logn) + i;
+#pragma unroll
+    for (int d = 0; d < MAXD; d++) {
+      if ((uint32_t)d < ndig) {
+        w0[d] = __ldg(kp0 + d * kstride);
+        w1[d] = __ldg(kp1 + d * kstride);
+        x[d] = dp[d * dstride];
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < MAXD; d++) {
+      if ((uint32_t)d < ndig) {
+        mac128(hi0[0], lo0[0], x[d], w0[d]);
+        mac128(hi1[0], lo1[0], x[d], w1[d]);
+        if (d % 15 == 14) {
+          lo0[0] = reduce128(hi0[0], lo0[0], pr);
+          hi0[0] = 0;
+          lo1[0] = reduce128(hi1[0], lo1[0], pr);
+          hi1[0] = 0;
+        }
+      }
+    }
+  }
+  for (uint32_t d = 0; d < (MAXD > 0 ? 0u : ndig); d++) {
     const uint64_t w0 = __ldg(kp0 + d * kstride), w1 = __ldg(kp1 + d * kstride);
 #pragma unroll
     for (int u = 0; u < KB; u++) {
@@ -350,8 +378,17 @@ void launch_key_mac(const DevPrime* primes, PolyRef D, const uint64_t* k0, const
   if (batch == 0) return;
   if (D.grp != 1) throw Error(FHEG_ERR_INTERNAL, "key inner product: digits must be a plain array");
   const uint64_t total = batch * lk << logn;
-  k_key_mac<1><<<nblocks(total, 256), 256, 0, st>>>(primes, D.base, D.grp_stride, k0, k1, add0, add0_stride, add0_e,
-                                                    add1, add1_stride, out, out_stride, ndig, lk, logn, batch, total);
+  if (ndig <= 8)
+    k_key_mac<1, 8><<<nblocks(total, 256), 256, 0, st>>>(primes, D.base, D.grp_stride, k0, k1, add0, add0_stride,
+                                                         add0_e, add1, add1_stride, out, out_stride, ndig, lk, logn,
+                                                         batch, total);
+  else if (ndig <= 16)
+    k_key_mac<1, 16><<<nblocks(total, 256), 256, 0, st>>>(primes, D.base, D.grp_stride, k0, k1, add0, add0_stride,
+                                                          add0_e, add1, add1_stride, out, out_stride, ndig, lk, logn,
+                                                          batch, total);
+  else
+    k_key_mac<1><<<nblocks(total, 256), 256, 0, st>>>(primes, D.base, D.grp_stride, k0, k1, add0, add0_stride, add0_e,
+                                                      add1, add1_stride, out, out_stride, ndig, lk, logn, batch, total);
   after_launch("k_key_mac");
 }
 
