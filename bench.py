@@ -61,21 +61,21 @@ STAGE_KERNELS = {
 STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # DRAM bytes (read + write) of each stage's kernels for one 64-pair
 # multiplication with the plan A,C,D,F = 12 (2^12-residue blocks; every
-# strided NTT stage applied inside the RNS scalers B and E), from the ncu
-# capture summarised in profiles/stages_mul_relin_n16384_b64.md.
-STAGE_TRAFFIC_BYTES = {"A": 354.2e6, "B": 383.7e6, "C": 417.2e6, "D": 730.2e6, "E": 671.7e6, "F": 707.3e6,
-                       "G": 493.2e6}
+# strided NTT stage applied inside the RNS scalers B and E; E's sums on the
+# tensor cores), from the ncu capture summarised in
+# profiles/stages_mul_relin_n16384_b64.md.
+STAGE_TRAFFIC_BYTES = {"A": 352.9e6, "B": 393.1e6, "C": 409.5e6, "D": 728.3e6, "E": 676.0e6, "F": 696.4e6,
+                       "G": 493.4e6}
 # The ncu figures above and below hold for the library sources they were
 # captured on: library_source_hash() of that tree. A run on other sources
 # reports null for them instead of stale numbers.
-PROFILED_SOURCE_HASH = "unprofiled"
+PROFILED_SOURCE_HASH = "cfe7cb3da8d605da"
 # Share of the elapsed cycles in which the integer multipliers (the FMA-heavy
-# pipe, which executes every IMAD) were busy, per stage, from the ncu capture
-# of one 32-pair multiplication under the same plan summarised in
-# profiles/pipes_mul_relin_n16384_b32.md (F: time-weighted over its two
-# launches). The whole multiplication: 72.0%, time-weighted.
-STAGE_FMAHEAVY_PCT = {"A": 67.0, "B": 85.5, "C": 70.3, "D": 65.3, "E": 79.8, "F": 68.6, "G": 58.5}
-MULTIPLY_FMAHEAVY_PCT = 72.0
+# pipe, which executes every IMAD) were busy, per stage, from the same ncu
+# capture of one 64-pair multiplication (F: time-weighted over its two
+# launches); the whole multiplication, time-weighted.
+STAGE_FMAHEAVY_PCT = {"A": 70.0, "B": 84.0, "C": 70.6, "D": 67.5, "E": 60.5, "F": 70.3, "G": 63.6}
+MULTIPLY_FMAHEAVY_PCT = 69.2
 
 
 def library_source_hash() -> str:
@@ -518,7 +518,7 @@ def run_ours(args, rank: int, world: int):
                          "int_pipe": {"kernel_fmaheavy_pct": STAGE_FMAHEAVY_PCT[dom] if traffic_plan_matches else None,
                                       "multiply_fmaheavy_pct": MULTIPLY_FMAHEAVY_PCT if traffic_plan_matches else None,
                                       "metric": "sm__pipe_fmaheavy_cycles_active.avg.pct_of_peak_sustained_elapsed",
-                                      "source": "ncu, profiles/pipes_mul_relin_n16384_b32.md"}},
+                                      "source": "ncu, profiles/stages_mul_relin_n16384_b64.md"}},
             "stages": {k: {"ms": stage_ms[k], "gbs": stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9,
                            "kernel": STAGE_KERNELS[k]} for k in stage_ms},
             "ntt": {"kernel": "forward / inverse NTT alone, 256 polys x 6 limbs", "fwd_gbs": fwd_gbs,
