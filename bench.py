@@ -1174,6 +1174,7 @@ def run_serve(args):
     ge.build()
     fg = ge.load_package()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    fg.rns_tensor_set(args.rns_tensor == "on")
     ring = 64
     setups = [_serve_setup(fg, ora, torch, n, nm, 100 + k, ring) for k, (n, nm) in enumerate(SERVE_SETS)]
     budget = int(args.serve_budget_gb * (1 << 30))
