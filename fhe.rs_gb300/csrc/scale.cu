@@ -795,25 +795,30 @@ uint64_t rns_tc_wait_failures() {
 // 228 KB of shared memory per SM over its 512 tensor-memory columns.
 constexpr size_t kTcSmemPerColumn = 233472 / 512;
 
-template <typename K>
-static size_t tc_static_smem(K kern) {
-  cudaFuncAttributes a{};
-  check_cuda(cudaFuncGetAttributes(&a, kern), "cudaFuncGetAttributes");
-  return a.sharedSizeBytes;
-}
-
-// Raises a kernel's dynamic shared-memory limit to `bytes` on the current
-// device (once per kernel and device).
-static void tc_prepare(const void* kern, size_t bytes) {
+// Once per tensor-core kernel and device: reads the kernel's static shared
+// memory and raises its dynamic limit to cover its largest operands
+// (`operands` bytes) and the floor of a 128-column CTA. Returns the static
+// shared memory.
+static size_t tc_prepare(const void* kern, size_t operands) {
+  struct Entry {
+    const void* kern;
+    int dev;
+    size_t stat;
+  };
   static std::mutex mu;
-  static std::vector<std::pair<const void*, int>> done;
+  static std::vector<Entry> done;
   int dev = 0;
   check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   std::lock_guard<std::mutex> lock(mu);
-  if (std::find(done.begin(), done.end(), std::make_pair(kern, dev)) != done.end()) return;
-  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+  for (const Entry& e : done)
+    if (e.kern == kern && e.dev == dev) return e.stat;
+  cudaFuncAttributes a{};
+  check_cuda(cudaFuncGetAttributes(&a, kern), "cudaFuncGetAttributes");
+  const size_t limit = std::max<size_t>(operands, 128 * kTcSmemPerColumn - 1024 - a.sharedSizeBytes);
+  check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit),
              "cudaFuncSetAttribute");
-  done.emplace_back(kern, dev);
+  done.push_back(Entry{kern, dev, a.sharedSizeBytes});
+  return a.sharedSizeBytes;
 }
 
 template <int MAXF, int MAXT, bool EXACT = false, int TOP = 0>
@@ -891,11 +896,9 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
         // At least cols * 456 bytes of shared memory per CTA (with the 1 KB
         // the SM reserves per CTA): the SM's 228 KB then never holds CTAs
         // asking for more than its 512 tensor-memory columns.
-        const size_t stat = tc_static_smem(kern);
+        const size_t stat = tc_prepare(reinterpret_cast<const void*>(kern), kBOff + 128 * 2 * KP);
         const size_t floor_dyn = cols * kTcSmemPerColumn - 1024 - stat;
         const size_t dyn = std::max<size_t>(kBOff + std::max(n0, n1) * 2 * KP, floor_dyn);
-        tc_prepare(reinterpret_cast<const void*>(kern),
-                   std::max<size_t>(kBOff + 128 * 2 * KP, 128 * kTcSmemPerColumn - 1024 - stat));
         kern<<<blocks_for(total, threads), threads, dyn, st>>>(s, logn, in, o, total, top ? top->primes : nullptr,
                                                               top ? top->mont : 0u, fe, tc);
         after_launch("k_rns_scale");

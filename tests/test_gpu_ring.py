@@ -148,6 +148,48 @@ def _scaler_boundaries(fg, ora, setup):
     assert np.array_equal(got, sc_o.scale(nt).coefficients)
 
 
+def _primes(ora, n, count, bits=62):
+    out, ub = [], 1 << bits
+    while len(out) < count:
+        ub = ora.generate_prime(bits, 2 * n, ub)
+        out.append(ub)
+    return out
+
+
+@pytest.mark.parametrize("F,T", [(12, 1), (12, 7), (12, 10), (12, 13), (13, 3), (13, 8), (13, 10)])
+@pytest.mark.parametrize("factor", ["one", "t_over_q", "3_1001"])
+def test_scaler_tensor_core_shapes(fg, ora, cuda, F, T, factor):
+    """Scalers from 12 and 13 source moduli (the tensor-core form; 13 into more
+    than 8 targets takes the generic kernel) into 1 to 13 target moduli of
+    mixed sizes, with and without the signed theta sum (factor one or not),
+    over 64 or 128 tensor-memory columns: equal to the oracle in both
+    representations and to the CUDA-core form."""
+    n = 4096
+    rng = np.random.default_rng(F * 100 + T)
+    pool = _primes(ora, n, F + T, 62)
+    frm = pool[:F]
+    to = pool[F:F + T - T // 2] + _primes(ora, n, T // 2, 40)  # some targets near 2^40
+    num, den = {"one": (1, 1), "t_over_q": (65537, ora.RnsContext(frm).modulus()), "3_1001": (3, 1001)}[factor]
+    frm_o, to_o = ora.Context(frm, n), ora.Context(to, n)
+    sc_o = ora.Scaler(frm_o, to_o, ora.ScalingFactor(num, den) if num != den else ora.ScalingFactor.one())
+    sc = fg.Scaler(fg.Context(frm, n), fg.Context(to, n),
+                   fg.ScalingFactor(num, den) if num != den else fg.ScalingFactor.one())
+    a = _rand(rng, frm, n, 2)
+    default = fg.rns_tensor_get()
+    try:
+        for rep in (ora.POWER_BASIS, ora.NTT):
+            r = 0 if rep == ora.POWER_BASIS else 1
+            fg.rns_tensor_set(True)
+            got = fg.to_host(sc.scale(fg.to_device(a), r))
+            fg.rns_tensor_set(False)
+            assert np.array_equal(got, fg.to_host(sc.scale(fg.to_device(a), r)))
+            for k in range(2):
+                assert np.array_equal(got[k], sc_o.scale(ora.Poly(frm_o, a[k], rep)).coefficients), (rep, k)
+    finally:
+        fg.rns_tensor_set(default)
+    assert fg.rns_tensor_wait_failures() == 0
+
+
 @pytest.mark.parametrize("tc", [True, False])
 @pytest.mark.parametrize("n,L", [(4096, 2), (8192, 3), (16384, 6)])
 def test_mul_scalers(fg, ora, cuda, n, L, tc):
