@@ -314,8 +314,9 @@ def run_reference(args, rank: int):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": "bfv_mul_relin", "degree": N, "moduli": L, "moduli_bits": 62, "plaintext": T,
-                   "batch_pairs_per_step": cores * per_thread, "parallelism": "host threads"},
+        "config": {"workload": "bfv_mul_relin_batched", "degree": N, "moduli": L, "moduli_bits": 62,
+                   "extension_moduli": 7, "plaintext": T, "batch_pairs": cores * per_thread,
+                   "keys": "resident in host memory", "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                          "sample": f"{cores * per_thread} products per step ({per_thread} per host thread) of the "
                                    "C++ restatement of fhe.rs Multiplicator::default().multiply (oracle.cpp, "
