@@ -1001,6 +1001,8 @@ def run_rotate(args):
     fg = ge.load_package()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     n, top, count = 1 << 15, 12, args.rot_count
+    if args.ntt_cluster != "default":
+        fg.ntt_cluster_set(15, args.ntt_cluster == "on")
     rng = np.random.default_rng(15)
     par_o = ora.BfvParameters(n, T, moduli_sizes=[62] * top)
     par = fg.BfvParameters(n, par_o.moduli, T)
@@ -1271,6 +1273,8 @@ def main():
     ap.add_argument("--rns-tensor", default="on", choices=["on", "off"],
                     help="RNS scalings of the multiplication on the tensor cores (on) or the CUDA cores (off)")
     ap.add_argument("--stage-runs", type=int, default=1, help="stages workload: median over this many runs")
+    ap.add_argument("--ntt-cluster", default="default", choices=["default", "on", "off"],
+                    help="rotate workload: cluster mode of the 2^15 NTT plan")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-budget-gb", type=float, default=24.0)
     ap.add_argument("--serve-streams", type=int, default=4)
