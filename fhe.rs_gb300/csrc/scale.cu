@@ -290,9 +290,10 @@ __device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const u
 //   sum_k r_k X_k = sum_c 2^(8c) D_c,  D_c = sum_(k,b) a_kb x_kbc,
 // a matrix product of the 128 x 8F byte matrix of a CTA's coefficients with
 // the 8F x N byte matrix of the launch. Bytes are exact FP16 values, every
-// product is below 2^16 and every D_c below 8F * 2^16 <= 2^23 (F <= 16), so
+// product is below 2^16 and every D_c below 8F * 2^16 <= 2^24 (F <= 32), so
 // tcgen05's FP16 MMA with FP32 accumulation in tensor memory computes the D_c
-// exactly. Each thread then reads its row and carries the D_c into the words
+// exactly (below 2^23 for F <= 16, which lets a float addition turn them into
+// integers; above, a conversion instruction does). Each thread then reads its row and carries the D_c into the words
 // of G, S and the output sums on the CUDA cores, instead of the ~300 32-bit
 // multiply-adds of the unrolled sums per coefficient.
 //
@@ -352,20 +353,25 @@ __device__ __forceinline__ uint32_t tc_bytes_half2(uint32_t w, uint32_t sel) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// An exact FP32 integer below 2^23 as an integer: its mantissa after adding 2^23.
+// An exact FP32 integer as an integer: below 2^23 (SMALL), its mantissa after
+// adding 2^23; below 2^24, by conversion.
+template <bool SMALL>
 __device__ __forceinline__ uint32_t tc_int(uint32_t f) {
-  return __float_as_uint(__fadd_rn(__uint_as_float(f), 8388608.0f)) - 0x4B000000u;
+  if constexpr (SMALL) return __float_as_uint(__fadd_rn(__uint_as_float(f), 8388608.0f)) - 0x4B000000u;
+  else return __float2uint_rz(__uint_as_float(f));
 }
 
-// Carries one group (8 column sums D_c, c = 8q .. 8q + 7) into two 32-bit
-// words of sum_c 2^(8c) D_c; acc holds the carry between groups.
+// Carries one group (8 column sums D_c, c = 8q .. 8q + 7, each below 2^24)
+// into two 32-bit words of sum_c 2^(8c) D_c; acc holds the carry between
+// groups.
+template <bool SMALL>
 __device__ __forceinline__ void tc_words(const uint32_t* c, uint64_t& acc, uint32_t* w) {
-  acc += (uint64_t)tc_int(c[0]) + ((uint64_t)tc_int(c[1]) << 8) + ((uint64_t)tc_int(c[2]) << 16) +
-         ((uint64_t)tc_int(c[3]) << 24);
+  acc += (uint64_t)tc_int<SMALL>(c[0]) + ((uint64_t)tc_int<SMALL>(c[1]) << 8) +
+         ((uint64_t)tc_int<SMALL>(c[2]) << 16) + ((uint64_t)tc_int<SMALL>(c[3]) << 24);
   w[0] = (uint32_t)acc;
   acc >>= 32;
-  acc += (uint64_t)tc_int(c[4]) + ((uint64_t)tc_int(c[5]) << 8) + ((uint64_t)tc_int(c[6]) << 16) +
-         ((uint64_t)tc_int(c[7]) << 24);
+  acc += (uint64_t)tc_int<SMALL>(c[4]) + ((uint64_t)tc_int<SMALL>(c[5]) << 8) +
+         ((uint64_t)tc_int<SMALL>(c[6]) << 16) + ((uint64_t)tc_int<SMALL>(c[7]) << 24);
   w[1] = (uint32_t)acc;
   acc >>= 32;
 }
@@ -548,7 +554,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     }
     uint64_t acc = 0;
 #pragma unroll
-    for (uint32_t q = 0; q < 3; q++) tc_words(gs + 8 * q, acc, g + 2 * q);
+    for (uint32_t q = 0; q < 3; q++) tc_words<(MAXF <= 16)>(gs + 8 * q, acc, g + 2 * q);
   } else if constexpr (FASTV) {
 #pragma unroll
     for (int k = 0; k < MAXF; k++)
@@ -584,7 +590,7 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     if constexpr (TC) {
       uint64_t acc = 0;
 #pragma unroll
-      for (uint32_t q = 0; q < 4; q++) tc_words(gs + 24 + 8 * q, acc, pos + 2 * q);
+      for (uint32_t q = 0; q < 4; q++) tc_words<(MAXF <= 16)>(gs + 24 + 8 * q, acc, pos + 2 * q);
       uint32_t vt[8];
       mul128x128w(vt, vlo, vhi, s.tg_lo, s.tg_hi);
       if (s.tg_sign) add256w(pos, vt);
@@ -673,11 +679,11 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
         // products and the two gamma terms keep hi below 4 q_j.
         uint64_t lo = 0, hi = 0, acc = 0;
         if constexpr (TC) {
-          // The output's sum below 2^80 (8 bytes of sums below 2^23), so hi
+          // The output's sum below 2^81 (8 bytes of sums below 2^24), so hi
           // stays below 4 q_j with the gamma terms for q_j above 2^20.
           uint32_t c[8], w2[2];
           tc_ld8(lane + 8 * o, c);
-          tc_words(c, acc, w2);
+          tc_words<(MAXF <= 16)>(c, acc, w2);
           lo = join(w2[0], w2[1]);
           hi = acc;
           acc = 0;
@@ -880,7 +886,7 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
     // The tensor-core form from 12 source moduli: with fewer, its carries
     // cost about what the multiplies they replace did, and its shared memory
     // halves the CTAs per SM (6 sources: 0.40 against 0.33 ms on GB300).
-    if constexpr (EXACT && MAXF >= 12 && MAXF <= 16) {
+    if constexpr (EXACT && MAXF >= 12 && MAXF <= 32) {
       const uint32_t head = h.is_one ? 3 : 7;
       const uint32_t n0 = (8 * head + 15) / 16 * 16, n1 = (8 * n + 15) / 16 * 16;
       if (sc.tc_mat.ptr && rns_tc_enabled() && n1 <= 128 && (TOP > 0 || total % 128 == 0)) {
@@ -1020,10 +1026,10 @@ static uint16_t half_bits(uint32_t v) {
 // rows 24-55 those of (+/- theta_omega_k) 2^(8b) mod 2^256, and rows 56 + 8j ..
 // 56 + 8j + 7 those of omega_jk 2^64 2^(8b) mod q_j; FP16 values in the
 // operand layout of tc.cuh (groups of 8 rows, 16 * kp bytes each). Built for
-// the exact source counts up to 16 with every target modulus above 2^20.
+// up to 32 source moduli with every target modulus above 2^20.
 void RnsScalerD::build_tc_matrix() {
   const size_t F = host.from_len, T = host.to_len;
-  if (!mont || F == 0 || F > 16) return;
+  if (!mont || F == 0 || F > 32) return;
   for (uint64_t q : to_moduli)
     if (q <= (1ull << 20)) return;
   const uint32_t kp = (uint32_t)((8 * F + 15) / 16 * 16);

@@ -166,10 +166,10 @@ FHEG_API int fheg_ntt_prefetch_set(int on);
 FHEG_API int fheg_ntt_cluster_set(uint32_t logn, int on);
 FHEG_API int fheg_ntt_cluster_get(uint32_t logn, int* on);
 /* Tensor-core form of the exact RNS scalings (rns/scaler.rs:249-352 through
- * RnsScaler::scale; no separate counterpart in the reference): for 12 to 16
+ * RnsScaler::scale; no separate counterpart in the reference): for 12 to 32
  * source moduli and odd target moduli above 2^20, the products of the
  * residues with the scaler's constants run as byte-sliced FP16 matrix
- * products on tcgen05 (exact: every column sum stays below 2^23), and the
+ * products on tcgen05 (exact: every column sum stays below 2^24), and the
  * carries, rounding and reductions on the CUDA cores. On by default;
  * results are identical either way. Process-wide. */
 FHEG_API int fheg_rns_tensor_set(int on);

@@ -156,14 +156,16 @@ def _primes(ora, n, count, bits=62):
     return out
 
 
-@pytest.mark.parametrize("F,T", [(12, 1), (12, 7), (12, 10), (12, 13), (13, 3), (13, 8), (13, 10)])
+@pytest.mark.parametrize("F,T", [(12, 1), (12, 7), (12, 10), (12, 13), (13, 3), (13, 8), (13, 10), (25, 5), (25, 12),
+                                 (25, 16)])
 @pytest.mark.parametrize("factor", ["one", "t_over_q", "3_1001"])
 def test_scaler_tensor_core_shapes(fg, ora, cuda, F, T, factor):
-    """Scalers from 12 and 13 source moduli (the tensor-core form; 13 into more
-    than 8 targets takes the generic kernel) into 1 to 13 target moduli of
-    mixed sizes, with and without the signed theta sum (factor one or not),
-    over 64 or 128 tensor-memory columns: equal to the oracle in both
-    representations and to the CUDA-core form."""
+    """Scalers from 12, 13 and 25 source moduli (the tensor-core form; 13 into
+    more than 8 targets takes the generic kernel; 25 has column sums above
+    2^23) into 1 to 16 target moduli of mixed sizes, with and without the
+    signed theta sum (factor one or not), over 64 or 128 tensor-memory
+    columns: equal to the oracle in both representations and to the CUDA-core
+    form."""
     n = 4096
     rng = np.random.default_rng(F * 100 + T)
     pool = _primes(ora, n, F + T, 62)
