@@ -293,9 +293,10 @@ __device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const u
 // product is below 2^16 and every D_c below 8F * 2^16 <= 2^24 (F <= 32), so
 // tcgen05's FP16 MMA with FP32 accumulation in tensor memory computes the D_c
 // exactly (below 2^23 for F <= 16, which lets a float addition turn them into
-// integers; above, a conversion instruction does). Each thread then reads its row and carries the D_c into the words
-// of G, S and the output sums on the CUDA cores, instead of the ~300 32-bit
-// multiply-adds of the unrolled sums per coefficient.
+// integers; above, a conversion instruction does). Each thread then reads its
+// row and carries the D_c into the words of G, S and the output sums on the
+// CUDA cores, instead of the multiply-adds of the unrolled sums (about 300
+// 32-bit ones per coefficient for the L = 6 scale-down).
 //
 // Column groups of 8 (one group = 8 bytes of one sum): 0-2 G, 3-6 S, then one
 // per output modulus. A launch runs two passes through the same tensor-memory
