@@ -478,6 +478,9 @@ def run_ours(args, rank: int, world: int):
     need_60 = 0.6 * peak * 1e9 / (data_bytes + tw_bytes) * bfly
 
     mixed = measure_mixed_levels(fg, ora, torch, par_o, sk)
+    # The uneven-level rotation batch (N = 2^15, 32 ciphertexts at 4 to 12
+    # moduli), after the headline's timed region.
+    rotations = measure_rotations(fg, ora, torch, 32, 20, 3)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -507,6 +510,7 @@ def run_ours(args, rank: int, world: int):
                              "note": "the batch without the graph"},
             "batch_vs_single": value / world / single_rate,
             "mixed_levels": mixed,
+            "rotations": rotations,
             "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
                     "d2h_bytes_per_step": int(h_o.nbytes)},
             "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
@@ -986,33 +990,27 @@ def run_intpeak(args):
     print(json.dumps(line), flush=True)
 
 
-def run_rotate(args):
+def measure_rotations(fg, ora, torch, count: int, steps: int, warmup: int, ntt_block: str = "auto",
+                      ntt_cluster: str = "default"):
     """Uneven-level rotation batch: N = 2^15, twelve 62-bit moduli at the top
-    level, 32 ciphertexts each switched to a random level (4 to 12 live
+    level, `count` ciphertexts each switched to a random level (4 to 12 live
     moduli) and rotated by a random column step in [1, N/2) with the Galois
-    key of its (step, level); ~1 GB of keys resident. One step = the whole
-    ragged batch in one call (one launch per stage)."""
-    import torch
-
-    import __graft_entry__ as ge
-    from oracle import ora
-
-    ge.build()
-    fg = ge.load_package()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    n, top, count = 1 << 15, 12, args.rot_count
-    if args.ntt_cluster != "default":
-        fg.ntt_cluster_set(15, args.ntt_cluster == "on")
+    key of its (step, level); ~1 GB of keys resident at 32. One step = the
+    whole ragged batch in one call (one launch per stage). The first and last
+    rotation are checked against the oracle before timing."""
+    n, top = 1 << 15, 12
+    if ntt_cluster != "default":
+        fg.ntt_cluster_set(15, ntt_cluster == "on")
     rng = np.random.default_rng(15)
     par_o = ora.BfvParameters(n, T, moduli_sizes=[62] * top)
     par = fg.BfvParameters(n, par_o.moduli, T)
     sk = ora.SecretKey.random(par_o, rng)
     levels = [int(x) for x in rng.integers(0, top - 3, count)]  # 4..12 live moduli
-    steps = [int(x) for x in rng.integers(1, n // 2, count)]
+    rot_steps = [int(x) for x in rng.integers(1, n // 2, count)]
     keys, gks_o, cts_o, cts_d = [], [], [], []
     key_bytes = 0
     for b in range(count):
-        e = ora.rotation_exponent(par_o, steps[b])
+        e = ora.rotation_exponent(par_o, rot_steps[b])
         gk = ora.GaloisKey(sk, e, levels[b], levels[b], rng)
         gks_o.append(gk)
         c0, c1 = gk.ksk.c0_array(), gk.ksk.c1_array()
@@ -1023,29 +1021,28 @@ def run_rotate(args):
         cts_o.append(ct)
         cts_d.append(fg.to_device(ct.to_array()))
     outs = [fg.empty(c.shape) for c in cts_d]
-    if args.ntt_block == "auto":
+    if ntt_block == "auto":
         fg.ntt_autotune(par.context_at_level(0), 64)
     else:
-        fg.ntt_plan_set(15, int(args.ntt_block))
+        fg.ntt_plan_set(15, int(ntt_block))
     fg.rotate_batch(par, keys, cts_d, outs)
     torch.cuda.synchronize()
     for b in (0, count - 1):
         if not np.array_equal(fg.to_host(outs[b]), gks_o[b].relinearize(cts_o[b]).to_array()):
             raise SystemExit(f"bench: rotation {b} is not bit-exact with the oracle")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         fg.rotate_batch(par, keys, cts_d, outs)
     stream = torch.cuda.current_stream()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     launches0 = fg.kernel_launch_count()
-    with ClockSampler(0) as clocks:
-        start.record(stream)
-        for _ in range(args.steps):
-            fg.rotate_batch(par, keys, cts_d, outs)
-        end.record(stream)
-        torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(steps):
+        fg.rotate_batch(par, keys, cts_d, outs)
+    end.record(stream)
+    torch.cuda.synchronize()
     launches = fg.kernel_launch_count() - launches0
-    ms = start.elapsed_time(end) / args.steps
+    ms = start.elapsed_time(end) / steps
     # One rotation per call (GaloisKey::relinearize on each ciphertext).
     start.record(stream)
     for b in range(count):
@@ -1053,15 +1050,33 @@ def run_rotate(args):
     end.record(stream)
     torch.cuda.synchronize()
     single_ms = start.elapsed_time(end)
-    lv = [top - l for l in levels]
-    line = {"metric": "ragged rotation ct/s N=2^15 L=4..12 (GaloisKey per level)", "value": count / (ms / 1000),
-            "unit": "ct/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (seeded encryptions and keys by the CPU oracle)",
+    return {"value": count / (ms / 1000), "unit": "ct/s", "ms_per_step": ms, "steps": steps,
             "config": {"workload": "rotation_uneven_levels", "degree": n, "top_moduli": top, "count": count,
-                       "live_moduli": lv, "key_bytes_resident": key_bytes, "ntt_block_logn": fg.ntt_plan_get(15)},
+                       "live_moduli": [top - l for l in levels], "key_bytes_resident": key_bytes,
+                       "ntt_block_logn": fg.ntt_plan_get(15)},
             "single": {"value": count / (single_ms / 1000), "unit": "ct/s", "note": "one call per ciphertext"},
-            "batch_vs_single": single_ms / ms, "gpu_launches": int(launches), "clocks": clocks.summary()}
+            "batch_vs_single": single_ms / ms, "gpu_launches": int(launches)}
+
+
+def run_rotate(args):
+    """The uneven-level rotation batch (measure_rotations) as its own line."""
+    import torch
+
+    import __graft_entry__ as ge
+    from oracle import ora
+
+    ge.build()
+    fg = ge.load_package()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    with ClockSampler(0) as clocks:
+        r = measure_rotations(fg, ora, torch, args.rot_count, args.steps, args.warmup, args.ntt_block,
+                              args.ntt_cluster)
+    line = {"metric": "ragged rotation ct/s N=2^15 L=4..12 (GaloisKey per level)", "value": r["value"],
+            "unit": "ct/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded encryptions and keys by the CPU oracle)", "config": r["config"],
+            "single": r["single"], "batch_vs_single": r["batch_vs_single"], "gpu_launches": r["gpu_launches"],
+            "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
 
 
