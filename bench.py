@@ -481,6 +481,8 @@ def run_ours(args, rank: int, world: int):
     # The uneven-level rotation batch (N = 2^15, 32 ciphertexts at 4 to 12
     # moduli), after the headline's timed region.
     rotations = measure_rotations(fg, ora, torch, 32, 20, 3)
+    # The batched NTT at the other degrees (256 polynomials x 6 limbs).
+    ntt_degrees = measure_ntt_degrees(fg, ora, torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -511,6 +513,7 @@ def run_ours(args, rank: int, world: int):
             "batch_vs_single": value / world / single_rate,
             "mixed_levels": mixed,
             "rotations": rotations,
+            "ntt_degrees": ntt_degrees,
             "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(lhs.nbytes + rhs.nbytes),
                     "d2h_bytes_per_step": int(h_o.nbytes)},
             "roofline": {"bound": "hbm", "achieved": dom_gbs, "peak": peak, "unit": "GB/s", "frac": dom_gbs / peak,
@@ -810,6 +813,55 @@ def run_serialize(args):
             "pack_from_ntt_ms": pack_ntt_ms, "unpack_to_ntt_ms": unpack_ntt_ms,
             "gpu_launches": int(launches), "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
+
+
+def measure_ntt_degrees(fg, ora, torch, logns=(13, 15, 16), polys: int = 256, reps: int = 10):
+    """Forward + inverse NTT of `polys` polynomials of six 62-bit moduli at
+    each degree, under the default plan of the degree (device resident; the
+    first polynomial checked against the oracle): GB/s of algorithmic traffic
+    (each residue read and written once per transform, plus the twiddles)."""
+    out = {}
+    stream = torch.cuda.current_stream()
+    start, mid, end = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    for logn in logns:
+        n = 1 << logn
+        moduli, ub = [], 1 << 62
+        while len(moduli) < L:
+            ub = ora.generate_prime(62, 2 * n, ub)
+            moduli.append(ub)
+        rng = np.random.default_rng(logn)
+        one = np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in moduli])
+        ctx = fg.Context(moduli, n)
+        buf = fg.to_device(np.tile(one[None], (polys, 1, 1)))
+        expect = one.copy()
+        for i, m in enumerate(moduli):
+            ora.ntt_operator(m, n).forward(expect[i])
+        fg.ntt_forward(ctx, buf)
+        torch.cuda.synchronize()
+        if not np.array_equal(fg.to_host(buf[:1])[0], expect):
+            raise SystemExit(f"bench: NTT at 2^{logn} is not bit-exact with the oracle")
+        fg.ntt_backward(ctx, buf)
+        for _ in range(3):
+            fg.ntt_forward(ctx, buf)
+            fg.ntt_backward(ctx, buf)
+        fwd = inv = 0.0
+        for _ in range(reps):
+            start.record(stream)
+            fg.ntt_forward(ctx, buf)
+            mid.record(stream)
+            fg.ntt_backward(ctx, buf)
+            end.record(stream)
+            torch.cuda.synchronize()
+            fwd += start.elapsed_time(mid)
+            inv += mid.elapsed_time(end)
+        fwd, inv = fwd / reps, inv / reps
+        nbytes = 2 * 8 * polys * L * n + 2 * 8 * L * n
+        out[f"2^{logn}"] = {"fwd_gbs": nbytes / (fwd / 1000) / 1e9, "inv_gbs": nbytes / (inv / 1000) / 1e9,
+                            "fwd_ms": fwd, "inv_ms": inv, "block_logn": fg.ntt_plan_get(logn),
+                            "cluster": fg.ntt_cluster_get(logn),
+                            "fwd_butterflies_per_s": polys * L * butterflies_per_transform(logn) / (fwd / 1000)}
+        del buf
+    return out
 
 
 def run_ntt(args):
