@@ -337,24 +337,27 @@ __global__ void k_key_mac(const DevPrime* primes, const uint64_t* D, uint64_t ds
       }
     }
   }
-  for (uint32_t d = 0; d < (MAXD > 0 ? 0u : ndig); d++) {
-    const uint64_t w0 = __ldg(kp0 + d * kstride), w1 = __ldg(kp1 + d * kstride);
-#pragma unroll
-    for (int u = 0; u < KB; u++) {
-      const uint64_t b = b0 + u;
-      if (b < batch) {
-        const uint64_t x = D[(b * ndig + d) * dstride + ((uint64_t)j << logn) + i];
-        mac128(hi0[u], lo0[u], x, w0);
-        mac128(hi1[u], lo1[u], x, w1);
-      }
-    }
-    if (d % 15 == 14) {
+  // The digits of the generic form (MAXD 0): the other forms took theirs above.
+  if constexpr (MAXD == 0) {
+    for (uint32_t d = 0; d < ndig; d++) {
+      const uint64_t w0 = __ldg(kp0 + d * kstride), w1 = __ldg(kp1 + d * kstride);
 #pragma unroll
       for (int u = 0; u < KB; u++) {
-        lo0[u] = reduce128(hi0[u], lo0[u], pr);
-        hi0[u] = 0;
-        lo1[u] = reduce128(hi1[u], lo1[u], pr);
-        hi1[u] = 0;
+        const uint64_t b = b0 + u;
+        if (b < batch) {
+          const uint64_t x = D[(b * ndig + d) * dstride + ((uint64_t)j << logn) + i];
+          mac128(hi0[u], lo0[u], x, w0);
+          mac128(hi1[u], lo1[u], x, w1);
+        }
+      }
+      if (d % 15 == 14) {
+#pragma unroll
+        for (int u = 0; u < KB; u++) {
+          lo0[u] = reduce128(hi0[u], lo0[u], pr);
+          hi0[u] = 0;
+          lo1[u] = reduce128(hi1[u], lo1[u], pr);
+          hi1[u] = 0;
+        }
       }
     }
   }

@@ -306,14 +306,20 @@ __device__ __noinline__ void rns_exact_s(const RnsLaunch<MAXF, MAXT>* s, const u
 // once pass 0's MMAs are done with it). N of a pass is 8 groups rounded up to
 // a multiple of 16; the rows beyond its groups hold stale bytes whose columns
 // are never read.
+//
+// Split form (a scale-down whose operand buffer would otherwise cost an SM a
+// CTA): four passes through a smaller buffer, G into columns 0-31, S into
+// 32-63, the first `chunk` outputs into 64.., and once every thread has read
+// G and S, the other outputs into 0.. .
 struct TcMat {
   const uint16_t* mat;   // FP16 bit patterns, 16 * kp bytes per group (tc.cuh layout)
   uint32_t kp;           // 8 F rounded up to a multiple of 16
   uint32_t head_groups;  // G (and S) groups: 3 or 7
   uint32_t out_group0;   // first output group of the launch (7 + start)
-  uint32_t n0, n1;       // N of pass 0 and pass 1
+  uint32_t n0, n1;       // N of pass 0 (G and S; split: G) and of the (first) output pass
   uint32_t cols;         // tensor-memory columns allocated (64 or 128)
   uint32_t b_offset;     // byte offset of B in the dynamic shared memory
+  uint32_t chunk, n2;    // split form: outputs of the first output pass, N of the second
 };
 
 // Count of waits of the tensor-core scaler that ran out (the MMA or the
@@ -322,15 +328,18 @@ __device__ uint32_t g_tc_wait_failures;
 
 constexpr uint32_t kTcWaitTries = 1u << 20;
 
-// Thread 0: the MMAs of one pass (K / 16 of them, N = n) once its operand B
-// has landed (phase `phase` of bar_b), committed to bar_mma. A copy that does
-// not land in time is counted, the pass's MMAs are skipped (its outputs are
-// then not valid) and bar_mma is released by hand so that no thread waits
-// longer than its own bounded wait.
+// Thread 0: the MMAs of pass `phase` (K / 16 of them, N = n, into the
+// columns at `tmem`) once its operand B has landed (that phase of bar_b),
+// committed to bar_mma, the pass's own single-use barrier (waited at parity
+// 0: a barrier shared by several passes aliases their phases for a thread
+// that waits after two of them have completed). A copy that does not land in
+// time is counted, the pass's MMAs are skipped (its outputs are then not
+// valid) and bar_mma is released by hand so that no thread waits longer than
+// its own bounded wait.
 template <uint32_t KP>
 __device__ __forceinline__ void tc_pass(uint32_t bar_b, uint32_t bar_mma, uint32_t phase, uint32_t tmem, uint32_t sa,
                                         uint32_t sb, uint32_t n) {
-  if (mbar_wait(bar_b, phase, kTcWaitTries)) {
+  if (mbar_wait(bar_b, phase & 1, kTcWaitTries)) {
     const uint32_t idesc = tc_idesc_f16_f32(128, n);
 #pragma unroll
     for (uint32_t kk = 0; kk < KP / 16; kk++)
@@ -340,7 +349,7 @@ __device__ __forceinline__ void tc_pass(uint32_t bar_b, uint32_t bar_mma, uint32
   } else {
     atomicAdd(&g_tc_wait_failures, 1u);
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_mma) : "memory");
-    mbar_wait(bar_b, phase, kTcWaitTries);
+    mbar_wait(bar_b, phase & 1, kTcWaitTries);
   }
 }
 
@@ -396,12 +405,14 @@ __device__ __forceinline__ uint64_t* scale_stage() {
 // scale-down (13 source moduli, which also forms w) by 15%, so only the
 // extensions' source counts use them and the rest sum exactly inline.
 //
-// TC (EXACT, 12 <= F <= 16): the sums come from the tensor core (above); every CTA
-// covers 128 coefficients with all its threads, holds 128 tensor-memory
-// columns and at least 57 KB of shared memory, so that at most four CTAs
-// share an SM's 512 columns. The stage buffer then lives in the dynamic
-// shared memory, where A overlays it once every thread holds its residues.
-template <int MAXF, int MAXT, bool EXACT, int TOP, bool FASTV, bool TC>
+// TC (EXACT, 12 <= F <= 32): the sums come from the tensor core (above); every
+// CTA covers 128 coefficients with all its threads and holds 64 or 128
+// tensor-memory columns and at least 456 bytes of shared memory per column,
+// so that the CTAs an SM holds never ask for more than its 512 columns. The
+// stage buffer then lives in the dynamic shared memory, where A overlays it
+// once every thread holds its residues. SPLIT (with TC): the split form, a
+// kernel of its own so that the two-pass form carries none of its branches.
+template <int MAXF, int MAXT, bool EXACT, int TOP, bool FASTV, bool TC, bool SPLIT = false>
 __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLaunch<MAXF, MAXT> s, uint32_t logn,
                                                    PolyRef in, PolyRef out, uint64_t total,
                                                    const DevPrime* src_primes, uint32_t src_mont,
@@ -412,9 +423,9 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   uint32_t i, poly, b0 = 0, logb = 0, t = 0, gi = 0;
   bool fwd_here = false, dig_here = false;  // uniform across the CTA (one polynomial)
   uint64_t r[MAXF];
-  [[maybe_unused]] uint32_t tmem = 0, bar_b = 0, bar_mma = 0;
+  [[maybe_unused]] uint32_t tmem = 0, bar_b = 0, bar_mma = 0;  // bar_mma: pass 0's; pass p's is bar_mma + 8 p
   [[maybe_unused]] uint8_t* tc_a = nullptr;
-  [[maybe_unused]] __shared__ __align__(8) uint64_t tc_bars[TC ? 2 : 1];
+  [[maybe_unused]] __shared__ __align__(8) uint64_t tc_bars[TC ? 5 : 1];
   [[maybe_unused]] __shared__ uint32_t tc_slot;
   if constexpr (TC) {
     // Operand B in flight and the tensor memory allocated while the sources
@@ -426,10 +437,12 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     const uint32_t group_bytes = 16 * KP;
     if (threadIdx.x == 0) {
       mbar_init(bar_b, 1);
-      mbar_init(bar_mma, 1);
+#pragma unroll
+      for (uint32_t p = 0; p < 4; p++) mbar_init(bar_mma + 8 * p, 1);
       fence_proxy_async_smem();
-      mbar_expect_tx(bar_b, tc.head_groups * group_bytes);
-      bulk_g2s(smem_u32(tc_b), tc.mat, tc.head_groups * group_bytes, bar_b);
+      const uint32_t first = (SPLIT ? 3 : tc.head_groups) * group_bytes;
+      mbar_expect_tx(bar_b, first);
+      bulk_g2s(smem_u32(tc_b), tc.mat, first, bar_b);
     }
     if ((threadIdx.x >> 5) == 1) tc_alloc(smem_u32(&tc_slot), tc.cols);
   }
@@ -523,13 +536,13 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
     if (threadIdx.x == 0) tc_pass<KP>(bar_b, bar_mma, 0, tmem, sa, sb, tc.n0);
     if (!mbar_wait(bar_mma, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
     tc_fence_after();
-    // Pass 0's MMAs are done with B: pass 1's operand lands while its columns
-    // are read.
+    // Pass 0's MMAs are done with B: pass 1's operand (S when split, else the
+    // outputs) lands while its columns are read.
     if (threadIdx.x == 0) {
       const uint32_t group_bytes = 16 * KP;
-      mbar_expect_tx(bar_b, s.out_len * group_bytes);
-      bulk_g2s(sb, reinterpret_cast<const uint8_t*>(tc.mat) + tc.out_group0 * group_bytes, s.out_len * group_bytes,
-               bar_b);
+      const uint32_t g0 = SPLIT ? 3 : tc.out_group0, ng = SPLIT ? 4 : s.out_len;
+      mbar_expect_tx(bar_b, ng * group_bytes);
+      bulk_g2s(sb, reinterpret_cast<const uint8_t*>(tc.mat) + g0 * group_bytes, ng * group_bytes, bar_b);
     }
     lane = tmem + (((threadIdx.x >> 5) * 32u) << 16);
   }
@@ -542,16 +555,44 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   // TC: the column sums of G (24) and S (32) in one tensor-memory round trip.
   [[maybe_unused]] uint32_t gs[TC ? 56 : 1];
   if constexpr (TC) {
-    if (s.is_one) tc_ld24(lane, gs);
-    else tc_ld56(lane, gs);
-    // Every lane's pass-0 columns are read: pass 1 may overwrite them, and
-    // its MMAs run while the sums below are carried and rounded.
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (threadIdx.x == 0) {
-      const uint32_t sa = smem_u32(tc_a);
-      tc_pass<KP>(bar_b, bar_mma, 1, tmem, sa, sa + tc.b_offset, tc.n1);
+    const uint32_t sa = smem_u32(tc_a), sb = sa + tc.b_offset;
+    if constexpr (!SPLIT) {
+      if (s.is_one) tc_ld24(lane, gs);
+      else tc_ld56(lane, gs);
+      // Every lane's pass-0 columns are read: pass 1 may overwrite them, and
+      // its MMAs run while the sums below are carried and rounded.
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (threadIdx.x == 0) tc_pass<KP>(bar_b, bar_mma + 8, 1, tmem, sa, sb, tc.n1);
+    } else {
+      // S (pass 1) into columns 32-63 while G is read.
+      if (threadIdx.x == 0) tc_pass<KP>(bar_b, bar_mma + 8, 1, tmem + 32, sa, sb, 32);
+      tc_ld24(lane, gs);
+      if (!mbar_wait(bar_mma + 8, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+      tc_fence_after();
+      const uint32_t group_bytes = 16 * KP;
+      if (threadIdx.x == 0) {
+        mbar_expect_tx(bar_b, tc.chunk * group_bytes);
+        bulk_g2s(sb, reinterpret_cast<const uint8_t*>(tc.mat) + tc.out_group0 * group_bytes, tc.chunk * group_bytes,
+                 bar_b);
+      }
+      tc_ld32(lane + 32, gs + 24);
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      // The first outputs (pass 2) into columns 64.., then, once their MMAs
+      // are done with B, the others (pass 3) over G and S.
+      if (threadIdx.x == 0) {
+        tc_pass<KP>(bar_b, bar_mma + 16, 2, tmem + 64, sa, sb, tc.n1);
+        if (!mbar_wait(bar_mma + 16, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+        tc_fence_after();
+        const uint32_t rest = s.out_len - tc.chunk;
+        mbar_expect_tx(bar_b, rest * group_bytes);
+        bulk_g2s(sb, reinterpret_cast<const uint8_t*>(tc.mat) + (tc.out_group0 + tc.chunk) * group_bytes,
+                 rest * group_bytes, bar_b);
+        tc_pass<KP>(bar_b, bar_mma + 24, 3, tmem, sa, sb, tc.n2);
+      }
     }
     uint64_t acc = 0;
 #pragma unroll
@@ -660,7 +701,14 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
   // modulo each q_j. The sum then holds at most 15 terms below 2^124 (and a
   // few small ones) between reductions: below 2^128.
   if constexpr (TC) {
-    if (!mbar_wait(bar_mma, 1, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+    // Every output pass done (split: passes 2 and 3) before the outputs, which
+    // may go to the stage buffer that A overlays.
+    if constexpr (!SPLIT) {
+      if (!mbar_wait(bar_mma + 8, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+    } else {
+      if (!mbar_wait(bar_mma + 16, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+      if (!mbar_wait(bar_mma + 24, 0, kTcWaitTries)) atomicAdd(&g_tc_wait_failures, 1u);
+    }
     tc_fence_after();
   }
   const uint64_t v_low = vlo & ((1ull << 62) - 1);
@@ -683,7 +731,8 @@ __global__ void __launch_bounds__(128) k_rns_scale(const __grid_constant__ RnsLa
           // The output's sum below 2^81 (8 bytes of sums below 2^24), so hi
           // stays below 4 q_j with the gamma terms for q_j above 2^20.
           uint32_t c[8], w2[2];
-          tc_ld8(lane + 8 * o, c);
+          const uint32_t col = !SPLIT ? 8 * o : (uint32_t)o < tc.chunk ? 64 + 8 * o : 8 * (o - tc.chunk);
+          tc_ld8(lane + col, c);
           tc_words<(MAXF <= 16)>(c, acc, w2);
           lo = join(w2[0], w2[1]);
           hi = acc;
@@ -894,18 +943,48 @@ void launch_rns_scale(const RnsScalerD& sc, uint32_t logn, PolyRef in, PolyRef o
         constexpr uint32_t KP = (8 * MAXF + 15) / 16 * 16;
         if (sc.tc_kp != KP) throw Error(FHEG_ERR_INTERNAL, "tensor-core scaler matrix of another width");
         auto kern = k_rns_scale<MAXF, MAXT, EXACT, TOP, false, true>;
-        const uint32_t cols = std::max(n0, n1) <= 64 ? 64 : 128;
         // The stage buffer (TOP > 0) overlaid by A, then B (the larger pass).
         constexpr size_t kStage = TOP > 0 ? (size_t)(MAXF > MAXT ? MAXF : MAXT) * 128 * 8 : 0;
         constexpr size_t kBOff = ((128 * KP * 2 > kStage ? 128 * KP * 2 : kStage) + 127) / 128 * 128;
-        const TcMat tc{static_cast<const uint16_t*>(sc.tc_mat.ptr), KP, head, 7 + start + first, n0, n1, cols,
-                       (uint32_t)kBOff};
-        // At least cols * 456 bytes of shared memory per CTA (with the 1 KB
-        // the SM reserves per CTA): the SM's 228 KB then never holds CTAs
-        // asking for more than its 512 tensor-memory columns.
         const size_t stat = tc_prepare(reinterpret_cast<const void*>(kern), kBOff + 128 * 2 * KP);
-        const size_t floor_dyn = cols * kTcSmemPerColumn - 1024 - stat;
-        const size_t dyn = std::max<size_t>(kBOff + std::max(n0, n1) * 2 * KP, floor_dyn);
+        // Shared memory of a form (operand buffer of `rows` rows), at least
+        // cols * 456 bytes with the 1 KB the SM reserves per CTA: the SM's
+        // 228 KB then never holds CTAs asking for more than its 512
+        // tensor-memory columns. CTAs per SM of a form by shared and tensor
+        // memory.
+        auto dyn_of = [&](uint32_t rows, uint32_t cols) {
+          return std::max<size_t>(kBOff + (size_t)rows * 2 * KP, cols * kTcSmemPerColumn - 1024 - stat);
+        };
+        auto ctas = [&](size_t dyn, uint32_t cols) {
+          return std::min<size_t>(233472 / (dyn + stat + 1024), 512 / cols);
+        };
+        uint32_t cols = std::max(n0, n1) <= 64 ? 64 : 128;
+        size_t dyn = dyn_of(std::max(n0, n1), cols);
+        TcMat tc{static_cast<const uint16_t*>(sc.tc_mat.ptr), KP, head, 7 + start + first, n0, n1, cols,
+                 (uint32_t)kBOff, 0, 0};
+        // The split form (scale-downs of two outputs or more) where it fits
+        // more CTAs on an SM. Only a wide A (over 16 sources) leaves it room
+        // to: with fewer, 64 columns or the same count of CTAs hold already.
+        if constexpr (MAXT > 8 && MAXF > 16) {
+          if (!h.is_one && n >= 2) {
+            const uint32_t chunk = (n + 1) / 2, s1 = (8 * chunk + 15) / 16 * 16, s2 = (8 * (n - chunk) + 15) / 16 * 16;
+            auto skern = k_rns_scale<MAXF, MAXT, EXACT, TOP, false, true, true>;
+            const size_t sstat = tc_prepare(reinterpret_cast<const void*>(skern), kBOff + 128 * 2 * KP);
+            const size_t sdyn = std::max<size_t>(kBOff + (size_t)std::max(32u, s1) * 2 * KP,
+                                                 128 * kTcSmemPerColumn - 1024 - sstat);
+            if (s1 <= 64 && std::min<size_t>(233472 / (sdyn + sstat + 1024), 4) > ctas(dyn, cols)) {
+              tc.n0 = 32;
+              tc.n1 = s1;
+              tc.n2 = s2;
+              tc.chunk = chunk;
+              tc.cols = 128;
+              skern<<<blocks_for(total, threads), threads, sdyn, st>>>(
+                  s, logn, in, o, total, top ? top->primes : nullptr, top ? top->mont : 0u, fe, tc);
+              after_launch("k_rns_scale");
+              continue;
+            }
+          }
+        }
         kern<<<blocks_for(total, threads), threads, dyn, st>>>(s, logn, in, o, total, top ? top->primes : nullptr,
                                                               top ? top->mont : 0u, fe, tc);
         after_launch("k_rns_scale");
