@@ -1116,7 +1116,7 @@ class Multiplicator:
                                                ctypes.byref(h)))
         return MultiplyGraph(h, [self, lhs, rhs, out])
 
-    def set_host_pipeline(self, chunk: int = 0, streams: int = 4):
+    def set_host_pipeline(self, chunk: int = 0, streams: int = 3):
         """Chunk size (pairs, 0 = automatic) and stream count of multiply_host."""
         check(lib().fheg_multiplicator_set_host_pipeline(self._h, chunk, streams))
 

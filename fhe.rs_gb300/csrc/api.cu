@@ -965,36 +965,44 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     const int ns = m->host_streams;
     for (int k = 0; k < ns; k++)
       if (!m->pipe[k]) check_cuda(cudaStreamCreateWithFlags(&m->pipe[k], cudaStreamNonBlocking), "stream");
-    // Chunks rotate over the pipeline's streams, so the copies of one chunk
-    // overlap the multiplication of others. The input copies of chunk i wait
-    // for those of chunk i-1: the host link carries one chunk at a time, and
-    // the first chunk's inputs arrive at full link speed. Small chunks (4
-    // pairs, run with the small-batch plan, four at a time) measured best
-    // on GB300 at 32 and 64 pairs: the fill and drain of the pipeline cost one
-    // small chunk's copies, and concurrent chunks keep the SMs busy.
+    if (!m->copy_in) check_cuda(cudaStreamCreateWithFlags(&m->copy_in, cudaStreamNonBlocking), "stream");
+    if (!m->copy_out) check_cuda(cudaStreamCreateWithFlags(&m->copy_out, cudaStreamNonBlocking), "stream");
+    // Every chunk's inputs cross the host link back to back on one stream and
+    // its output on another, in chunk order; chunk i multiplies on compute
+    // stream i % ns once its inputs have landed. Each chunk has its own
+    // staging rows, so no copy waits for a multiplication other than its
+    // own chunk's, and no multiplication for a copy of another chunk. Small
+    // chunks (4 pairs, four at a time) keep the fill (one chunk's inputs)
+    // and the drain (one chunk's output) short.
     const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 8 ? 4 : count);
     const size_t nchunks = (count + chunk - 1) / chunk;
-    while (m->copied.size() < nchunks) {
-      cudaEvent_t e;
-      check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
-      m->copied.push_back(e);
-    }
+    for (auto* evs : {&m->copied, &m->computed})
+      while (evs->size() < nchunks) {
+        cudaEvent_t e;
+        check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        evs->push_back(e);
+      }
     const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * out_L * N;
     for (size_t i = 0; i < nchunks; i++) {
       const size_t first = i * chunk, c = std::min(chunk, count - first);
       const int k = (int)(i % ns);
       cudaStream_t st = m->pipe[k];
-      if (i > 0) check_cuda(cudaStreamWaitEvent(st, m->copied[i - 1], 0), "cudaStreamWaitEvent");
       check_cuda(cudaMemcpyAsync(d_lhs + first * in_pair, h_lhs + first * in_pair, c * in_pair * 8,
-                                 cudaMemcpyHostToDevice, st), "H2D");
+                                 cudaMemcpyHostToDevice, m->copy_in), "H2D");
       check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
-                                 cudaMemcpyHostToDevice, st), "H2D");
-      check_cuda(cudaEventRecord(m->copied[i], st), "cudaEventRecord");
+                                 cudaMemcpyHostToDevice, m->copy_in), "H2D");
+      check_cuda(cudaEventRecord(m->copied[i], m->copy_in), "cudaEventRecord");
+      check_cuda(cudaStreamWaitEvent(st, m->copied[i], 0), "cudaStreamWaitEvent");
       mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
                   &m->pipe_ws[k]);
+      check_cuda(cudaEventRecord(m->computed[i], st), "cudaEventRecord");
+      check_cuda(cudaStreamWaitEvent(m->copy_out, m->computed[i], 0), "cudaStreamWaitEvent");
       check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
-                                 cudaMemcpyDeviceToHost, st), "D2H");
+                                 cudaMemcpyDeviceToHost, m->copy_out), "D2H");
     }
+    // The output stream waits for every chunk, and every chunk for its inputs.
+    check_cuda(cudaStreamSynchronize(m->copy_out), "cudaStreamSynchronize");
     for (int k = 0; k < ns; k++) check_cuda(cudaStreamSynchronize(m->pipe[k]), "cudaStreamSynchronize");
+    check_cuda(cudaStreamSynchronize(m->copy_in), "cudaStreamSynchronize");
   });
 }

@@ -43,11 +43,14 @@ struct fheg_rgsw {
 struct fheg_multiplicator {
   static constexpr int kPipe = 4;  // most streams of the host entry point's copy / compute pipeline
   std::unique_ptr<fheg::Multiplicator> m;
-  cudaStream_t pipe[kPipe] = {};
+  cudaStream_t pipe[kPipe] = {};      // compute streams
+  cudaStream_t copy_in = nullptr;      // every chunk's input copies, in chunk order
+  cudaStream_t copy_out = nullptr;     // every chunk's output copy, in chunk order
   fheg::Workspace pipe_ws[kPipe];
-  std::vector<cudaEvent_t> copied;  // end of each chunk's input copies
+  std::vector<cudaEvent_t> copied;    // end of each chunk's input copies
+  std::vector<cudaEvent_t> computed;  // end of each chunk's multiplication
   size_t host_chunk = 0;            // pairs per chunk (0 = automatic)
-  int host_streams = 4;
+  int host_streams = 3;
   // Second branch of a large direct multiplication (api.cu): its stream,
   // fork / join events and scratch.
   cudaStream_t side = nullptr;
@@ -56,7 +59,10 @@ struct fheg_multiplicator {
   ~fheg_multiplicator() {
     for (auto& s : pipe)
       if (s) cudaStreamDestroy(s);
+    if (copy_in) cudaStreamDestroy(copy_in);
+    if (copy_out) cudaStreamDestroy(copy_out);
     for (auto& e : copied) cudaEventDestroy(e);
+    for (auto& e : computed) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);

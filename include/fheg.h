@@ -419,10 +419,11 @@ FHEG_API int fheg_multiplicator_set_small_plan(fheg_multiplicator* m, size_t max
  * A count within the small-batch threshold tunes the small-batch plan. */
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan);
 /* Pipeline of fheg_multiplicator_multiply_host: `chunk` pairs per chunk
- * (0 = automatic: 4 when count >= 8, else the whole call) rotating over
- * `streams` streams (1..4, default 4), each with its own scratch. Changes
- * only the overlap of copies and compute, never the results. No counterpart
- * in the reference. */
+ * (0 = automatic: 4 when count >= 8, else the whole call) multiplied on
+ * `streams` compute streams in turn (1..4, default 3), each with its own
+ * scratch; the inputs and outputs cross the host link on two copy streams
+ * of their own. Changes only the overlap of copies and compute, never the
+ * results. No counterpart in the reference. */
 FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t chunk, int streams);
 /* Multiplicator::multiply end to end from host buffers (h_lhs, h_rhs
  * [count][2][L][N], h_out the output shape): copies the inputs to the
