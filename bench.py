@@ -188,13 +188,13 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_inputs(ora, batch: int, seed: int = 2026, distinct: int = 16):
+def make_inputs(ora, batch: int, seed: int = 2026, distinct: int = 16, degree: int = N, moduli: int = L):
     """Keys and `batch` ciphertext pairs (cycled from `distinct` encryptions)."""
     rng = np.random.default_rng(seed)
-    par = ora.BfvParameters(N, T, moduli_sizes=[62] * L)
+    par = ora.BfvParameters(degree, T, moduli_sizes=[62] * moduli)
     sk = ora.SecretKey.random(par, rng)
     rk = ora.RelinearizationKey(sk, rng)
-    cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, N, dtype=np.uint64), "simd", par), rng)
+    cts = [sk.encrypt(ora.Plaintext.encode(rng.integers(0, T, degree, dtype=np.uint64), "simd", par), rng)
            for _ in range(distinct)]
     arrs = [c.to_array() for c in cts]
     lhs = np.stack([arrs[i % distinct] for i in range(batch)])
@@ -552,7 +552,8 @@ def run_ours(args, rank: int, world: int):
 
 def run_stages(args):
     """Stage breakdown of the batched multiplication (64 pairs at N = 2^14,
-    L = 6): W warm-up multiplies, then one multiply with events at the stage
+    L = 6 by default; --logn and --moduli choose another parameter set): W
+    warm-up multiplies, then one multiply with events at the stage
     boundaries. Small enough to run under a profiler (14 launches a multiply)."""
     import torch
 
@@ -562,23 +563,23 @@ def run_stages(args):
     ge.build()
     fg = ge.load_package()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-    B = args.batch
-    par_o, sk, rk_o, cts, lhs, rhs = make_inputs(ora, B)
-    par = fg.BfvParameters(N, par_o.moduli, T)
+    B, n, nmod = args.batch, 1 << args.logn, args.moduli
+    par_o, sk, rk_o, cts, lhs, rhs = make_inputs(ora, B, distinct=min(16, B), degree=n, moduli=nmod)
+    par = fg.BfvParameters(n, par_o.moduli, T)
     rk = fg.RelinearizationKey(par, rk_o.ksk.c0_array(), rk_o.ksk.c1_array())
     mult = fg.Multiplicator.default(rk)
     if args.stage_plan:
         mult.plan = [int(x) for x in args.stage_plan.split(",")]
     lhs_d, rhs_d = fg.to_device(lhs), fg.to_device(rhs)
-    out_d = fg.empty((B, 2, L, N))
+    out_d = fg.empty((B, 2, nmod, n))
     fg.rns_tensor_set(args.rns_tensor == "on")
     for _ in range(args.warmup):
         mult.multiply(lhs_d, rhs_d, out_d)
     runs = [mult.stage_times(lhs_d, rhs_d, out_d) for _ in range(max(1, args.stage_runs))]
     ms = {k: statistics.median(r[k] for r in runs) for k in runs[0]}
     torch.cuda.synchronize()
-    print(json.dumps({"workload": "stages", "batch_pairs": B, "plan": mult.plan, "rns_tensor": args.rns_tensor,
-                      "runs": len(runs), "stage_ms": ms}), flush=True)
+    print(json.dumps({"workload": "stages", "batch_pairs": B, "degree": n, "moduli": nmod, "plan": mult.plan,
+                      "rns_tensor": args.rns_tensor, "runs": len(runs), "stage_ms": ms}), flush=True)
 
 
 def run_codec(args):
@@ -1333,6 +1334,7 @@ def main():
     ap.add_argument("--rot-count", type=int, default=32)
     ap.add_argument("--polys", type=int, default=256)
     ap.add_argument("--logn", type=int, default=14)
+    ap.add_argument("--moduli", type=int, default=L, help="stages workload: ciphertext moduli")
     ap.add_argument("--ntt-prefetch", default="off", choices=["on", "off"],
                     help="L2 prefetch of the next CTA's NTT input")
     ap.add_argument("--stage-plan", default="", help="A,C,D,F,F-split,D-split plan of the multiply stages")
