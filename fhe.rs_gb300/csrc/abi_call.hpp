@@ -35,4 +35,14 @@ inline void abi_need(bool cond, const char* what) {
   if (!cond) throw Error(FHEG_ERR_INVALID_ARGUMENT, what);
 }
 
+// Most items one call takes (ciphertexts, polynomials, requests): 2^24.
+// Device memory holds far fewer of the smallest items, and below this bound
+// no size an entry point derives from the count (count x parts x moduli x
+// degree x 8 bytes, with at most 2^33 bytes an item) can wrap around 2^64 to
+// a small allocation that the kernels would then overrun.
+constexpr size_t kMaxItems = size_t(1) << 24;
+inline void abi_count(size_t count) {
+  if (count > kMaxItems) throw Error(FHEG_ERR_INVALID_ARGUMENT, "item count above 2^24 per call");
+}
+
 }  // namespace fheg

@@ -140,6 +140,7 @@ FHEG_API size_t fheg_context_degree(const fheg_context* ctx) { return ctx ? ctx-
 
 FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t count, int lazy, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && (d_polys || !count), "null input");
     PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
     ntt_forward(*ctx->c, r, r, count, lazy != 0, as_stream(stream));
@@ -148,6 +149,7 @@ FHEG_API int fheg_ntt_forward(const fheg_context* ctx, uint64_t* d_polys, size_t
 
 FHEG_API int fheg_ntt_backward(const fheg_context* ctx, uint64_t* d_polys, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && (d_polys || !count), "null input");
     PolyRef r = plain_ref(d_polys, ctx->c->L(), ctx->c->logn);
     ntt_backward(*ctx->c, r, r, count, as_stream(stream));
@@ -250,6 +252,7 @@ uint32_t autotune_plans(uint32_t logn, cudaStream_t st, F run) {
 
 FHEG_API int fheg_ntt_autotune(const fheg_context* ctx, size_t count, void* stream, uint32_t* block_logn) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && count && block_logn, "null input");
     const Context& c = *ctx->c;
     cudaStream_t st = as_stream(stream);
@@ -323,6 +326,7 @@ void set_mul_plan(Multiplicator& m, const uint32_t* plan) {
 FHEG_API int fheg_multiplicator_stage_times(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                             uint64_t* d_out, size_t count, void* stream, float* ms) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(m && d_lhs && d_rhs && d_out && count && ms, "null input");
     cudaStream_t st = as_stream(stream);
     cudaEvent_t ev[8] = {};
@@ -369,6 +373,7 @@ FHEG_API int fheg_multiplicator_set_plan(fheg_multiplicator* m, const uint32_t* 
 
 FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, void* stream, uint32_t* plan) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(m && count, "null input");
     Multiplicator& mult = *m->m;
     const Context& bc = *mult.base;
@@ -426,6 +431,7 @@ FHEG_API int fheg_multiplicator_autotune(fheg_multiplicator* m, size_t count, vo
 FHEG_API int fheg_poly_scalar_mul(const fheg_context* ctx, const uint64_t* scalar, size_t scalar_words,
                                   const uint64_t* d_in, uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_in && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     poly_scalar_mul(c, big(scalar, scalar_words), plain_ref(const_cast<uint64_t*>(d_in), c.L(), c.logn),
@@ -468,6 +474,7 @@ FHEG_API int fheg_copy_to_host(void* h_dst, const void* d_src, size_t bytes, voi
 FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out,
                           size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && op >= 0 && op <= 3, "bad context or op");
     abi_need((d_a && d_out && (op == 3 || d_b)) || !count, "null input");
     const Context& c = *ctx->c;
@@ -481,6 +488,7 @@ FHEG_API int fheg_poly_op(const fheg_context* ctx, int op, const uint64_t* d_a, 
 FHEG_API int fheg_poly_compute_shoup(const fheg_context* ctx, const uint64_t* d_polys, uint64_t* d_shoup,
                                      size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_polys && d_shoup) || !count), "null input");
     const Context& c = *ctx->c;
     poly_compute_shoup(c, plain_ref(const_cast<uint64_t*>(d_polys), c.L(), c.logn), plain_ref(d_shoup, c.L(), c.logn),
@@ -491,6 +499,7 @@ FHEG_API int fheg_poly_compute_shoup(const fheg_context* ctx, const uint64_t* d_
 FHEG_API int fheg_poly_mul_shoup(const fheg_context* ctx, const uint64_t* d_a, const uint64_t* d_b,
                                  const uint64_t* d_b_shoup, uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_a && d_b && d_b_shoup && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     poly_mul_shoup(c, plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn),
@@ -503,6 +512,7 @@ FHEG_API int fheg_poly_mul_shoup(const fheg_context* ctx, const uint64_t* d_a, c
 FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int representation, const uint64_t* d_in,
                                   uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_in && d_out) || !count), "null input");
     abi_need(d_in != d_out || !count, "d_out must not alias d_in");
     const Context& c = *ctx->c;
@@ -515,6 +525,7 @@ FHEG_API int fheg_poly_substitute(const fheg_context* ctx, size_t exponent, int 
 FHEG_API int fheg_poly_switch_down(const fheg_context* ctx, int representation, uint64_t* d_in, uint64_t* d_out,
                                    size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_in && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     PolyRef i = plain_ref(d_in, c.L(), c.logn);
@@ -546,6 +557,7 @@ FHEG_API void fheg_scaler_destroy(fheg_scaler* s) { delete s; }
 FHEG_API int fheg_scaler_scale(const fheg_scaler* s, int representation, const uint64_t* d_in, uint64_t* d_out,
                                size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(s && ((d_in && d_out) || !count), "null input");
     abi_need(d_in != d_out || !count, "d_out must not alias d_in");
     const Scaler& sc = *s->s;
@@ -632,6 +644,7 @@ fheg_ksk* new_ksk_handle(const fheg_params* par, size_t ciphertext_level, size_t
 FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, size_t ksk_level, const uint64_t* h_c0,
                              const uint64_t* h_c1, size_t count, fheg_ksk** out) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && h_c0 && h_c1 && out, "null input");
     fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
@@ -648,6 +661,7 @@ FHEG_API int fheg_ksk_create(const fheg_params* par, size_t ciphertext_level, si
 FHEG_API int fheg_ksk_create_seeded(const fheg_params* par, size_t ciphertext_level, size_t ksk_level,
                                     const uint64_t* h_c0, const uint8_t* seed, size_t count, fheg_ksk** out) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && h_c0 && seed && out, "null input");
     fheg_ksk* h = new_ksk_handle(par, ciphertext_level, ksk_level, h_c0, count);
     try {
@@ -672,6 +686,7 @@ FHEG_API void fheg_ksk_destroy(fheg_ksk* k) { delete k; }
 
 FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(rk && ((d_ct3 && d_out) || !count), "null input");
     relinearize(rk->k, d_ct3, d_out, count, rk->k.ws, as_stream(stream));
   });
@@ -680,6 +695,7 @@ FHEG_API int fheg_relinearize(const fheg_ksk* rk, const uint64_t* d_ct3, uint64_
 FHEG_API int fheg_galois_relinearize(const fheg_ksk* gk, size_t exponent, const uint64_t* d_ct, uint64_t* d_out,
                                      size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(gk && ((d_ct && d_out) || !count), "null input");
     abi_need(d_ct != d_out || !count, "d_out must not alias d_ct");
     galois_relinearize(gk->k, exponent, d_ct, d_out, count, gk->k.ws, as_stream(stream));
@@ -722,6 +738,7 @@ FHEG_API void fheg_rgsw_destroy(fheg_rgsw* rgsw) { delete rgsw; }
 FHEG_API int fheg_external_product(const fheg_rgsw* rgsw, const uint64_t* d_ct, uint64_t* d_out, size_t count,
                                    void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(rgsw && ((d_ct && d_out) || !count), "null input");
     external_product(rgsw->k, d_ct, d_out, count, rgsw->k.ws, as_stream(stream));
   });
@@ -731,6 +748,7 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
                                            const size_t* exponents, const uint64_t* const* d_cts,
                                            uint64_t* const* d_outs, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((keys && exponents && d_cts && d_outs) || !count), "null input");
     std::vector<RotRequest> req(count);
     for (size_t b = 0; b < count; b++) {
@@ -765,6 +783,7 @@ FHEG_API int fheg_galois_relinearize_batch(const fheg_params* par, const fheg_ks
 FHEG_API int fheg_ciphertext_switch_down(const fheg_params* par, size_t level, size_t parts, uint64_t* d_ct,
                                          uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && parts >= 1 && ((d_ct && d_out) || !count), "null input");
     ciphertext_switch_down(*par->p, level, parts, d_ct, d_out, count, as_stream(stream));
   });
@@ -774,6 +793,7 @@ FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t leve
                                              size_t parts, uint64_t* d_ct, uint64_t* d_out, size_t count,
                                              void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((d_ct && d_out) || !count), "null input");
     const Params& p = *par->p;
     if (target_level < level || target_level > p.max_level())
@@ -802,6 +822,7 @@ FHEG_API int fheg_ciphertext_switch_to_level(const fheg_params* par, size_t leve
 FHEG_API int fheg_ciphertext_add(const fheg_params* par, size_t level, size_t parts, const uint64_t* d_a,
                                  const uint64_t* d_b, uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((d_a && d_b && d_out) || !count), "null input");
     const Context& c = *par->p->ctx(level);
     PolyRef a = plain_ref(const_cast<uint64_t*>(d_a), c.L(), c.logn);
@@ -881,6 +902,7 @@ FHEG_API int fheg_multiplicator_output_shape(const fheg_multiplicator* m, size_t
 FHEG_API int fheg_multiplicator_multiply(fheg_multiplicator* m, const uint64_t* d_lhs, const uint64_t* d_rhs,
                                          uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(m && ((d_lhs && d_rhs && d_out) || !count), "null input");
     cudaStream_t st = as_stream(stream);
     Multiplicator& mm = *m->m;
@@ -951,6 +973,7 @@ FHEG_API int fheg_multiplicator_set_host_pipeline(fheg_multiplicator* m, size_t 
 FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint64_t* h_lhs, const uint64_t* h_rhs,
                                               uint64_t* h_out, size_t count) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(m && ((h_lhs && h_rhs && h_out) || !count), "null input");
     if (!count) return;
     Multiplicator& mm = *m->m;

@@ -330,6 +330,7 @@ using namespace fheg;
 FHEG_API int fheg_plaintext_encode(const fheg_params* par, size_t level, const uint64_t* d_values, int simd,
                                    uint64_t* d_pt_ntt, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((d_values && d_pt_ntt) || !count), "null input");
     plaintext_encode(*par->p, level, d_values, simd != 0, d_pt_ntt, count, const_cast<fheg_params*>(par)->ws,
                      static_cast<cudaStream_t>(stream));
@@ -340,6 +341,7 @@ FHEG_API int fheg_ciphertext_mul_plain(const fheg_params* par, size_t level, siz
                                        const uint64_t* d_pt_ntt, int pt_per_ciphertext, uint64_t* d_out,
                                        size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && parts >= 1 && ((d_ct && d_pt_ntt && d_out) || !count), "null input");
     ciphertext_mul_plain(*par->p, level, parts, d_ct, d_pt_ntt, pt_per_ciphertext != 0, d_out, count,
                          static_cast<cudaStream_t>(stream));
@@ -379,6 +381,7 @@ FHEG_API void fheg_secret_key_destroy(fheg_secret_key* sk) { delete sk; }
 FHEG_API int fheg_encrypt(const fheg_secret_key* sk, size_t level, const uint64_t* d_values, int simd,
                           const uint64_t* d_a, const int64_t* d_e, uint64_t* d_ct, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(sk && ((d_values && d_a && d_e && d_ct) || !count), "null input");
     encrypt(sk->k, level, d_values, simd != 0, d_a, d_e, d_ct, count, sk->ws, static_cast<cudaStream_t>(stream));
   });
@@ -387,6 +390,7 @@ FHEG_API int fheg_encrypt(const fheg_secret_key* sk, size_t level, const uint64_
 FHEG_API int fheg_decrypt(const fheg_secret_key* sk, size_t level, size_t parts, const uint64_t* d_ct, int simd,
                           uint64_t* d_values, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(sk && ((d_ct && d_values) || !count), "null input");
     decrypt(sk->k, level, parts, d_ct, simd != 0, d_values, count, sk->ws, static_cast<cudaStream_t>(stream));
   });

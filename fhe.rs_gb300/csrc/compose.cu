@@ -157,6 +157,7 @@ FHEG_API int fheg_dot_product_scalar(const fheg_params* par, size_t level, size_
                                      const uint64_t* d_pts, size_t count, size_t groups, uint64_t* d_out,
                                      void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && parts >= 1 && ((d_cts && d_pts && d_out) || !groups), "null input");
     dot_product_scalar(*par->p, level, parts, d_cts, d_pts, count, groups, d_out, static_cast<cudaStream_t>(stream));
   });
@@ -165,6 +166,7 @@ FHEG_API int fheg_dot_product_scalar(const fheg_params* par, size_t level, size_
 FHEG_API int fheg_inner_sum(const fheg_params* par, const fheg_ksk* const* keys, const size_t* exponents,
                             size_t nkeys, const uint64_t* d_ct, uint64_t* d_out, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && keys && exponents && nkeys && ((d_ct && d_out) || !count), "null input");
     std::vector<uint64_t> ex(exponents, exponents + nkeys);
     const auto k = key_list(keys, nkeys);

@@ -9,6 +9,7 @@
 
 #include <vector>
 
+#include "abi_call.hpp"
 #include "fheg.h"
 #include "handles.hpp"
 #include "lib.hpp"
@@ -54,6 +55,7 @@ FHEG_API int fheg_multiplicator_capture(fheg_multiplicator* m, const uint64_t* d
   fheg::set_last_error("");
   if (!m || !d_lhs || !d_rhs || !d_out || !count || !out)
     return fail(fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "null input"));
+  if (count > fheg::kMaxItems) return fail(fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "item count above 2^24 per call"));
   cudaStream_t st = nullptr, st2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   auto release = [&] {
@@ -125,6 +127,7 @@ FHEG_API int fheg_galois_relinearize_batch_capture(const fheg_params* par, const
   fheg::set_last_error("");
   if (!par || !out || !count || !keys || !exponents || !d_cts || !d_outs)
     return fail(fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "null input"));
+  if (count > fheg::kMaxItems) return fail(fheg::Error(FHEG_ERR_INVALID_ARGUMENT, "item count above 2^24 per call"));
   cudaStream_t st = nullptr, st2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   auto release = [&] {

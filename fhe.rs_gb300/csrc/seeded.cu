@@ -366,6 +366,8 @@ using namespace fheg;
 FHEG_API int fheg_sample_cbd_from_seed(const uint8_t* d_seeds, size_t variance, size_t n, size_t count,
                                        int64_t* d_out, void* stream) {
   return abi_call([&] {
+    abi_count(n);
+    abi_count(count);
     abi_need((d_seeds && d_out) || !count || !n, "null input");
     sample_cbd_from_seed(d_seeds, variance, n, count, d_out, static_cast<cudaStream_t>(stream));
   });
@@ -374,6 +376,7 @@ FHEG_API int fheg_sample_cbd_from_seed(const uint8_t* d_seeds, size_t variance, 
 FHEG_API int fheg_poly_random_from_seed(const fheg_context* ctx, const uint8_t* d_seeds, uint64_t* d_out,
                                         size_t poly_stride, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && ((d_seeds && d_out) || !count), "null input");
     const Context& c = *ctx->c;
     poly_random_from_seed(c, d_seeds, d_out, poly_stride ? poly_stride : c.L() * c.N(), count, *ctx->ws,

@@ -601,6 +601,7 @@ FHEG_API int fheg_poly_serialized_size(const fheg_context* ctx, size_t* bytes) {
 FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, const uint64_t* d_polys,
                                  uint8_t* d_bytes, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && representation >= 0 && representation <= 2, "bad context or representation");
     abi_need((d_polys && d_bytes) || !count, "null input");
     DevBuf scratch;
@@ -612,6 +613,7 @@ FHEG_API int fheg_poly_serialize(const fheg_context* ctx, int representation, co
 FHEG_API int fheg_poly_deserialize(const fheg_context* ctx, int representation, const uint8_t* d_bytes,
                                    uint64_t* d_polys, size_t count, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(ctx && representation >= 0 && representation <= 2, "bad context or representation");
     abi_need((d_polys && d_bytes) || !count, "null input");
     poly_deserialize(*ctx->c, representation, d_bytes, d_polys, count, static_cast<cudaStream_t>(stream));
@@ -632,6 +634,7 @@ FHEG_API int fheg_ciphertext_to_bytes(const fheg_params* par, size_t level, size
                                       size_t count, const uint8_t* h_seeds, int allow_variable_time, uint8_t* h_out,
                                       size_t out_capacity, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((d_ct && h_out) || !count), "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     if (parts < 1 || (h_seeds && parts < 2)) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
@@ -653,6 +656,7 @@ FHEG_API int fheg_ciphertext_peek(const fheg_params* par, const uint8_t* h_msg, 
 FHEG_API int fheg_ciphertext_from_bytes(const fheg_params* par, const uint8_t* const* h_msgs, const size_t* lens,
                                         size_t count, size_t level, size_t parts, uint64_t* d_out, void* stream) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(par && ((h_msgs && lens && d_out) || !count), "null input");
     if (level > par->p->max_level()) throw Error(FHEG_ERR_INVALID_LEVEL, "InvalidLevel");
     if (parts < 2) throw Error(FHEG_ERR_WRONG_PARTS, "Not enough polynomials");
@@ -676,6 +680,7 @@ FHEG_API int fheg_evaluation_key_to_bytes(const fheg_ksk* const* keys, const siz
                                           size_t ciphertext_level, size_t evaluation_key_level, uint8_t* h_out,
                                           size_t cap, size_t* len) {
   return abi_call([&] {
+    abi_count(count);
     abi_need(len && ((keys && exponents) || !count), "null input");
     // evaluation_key.rs:382-392: { repeated GaloisKey gk = 2; ciphertext_level = 3;
     // evaluation_key_level = 4 }, keys in the order given.

@@ -14,6 +14,8 @@
  *    layout of `Poly::coefficients` (fhe-math/src/rq/mod.rs:124-132). A batch
  *    of `count` polynomials is `uint64_t[count][L][N]`; a batch of
  *    ciphertexts with `parts` polynomials each is `uint64_t[count][parts][L][N]`.
+ *    A call takes at most 2^24 items (counts above return
+ *    FHEG_ERR_INVALID_ARGUMENT).
  *  - `d_` pointers are device pointers (any CUDA allocation on the current
  *    device); `h_` pointers are host pointers. `stream` is a `cudaStream_t`
  *    (NULL = the legacy default stream).

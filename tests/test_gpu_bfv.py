@@ -497,6 +497,35 @@ def test_errors_of_the_wider_api(fg, ora, cuda):
     fg.plaintext_encode(par2, 0, fg.to_device(np.zeros((1, 16), dtype=np.uint64)), simd=False)
 
 
+def test_item_count_bound(fg, ora, cuda):
+    """Counts above 2^24 items are refused before any size is derived from
+    them (so none can wrap around to a small scratch allocation); the
+    buffers passed are far smaller than such a count would need, and no
+    kernel runs."""
+    s = Setup(fg, ora, 16, 3, 1153, seed=98)
+    rk_o, rk = s.rk()
+    m = fg.Multiplicator.default(rk)
+    _, cts = s.encrypt(2)
+    ct = fg.to_device(np.stack([c.to_array() for c in cts]))
+    out = fg.empty(tuple(ct.shape))
+    ctx = s.par.context_at_level(0)
+    huge = (1 << 24) + 1
+    dp, st = fg._dp, fg._stream()
+    calls = [
+        lambda: fg.lib().fheg_ntt_forward(ctx._h, dp(ct), huge, 0, st),
+        lambda: fg.lib().fheg_poly_op(ctx._h, 0, dp(ct), dp(ct), dp(out), huge, st),
+        lambda: fg.lib().fheg_multiplicator_multiply(m._h, dp(ct), dp(ct), dp(out), huge, st),
+        lambda: fg.lib().fheg_relinearize(rk._h, dp(ct), dp(out), huge, st),
+        lambda: fg.lib().fheg_ciphertext_add(s.par._h, 0, 2, dp(ct), dp(ct), dp(out), huge, st),
+    ]
+    for call in calls:
+        with pytest.raises(fg.FhegError) as e:
+            fg.check(call())
+        assert e.value.code == fg.ERR_INVALID_ARGUMENT and "2^24" in str(e.value)
+    cuda.cuda.synchronize()
+    assert np.array_equal(fg.to_host(ct), np.stack([c.to_array() for c in cts]))
+
+
 def test_small_batch_plan(fg, ora, cuda):
     """Batches up to the small-batch threshold use their own plan; results
     are the same with it, without it and with a custom one."""
