@@ -73,43 +73,61 @@ struct SrcTensor {
     return row(b, w, limb)[i];
   }
   // Staged load for the inverse NTT (k_ntt_inv): the operand rows stream
-  // into shared memory with asynchronous copies, half a block at a time (the
-  // two operands of a product fill the buffer), so every load of the phase is
-  // in flight at once instead of what the registers can hold; the products of
-  // the cross term are Montgomery-reduced separately and added (both carry
-  // the factor 2^-64).
+  // into shared memory with asynchronous copies, so every load of the phase
+  // is in flight at once instead of what the registers can hold. A square
+  // part (l0 r0 or l1 r1) stages half a block of its two operands at a time;
+  // the cross term (l0 r1 + l1 r0) a quarter block of its four, so that its
+  // two products are summed exactly (below 2 q_j^2 < q_j 2^64) and reduced
+  // once, as the unstaged path does.
   template <int LOGN, int T, int E>
   __device__ __forceinline__ void stage(const NttJob& j, const DevPrime& pr, uint32_t base, uint64_t* sm,
                                         uint32_t tid, uint64_t* x) const {
-    constexpr uint32_t HALF = 1u << (LOGN - 1);
+    constexpr uint32_t HALF = 1u << (LOGN - 1), QTR = HALF / 2;
     const uint32_t b = j.poly / 3, part = j.poly % 3;
-    const int npairs = part == 1 ? 2 : 1;
+    if (part != 1) {
+      const uint64_t* ra = row(b, part >> 1, j.limb) + base;
+      const uint64_t* rb = row(b, 2 + (part >> 1), j.limb) + base;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        if (q < npairs) {
-          // part 0: l0 r0; part 2: l1 r1; part 1: l0 r1 + l1 r0.
-          const uint32_t wa = part == 0 ? 0 : (part == 2 ? 1 : (uint32_t)q);
-          const uint32_t wb = part == 0 ? 2 : (part == 2 ? 3 : (q == 0 ? 3u : 2u));
-          const uint64_t* ra = row(b, wa, j.limb) + base + h * HALF;
-          const uint64_t* rb = row(b, wb, j.limb) + base + h * HALF;
-          for (uint32_t c = tid; c < HALF / 2; c += T) {
-            cp_async16(sm + 2 * c, ra + 2 * c);
-            cp_async16(sm + HALF + 2 * c, rb + 2 * c);
-          }
-          cp_async_wait_all();
-          __syncthreads();
-#pragma unroll
-          for (int e = 0; e < E / 2; e++) {
-            const uint32_t idx = tid + e * T;
-            const uint64_t u = sm[idx], v = sm[HALF + idx];
-            const uint64_t m = mont_reduce(__umul64hi(u, v), u * v, pr);
-            x[h * (E / 2) + e] = q == 0 ? m : csub(x[h * (E / 2) + e] + m, pr.p2);
-          }
-          __syncthreads();
+      for (int h = 0; h < 2; h++) {
+        for (uint32_t c = tid; c < HALF / 2; c += T) {
+          cp_async16(sm + 2 * c, ra + h * HALF + 2 * c);
+          cp_async16(sm + HALF + 2 * c, rb + h * HALF + 2 * c);
         }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < E / 2; e++) {
+          const uint32_t idx = tid + e * T;
+          const uint64_t u = sm[idx], v = sm[HALF + idx];
+          x[h * (E / 2) + e] = mont_reduce(__umul64hi(u, v), u * v, pr);
+        }
+        __syncthreads();
       }
+      return;
+    }
+    const uint64_t* r0 = row(b, 0, j.limb) + base;
+    const uint64_t* r1 = row(b, 3, j.limb) + base;
+    const uint64_t* r2 = row(b, 1, j.limb) + base;
+    const uint64_t* r3 = row(b, 2, j.limb) + base;
+#pragma unroll
+    for (int qt = 0; qt < 4; qt++) {
+      for (uint32_t c = tid; c < QTR / 2; c += T) {
+        cp_async16(sm + 2 * c, r0 + qt * QTR + 2 * c);
+        cp_async16(sm + QTR + 2 * c, r1 + qt * QTR + 2 * c);
+        cp_async16(sm + 2 * QTR + 2 * c, r2 + qt * QTR + 2 * c);
+        cp_async16(sm + 3 * QTR + 2 * c, r3 + qt * QTR + 2 * c);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E / 4; e++) {
+        const uint32_t idx = tid + e * T;
+        uint64_t hi = 0, lo = 0;
+        mac128(hi, lo, sm[idx], sm[QTR + idx]);
+        mac128(hi, lo, sm[2 * QTR + idx], sm[3 * QTR + idx]);
+        x[qt * (E / 4) + e] = mont_reduce(hi, lo, pr);
+      }
+      __syncthreads();
     }
   }
   __device__ __forceinline__ void prefetch(const NttJob& j, uint32_t i) const {
