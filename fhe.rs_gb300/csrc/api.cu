@@ -999,12 +999,8 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     // and the drain (one chunk's output) short.
     const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 8 ? 4 : count);
     const size_t nchunks = (count + chunk - 1) / chunk;
-    for (auto* evs : {&m->copied, &m->computed})
-      while (evs->size() < nchunks) {
-        cudaEvent_t e;
-        check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
-        evs->push_back(e);
-      }
+    for (cudaEvent_t* e : {&m->copied, &m->computed})
+      if (!*e) check_cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * out_L * N;
     for (size_t i = 0; i < nchunks; i++) {
       const size_t first = i * chunk, c = std::min(chunk, count - first);
@@ -1014,12 +1010,12 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
                                  cudaMemcpyHostToDevice, m->copy_in), "H2D");
       check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
                                  cudaMemcpyHostToDevice, m->copy_in), "H2D");
-      check_cuda(cudaEventRecord(m->copied[i], m->copy_in), "cudaEventRecord");
-      check_cuda(cudaStreamWaitEvent(st, m->copied[i], 0), "cudaStreamWaitEvent");
+      check_cuda(cudaEventRecord(m->copied, m->copy_in), "cudaEventRecord");
+      check_cuda(cudaStreamWaitEvent(st, m->copied, 0), "cudaStreamWaitEvent");
       mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
                   &m->pipe_ws[k]);
-      check_cuda(cudaEventRecord(m->computed[i], st), "cudaEventRecord");
-      check_cuda(cudaStreamWaitEvent(m->copy_out, m->computed[i], 0), "cudaStreamWaitEvent");
+      check_cuda(cudaEventRecord(m->computed, st), "cudaEventRecord");
+      check_cuda(cudaStreamWaitEvent(m->copy_out, m->computed, 0), "cudaStreamWaitEvent");
       check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
                                  cudaMemcpyDeviceToHost, m->copy_out), "D2H");
     }

@@ -47,8 +47,10 @@ struct fheg_multiplicator {
   cudaStream_t copy_in = nullptr;      // every chunk's input copies, in chunk order
   cudaStream_t copy_out = nullptr;     // every chunk's output copy, in chunk order
   fheg::Workspace pipe_ws[kPipe];
-  std::vector<cudaEvent_t> copied;    // end of each chunk's input copies
-  std::vector<cudaEvent_t> computed;  // end of each chunk's multiplication
+  // End of a chunk's input copies / of its multiplication. One event each
+  // serves every chunk: each record is waited on right after it is made,
+  // and a wait holds the work of the record it follows.
+  cudaEvent_t copied = nullptr, computed = nullptr;
   size_t host_chunk = 0;            // pairs per chunk (0 = automatic)
   int host_streams = 3;
   // Second branch of a large direct multiplication (api.cu): its stream,
@@ -61,8 +63,8 @@ struct fheg_multiplicator {
       if (s) cudaStreamDestroy(s);
     if (copy_in) cudaStreamDestroy(copy_in);
     if (copy_out) cudaStreamDestroy(copy_out);
-    for (auto& e : copied) cudaEventDestroy(e);
-    for (auto& e : computed) cudaEventDestroy(e);
+    if (copied) cudaEventDestroy(copied);
+    if (computed) cudaEventDestroy(computed);
     if (side) cudaStreamDestroy(side);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
