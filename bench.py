@@ -64,18 +64,18 @@ STAGE_LAUNCHES = {"A": 1, "B": 1, "C": 1, "D": 1, "E": 1, "F": 2, "G": 1}
 # strided NTT stage applied inside the RNS scalers B and E; E's sums on the
 # tensor cores), from the ncu capture summarised in
 # profiles/stages_mul_relin_n16384_b64.md.
-STAGE_TRAFFIC_BYTES = {"A": 352.9e6, "B": 393.5e6, "C": 409.6e6, "D": 727.8e6, "E": 675.8e6, "F": 696.6e6,
-                       "G": 493.4e6}
+STAGE_TRAFFIC_BYTES = {"A": 353.2e6, "B": 393.2e6, "C": 409.4e6, "D": 728.0e6, "E": 675.7e6, "F": 696.2e6,
+                       "G": 493.6e6}
 # The ncu figures above and below hold for the library sources they were
 # captured on: library_source_hash() of that tree. A run on other sources
 # reports null for them instead of stale numbers.
-PROFILED_SOURCE_HASH = "89774cd5a4d553d9"
+PROFILED_SOURCE_HASH = "e7052cef359c4eb3"
 # Share of the elapsed cycles in which the integer multipliers (the FMA-heavy
 # pipe, which executes every IMAD) were busy, per stage, from the same ncu
 # capture of one 64-pair multiplication (F: time-weighted over its two
 # launches); the whole multiplication, time-weighted.
-STAGE_FMAHEAVY_PCT = {"A": 70.0, "B": 84.0, "C": 70.9, "D": 67.4, "E": 61.7, "F": 70.4, "G": 63.8}
-MULTIPLY_FMAHEAVY_PCT = 69.5
+STAGE_FMAHEAVY_PCT = {"A": 69.9, "B": 84.0, "C": 70.6, "D": 67.1, "E": 61.3, "F": 70.4, "G": 63.7}
+MULTIPLY_FMAHEAVY_PCT = 69.3
 
 
 def library_source_hash() -> str:

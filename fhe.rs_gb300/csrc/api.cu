@@ -995,29 +995,42 @@ FHEG_API int fheg_multiplicator_multiply_host(fheg_multiplicator* m, const uint6
     // stream i % ns once its inputs have landed. Each chunk has its own
     // staging rows, so no copy waits for a multiplication other than its
     // own chunk's, and no multiplication for a copy of another chunk. Small
-    // chunks (4 pairs, four at a time) keep the fill (one chunk's inputs)
+    // chunks (4 pairs, three at a time) keep the fill (one chunk's inputs)
     // and the drain (one chunk's output) short.
     const size_t chunk = m->host_chunk ? std::min(m->host_chunk, count) : (count >= 8 ? 4 : count);
     const size_t nchunks = (count + chunk - 1) / chunk;
     for (cudaEvent_t* e : {&m->copied, &m->computed})
       if (!*e) check_cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     const size_t in_pair = 2 * L * N, out_pair = mm.out_parts() * out_L * N;
-    for (size_t i = 0; i < nchunks; i++) {
-      const size_t first = i * chunk, c = std::min(chunk, count - first);
-      const int k = (int)(i % ns);
-      cudaStream_t st = m->pipe[k];
-      check_cuda(cudaMemcpyAsync(d_lhs + first * in_pair, h_lhs + first * in_pair, c * in_pair * 8,
-                                 cudaMemcpyHostToDevice, m->copy_in), "H2D");
-      check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
-                                 cudaMemcpyHostToDevice, m->copy_in), "H2D");
-      check_cuda(cudaEventRecord(m->copied, m->copy_in), "cudaEventRecord");
-      check_cuda(cudaStreamWaitEvent(st, m->copied, 0), "cudaStreamWaitEvent");
-      mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
-                  &m->pipe_ws[k]);
-      check_cuda(cudaEventRecord(m->computed, st), "cudaEventRecord");
-      check_cuda(cudaStreamWaitEvent(m->copy_out, m->computed, 0), "cudaStreamWaitEvent");
-      check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
-                                 cudaMemcpyDeviceToHost, m->copy_out), "D2H");
+    // A chunk that fails to launch ends the call only once the copies already
+    // queued have finished: none of them may write into h_out after the
+    // caller regains it.
+    auto drain = [&] {
+      cudaStreamSynchronize(m->copy_in);
+      for (int k = 0; k < ns; k++) cudaStreamSynchronize(m->pipe[k]);
+      cudaStreamSynchronize(m->copy_out);
+    };
+    try {
+      for (size_t i = 0; i < nchunks; i++) {
+        const size_t first = i * chunk, c = std::min(chunk, count - first);
+        const int k = (int)(i % ns);
+        cudaStream_t st = m->pipe[k];
+        check_cuda(cudaMemcpyAsync(d_lhs + first * in_pair, h_lhs + first * in_pair, c * in_pair * 8,
+                                   cudaMemcpyHostToDevice, m->copy_in), "H2D");
+        check_cuda(cudaMemcpyAsync(d_rhs + first * in_pair, h_rhs + first * in_pair, c * in_pair * 8,
+                                   cudaMemcpyHostToDevice, m->copy_in), "H2D");
+        check_cuda(cudaEventRecord(m->copied, m->copy_in), "cudaEventRecord");
+        check_cuda(cudaStreamWaitEvent(st, m->copied, 0), "cudaStreamWaitEvent");
+        mm.multiply(d_lhs + first * in_pair, d_rhs + first * in_pair, d_out + first * out_pair, c, st,
+                    &m->pipe_ws[k]);
+        check_cuda(cudaEventRecord(m->computed, st), "cudaEventRecord");
+        check_cuda(cudaStreamWaitEvent(m->copy_out, m->computed, 0), "cudaStreamWaitEvent");
+        check_cuda(cudaMemcpyAsync(h_out + first * out_pair, d_out + first * out_pair, c * out_pair * 8,
+                                   cudaMemcpyDeviceToHost, m->copy_out), "D2H");
+      }
+    } catch (...) {
+      drain();
+      throw;
     }
     // The output stream waits for every chunk, and every chunk for its inputs.
     check_cuda(cudaStreamSynchronize(m->copy_out), "cudaStreamSynchronize");
